@@ -1,0 +1,183 @@
+/* sph_gb300: GB300 (sm_103a) implementation of the per-step particle loop of
+ * josemanuel28v/SPH, behind a plain C ABI.
+ *
+ * One context (sph_ctx) holds one scene: one fluid model and one boundary
+ * model, the way the reference's Simulation singleton holds them, but with
+ * explicit handles instead of a process-global (src/Simulation.cpp:84-90), so
+ * contexts are independent and many can live in one process.  All state is
+ * device-resident; host buffers are touched only by the upload/download
+ * calls.  Every function returns SPH_OK (0) or a negative SPH_ERR_* code and
+ * never throws; sph_ctx_last_error() describes the last failure.
+ *
+ * Reference interfaces replaced (paths in the reference repository):
+ *   SPHSolver::init/step/resizeData            src/SPHSolver.h:37-39
+ *   Simulation::init / step                    src/Simulation.cpp:102-182
+ *   WCSPHSolver / PCISPHSolver / DFSPHSolver    src/*Solver.{h,cpp}
+ *   NonPressureForce::step (the five plugins)  src/NonPressureForce.h:17
+ *   AkinciBoundaryModel::addCube/addSphere/computeVolume
+ *                                              src/AkinciBoundayModel.cpp:11-164
+ *   CubeBoundaryModel::correctPositionAndVelocity src/CubeBoundaryModel.cpp:16-94
+ *   HashTable insert / neighborhoodSearch      src/HashTable.h:79-170
+ */
+#ifndef SPH_GB300_H
+#define SPH_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPH_OK 0
+#define SPH_ERR_INVALID -1      /* bad argument or call order */
+#define SPH_ERR_CUDA -2         /* a CUDA call failed */
+#define SPH_ERR_UNSUPPORTED -3  /* feature not available in this build */
+#define SPH_ERR_CAPACITY -4     /* grid or particle capacity exceeded */
+
+/* Method ids, identical to the reference's (src/Simulation.cpp:21-43). */
+#define SPH_WCSPH 0
+#define SPH_PCISPH 1
+#define SPH_DFSPH 2
+#define SPH_BOUNDARY_CUBE 0
+#define SPH_BOUNDARY_PCISPH 1
+#define SPH_BOUNDARY_AKINCI 2
+#define SPH_VISCOSITY_STANDARD 0
+#define SPH_VISCOSITY_ARTIFICIAL 1
+#define SPH_VISCOSITY_XSPH 2
+#define SPH_SURFACE_TENSION_AKINCI 3
+#define SPH_ADHESION_AKINCI 4
+
+/* Arithmetic of the device path. */
+#define SPH_PRECISION_F32 0   /* production: FP32 bulk, cell-relative positions, FP64 reductions */
+#define SPH_PRECISION_F64 1   /* parity: FP64 throughout, the reference's expression order */
+
+/* Fields for sph_ctx_download (original particle order, FP64). */
+#define SPH_FIELD_POSITION 0        /* 3 per fluid particle */
+#define SPH_FIELD_VELOCITY 1        /* 3 */
+#define SPH_FIELD_ACCELERATION 2    /* 3, non-pressure acceleration */
+#define SPH_FIELD_DENSITY 3         /* 1 */
+#define SPH_FIELD_PRESSURE 4        /* 1 (WCSPH / PCISPH) */
+#define SPH_FIELD_ALPHA 5           /* 1 (DFSPH) */
+#define SPH_FIELD_PRED_DENSITY 6    /* 1 (DFSPH) */
+#define SPH_FIELD_DIV_ERROR 7       /* 1 (DFSPH) */
+#define SPH_FIELD_KAPPA 8           /* 1 (DFSPH k) */
+#define SPH_FIELD_KAPPA_V 9         /* 1 (DFSPH kv) */
+#define SPH_FIELD_PRESSURE_ACC 10   /* 3 (PCISPH) */
+#define SPH_FIELD_NORMAL 11         /* 3 (surface tension) */
+#define SPH_FIELD_BOUNDARY_POSITION 12 /* 3 per boundary particle */
+#define SPH_FIELD_BOUNDARY_VOLUME 13   /* 1 per boundary particle (psi) */
+
+/* Device status bits (sph_stats.status). */
+#define SPH_STATUS_OUT_OF_GRID 1u   /* a particle left the grid box; it was kept in the border cell */
+#define SPH_STATUS_NONFINITE 2u     /* a solver reduction produced NaN/Inf */
+#define SPH_STATUS_ITER_CAP 4u      /* density / pressure solve stopped at maxIterations */
+#define SPH_STATUS_ITER_CAP_V 8u    /* divergence solve stopped at the iteration cap */
+
+typedef struct sph_ctx sph_ctx;
+
+/* Scene description: the fields of the reference's SceneInfo / Fluid /
+ * Boundary structs (src/Simulation.h:47-131) that the particle loop uses,
+ * plus device-path settings.  Fill with sph_scene_desc_init first. */
+typedef struct sph_scene_desc {
+    int simulation_method;        /* SPH_WCSPH / SPH_PCISPH / SPH_DFSPH */
+    int boundary_method;          /* SPH_BOUNDARY_* */
+    int precision;                /* SPH_PRECISION_* */
+    double particle_radius;       /* r; support radius h = 4 r (Simulation.cpp:197) */
+    double gravity[3];
+    double time_step;             /* initial dt */
+    double min_time_step, max_time_step, fps; /* min dt is min(min_time_step, 1/fps) (TimeManager.h:55) */
+    double density0;
+    double stiffness, gamma;      /* WCSPH */
+    double max_error;             /* eta: PCISPH max / DFSPH average density error */
+    double max_error_v;           /* DFSPH etaV */
+    double cfl_factor;            /* DFSPH */
+    int min_iterations, max_iterations;     /* < 0: solver default */
+    int min_iterations_v, max_iterations_v; /* < 0: solver default */
+    int viscosity_method;         /* SPH_VISCOSITY_* or -1 */
+    double viscosity, boundary_viscosity;
+    int surface_tension_method;   /* SPH_SURFACE_TENSION_AKINCI or -1 */
+    double surface_tension;
+    int adhesion_method;          /* SPH_ADHESION_AKINCI or -1 */
+    double adhesion;
+    int has_cube;                 /* cube boundary present (boundary_method 0) */
+    double cube_min[3], cube_max[3];
+    double domain_min[3], domain_max[3]; /* grid box; equal min/max: derive from the points */
+    int threads_per_particle;     /* 1, 2, 4, 8 (FP32); 0: default */
+} sph_scene_desc;
+
+typedef struct sph_stats {
+    double time;                  /* simulated time */
+    double dt;                    /* current time step */
+    double avg_density_error;     /* DFSPH: last predicted average density error */
+    double avg_divergence_error;  /* DFSPH: last average divergence error */
+    double max_density_error;     /* PCISPH: last maximum density error */
+    double max_velocity;          /* DFSPH: max(0.1, sqrt(|v|)) of the last CFL step */
+    unsigned iterations;          /* density / pressure iterations of the last step */
+    unsigned iterations_v;        /* divergence iterations of the last step */
+    unsigned steps;
+    unsigned status;              /* SPH_STATUS_* bits, sticky */
+    unsigned long long sum_iterations, sum_iterations_v;
+    unsigned num_fluid, num_boundary;
+} sph_stats;
+
+/* Defaults of the reference (SPHSolver.cpp:12-19, DFSPHSolver.cpp:10-22,
+ * TimeManager.h:43-47, FluidModel.cpp:98). */
+int sph_scene_desc_init(sph_scene_desc* desc);
+
+/* Simulation::setSimulationMethod + setters (Simulation.cpp:207-231). */
+int sph_ctx_create(const sph_scene_desc* desc, sph_ctx** out);
+int sph_ctx_destroy(sph_ctx* ctx);
+
+/* FluidModel::init (FluidModel.cpp:37-49): positions/velocities, xyz per
+ * particle, FP64.  v may be NULL (zero). */
+int sph_ctx_set_fluid(sph_ctx* ctx, const double* x, const double* v, unsigned n);
+/* Simulation::buildFluidBlock (Simulation.cpp:512-539); appends. */
+int sph_ctx_add_fluid_block(sph_ctx* ctx, const double min[3], const double max[3]);
+/* AkinciBoundaryModel::addCube / addSphere (AkinciBoundayModel.cpp:42-98,
+ * sampling :100-164); appends to the scene's boundary model. */
+int sph_ctx_add_boundary_box(sph_ctx* ctx, const double min[3], const double max[3]);
+int sph_ctx_add_boundary_sphere(sph_ctx* ctx, const double center[3], double radius);
+/* Raw boundary points (xyz, FP64). */
+int sph_ctx_add_boundary_points(sph_ctx* ctx, const double* x, unsigned n);
+
+/* Simulation::init -> solver->init (Simulation.cpp:102-110,
+ * SPHSolver.cpp:22-39, DFSPHSolver.cpp:24-36, PCISPHSolver.cpp:12-19):
+ * uploads, builds the grids, boundary volumes, and DFSPH densities/alpha. */
+int sph_ctx_init(sph_ctx* ctx);
+
+/* nsteps calls of Simulation::step -> solver->step (Simulation.cpp:148-182).
+ * Asynchronous on the context's stream except where a solver loop needs a
+ * convergence test read back (see sph_ctx_set_graph). */
+int sph_ctx_step(sph_ctx* ctx, int nsteps);
+/* Wait for the context's stream. */
+int sph_ctx_synchronize(sph_ctx* ctx);
+
+/* Run whole steps as one CUDA graph with device-side solver loops
+ * (conditional WHILE nodes): no host round trip per iteration.  1 = on. */
+int sph_ctx_set_graph(sph_ctx* ctx, int enable);
+
+int sph_ctx_num_particles(const sph_ctx* ctx, unsigned* num_fluid, unsigned* num_boundary);
+/* Copy a field to host memory in original particle order (FP64). */
+int sph_ctx_download(sph_ctx* ctx, int field, double* out);
+int sph_ctx_get_stats(sph_ctx* ctx, sph_stats* out);
+const char* sph_ctx_last_error(const sph_ctx* ctx);
+
+/* Test hook: per fluid particle (original order) its cell floor(x/h)
+ * (3 ints), its rank inside the cell, and the neighbour lists the solver
+ * walks (fluid and boundary candidates with |xi - xj| / h <= 1, in walk
+ * order).  Call with NULL arrays to get totals[0] (fluid pairs) and
+ * totals[1] (boundary pairs) first. */
+int sph_ctx_neighbors(sph_ctx* ctx, int* cells, int* cell_rank, int* nbr_off, int* nbr, int* bnbr_off, int* bnbr,
+                      long long* totals);
+
+/* Sampling helpers with the reference's point sets, usable without a
+ * context; out may be NULL to query the count.  Return the point count. */
+long long sph_sample_box(double support_radius, const double min[3], const double max[3], double* out);
+long long sph_sample_sphere(double particle_radius, const double center[3], double radius, double* out);
+long long sph_fluid_block(double particle_radius, const double min[3], const double max[3], double* out);
+
+/* Build identification string. */
+const char* sph_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,327 @@
+"""sph_gb300: GB300 (sm_103a) per-step SPH particle loop behind a C ABI.
+
+This module is a thin ctypes layer over ``lib/libsph_gb300.so`` (declared in
+``include/sph_gb300.h``).  All computation happens in the library's CUDA
+kernels; if the library is missing or fails to load, every entry point raises
+-- there is no CPU fallback.
+
+Vocabulary follows the reference simulator (josemanuel28v/SPH):
+``Scene`` bundles what the reference's ``Simulation`` singleton holds for one
+fluid model and one boundary model -- ``add_fluid_block`` is
+``Simulation::buildFluidBlock``, ``add_boundary_box`` / ``add_boundary_sphere``
+are ``AkinciBoundaryModel::addCube`` / ``addSphere``, ``init`` is
+``Simulation::init`` and ``step`` is ``Simulation::step``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libsph_gb300.so")
+
+# Method ids (src/Simulation.cpp:21-43 of the reference)
+WCSPH, PCISPH, DFSPH = 0, 1, 2
+BOUNDARY_CUBE, BOUNDARY_PCISPH, BOUNDARY_AKINCI = 0, 1, 2
+VISCOSITY_STANDARD, VISCOSITY_ARTIFICIAL, VISCOSITY_XSPH = 0, 1, 2
+SURFACE_TENSION_AKINCI, ADHESION_AKINCI = 3, 4
+PRECISION_F32, PRECISION_F64 = 0, 1
+
+FIELDS = {
+    "x": (0, 3), "v": (1, 3), "a": (2, 3), "rho": (3, 1), "p": (4, 1), "alpha": (5, 1), "pred": (6, 1),
+    "div": (7, 1), "k": (8, 1), "kv": (9, 1), "pacc": (10, 3), "normal": (11, 3), "bx": (12, 3), "psi": (13, 1),
+}
+
+STATUS_OUT_OF_GRID, STATUS_NONFINITE, STATUS_ITER_CAP, STATUS_ITER_CAP_V = 1, 2, 4, 8
+
+
+class SceneDesc(ctypes.Structure):
+    _fields_ = [
+        ("simulation_method", ctypes.c_int),
+        ("boundary_method", ctypes.c_int),
+        ("precision", ctypes.c_int),
+        ("particle_radius", ctypes.c_double),
+        ("gravity", ctypes.c_double * 3),
+        ("time_step", ctypes.c_double),
+        ("min_time_step", ctypes.c_double),
+        ("max_time_step", ctypes.c_double),
+        ("fps", ctypes.c_double),
+        ("density0", ctypes.c_double),
+        ("stiffness", ctypes.c_double),
+        ("gamma", ctypes.c_double),
+        ("max_error", ctypes.c_double),
+        ("max_error_v", ctypes.c_double),
+        ("cfl_factor", ctypes.c_double),
+        ("min_iterations", ctypes.c_int),
+        ("max_iterations", ctypes.c_int),
+        ("min_iterations_v", ctypes.c_int),
+        ("max_iterations_v", ctypes.c_int),
+        ("viscosity_method", ctypes.c_int),
+        ("viscosity", ctypes.c_double),
+        ("boundary_viscosity", ctypes.c_double),
+        ("surface_tension_method", ctypes.c_int),
+        ("surface_tension", ctypes.c_double),
+        ("adhesion_method", ctypes.c_int),
+        ("adhesion", ctypes.c_double),
+        ("has_cube", ctypes.c_int),
+        ("cube_min", ctypes.c_double * 3),
+        ("cube_max", ctypes.c_double * 3),
+        ("domain_min", ctypes.c_double * 3),
+        ("domain_max", ctypes.c_double * 3),
+        ("threads_per_particle", ctypes.c_int),
+    ]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [
+        ("time", ctypes.c_double),
+        ("dt", ctypes.c_double),
+        ("avg_density_error", ctypes.c_double),
+        ("avg_divergence_error", ctypes.c_double),
+        ("max_density_error", ctypes.c_double),
+        ("max_velocity", ctypes.c_double),
+        ("iterations", ctypes.c_uint),
+        ("iterations_v", ctypes.c_uint),
+        ("steps", ctypes.c_uint),
+        ("status", ctypes.c_uint),
+        ("sum_iterations", ctypes.c_ulonglong),
+        ("sum_iterations_v", ctypes.c_ulonglong),
+        ("num_fluid", ctypes.c_uint),
+        ("num_boundary", ctypes.c_uint),
+    ]
+
+
+# The C ABI, as (name, restype, argtypes); the CPU tests check that the
+# library exports each of these.
+_vp, _dp, _ip = ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)
+ABI = [
+    ("sph_scene_desc_init", ctypes.c_int, [ctypes.POINTER(SceneDesc)]),
+    ("sph_ctx_create", ctypes.c_int, [ctypes.POINTER(SceneDesc), ctypes.POINTER(_vp)]),
+    ("sph_ctx_destroy", ctypes.c_int, [_vp]),
+    ("sph_ctx_set_fluid", ctypes.c_int, [_vp, _dp, _dp, ctypes.c_uint]),
+    ("sph_ctx_add_fluid_block", ctypes.c_int, [_vp, _dp, _dp]),
+    ("sph_ctx_add_boundary_box", ctypes.c_int, [_vp, _dp, _dp]),
+    ("sph_ctx_add_boundary_sphere", ctypes.c_int, [_vp, _dp, ctypes.c_double]),
+    ("sph_ctx_add_boundary_points", ctypes.c_int, [_vp, _dp, ctypes.c_uint]),
+    ("sph_ctx_init", ctypes.c_int, [_vp]),
+    ("sph_ctx_step", ctypes.c_int, [_vp, ctypes.c_int]),
+    ("sph_ctx_synchronize", ctypes.c_int, [_vp]),
+    ("sph_ctx_set_graph", ctypes.c_int, [_vp, ctypes.c_int]),
+    ("sph_ctx_num_particles", ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_uint), ctypes.POINTER(ctypes.c_uint)]),
+    ("sph_ctx_download", ctypes.c_int, [_vp, ctypes.c_int, _dp]),
+    ("sph_ctx_get_stats", ctypes.c_int, [_vp, ctypes.POINTER(Stats)]),
+    ("sph_ctx_last_error", ctypes.c_char_p, [_vp]),
+    ("sph_ctx_neighbors", ctypes.c_int, [_vp, _ip, _ip, _ip, _ip, _ip, _ip, ctypes.POINTER(ctypes.c_longlong)]),
+    ("sph_sample_box", ctypes.c_longlong, [ctypes.c_double, _dp, _dp, _dp]),
+    ("sph_sample_sphere", ctypes.c_longlong, [ctypes.c_double, _dp, ctypes.c_double, _dp]),
+    ("sph_fluid_block", ctypes.c_longlong, [ctypes.c_double, _dp, _dp, _dp]),
+    ("sph_version", ctypes.c_char_p, []),
+]
+
+_lib = None
+
+
+class SPHError(RuntimeError):
+    pass
+
+
+def build(verbose: bool = False, force: bool = False) -> str:
+    from . import buildlib as _b
+
+    return _b.build(verbose=verbose, force=force)
+
+
+def lib():
+    """Load the CUDA library (raises if it is missing: no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise SPHError(f"{LIB_PATH} is missing; build it with sph_gb300.build()")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, res, args in ABI:
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _d(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _i(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+
+
+def _v3(v):
+    return np.ascontiguousarray(np.asarray(v, dtype=np.float64).reshape(3))
+
+
+# parameter names shared with the oracle's scene parameters
+_PARAM_MAP = {
+    "method": "simulation_method", "boundary": "boundary_method", "radius": "particle_radius",
+    "dt": "time_step", "min_dt": "min_time_step", "max_dt": "max_time_step", "fps": "fps",
+    "density0": "density0", "stiffness": "stiffness", "gamma": "gamma", "eta": "max_error",
+    "eta_v": "max_error_v", "cfl": "cfl_factor", "min_it": "min_iterations", "max_it": "max_iterations",
+    "min_it_v": "min_iterations_v", "max_it_v": "max_iterations_v", "visc_method": "viscosity_method",
+    "visc": "viscosity", "bvisc": "boundary_viscosity", "st_method": "surface_tension_method",
+    "st": "surface_tension", "adh_method": "adhesion_method", "adh": "adhesion", "has_cube": "has_cube",
+    "precision": "precision", "threads_per_particle": "threads_per_particle",
+}
+_VEC = {"gravity", "cube_min", "cube_max", "domain_min", "domain_max"}
+
+
+def make_desc(**params) -> SceneDesc:
+    d = SceneDesc()
+    lib().sph_scene_desc_init(ctypes.byref(d))
+    for k, v in params.items():
+        if k in _VEC:
+            getattr(d, k)[:] = [float(t) for t in v]
+            continue
+        name = _PARAM_MAP.get(k, k)
+        if not hasattr(d, name):
+            raise KeyError(f"unknown scene parameter {k}")
+        if k == "precision" and isinstance(v, str):
+            v = PRECISION_F64 if v in ("f64", "fp64", "double") else PRECISION_F32
+        setattr(d, name, v)
+    return d
+
+
+class Scene:
+    """One device-resident scene (one fluid model, one boundary model)."""
+
+    def __init__(self, **params):
+        L = lib()
+        self._desc = make_desc(**params)
+        self._h = ctypes.c_void_p()
+        rc = L.sph_ctx_create(ctypes.byref(self._desc), ctypes.byref(self._h))
+        if rc != 0:
+            raise SPHError(f"sph_ctx_create failed ({rc})")
+        self._inited = False
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            lib().sph_ctx_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc, what):
+        if rc != 0:
+            msg = lib().sph_ctx_last_error(self._h)
+            raise SPHError(f"{what} failed ({rc}): {msg.decode() if msg else ''}")
+
+    # -- construction -------------------------------------------------------
+    def set_fluid(self, x, v=None):
+        x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, 3)
+        vv = None if v is None else np.ascontiguousarray(v, dtype=np.float64).reshape(-1, 3)
+        self._check(lib().sph_ctx_set_fluid(self._h, _d(x), None if vv is None else _d(vv), x.shape[0]),
+                    "sph_ctx_set_fluid")
+        return self
+
+    def add_fluid_block(self, mn, mx):
+        self._check(lib().sph_ctx_add_fluid_block(self._h, _d(_v3(mn)), _d(_v3(mx))), "sph_ctx_add_fluid_block")
+        return self
+
+    def add_boundary_box(self, mn, mx):
+        self._check(lib().sph_ctx_add_boundary_box(self._h, _d(_v3(mn)), _d(_v3(mx))), "sph_ctx_add_boundary_box")
+        return self
+
+    def add_boundary_sphere(self, c, radius):
+        self._check(lib().sph_ctx_add_boundary_sphere(self._h, _d(_v3(c)), float(radius)),
+                    "sph_ctx_add_boundary_sphere")
+        return self
+
+    def add_boundary_points(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, 3)
+        self._check(lib().sph_ctx_add_boundary_points(self._h, _d(x), x.shape[0]), "sph_ctx_add_boundary_points")
+        return self
+
+    def init(self):
+        self._check(lib().sph_ctx_init(self._h), "sph_ctx_init")
+        self._inited = True
+        return self
+
+    # -- running ------------------------------------------------------------
+    def step(self, n=1):
+        self._check(lib().sph_ctx_step(self._h, int(n)), "sph_ctx_step")
+
+    def synchronize(self):
+        self._check(lib().sph_ctx_synchronize(self._h), "sph_ctx_synchronize")
+
+    def set_graph(self, enable=True):
+        self._check(lib().sph_ctx_set_graph(self._h, int(bool(enable))), "sph_ctx_set_graph")
+
+    # -- results ------------------------------------------------------------
+    def counts(self):
+        nf, nb = ctypes.c_uint(), ctypes.c_uint()
+        lib().sph_ctx_num_particles(self._h, ctypes.byref(nf), ctypes.byref(nb))
+        return nf.value, nb.value
+
+    @property
+    def n(self):
+        return self.counts()[0]
+
+    @property
+    def nb(self):
+        return self.counts()[1]
+
+    def get(self, field):
+        fid, width = FIELDS[field]
+        count = self.nb if field in ("bx", "psi") else self.n
+        out = np.zeros((count, 3) if width == 3 else count)
+        if count:
+            self._check(lib().sph_ctx_download(self._h, fid, _d(out)), f"sph_ctx_download({field})")
+        return out
+
+    def stats(self) -> dict:
+        s = Stats()
+        self._check(lib().sph_ctx_get_stats(self._h, ctypes.byref(s)), "sph_ctx_get_stats")
+        return {name: getattr(s, name) for name, _ in Stats._fields_}
+
+    def neighbors(self):
+        L = lib()
+        tot = (ctypes.c_longlong * 2)()
+        self._check(L.sph_ctx_neighbors(self._h, None, None, None, None, None, None, tot), "sph_ctx_neighbors")
+        n = self.n
+        cells = np.zeros(3 * n, np.int32)
+        rank = np.zeros(n, np.int32)
+        off = np.zeros(n + 1, np.int32)
+        nbr = np.zeros(max(tot[0], 1), np.int32)
+        boff = np.zeros(n + 1, np.int32)
+        bnbr = np.zeros(max(tot[1], 1), np.int32)
+        self._check(L.sph_ctx_neighbors(self._h, _i(cells), _i(rank), _i(off), _i(nbr), _i(boff), _i(bnbr), tot),
+                    "sph_ctx_neighbors")
+        return dict(cell=cells.reshape(n, 3), cell_rank=rank, nbr_off=off, nbr=nbr[: tot[0]], bnbr_off=boff,
+                    bnbr=bnbr[: tot[1]])
+
+
+def sample_box(support_radius, mn, mx):
+    L = lib()
+    m = L.sph_sample_box(support_radius, _d(_v3(mn)), _d(_v3(mx)), None)
+    out = np.zeros((m, 3))
+    L.sph_sample_box(support_radius, _d(_v3(mn)), _d(_v3(mx)), _d(out))
+    return out
+
+
+def sample_sphere(particle_radius, c, radius):
+    L = lib()
+    m = L.sph_sample_sphere(particle_radius, _d(_v3(c)), radius, None)
+    out = np.zeros((m, 3))
+    L.sph_sample_sphere(particle_radius, _d(_v3(c)), radius, _d(out))
+    return out
+
+
+def fluid_block(particle_radius, mn, mx):
+    L = lib()
+    m = L.sph_fluid_block(particle_radius, _d(_v3(mn)), _d(_v3(mx)), None)
+    out = np.zeros((m, 3))
+    L.sph_fluid_block(particle_radius, _d(_v3(mn)), _d(_v3(mx)), _d(out))
+    return out

@@ -1,0 +1,330 @@
+// C ABI of sph_gb300 (include/sph_gb300.h).  No C++ exception crosses this
+// boundary; every entry point returns an SPH_* status.
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "../../include/sph_gb300.h"
+#include "sph_scene_base.h"
+
+struct sph_ctx {
+    sph::SceneBase* scene = nullptr;
+    std::string err;
+};
+
+namespace sph {
+
+// AkinciBoundaryModel::sampleCube AkinciBoundayModel.cpp:100-134: the
+// surface nodes of an (nx+1) x (ny+1) x (nz+1) lattice, spacing ~h/2.
+long long sample_box(double supportRadius, const double mn[3], const double mx[3], double* out)
+{
+    const double lx = std::fabs(mn[0] - mx[0]), ly = std::fabs(mn[1] - mx[1]), lz = std::fabs(mn[2] - mx[2]);
+    const unsigned nx = (unsigned)std::ceil(lx / (0.5 * supportRadius));
+    const unsigned ny = (unsigned)std::ceil(ly / (0.5 * supportRadius));
+    const unsigned nz = (unsigned)std::ceil(lz / (0.5 * supportRadius));
+    const double dx = lx / nx, dy = ly / ny, dz = lz / nz;
+    long long count = 0;
+    for (unsigned i = 0; i <= nx; i++)
+        for (unsigned j = 0; j <= ny; j++)
+            for (unsigned k = 0; k <= nz; k++) {
+                const bool surface = (i == 0 || i == nx) || (j == 0 || j == ny) || (k == 0 || k == nz);
+                if (!surface) continue;
+                if (out) {
+                    out[3 * count] = i * dx + mn[0];
+                    out[3 * count + 1] = j * dy + mn[1];
+                    out[3 * count + 2] = k * dz + mn[2];
+                }
+                ++count;
+            }
+    return count;
+}
+
+// AkinciBoundaryModel::sampleSphere AkinciBoundayModel.cpp:136-164:
+// equal-area latitude rings, 1.5x the surface / particle-disc count.
+long long sample_sphere(double particleRadius, const double c[3], double radius, double* out)
+{
+    const double separation = 1.5;
+    const unsigned num = (unsigned)std::floor(4.0 * M_PI * radius * radius / (M_PI * particleRadius * particleRadius) * separation);
+    const double a = 4.0 * M_PI / num;
+    const double dd = std::sqrt(a);
+    const int m_theta = (int)std::round(M_PI / dd);
+    const double d_theta = M_PI / m_theta;
+    const double d_phi = a / d_theta;
+    long long count = 0;
+    for (int m = 0; m < m_theta; ++m) {
+        const double theta = M_PI * (m + 0.5) / m_theta;
+        const int m_phi = (int)std::round(2.0 * M_PI * std::sin(theta) / d_phi);
+        for (int n = 0; n < m_phi; ++n) {
+            const double phi = 2.0 * M_PI * n / m_phi;
+            const double x = std::sin(theta) * std::cos(phi);
+            const double y = std::sin(theta) * std::sin(phi);
+            const double z = std::cos(theta);
+            if (out) {
+                out[3 * count] = radius * x + c[0];
+                out[3 * count + 1] = radius * y + c[1];
+                out[3 * count + 2] = radius * z + c[2];
+            }
+            ++count;
+        }
+    }
+    return count;
+}
+
+// Simulation::buildFluidBlock Simulation.cpp:512-539: lattice at spacing 2r
+// starting at min + r.
+long long fluid_block(double r, const double mn[3], const double mx[3], double* out)
+{
+    const double dist = 2.0 * r;
+    const int px = (int)std::floor((mx[0] - mn[0]) / dist + 1e-5);
+    const int py = (int)std::floor((mx[1] - mn[1]) / dist + 1e-5);
+    const int pz = (int)std::floor((mx[2] - mn[2]) / dist + 1e-5);
+    long long count = 0;
+    for (int i = 0; i < px; ++i)
+        for (int j = 0; j < py; ++j)
+            for (int k = 0; k < pz; ++k) {
+                if (out) {
+                    out[3 * count] = i * dist + (mn[0] + r);
+                    out[3 * count + 1] = j * dist + (mn[1] + r);
+                    out[3 * count + 2] = k * dist + (mn[2] + r);
+                }
+                ++count;
+            }
+    return count;
+}
+
+}  // namespace sph
+
+static int bad(sph_ctx* ctx, const char* m)
+{
+    if (ctx) ctx->err = m;
+    return SPH_ERR_INVALID;
+}
+
+static int relay(sph_ctx* ctx, int rc)
+{
+    if (rc != SPH_OK && ctx && ctx->scene) ctx->err = ctx->scene->err;
+    return rc;
+}
+
+extern "C" {
+
+int sph_scene_desc_init(sph_scene_desc* d)
+{
+    if (!d) return SPH_ERR_INVALID;
+    std::memset(d, 0, sizeof *d);
+    d->simulation_method = SPH_DFSPH;
+    d->boundary_method = SPH_BOUNDARY_AKINCI;
+    d->precision = SPH_PRECISION_F32;
+    d->particle_radius = 0.025;
+    d->gravity[1] = -9.81;
+    d->time_step = 0.0001;       // TimeManager.h:44
+    d->min_time_step = 0.00001;
+    d->max_time_step = 0.005;
+    d->fps = 60.0;
+    d->density0 = 1000.0;        // FluidModel.cpp:98
+    d->stiffness = 1000.0;
+    d->gamma = 7.0;
+    d->max_error = 0.01;         // SPHSolver.cpp:18
+    d->max_error_v = 0.001;
+    d->cfl_factor = 1.0;         // DFSPHSolver.cpp:21
+    d->min_iterations = -1;
+    d->max_iterations = -1;
+    d->min_iterations_v = -1;
+    d->max_iterations_v = -1;
+    d->viscosity_method = -1;
+    d->surface_tension_method = -1;
+    d->adhesion_method = -1;
+    d->cube_max[0] = d->cube_max[1] = d->cube_max[2] = 1.0;
+    d->threads_per_particle = 0;
+    return SPH_OK;
+}
+
+int sph_ctx_create(const sph_scene_desc* desc, sph_ctx** out)
+{
+    if (!desc || !out) return SPH_ERR_INVALID;
+    *out = nullptr;
+    if (desc->simulation_method < 0 || desc->simulation_method > 2) return SPH_ERR_INVALID;
+    if (desc->boundary_method < 0 || desc->boundary_method > 2) return SPH_ERR_INVALID;
+    if (!(desc->particle_radius > 0.0) || !(desc->density0 > 0.0) || !(desc->time_step > 0.0) || !(desc->fps > 0.0))
+        return SPH_ERR_INVALID;
+    sph_ctx* c = new (std::nothrow) sph_ctx();
+    if (!c) return SPH_ERR_INVALID;
+    try {
+        c->scene = desc->precision == SPH_PRECISION_F64 ? sph::make_scene_f64(*desc) : sph::make_scene_f32(*desc);
+    } catch (...) {
+        delete c;
+        return SPH_ERR_INVALID;
+    }
+    *out = c;
+    return SPH_OK;
+}
+
+int sph_ctx_destroy(sph_ctx* ctx)
+{
+    if (!ctx) return SPH_ERR_INVALID;
+    delete ctx->scene;
+    delete ctx;
+    return SPH_OK;
+}
+
+int sph_ctx_set_fluid(sph_ctx* ctx, const double* x, const double* v, unsigned n)
+{
+    if (!ctx || (!x && n)) return bad(ctx, "invalid argument");
+    if (ctx->scene->inited) return bad(ctx, "fluid must be set before sph_ctx_init");
+    try {
+        ctx->scene->hx.assign(x, x + 3 * (size_t)n);
+        if (v) ctx->scene->hv.assign(v, v + 3 * (size_t)n);
+        else ctx->scene->hv.assign(3 * (size_t)n, 0.0);
+    } catch (...) {
+        return bad(ctx, "out of host memory");
+    }
+    return SPH_OK;
+}
+
+int sph_ctx_add_fluid_block(sph_ctx* ctx, const double mn[3], const double mx[3])
+{
+    if (!ctx || !mn || !mx) return bad(ctx, "invalid argument");
+    if (ctx->scene->inited) return bad(ctx, "fluid must be added before sph_ctx_init");
+    const double r = ctx->scene->d.particle_radius;
+    const long long m = sph::fluid_block(r, mn, mx, nullptr);
+    try {
+        auto& hx = ctx->scene->hx;
+        auto& hv = ctx->scene->hv;
+        if (hv.size() != hx.size()) hv.assign(hx.size(), 0.0);
+        const size_t at = hx.size();
+        hx.resize(at + 3 * (size_t)m);
+        hv.resize(at + 3 * (size_t)m, 0.0);
+        sph::fluid_block(r, mn, mx, hx.data() + at);
+    } catch (...) {
+        return bad(ctx, "out of host memory");
+    }
+    return SPH_OK;
+}
+
+static int add_boundary(sph_ctx* ctx, const double* pts, long long m)
+{
+    try {
+        auto& hb = ctx->scene->hb;
+        hb.insert(hb.end(), pts, pts + 3 * m);
+    } catch (...) {
+        return bad(ctx, "out of host memory");
+    }
+    return SPH_OK;
+}
+
+int sph_ctx_add_boundary_box(sph_ctx* ctx, const double mn[3], const double mx[3])
+{
+    if (!ctx || !mn || !mx) return bad(ctx, "invalid argument");
+    if (ctx->scene->inited) return bad(ctx, "boundary must be added before sph_ctx_init");
+    const double h = 4.0 * ctx->scene->d.particle_radius;
+    const long long m = sph::sample_box(h, mn, mx, nullptr);
+    std::string tmp;
+    double* buf = new (std::nothrow) double[3 * m + 1];
+    if (!buf) return bad(ctx, "out of host memory");
+    sph::sample_box(h, mn, mx, buf);
+    const int rc = add_boundary(ctx, buf, m);
+    delete[] buf;
+    return rc;
+}
+
+int sph_ctx_add_boundary_sphere(sph_ctx* ctx, const double c[3], double radius)
+{
+    if (!ctx || !c || !(radius > 0.0)) return bad(ctx, "invalid argument");
+    if (ctx->scene->inited) return bad(ctx, "boundary must be added before sph_ctx_init");
+    const double r = ctx->scene->d.particle_radius;
+    const long long m = sph::sample_sphere(r, c, radius, nullptr);
+    double* buf = new (std::nothrow) double[3 * m + 1];
+    if (!buf) return bad(ctx, "out of host memory");
+    sph::sample_sphere(r, c, radius, buf);
+    const int rc = add_boundary(ctx, buf, m);
+    delete[] buf;
+    return rc;
+}
+
+int sph_ctx_add_boundary_points(sph_ctx* ctx, const double* x, unsigned n)
+{
+    if (!ctx || (!x && n)) return bad(ctx, "invalid argument");
+    if (ctx->scene->inited) return bad(ctx, "boundary must be added before sph_ctx_init");
+    return add_boundary(ctx, x, n);
+}
+
+int sph_ctx_init(sph_ctx* ctx)
+{
+    if (!ctx) return SPH_ERR_INVALID;
+    return relay(ctx, ctx->scene->init());
+}
+
+int sph_ctx_step(sph_ctx* ctx, int nsteps)
+{
+    if (!ctx || nsteps < 0) return bad(ctx, "invalid argument");
+    return relay(ctx, ctx->scene->step(nsteps));
+}
+
+int sph_ctx_synchronize(sph_ctx* ctx)
+{
+    if (!ctx) return SPH_ERR_INVALID;
+    if (!ctx->scene->inited) return SPH_OK;
+    return relay(ctx, ctx->scene->sync());
+}
+
+int sph_ctx_set_graph(sph_ctx* ctx, int enable)
+{
+    if (!ctx) return SPH_ERR_INVALID;
+    return relay(ctx, ctx->scene->set_graph(enable));
+}
+
+int sph_ctx_num_particles(const sph_ctx* ctx, unsigned* nf, unsigned* nb)
+{
+    if (!ctx) return SPH_ERR_INVALID;
+    if (nf) *nf = ctx->scene->nfluid();
+    if (nb) *nb = ctx->scene->nboundary();
+    return SPH_OK;
+}
+
+int sph_ctx_download(sph_ctx* ctx, int field, double* out)
+{
+    if (!ctx || !out) return bad(ctx, "invalid argument");
+    return relay(ctx, ctx->scene->download(field, out));
+}
+
+int sph_ctx_get_stats(sph_ctx* ctx, sph_stats* out)
+{
+    if (!ctx || !out) return bad(ctx, "invalid argument");
+    return relay(ctx, ctx->scene->stats(out));
+}
+
+const char* sph_ctx_last_error(const sph_ctx* ctx)
+{
+    if (!ctx) return "null context";
+    return ctx->err.c_str();
+}
+
+int sph_ctx_neighbors(sph_ctx* ctx, int* cells, int* cell_rank, int* nbr_off, int* nbr, int* bnbr_off, int* bnbr,
+                      long long* totals)
+{
+    if (!ctx) return SPH_ERR_INVALID;
+    return relay(ctx, ctx->scene->neighbors(cells, cell_rank, nbr_off, nbr, bnbr_off, bnbr, totals));
+}
+
+long long sph_sample_box(double support_radius, const double mn[3], const double mx[3], double* out)
+{
+    if (!mn || !mx || !(support_radius > 0.0)) return -1;
+    return sph::sample_box(support_radius, mn, mx, out);
+}
+
+long long sph_sample_sphere(double particle_radius, const double c[3], double radius, double* out)
+{
+    if (!c || !(particle_radius > 0.0) || !(radius > 0.0)) return -1;
+    return sph::sample_sphere(particle_radius, c, radius, out);
+}
+
+long long sph_fluid_block(double particle_radius, const double mn[3], const double mx[3], double* out)
+{
+    if (!mn || !mx || !(particle_radius > 0.0)) return -1;
+    return sph::fluid_block(particle_radius, mn, mx, out);
+}
+
+const char* sph_version(void) { return "sph_gb300 0.1 (sm_103a)"; }
+
+}  // extern "C"

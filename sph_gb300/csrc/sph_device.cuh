@@ -1,0 +1,314 @@
+// Device-side building blocks of the GB300 SPH particle loop: smoothing
+// kernels, the cell-grid neighbour walk and deterministic block reductions.
+//
+// Two numeric forms share this code (template parameter R):
+//   R = double  parity form: absolute positions, the reference's expression
+//               order and IEEE division, for checks against the CPU solver;
+//   R = float   production form: positions stored relative to the corner of
+//               the particle's grid cell (cell index kept as an integer), so
+//               pair distances keep ~ulp(h) precision anywhere in the domain.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace sph {
+
+// ---------------------------------------------------------------------------
+// Vector types
+// ---------------------------------------------------------------------------
+template <typename R> struct alignas(4 * sizeof(R)) P4 { R x, y, z, w; };
+template <typename R> struct V3 { R x, y, z; };
+
+template <typename R> __host__ __device__ __forceinline__ V3<R> v3(R x, R y, R z) { return V3<R>{x, y, z}; }
+template <typename R> __device__ __forceinline__ V3<R> operator+(V3<R> a, V3<R> b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+template <typename R> __device__ __forceinline__ V3<R> operator-(V3<R> a, V3<R> b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+template <typename R> __device__ __forceinline__ V3<R> operator*(R s, V3<R> a) { return {s * a.x, s * a.y, s * a.z}; }
+template <typename R> __device__ __forceinline__ V3<R> operator*(V3<R> a, R s) { return {a.x * s, a.y * s, a.z * s}; }
+template <typename R> __device__ __forceinline__ V3<R> operator/(V3<R> a, R s) { return {a.x / s, a.y / s, a.z / s}; }
+template <typename R> __device__ __forceinline__ V3<R> operator-(V3<R> a) { return {-a.x, -a.y, -a.z}; }
+// (x*x' + y*y') + z*z', the order GLM's dot uses
+template <typename R> __device__ __forceinline__ R dot3(V3<R> a, V3<R> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+template <typename R> __device__ __forceinline__ V3<R> xyz(const P4<R>& p) { return {p.x, p.y, p.z}; }
+
+__device__ __forceinline__ P4<float> ldg4(const P4<float>* p)
+{
+    float4 t = __ldg(reinterpret_cast<const float4*>(p));
+    return P4<float>{t.x, t.y, t.z, t.w};
+}
+__device__ __forceinline__ P4<double> ldg4(const P4<double>* p)
+{
+    const double2* q = reinterpret_cast<const double2*>(p);
+    double2 a = __ldg(q), b = __ldg(q + 1);
+    return P4<double>{a.x, a.y, b.x, b.y};
+}
+template <typename R> __device__ __forceinline__ R ldg1(const R* p) { return __ldg(p); }
+
+// Division by the support radius: IEEE division in the parity form (the
+// reference divides), multiplication by 1/h in the production form.
+__device__ __forceinline__ double div_h(double r, double h, double) { return r / h; }
+__device__ __forceinline__ float div_h(float r, float, float inv_h) { return r * inv_h; }
+
+// ---------------------------------------------------------------------------
+// Per-scene constants (kernel coefficients as each reference kernel's
+// setSupportRadius computes them, evaluated in double on the host).
+// ---------------------------------------------------------------------------
+template <typename R> struct Consts {
+    R h, inv_h, h2, cull2;
+    R cs_k, cs_l;                  // CubicSpline.h:18-26
+    R p6_h2, p6_value, p6_grad;    // Poly6.h:19-28
+    R sp_value, sp_grad;           // Spiky.h:18-27
+    R vk_lapl;                     // ViscoK.h:18-26
+    R co_c1, co_c2;                // Cohesion.h:20-27
+    R mass, density0, eps;
+    R gx, gy, gz;
+    R stiffness, gamma, k_eos;     // k_eos = stiffness * density0 / gamma
+    R visc, bvisc, st, adh;
+    R cube_min[3], cube_max[3];
+    int force_flags;
+    int has_cube;
+};
+
+enum ForceFlags : int {
+    F_XSPH = 1, F_STD_VISC = 2, F_ART_VISC = 4, F_SURFACE_TENSION = 8, F_ADHESION = 16, F_BVISC = 32,
+};
+
+// Scalars that change during a run and live on the device so that whole
+// steps run without host round trips (the CFL step writes dt, reductions
+// write the errors and the loop flags).
+struct DevScalars {
+    double dt, time;
+    double avgDensError, avgDivError, maxDensityError;
+    double maxVel;
+    double scaling;                // PCISPH delta
+    unsigned iterations, iterationsV, next_active;
+    unsigned active;               // loop flag of the solve in progress
+    unsigned steps;
+    unsigned long long sumIterations, sumIterationsV;
+    unsigned status;               // SPH_STATUS_* bits
+    unsigned block_counter;        // last-block-done counter of reductions
+    unsigned pad;
+};
+
+enum StatusBits : unsigned {
+    ST_OUT_OF_GRID = 1u, ST_NONFINITE = 2u, ST_ITER_CAP = 4u, ST_ITER_CAP_V = 8u,
+};
+
+// Solver limits used by the device-side loop controls.
+struct LoopLimits {
+    double maxError, maxErrorV;
+    unsigned minIt, maxIt, minItV, maxItV;
+    double cflFactor, particleRadius, minTs, maxTs;
+};
+
+// ---------------------------------------------------------------------------
+// Grid: dense cell box around the domain.  A cell (cx, cy, cz) sits in
+// column col = morton(cx, cy); cells of a column are consecutive in z, so the
+// three cells z-1..z+1 of a neighbour column are one contiguous particle
+// range, visited in the reference's x -> y -> z offset order
+// (HashTable.h:147-167).  key = col * nz + cz.
+// ---------------------------------------------------------------------------
+struct GridView {
+    int nx, ny, nz;
+    int ox, oy, oz;                 // absolute cell index of grid cell (0,0,0)
+    const uint32_t* mortx;          // spread bits of cx
+    const uint32_t* morty;          // spread bits of cy
+};
+
+__device__ __forceinline__ uint32_t pack_cell(int cx, int cy, int cz) { return (uint32_t)cx | ((uint32_t)cy << 11) | ((uint32_t)cz << 22); }
+__device__ __forceinline__ int cell_x(uint32_t c) { return (int)(c & 2047u); }
+__device__ __forceinline__ int cell_y(uint32_t c) { return (int)((c >> 11) & 2047u); }
+__device__ __forceinline__ int cell_z(uint32_t c) { return (int)(c >> 22); }
+__device__ __forceinline__ uint32_t cell_key(const GridView& g, int cx, int cy, int cz)
+{
+    return (__ldg(g.mortx + cx) | __ldg(g.morty + cy)) * (uint32_t)g.nz + (uint32_t)cz;
+}
+
+// Visit every candidate j of the 27 cells around the particle's cell, calling
+// f(j, s) with s the particle's position expressed in the frame of j's cell
+// (so that r_ij = s - pos_j).  Threads of a group of G lanes split each range.
+template <typename R, int G, typename F>
+__device__ __forceinline__ void walk(const GridView& g, const uint32_t* __restrict__ starts, uint32_t pc, V3<R> xi, R h,
+                                     int lane, F&& f)
+{
+    constexpr bool REL = sizeof(R) == 4;
+    const int cx = cell_x(pc), cy = cell_y(pc), cz = cell_z(pc);
+    const int z0 = cz > 0 ? cz - 1 : 0;
+    const int z1 = cz + 1 < g.nz ? cz + 1 : g.nz - 1;
+#pragma unroll
+    for (int dx = -1; dx <= 1; ++dx) {
+        const int x = cx + dx;
+        if (x < 0 || x >= g.nx) continue;
+        const uint32_t mx = __ldg(g.mortx + x);
+#pragma unroll
+        for (int dy = -1; dy <= 1; ++dy) {
+            const int y = cy + dy;
+            if (y < 0 || y >= g.ny) continue;
+            const uint32_t base = (mx | __ldg(g.morty + y)) * (uint32_t)g.nz;
+            if constexpr (REL) {
+                const R sx = xi.x - (R)dx * h, sy = xi.y - (R)dy * h;
+                uint32_t b = __ldg(starts + base + z0);
+                for (int z = z0; z <= z1; ++z) {
+                    const uint32_t e = __ldg(starts + base + z + 1);
+                    const V3<R> s = {sx, sy, xi.z - (R)(z - cz) * h};
+                    for (uint32_t j = b + lane; j < e; j += G) f(j, s);
+                    b = e;
+                }
+            } else {
+                const uint32_t b = __ldg(starts + base + z0), e = __ldg(starts + base + z1 + 1);
+                for (uint32_t j = b + lane; j < e; j += G) f(j, xi);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Smoothing kernels
+// ---------------------------------------------------------------------------
+
+// CubicSpline::W CubicSpline.h:28-46, from the distance r.
+template <typename R> __device__ __forceinline__ R cubic_W(const Consts<R>& c, R r)
+{
+    R res = 0;
+    const R q = div_h(r, c.h, c.inv_h);
+    if (q <= (R)1) {
+        if (q <= (R)0.5) {
+            const R q2 = q * q;
+            const R q3 = q2 * q;
+            res = c.cs_k * ((R)6 * q3 - (R)6 * q2 + (R)1);
+        } else {
+            const R f = (R)1 - q;
+            res = c.cs_k * ((R)2 * (f * f * f));
+        }
+    }
+    return res;
+}
+
+// CubicSpline::gradW CubicSpline.h:53-73, given r and |r|^2.
+template <typename R> __device__ __forceinline__ V3<R> cubic_gradW(const Consts<R>& c, V3<R> r, R r2)
+{
+    V3<R> res = {0, 0, 0};
+    const R rl = sqrt(r2);
+    const R q = div_h(rl, c.h, c.inv_h);
+    if ((rl > (R)1.0e-5) && (q <= (R)1)) {
+        const V3<R> gradq = r * ((R)1 / (rl * c.h));
+        if (q <= (R)0.5) {
+            res = (c.cs_l * q * ((R)3 * q - (R)2)) * gradq;
+        } else {
+            const R factor = (R)1 - q;
+            res = (c.cs_l * (-factor * factor)) * gradq;
+        }
+    }
+    return res;
+}
+
+// Spiky::gradW Spiky.h:43-55
+template <typename R> __device__ __forceinline__ V3<R> spiky_gradW(const Consts<R>& c, V3<R> r, R r2)
+{
+    const R mod_r = sqrt(r2);
+    if (mod_r != (R)0 && mod_r <= c.h) {
+        const R diff = c.h - mod_r;
+        return (-c.sp_grad * diff * diff / mod_r) * r;
+    }
+    return V3<R>{0, 0, 0};
+}
+
+// ViscoK::laplW ViscoK.h:27-35
+template <typename R> __device__ __forceinline__ R visc_laplW(const Consts<R>& c, R r2)
+{
+    const R mod_r = sqrt(r2);
+    if (mod_r <= c.h) return c.vk_lapl * (c.h - mod_r);
+    return 0;
+}
+
+// Cohesion::W Cohesion.h:29-40
+template <typename R> __device__ __forceinline__ R cohesion_W(const Consts<R>& c, R mod_r)
+{
+    R value = 0;
+    const R sr = c.h;
+    if (((R)2 * mod_r > sr) && (mod_r <= sr)) {
+        const R a = sr - mod_r;
+        value = c.co_c1 * (a * a * a) * (mod_r * mod_r * mod_r);
+    } else if ((mod_r > (R)0) && ((R)2 * mod_r <= sr)) {
+        const R a = sr - mod_r;
+        value = c.co_c1 * (R)2 * (a * a * a) * (mod_r * mod_r * mod_r) - c.co_c2;
+    }
+    return value;
+}
+
+// Adhesion::W Adhesion.h:23-35 (the reference never applies its valueCoef)
+template <typename R> __device__ __forceinline__ R adhesion_W(const Consts<R>& c, R mod_r)
+{
+    const R sr = c.h;
+    if (((R)2 * mod_r > sr) && (mod_r <= sr)) {
+        const R value = (R)-4 * mod_r * mod_r / sr + (R)6 * mod_r - (R)2 * sr;
+        return sqrt(sqrt(value));   // value^(1/4)
+    }
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Block reductions in FP64 with a deterministic last-block finish.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_max(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Sum (or max) of v over the block; the result is valid in thread 0.
+template <bool MAX> __device__ __forceinline__ double block_reduce(double v, double* sh)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    v = MAX ? warp_max(v) : warp_sum(v);
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        double t = lane < nw ? sh[lane] : (MAX ? -1.0e300 : 0.0);
+        t = MAX ? warp_max(t) : warp_sum(t);
+        if (lane == 0) sh[0] = t;
+    }
+    __syncthreads();
+    const double r = sh[0];
+    __syncthreads();
+    return r;
+}
+
+// Writes this block's partial and returns true in exactly one block (the
+// last to finish), in which every thread sees the total in *total_out.  The
+// total is summed in block-index order, so the result does not depend on
+// which block finished last.
+template <bool MAX>
+__device__ __forceinline__ bool finish_reduction(double v, double* partials, unsigned* counter, double* sh,
+                                                 double* total_out)
+{
+    const double b = block_reduce<MAX>(v, sh);
+    __shared__ bool is_last;
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = b;
+        __threadfence();
+        const unsigned done = atomicAdd(counter, 1u);
+        is_last = (done == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!is_last) return false;
+    __threadfence();
+    double t = MAX ? -1.0e300 : 0.0;
+    for (unsigned i = threadIdx.x; i < gridDim.x; i += blockDim.x) {
+        const double p = *((volatile double*)(partials + i));
+        t = MAX ? fmax(t, p) : t + p;
+    }
+    const double tot = block_reduce<MAX>(t, sh);
+    if (threadIdx.x == 0) *counter = 0u;
+    *total_out = tot;
+    return true;
+}
+
+}  // namespace sph

@@ -1,0 +1,807 @@
+// Host side of one scene: device buffers, the grid build, and the per-step
+// orchestration of WCSPHSolver::step (WCSPHSolver.cpp:14-78),
+// PCISPHSolver::step (PCISPHSolver.cpp:21-81) and DFSPHSolver::step
+// (DFSPHSolver.cpp:38-112) as sequences of kernels on one CUDA stream.
+//
+// Solver loops whose trip count depends on a convergence test run either
+// host-driven (kernels of finished loops exit at once; the host reads the
+// loop flag every few iterations) or, in graph mode, as CUDA-graph
+// conditional WHILE nodes whose condition the reduction kernels set on the
+// device, so a whole step is one graph launch with no host round trip.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "sph_scene_base.h"
+#include "sph_kernels.cuh"
+
+namespace sph {
+
+template <typename T> struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    ~DevBuf() { if (p) cudaFree(p); }
+    cudaError_t alloc(size_t count)
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = count;
+        return cudaMalloc((void**)&p, std::max<size_t>(count, 1) * sizeof(T));
+    }
+};
+
+template <typename R> class Scene : public SceneBase {
+public:
+    explicit Scene(const sph_scene_desc& desc) { d = desc; }
+    ~Scene() override
+    {
+        for (int k = 0; k < 2; ++k)
+            if (gexec_[k]) cudaGraphExecDestroy(gexec_[k]);
+        if (st_) cudaStreamDestroy(st_);
+        if (st2_) cudaStreamDestroy(st2_);
+        if (h_sc_) cudaFreeHost(h_sc_);
+    }
+
+    unsigned nfluid() const override { return inited ? n_ : (unsigned)(hx.size() / 3); }
+    unsigned nboundary() const override { return inited ? nb_ : (unsigned)(hb.size() / 3); }
+
+    // ------------------------------------------------------------------
+    int init() override
+    {
+        if (inited) { fail("scene already initialised"); return SPH_ERR_INVALID; }
+        const int G = d.threads_per_particle;
+        if (sizeof(R) == 8) G_ = 1;
+        else G_ = (G == 2 || G == 4 || G == 8) ? G : 1;
+        SPH_CUDA(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
+        SPH_CUDA(cudaStreamCreateWithFlags(&st2_, cudaStreamNonBlocking));
+        ls_ = st_;
+        SPH_CUDA(cudaMallocHost((void**)&h_sc_, sizeof(DevScalars)));
+        n_ = (unsigned)(hx.size() / 3);
+        akinci_ = d.boundary_method == SPH_BOUNDARY_AKINCI ? 1 : 0;
+        nb_ = akinci_ ? (unsigned)(hb.size() / 3) : 0u;
+        if (n_ == 0) { fail("no fluid particles"); return SPH_ERR_INVALID; }
+        if (d.boundary_method == SPH_BOUNDARY_PCISPH) { fail("PCISPH boundary particles are not implemented"); return SPH_ERR_UNSUPPORTED; }
+        setup_constants();
+        int rc = setup_grid();
+        if (rc) return rc;
+        rc = allocate();
+        if (rc) return rc;
+        // scalars
+        DevScalars s{};
+        s.dt = d.time_step;
+        s.scaling = pcisph_scaling();
+        SPH_CUDA(cudaMemcpyAsync(sc_.p, &s, sizeof s, cudaMemcpyHostToDevice, st_));
+        // fluid upload
+        {
+            DevBuf<double> tx, tv;
+            SPH_CUDA(tx.alloc(hx.size()));
+            SPH_CUDA(tv.alloc(hx.size()));
+            if (hv.size() != hx.size()) hv.assign(hx.size(), 0.0);
+            SPH_CUDA(cudaMemcpyAsync(tx.p, hx.data(), hx.size() * 8, cudaMemcpyHostToDevice, st_));
+            SPH_CUDA(cudaMemcpyAsync(tv.p, hv.data(), hv.size() * 8, cudaMemcpyHostToDevice, st_));
+            k_upload_fluid<R><<<blocks(n_, 256), 256, 0, st_>>>(tx.p, tv.p, n_, 0, F(), gv_, hd_, sc_.p);
+            SPH_CUDA(cudaGetLastError());
+            SPH_CUDA(cudaStreamSynchronize(st_));
+        }
+        // boundary upload, sort, volumes (SPHSolver::init SPHSolver.cpp:22-39)
+        if (nb_) {
+            DevBuf<double> tb;
+            SPH_CUDA(tb.alloc(hb.size()));
+            SPH_CUDA(cudaMemcpyAsync(tb.p, hb.data(), hb.size() * 8, cudaMemcpyHostToDevice, st_));
+            k_upload_boundary<R><<<blocks(nb_, 256), 256, 0, st_>>>(tb.p, nb_, B(0), gv_, hd_, sc_.p);
+            SPH_CUDA(cudaGetLastError());
+            k_cell_count<<<blocks(nb_, 256), 256, 0, st_>>>(nb_, B(0).cell, key_.p, slot_.p, count_.p, gv_);
+            rc = scan(bstarts_.p);
+            if (rc) return rc;
+            k_scatter<<<blocks(nb_, 256), 256, 0, st_>>>(nb_, key_.p, slot_.p, bstarts_.p, tmp_.p);
+            k_gather_boundary<R><<<blocks(nb_, 256), 256, 0, st_>>>(nb_, tmp_.p, key_.p, bstarts_.p, B(0), B(1));
+            SPH_CUDA(cudaGetLastError());
+            k_boundary_psi<R><<<blocks(nb_, 128), 128, 0, st_>>>(B(1), gv_, bstarts_.p, c_);
+            SPH_CUDA(cudaGetLastError());
+            SPH_CUDA(cudaStreamSynchronize(st_));
+        } else {
+            SPH_CUDA(cudaMemsetAsync(bstarts_.p, 0, (nkeys_ + 1) * sizeof(uint32_t), st_));
+        }
+        rc = build_grid(false);
+        if (rc) return rc;
+        if (d.simulation_method == SPH_DFSPH) {
+            // DFSPHSolver::init DFSPHSolver.cpp:24-36
+            rc = launch_density(true, false);
+            if (rc) return rc;
+        }
+        SPH_CUDA(cudaStreamSynchronize(st_));
+        inited = true;
+        return SPH_OK;
+    }
+
+    int step(int nsteps) override
+    {
+        if (!inited) { fail("sph_ctx_init has not been called"); return SPH_ERR_INVALID; }
+        for (int s = 0; s < nsteps; ++s) {
+            int rc;
+            if (graph_) {
+                rc = graph_step();
+            } else {
+                rc = one_step();
+            }
+            if (rc) return rc;
+        }
+        return SPH_OK;
+    }
+
+    int sync() override
+    {
+        SPH_CUDA(cudaStreamSynchronize(st_));
+        return SPH_OK;
+    }
+
+    int set_graph(int on) override
+    {
+        graph_ = on != 0;
+        return SPH_OK;
+    }
+
+    int download(int field, double* out) override
+    {
+        if (!inited) { fail("not initialised"); return SPH_ERR_INVALID; }
+        const bool bnd = field == SPH_FIELD_BOUNDARY_POSITION || field == SPH_FIELD_BOUNDARY_VOLUME;
+        const unsigned n = bnd ? nb_ : n_;
+        const bool vec = field == SPH_FIELD_POSITION || field == SPH_FIELD_VELOCITY || field == SPH_FIELD_ACCELERATION ||
+                         field == SPH_FIELD_PRESSURE_ACC || field == SPH_FIELD_NORMAL ||
+                         field == SPH_FIELD_BOUNDARY_POSITION;
+        const size_t count = (size_t)n * (vec ? 3 : 1);
+        if (count == 0) return SPH_OK;
+        DevBuf<double> o;
+        SPH_CUDA(o.alloc(count));
+        Fluid<R> f = F();
+        Boundary<R> b = B(1);
+        const P4<R>* v4 = nullptr;
+        const R* s = nullptr;
+        int kind = 0;
+        switch (field) {
+            case SPH_FIELD_POSITION: v4 = f.pos; kind = 1; break;
+            case SPH_FIELD_VELOCITY: v4 = f.vel; break;
+            case SPH_FIELD_ACCELERATION: v4 = f.acc; break;
+            case SPH_FIELD_PRESSURE_ACC: v4 = f.pacc; break;
+            case SPH_FIELD_NORMAL: v4 = f.normal; break;
+            case SPH_FIELD_DENSITY: s = f.rho; kind = 2; break;
+            case SPH_FIELD_PRESSURE: s = f.press; kind = 2; break;
+            case SPH_FIELD_ALPHA: s = f.alpha; kind = 2; break;
+            case SPH_FIELD_PRED_DENSITY: s = f.pred; kind = 2; break;
+            case SPH_FIELD_DIV_ERROR: s = f.div; kind = 2; break;
+            case SPH_FIELD_KAPPA: s = f.kappa; kind = 2; break;
+            case SPH_FIELD_KAPPA_V: s = f.kappav; kind = 2; break;
+            case SPH_FIELD_BOUNDARY_POSITION: v4 = b.pos; kind = 1; break;
+            case SPH_FIELD_BOUNDARY_VOLUME: s = b.psi; kind = 2; break;
+            default: fail("unknown field"); return SPH_ERR_INVALID;
+        }
+        k_download<R><<<blocks(n, 256), 256, 0, st_>>>(n, v4, s, bnd ? b.id : f.id, bnd ? b.cell : f.cell, gv_, hd_, kind,
+                                                      o.p);
+        SPH_CUDA(cudaGetLastError());
+        SPH_CUDA(cudaMemcpyAsync(out, o.p, count * 8, cudaMemcpyDeviceToHost, st_));
+        SPH_CUDA(cudaStreamSynchronize(st_));
+        return SPH_OK;
+    }
+
+    int stats(sph_stats* out) override
+    {
+        if (!inited) { fail("not initialised"); return SPH_ERR_INVALID; }
+        SPH_CUDA(cudaMemcpyAsync(h_sc_, sc_.p, sizeof(DevScalars), cudaMemcpyDeviceToHost, st_));
+        SPH_CUDA(cudaStreamSynchronize(st_));
+        const DevScalars& s = *h_sc_;
+        std::memset(out, 0, sizeof *out);
+        out->time = s.time;
+        out->dt = s.dt;
+        out->avg_density_error = s.avgDensError;
+        out->avg_divergence_error = s.avgDivError;
+        out->max_density_error = s.maxDensityError;
+        out->max_velocity = s.maxVel;
+        out->iterations = s.iterations;
+        out->iterations_v = s.iterationsV;
+        out->steps = s.steps;
+        out->status = s.status;
+        out->sum_iterations = s.sumIterations;
+        out->sum_iterations_v = s.sumIterationsV;
+        out->num_fluid = n_;
+        out->num_boundary = nb_;
+        return SPH_OK;
+    }
+
+    int neighbors(int* cells, int* rank, int* off, int* nbr, int* boff, int* bnbr, long long* totals) override
+    {
+        if (!inited) { fail("not initialised"); return SPH_ERR_INVALID; }
+        DevBuf<int> cnt, bcnt, dcells, drank;
+        SPH_CUDA(cnt.alloc(n_));
+        SPH_CUDA(bcnt.alloc(n_));
+        SPH_CUDA(dcells.alloc(3 * (size_t)n_));
+        SPH_CUDA(drank.alloc(n_));
+        Fluid<R> f = F();
+        Boundary<R> b = B(1);
+        k_neighbors<R><<<blocks(n_, 128), 128, 0, st_>>>(f, b.pos, b.id, b.cell, gv_, starts_.p, bstarts_.p, c_, hd_, nullptr,
+                                                         nullptr, cnt.p, bcnt.p, nullptr, nullptr, dcells.p, drank.p);
+        SPH_CUDA(cudaGetLastError());
+        std::vector<int> hc(n_), hbc(n_);
+        SPH_CUDA(cudaMemcpyAsync(hc.data(), cnt.p, n_ * 4, cudaMemcpyDeviceToHost, st_));
+        SPH_CUDA(cudaMemcpyAsync(hbc.data(), bcnt.p, n_ * 4, cudaMemcpyDeviceToHost, st_));
+        if (cells) SPH_CUDA(cudaMemcpyAsync(cells, dcells.p, 3 * (size_t)n_ * 4, cudaMemcpyDeviceToHost, st_));
+        if (rank) SPH_CUDA(cudaMemcpyAsync(rank, drank.p, (size_t)n_ * 4, cudaMemcpyDeviceToHost, st_));
+        SPH_CUDA(cudaStreamSynchronize(st_));
+        std::vector<int> ho(n_ + 1), hbo(n_ + 1);
+        long long a = 0, bt = 0;
+        for (unsigned i = 0; i < n_; ++i) {
+            ho[i] = (int)a; hbo[i] = (int)bt;
+            a += hc[i]; bt += hbc[i];
+        }
+        ho[n_] = (int)a; hbo[n_] = (int)bt;
+        if (totals) { totals[0] = a; totals[1] = bt; }
+        if (off) std::memcpy(off, ho.data(), (n_ + 1) * 4);
+        if (boff) std::memcpy(boff, hbo.data(), (n_ + 1) * 4);
+        if (nbr || bnbr) {
+            DevBuf<int> doff, dboff, dn, dbn;
+            SPH_CUDA(doff.alloc(n_ + 1));
+            SPH_CUDA(dboff.alloc(n_ + 1));
+            SPH_CUDA(dn.alloc((size_t)std::max<long long>(a, 1)));
+            SPH_CUDA(dbn.alloc((size_t)std::max<long long>(bt, 1)));
+            SPH_CUDA(cudaMemcpyAsync(doff.p, ho.data(), (n_ + 1) * 4, cudaMemcpyHostToDevice, st_));
+            SPH_CUDA(cudaMemcpyAsync(dboff.p, hbo.data(), (n_ + 1) * 4, cudaMemcpyHostToDevice, st_));
+            k_neighbors<R><<<blocks(n_, 128), 128, 0, st_>>>(f, b.pos, b.id, b.cell, gv_, starts_.p, bstarts_.p, c_, hd_,
+                                                             doff.p, dboff.p, nullptr, nullptr, dn.p, dbn.p, nullptr,
+                                                             nullptr);
+            SPH_CUDA(cudaGetLastError());
+            if (nbr && a) SPH_CUDA(cudaMemcpyAsync(nbr, dn.p, a * 4, cudaMemcpyDeviceToHost, st_));
+            if (bnbr && bt) SPH_CUDA(cudaMemcpyAsync(bnbr, dbn.p, bt * 4, cudaMemcpyDeviceToHost, st_));
+            SPH_CUDA(cudaStreamSynchronize(st_));
+        }
+        return SPH_OK;
+    }
+
+private:
+    // ------------------------------------------------------------------
+    static unsigned blocks(size_t n, unsigned b) { return (unsigned)std::max<size_t>(1, (n + b - 1) / b); }
+
+    Fluid<R> F() const { return fl_[cur_]; }
+    Boundary<R> B(int k) const { return bd_[k]; }
+
+    // Kernel coefficients, evaluated in double as each reference kernel's
+    // setSupportRadius does (CubicSpline.h:18-26, Poly6.h:19-28,
+    // Spiky.h:18-27, ViscoK.h:18-26, Cohesion.h:20-27), and the particle
+    // mass of Simulation::initMasses (Simulation.cpp:134-146).
+    void setup_constants()
+    {
+        const double r = d.particle_radius;
+        const double sr = 4.0 * r;
+        hd_ = sr;
+        const double pi = M_PI;
+        const double h3 = sr * sr * sr;
+        const double h6 = sr * sr * sr * sr * sr * sr;
+        const double h9 = sr * sr * sr * sr * sr * sr * sr * sr * sr;
+        const double diameter = 2.0 * r;
+        mass_ = d.density0 * std::pow(diameter, 3.0);
+        Consts<R> c{};
+        c.h = (R)sr;
+        c.inv_h = (R)(1.0 / sr);
+        c.h2 = (R)(sr * sr);
+        c.cull2 = (R)(sr * sr * (sizeof(R) == 8 ? (1.0 + 1e-12) : (1.0 + 1e-6)));
+        c.cs_k = (R)(8.0 / (pi * h3));
+        c.cs_l = (R)(48.0 / (pi * h3));
+        c.p6_h2 = (R)(sr * sr);
+        c.p6_value = (R)(315.0 / (64.0 * M_PI * h9));
+        c.p6_grad = (R)(945.0 / (32.0 * M_PI * h9));
+        c.sp_value = (R)(15.0 / (M_PI * h6));
+        c.sp_grad = (R)(45.0 / (M_PI * h6));
+        c.vk_lapl = (R)(45 / (M_PI * h6));
+        c.co_c1 = (R)(32.0 / (M_PI * h9));
+        c.co_c2 = (R)(h6 / 64.0);
+        c.mass = (R)mass_;
+        c.density0 = (R)d.density0;
+        c.eps = (R)1e-5;
+        c.gx = (R)d.gravity[0]; c.gy = (R)d.gravity[1]; c.gz = (R)d.gravity[2];
+        c.stiffness = (R)d.stiffness;
+        c.gamma = (R)d.gamma;
+        c.k_eos = (R)(d.stiffness * d.density0 / d.gamma);
+        c.visc = (R)d.viscosity;
+        c.bvisc = (R)d.boundary_viscosity;
+        c.st = (R)d.surface_tension;
+        c.adh = (R)d.adhesion;
+        for (int k = 0; k < 3; ++k) { c.cube_min[k] = (R)d.cube_min[k]; c.cube_max[k] = (R)d.cube_max[k]; }
+        c.has_cube = (d.boundary_method == SPH_BOUNDARY_CUBE && d.has_cube) ? 1 : 0;
+        int fl = 0;
+        // plugin selection of FluidModel::setViscosityForce / setSurfaceTensionForce /
+        // setAdhesionForce (FluidModel.cpp:73-122) as called by Simulation::importScene
+        // (Simulation.cpp:423-430)
+        if (d.viscosity_method > -1 && d.viscosity != 0.0) {
+            if (d.viscosity_method == SPH_VISCOSITY_STANDARD) fl |= F_STD_VISC;
+            else if (d.viscosity_method == SPH_VISCOSITY_ARTIFICIAL) fl |= F_ART_VISC;
+            else if (d.viscosity_method == SPH_VISCOSITY_XSPH) fl |= F_XSPH;
+            if (d.boundary_viscosity != 0.0) fl |= F_BVISC;
+        }
+        if (d.surface_tension_method == SPH_SURFACE_TENSION_AKINCI && d.surface_tension != 0.0) fl |= F_SURFACE_TENSION;
+        if (d.adhesion_method == SPH_ADHESION_AKINCI && d.adhesion != 0.0) fl |= F_ADHESION;
+        c.force_flags = fl;
+        c_ = c;
+        // solver limits (defaults SPHSolver.cpp:12-19, DFSPHSolver.cpp:10-22)
+        LoopLimits l{};
+        l.maxError = 0.01; l.minIt = 3; l.maxIt = 100; l.maxErrorV = 0.001; l.minItV = 1; l.maxItV = 100;
+        l.cflFactor = 1.0;
+        if (d.simulation_method == SPH_DFSPH) { l.minIt = 2; l.maxIt = 100; }
+        if (d.simulation_method != SPH_WCSPH) l.maxError = d.max_error;
+        if (d.simulation_method == SPH_DFSPH) { l.maxErrorV = d.max_error_v; l.cflFactor = d.cfl_factor; }
+        if (d.min_iterations >= 0) l.minIt = (unsigned)d.min_iterations;
+        if (d.max_iterations >= 0) l.maxIt = (unsigned)d.max_iterations;
+        if (d.min_iterations_v >= 0) l.minItV = (unsigned)d.min_iterations_v;
+        if (d.max_iterations_v >= 0) l.maxItV = (unsigned)d.max_iterations_v;
+        l.particleRadius = d.particle_radius;
+        // TimeManager::setMinTimeStep keeps min(minTs, 1/fps) (TimeManager.h:55)
+        const double minFPSTimeStep = 1.0 / d.fps;
+        l.minTs = minFPSTimeStep < d.min_time_step ? minFPSTimeStep : d.min_time_step;
+        l.maxTs = d.max_time_step;
+        lim_ = l;
+    }
+
+    // PCISPHSolver::computeScalingFactor PCISPHSolver.cpp:389-421 (Poly6
+    // gradient on a 3x3x3 lattice prototype at spacing 2r, init-time dt).
+    double pcisph_scaling() const
+    {
+        const double sr = hd_;
+        const double h9 = sr * sr * sr * sr * sr * sr * sr * sr * sr;
+        const double gradCoef = 945.0 / (32.0 * M_PI * h9);
+        const double h2 = sr * sr;
+        const double dist = 2.0 * d.particle_radius;
+        double sg[3] = {0, 0, 0}, sumSqGrad = 0;
+        for (int i = -1; i <= 1; i++)
+            for (int j = -1; j <= 1; j++)
+                for (int k = -1; k <= 1; k++) {
+                    double r[3] = {(double)-i * dist, (double)-j * dist, (double)-k * dist};
+                    const double mod_r = std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+                    const double mod_r2 = mod_r * mod_r;
+                    double gr[3] = {0, 0, 0};
+                    if (mod_r2 <= h2) {
+                        const double diff = h2 - mod_r2;
+                        const double s = -diff * diff * gradCoef;
+                        gr[0] = s * r[0]; gr[1] = s * r[1]; gr[2] = s * r[2];
+                    }
+                    sg[0] += gr[0]; sg[1] += gr[1]; sg[2] += gr[2];
+                    sumSqGrad += gr[0] * gr[0] + gr[1] * gr[1] + gr[2] * gr[2];
+                }
+        const double beta = 2 * std::pow(mass_ * d.time_step / d.density0, 2);
+        const double dotSumGrad = sg[0] * sg[0] + sg[1] * sg[1] + sg[2] * sg[2];
+        return -1.0 / (beta * (-dotSumGrad - sumSqGrad));
+    }
+
+    // Dense cell box over the domain with a margin; column-Morton key space.
+    int setup_grid()
+    {
+        double lo[3], hi[3];
+        bool given = false;
+        for (int k = 0; k < 3; ++k) given |= d.domain_max[k] > d.domain_min[k];
+        if (given) {
+            for (int k = 0; k < 3; ++k) { lo[k] = d.domain_min[k]; hi[k] = d.domain_max[k]; }
+        } else {
+            for (int k = 0; k < 3; ++k) { lo[k] = 1e300; hi[k] = -1e300; }
+            auto acc = [&](const std::vector<double>& v) {
+                for (size_t i = 0; i + 2 < v.size(); i += 3)
+                    for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], v[i + k]); hi[k] = std::max(hi[k], v[i + k]); }
+            };
+            acc(hx);
+            if (akinci_) acc(hb);
+            if (d.boundary_method == SPH_BOUNDARY_CUBE && d.has_cube)
+                for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], d.cube_min[k]); hi[k] = std::max(hi[k], d.cube_max[k]); }
+            for (int k = 0; k < 3; ++k) {
+                const double ext = hi[k] - lo[k];
+                lo[k] -= 0.05 * ext;
+                hi[k] += 0.05 * ext;
+            }
+        }
+        const double h = hd_;
+        int o[3], nn[3];
+        for (int k = 0; k < 3; ++k) {
+            o[k] = (int)std::floor(lo[k] / h) - 2;
+            nn[k] = (int)std::floor(hi[k] / h) + 3 - o[k];
+        }
+        if (nn[0] > 2048 || nn[1] > 2048 || nn[2] > 1024 || nn[0] < 1 || nn[1] < 1 || nn[2] < 1) {
+            fail("grid box too large for the cell packing (max 2048 x 2048 x 1024 cells)");
+            return SPH_ERR_CAPACITY;
+        }
+        int bx = 0, by = 0;
+        while ((1 << bx) < nn[0]) ++bx;
+        while ((1 << by) < nn[1]) ++by;
+        std::vector<uint32_t> mx(nn[0]), my(nn[1]);
+        // interleave bit k of x and y (x first) while both have bits left
+        int pos = 0;
+        std::vector<int> px(bx), py(by);
+        for (int k = 0; k < std::max(bx, by); ++k) {
+            if (k < bx) px[k] = pos++;
+            if (k < by) py[k] = pos++;
+        }
+        for (int v = 0; v < nn[0]; ++v) {
+            uint32_t m = 0;
+            for (int k = 0; k < bx; ++k) if (v >> k & 1) m |= 1u << px[k];
+            mx[v] = m;
+        }
+        for (int v = 0; v < nn[1]; ++v) {
+            uint32_t m = 0;
+            for (int k = 0; k < by; ++k) if (v >> k & 1) m |= 1u << py[k];
+            my[v] = m;
+        }
+        const uint64_t ncols = 1ull << (bx + by);
+        const uint64_t nkeys = ncols * (uint64_t)nn[2];
+        if (nkeys > (1ull << 30)) { fail("grid key space too large"); return SPH_ERR_CAPACITY; }
+        nkeys_ = (uint32_t)nkeys;
+        SPH_CUDA(mortx_.alloc(nn[0]));
+        SPH_CUDA(morty_.alloc(nn[1]));
+        SPH_CUDA(cudaMemcpy(mortx_.p, mx.data(), nn[0] * 4, cudaMemcpyHostToDevice));
+        SPH_CUDA(cudaMemcpy(morty_.p, my.data(), nn[1] * 4, cudaMemcpyHostToDevice));
+        gv_.nx = nn[0]; gv_.ny = nn[1]; gv_.nz = nn[2];
+        gv_.ox = o[0]; gv_.oy = o[1]; gv_.oz = o[2];
+        gv_.mortx = mortx_.p;
+        gv_.morty = morty_.p;
+        return SPH_OK;
+    }
+
+    int allocate()
+    {
+        const size_t n = n_, nb = std::max(nb_, 1u);
+        for (int k = 0; k < 2; ++k) {
+            SPH_CUDA(pos_[k].alloc(n)); SPH_CUDA(vel_[k].alloc(n)); SPH_CUDA(kappa_[k].alloc(n));
+            SPH_CUDA(kappav_[k].alloc(n)); SPH_CUDA(cell_[k].alloc(n)); SPH_CUDA(id_[k].alloc(n));
+            SPH_CUDA(bpos_[k].alloc(nb)); SPH_CUDA(bcell_[k].alloc(nb)); SPH_CUDA(bid_[k].alloc(nb));
+        }
+        SPH_CUDA(bpsi_.alloc(nb));
+        SPH_CUDA(acc_.alloc(n)); SPH_CUDA(xk_.alloc(n)); SPH_CUDA(rho_.alloc(n)); SPH_CUDA(alpha_.alloc(n));
+        SPH_CUDA(pred_.alloc(n)); SPH_CUDA(div_.alloc(n)); SPH_CUDA(press_.alloc(n));
+        const bool pci = d.simulation_method == SPH_PCISPH;
+        const bool st = (c_.force_flags & F_SURFACE_TENSION) != 0;
+        SPH_CUDA(predR_.alloc(pci ? n : 1)); SPH_CUDA(predV_.alloc(pci ? n : 1)); SPH_CUDA(pacc_.alloc(pci ? n : 1));
+        SPH_CUDA(normal_.alloc(st ? n : 1));
+        const size_t nmax = std::max(n, nb);
+        SPH_CUDA(key_.alloc(nmax)); SPH_CUDA(slot_.alloc(nmax)); SPH_CUDA(tmp_.alloc(nmax));
+        SPH_CUDA(count_.alloc(nkeys_)); SPH_CUDA(starts_.alloc(nkeys_ + 1)); SPH_CUDA(bstarts_.alloc(nkeys_ + 1));
+        SPH_CUDA(tile_sums_.alloc(blocks(nkeys_, kScanTile)));
+        SPH_CUDA(cudaMemsetAsync(count_.p, 0, nkeys_ * sizeof(uint32_t), st_));
+        SPH_CUDA(partials_.alloc(blocks(n * 8, kBlock) + blocks(n, 256) + 64));
+        SPH_CUDA(sc_.alloc(1));
+        SPH_CUDA(cudaMemsetAsync(sc_.p, 0, sizeof(DevScalars), st_));
+        SPH_CUDA(cudaMemsetAsync(normal_.p, 0, normal_.n * sizeof(P4<R>), st_));
+        SPH_CUDA(cudaMemsetAsync(pacc_.p, 0, pacc_.n * sizeof(P4<R>), st_));
+        SPH_CUDA(cudaMemsetAsync(alpha_.p, 0, n * sizeof(R), st_));
+        SPH_CUDA(cudaMemsetAsync(div_.p, 0, n * sizeof(R), st_));
+        SPH_CUDA(cudaMemsetAsync(pred_.p, 0, n * sizeof(R), st_));
+        SPH_CUDA(cudaMemsetAsync(rho_.p, 0, n * sizeof(R), st_));
+        for (int k = 0; k < 2; ++k) {
+            Fluid<R>& f = fl_[k];
+            f.pos = pos_[k].p; f.vel = vel_[k].p; f.kappa = kappa_[k].p; f.kappav = kappav_[k].p;
+            f.cell = cell_[k].p; f.id = id_[k].p;
+            f.acc = acc_.p; f.xk = xk_.p; f.predR = predR_.p; f.predV = predV_.p; f.pacc = pacc_.p; f.normal = normal_.p;
+            f.rho = rho_.p; f.alpha = alpha_.p; f.pred = pred_.p; f.div = div_.p; f.press = press_.p;
+            f.n = (uint32_t)n_;
+            Boundary<R>& b = bd_[k];
+            b.pos = bpos_[k].p; b.cell = bcell_[k].p; b.id = bid_[k].p; b.psi = bpsi_.p; b.n = nb_;
+        }
+        cur_ = 0;
+        return SPH_OK;
+    }
+
+    // Exclusive scan of count_ into out (nkeys + 1 entries); zeroes count_.
+    int scan(uint32_t* out)
+    {
+        const unsigned nt = blocks(nkeys_, kScanTile);
+        k_scan_tiles<<<nt, kScanThreads, 0, ls_>>>(nkeys_, count_.p, out, tile_sums_.p);
+        k_scan_tile_sums<<<1, 1024, 0, ls_>>>(nt, tile_sums_.p, out, nkeys_);
+        k_scan_add<<<nt, kScanThreads, 0, ls_>>>(nkeys_, tile_sums_.p, out);
+        SPH_CUDA(cudaGetLastError());
+        return SPH_OK;
+    }
+
+    // SPHSolver::insertFluidParticles + neighborhoodSearch
+    // (SPHSolver.cpp:172-221): recompute cells (after the position update
+    // when MOVE), counting sort by cell key, in-cell order by id.
+    int build_grid(bool move)
+    {
+        Fluid<R> a = F();
+        if (move)
+            k_cell_update<R, true><<<blocks(n_, 256), 256, 0, ls_>>>(n_, a.pos, a.vel, a.cell, key_.p, slot_.p, count_.p, gv_,
+                                                                     c_.h, hd_, sc_.p);
+        else
+            k_cell_update<R, false><<<blocks(n_, 256), 256, 0, ls_>>>(n_, a.pos, a.vel, a.cell, key_.p, slot_.p, count_.p,
+                                                                      gv_, c_.h, hd_, sc_.p);
+        SPH_CUDA(cudaGetLastError());
+        int rc = scan(starts_.p);
+        if (rc) return rc;
+        k_scatter<<<blocks(n_, 256), 256, 0, ls_>>>(n_, key_.p, slot_.p, starts_.p, tmp_.p);
+        k_gather_fluid<R><<<blocks(n_, 256), 256, 0, ls_>>>(n_, tmp_.p, key_.p, starts_.p, fl_[cur_], fl_[1 - cur_]);
+        SPH_CUDA(cudaGetLastError());
+        cur_ = 1 - cur_;
+        return SPH_OK;
+    }
+
+    template <typename Fn> void withG(Fn&& fn)
+    {
+        if constexpr (sizeof(R) == 8) {
+            fn(std::integral_constant<int, 1>{});
+        } else {
+            switch (G_) {
+                case 2: fn(std::integral_constant<int, 2>{}); break;
+                case 4: fn(std::integral_constant<int, 4>{}); break;
+                case 8: fn(std::integral_constant<int, 8>{}); break;
+                default: fn(std::integral_constant<int, 1>{}); break;
+            }
+        }
+    }
+    unsigned wblocks() const { return blocks((size_t)n_ * G_, kBlock); }
+
+    int launch_density(bool alpha, bool eos)
+    {
+        Fluid<R> f = F();
+        const P4<R>* bp = bd_[1].pos;
+        withG([&](auto gt) {
+            constexpr int G = decltype(gt)::value;
+            if (alpha)
+                k_density<R, G, true, false><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_);
+            else if (eos)
+                k_density<R, G, false, true><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_);
+            else
+                k_density<R, G, false, false><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_);
+        });
+        SPH_CUDA(cudaGetLastError());
+        return SPH_OK;
+    }
+
+    // Simulation::computeNonPressureForces (Simulation.cpp:313-323)
+    int launch_npforces()
+    {
+        if (!c_.force_flags) return SPH_OK;
+        Fluid<R> f = F();
+        const P4<R>* bp = bd_[1].pos;
+        withG([&](auto gt) {
+            constexpr int G = decltype(gt)::value;
+            if (c_.force_flags & F_SURFACE_TENSION)
+                k_st_normals<R, G><<<wblocks(), kBlock, 0, ls_>>>(f, gv_, starts_.p, c_);
+            k_npforce<R, G><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_, sc_.p);
+        });
+        SPH_CUDA(cudaGetLastError());
+        return SPH_OK;
+    }
+
+    // A solver loop: init(h) launches the kernel that sets the first loop
+    // test, body(h) one iteration whose last kernel sets the next.  Host mode
+    // reads the flag back every few iterations (finished-loop kernels exit at
+    // once); capture mode makes it a conditional WHILE node.
+    template <typename Init, typename Body> int solve_loop(Init&& init, Body&& body, unsigned minIt, unsigned maxIt)
+    {
+        if (capturing_) {
+            cudaStreamCaptureStatus cs;
+            cudaGraph_t g;
+            const cudaGraphNode_t* deps = nullptr;
+            size_t ndeps = 0;
+            SPH_CUDA(cudaStreamGetCaptureInfo(st_, &cs, nullptr, &g, nullptr, nullptr, nullptr));
+            cudaGraphConditionalHandle h;
+            SPH_CUDA(cudaGraphConditionalHandleCreate(&h, g, 0, 0));
+            init(h);
+            SPH_CUDA(cudaGetLastError());
+            SPH_CUDA(cudaStreamGetCaptureInfo(st_, &cs, nullptr, &g, &deps, nullptr, &ndeps));
+            cudaGraphNodeParams p{};
+            p.type = cudaGraphNodeTypeConditional;
+            p.conditional.handle = h;
+            p.conditional.type = cudaGraphCondTypeWhile;
+            p.conditional.size = 1;
+            cudaGraphNode_t node;
+            SPH_CUDA(cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &p));
+            cudaGraph_t bodyg = p.conditional.phGraph_out[0];
+            SPH_CUDA(cudaStreamUpdateCaptureDependencies(st_, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+            SPH_CUDA(cudaStreamBeginCaptureToGraph(st2_, bodyg, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+            ls_ = st2_;
+            body(h);
+            ls_ = st_;
+            cudaGraph_t out;
+            SPH_CUDA(cudaStreamEndCapture(st2_, &out));
+            return SPH_OK;
+        }
+        init((cudaGraphConditionalHandle)0);
+        SPH_CUDA(cudaGetLastError());
+        unsigned launched = 0;
+        const unsigned first = std::min(std::max(minIt, 1u) + 1u, maxIt);
+        while (launched < maxIt) {
+            unsigned batch = launched == 0 ? first : 2u;
+            batch = std::min(batch, maxIt - launched);
+            for (unsigned b = 0; b < batch; ++b) body((cudaGraphConditionalHandle)0);
+            SPH_CUDA(cudaGetLastError());
+            launched += batch;
+            SPH_CUDA(cudaMemcpyAsync(&h_sc_->active, &sc_.p->active, sizeof(unsigned), cudaMemcpyDeviceToHost, st_));
+            SPH_CUDA(cudaStreamSynchronize(st_));
+            if (!h_sc_->active) break;
+        }
+        return SPH_OK;
+    }
+
+    // DFSPHSolver::step DFSPHSolver.cpp:38-112
+    int dfsph_step()
+    {
+        int rc = launch_npforces();
+        if (rc) return rc;
+        {
+            Fluid<R> f = F();
+            k_dfsph_cfl<R><<<blocks(n_, 256), 256, 0, ls_>>>(f, c_, sc_.p, lim_, partials_.p);
+            k_dfsph_predict_v_warm<R><<<blocks(n_, 256), 256, 0, ls_>>>(f, c_, sc_.p);
+            SPH_CUDA(cudaGetLastError());
+            const P4<R>* bp = bd_[1].pos;
+            withG([&](auto gt) {
+                constexpr int G = decltype(gt)::value;
+                k_dfsph_correct<R, G, 0><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_, sc_.p);
+            });
+            SPH_CUDA(cudaGetLastError());
+            // correctDensityError DFSPHSolver.cpp:311-406
+            rc = solve_loop(
+                [&](cudaGraphConditionalHandle h) {
+                    withG([&](auto gt) {
+                        constexpr int G = decltype(gt)::value;
+                        k_dfsph_predict_density<R, G, true><<<wblocks(), kBlock, 0, ls_>>>(
+                            f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_, sc_.p, lim_, partials_.p, h);
+                    });
+                },
+                [&](cudaGraphConditionalHandle h) {
+                    withG([&](auto gt) {
+                        constexpr int G = decltype(gt)::value;
+                        k_dfsph_correct<R, G, 1><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_,
+                                                                                 sc_.p);
+                        k_dfsph_predict_density<R, G, false><<<wblocks(), kBlock, 0, ls_>>>(
+                            f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_, sc_.p, lim_, partials_.p, h);
+                    });
+                },
+                lim_.minIt, lim_.maxIt);
+            if (rc) return rc;
+        }
+        rc = build_grid(true);  // updatePositions + fill grid + neighbour search
+        if (rc) return rc;
+        rc = launch_density(true, false);  // computeDensities + computeAlpha
+        if (rc) return rc;
+        {
+            Fluid<R> f = F();
+            const P4<R>* bp = bd_[1].pos;
+            // correctDivergenceError DFSPHSolver.cpp:494-590
+            rc = solve_loop(
+                [&](cudaGraphConditionalHandle h) {
+                    withG([&](auto gt) {
+                        constexpr int G = decltype(gt)::value;
+                        k_dfsph_divergence<R, G, true><<<wblocks(), kBlock, 0, ls_>>>(
+                            f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_, sc_.p, lim_, partials_.p, h);
+                    });
+                },
+                [&](cudaGraphConditionalHandle h) {
+                    withG([&](auto gt) {
+                        constexpr int G = decltype(gt)::value;
+                        k_dfsph_correct<R, G, 2><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_,
+                                                                                 sc_.p);
+                        k_dfsph_divergence<R, G, false><<<wblocks(), kBlock, 0, ls_>>>(
+                            f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_, sc_.p, lim_, partials_.p, h);
+                    });
+                },
+                lim_.minItV, lim_.maxIt);
+            if (rc) return rc;
+            if (c_.has_cube) k_dfsph_cube<R><<<blocks(n_, 256), 256, 0, ls_>>>(f, gv_, hd_, c_);
+        }
+        k_finish_step<<<1, 1, 0, ls_>>>(sc_.p);
+        SPH_CUDA(cudaGetLastError());
+        return SPH_OK;
+    }
+
+    // WCSPHSolver::step WCSPHSolver.cpp:14-78
+    int wcsph_step()
+    {
+        int rc = build_grid(false);
+        if (rc) return rc;
+        rc = launch_density(false, true);
+        if (rc) return rc;
+        Fluid<R> f = F();
+        const P4<R>* bp = bd_[1].pos;
+        withG([&](auto gt) {
+            constexpr int G = decltype(gt)::value;
+            k_wcsph_pressure_force<R, G><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_);
+        });
+        SPH_CUDA(cudaGetLastError());
+        rc = launch_npforces();
+        if (rc) return rc;
+        k_integrate<R, false><<<blocks(n_, 256), 256, 0, ls_>>>(f, gv_, hd_, c_, sc_.p);
+        k_finish_step<<<1, 1, 0, ls_>>>(sc_.p);
+        SPH_CUDA(cudaGetLastError());
+        return SPH_OK;
+    }
+
+    // PCISPHSolver::step PCISPHSolver.cpp:21-81
+    int pcisph_step()
+    {
+        int rc = build_grid(false);
+        if (rc) return rc;
+        rc = launch_density(false, false);
+        if (rc) return rc;
+        rc = launch_npforces();
+        if (rc) return rc;
+        Fluid<R> f = F();
+        const P4<R>* bp = bd_[1].pos;
+        k_pcisph_init<R><<<blocks(n_, 256), 256, 0, ls_>>>(f);
+        rc = solve_loop(
+            [&](cudaGraphConditionalHandle h) { k_pcisph_loop_begin<<<1, 1, 0, ls_>>>(sc_.p, lim_, h); },
+            [&](cudaGraphConditionalHandle h) {
+                k_pcisph_predict<R><<<blocks(n_, 256), 256, 0, ls_>>>(f, c_, sc_.p);
+                withG([&](auto gt) {
+                    constexpr int G = decltype(gt)::value;
+                    k_pcisph_density_pressure<R, G><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_,
+                                                                                   akinci_, sc_.p, lim_, partials_.p);
+                    k_pcisph_pressure_acc<R, G><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_,
+                                                                               sc_.p);
+                });
+                k_pcisph_loop_next<<<1, 1, 0, ls_>>>(sc_.p, lim_, h);
+            },
+            lim_.minIt, lim_.maxIt);
+        if (rc) return rc;
+        k_integrate<R, true><<<blocks(n_, 256), 256, 0, ls_>>>(f, gv_, hd_, c_, sc_.p);
+        k_finish_step<<<1, 1, 0, ls_>>>(sc_.p);
+        SPH_CUDA(cudaGetLastError());
+        return SPH_OK;
+    }
+
+    int one_step()
+    {
+        switch (d.simulation_method) {
+            case SPH_WCSPH: return wcsph_step();
+            case SPH_PCISPH: return pcisph_step();
+            default: return dfsph_step();
+        }
+    }
+
+    // One graph per buffer parity (each step swaps the sorted buffers once).
+    int graph_step()
+    {
+        const int k = cur_;
+        if (!gexec_[k]) {
+            cudaGraph_t g;
+            SPH_CUDA(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
+            capturing_ = true;
+            const int rc = one_step();
+            capturing_ = false;
+            cudaError_t e = cudaStreamEndCapture(st_, &g);
+            if (rc) { if (e == cudaSuccess) cudaGraphDestroy(g); cur_ = k; return rc; }
+            SPH_CUDA(e);
+            SPH_CUDA(cudaGraphInstantiate(&gexec_[k], g, 0));
+            cudaGraphDestroy(g);
+            cur_ = k;  // capture recorded the swap; the launch performs it
+        }
+        SPH_CUDA(cudaGraphLaunch(gexec_[k], st_));
+        cur_ = 1 - k;
+        return SPH_OK;
+    }
+
+    // ------------------------------------------------------------------
+    cudaStream_t st_ = nullptr, st2_ = nullptr, ls_ = nullptr;
+    DevScalars* h_sc_ = nullptr;
+    Consts<R> c_{};
+    LoopLimits lim_{};
+    GridView gv_{};
+    double hd_ = 0, mass_ = 0;
+    unsigned n_ = 0, nb_ = 0;
+    int akinci_ = 0;
+    int G_ = 1;
+    uint32_t nkeys_ = 0;
+    int cur_ = 0;
+    bool graph_ = false, capturing_ = false;
+    cudaGraphExec_t gexec_[2] = {nullptr, nullptr};
+    Fluid<R> fl_[2]{};
+    Boundary<R> bd_[2]{};
+    DevBuf<P4<R>> pos_[2], vel_[2], bpos_[2];
+    DevBuf<R> kappa_[2], kappav_[2];
+    DevBuf<uint32_t> cell_[2], id_[2], bcell_[2], bid_[2];
+    DevBuf<P4<R>> acc_, xk_, predR_, predV_, pacc_, normal_;
+    DevBuf<R> rho_, alpha_, pred_, div_, press_, bpsi_;
+    DevBuf<uint32_t> mortx_, morty_, key_, slot_, tmp_, count_, starts_, bstarts_, tile_sums_;
+    DevBuf<double> partials_;
+    DevBuf<DevScalars> sc_;
+};
+
+}  // namespace sph

@@ -1,0 +1,49 @@
+"""Generate the golden fixtures from the reference simulator itself.
+
+Runs the reference's own solver (its sources compiled headless with the
+project's GLM shim, `make -C oracle ref`, parity build, one OpenMP thread) on
+every scene of tests/scenes.py and stores inputs and per-step outputs as
+compressed .npz files in this directory.  Needs the reference tree, so it
+runs only where that tree is mounted:
+
+    python tests/golden/make_golden.py [/path/to/reference]
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+import oracle  # noqa: E402
+from scenes import SCENES, scene  # noqa: E402
+
+STEPS = 3
+KEEP = ("x", "v", "a", "rho", "p", "alpha", "div", "pred", "k", "kv", "pacc", "time", "dt", "iterations",
+        "iterationsV", "avgDensError", "avgDivError", "maxDensityError", "scaling")
+
+
+def main(ref_tree="/root/reference"):
+    if not oracle.reference_available():
+        if not oracle.build_reference(ref_tree):
+            raise SystemExit("reference tree not found; cannot generate fixtures")
+    here = os.path.dirname(os.path.abspath(__file__))
+    for name in SCENES:
+        params, x, boxes, spheres = scene(name)
+        dump = oracle.run_reference(params, x, boxes=boxes, spheres=spheres, steps=STEPS,
+                                    dump_neighbors=params["method"] == 2)
+        out = {"input.x": x}
+        for k, v in dump.items():
+            tag, _, field = k.partition(".")
+            if k in ("b.x", "b.psi", "h", "mass") or k.startswith("init.") or field in KEEP:
+                out[k] = v
+        np.savez_compressed(os.path.join(here, f"{name}.npz"), **out)
+        print(name, x.shape[0], "fluid,", len(dump.get("b.psi", [])), "boundary")
+
+
+if __name__ == "__main__":
+    main(*sys.argv[1:])

@@ -1,0 +1,93 @@
+"""Parity scenes shared by the oracle, the golden fixtures and the GPU tests.
+
+Each scene is a dict of parameters (the oracle's names, which sph_gb300.Scene
+also accepts), an initial fluid state built on the reference's lattice
+(Simulation::buildFluidBlock: spacing 2r from min + r) with optional seeded
+jitter, and the Akinci boundary shapes.  Sizes are small so the FP64 CPU
+oracle finishes in seconds.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def lattice(r, mn, mx):
+    """Simulation::buildFluidBlock (Simulation.cpp:512-539), vectorised."""
+    dist = 2.0 * r
+    n = [int(np.floor((mx[k] - mn[k]) / dist + 1e-5)) for k in range(3)]
+    i, j, k = np.meshgrid(np.arange(n[0]), np.arange(n[1]), np.arange(n[2]), indexing="ij")
+    out = np.stack([i.ravel() * dist + (mn[0] + r), j.ravel() * dist + (mn[1] + r), k.ravel() * dist + (mn[2] + r)],
+                   axis=1)
+    return out.astype(np.float64)
+
+
+def jitter(x, r, seed):
+    rng = np.random.default_rng(seed)
+    return x + rng.uniform(-0.01 * r, 0.01 * r, x.shape)
+
+
+SCENES = {
+    # DFSPH dam break with Akinci walls (the headline solver)
+    "dfsph_akinci": dict(
+        params=dict(method=2, boundary=2, radius=0.02, eta=0.001, eta_v=0.001, cfl=1.0, dt=1e-4, min_dt=1e-5,
+                    max_dt=5e-3, fps=60.0),
+        fluid=lambda: lattice(0.02, (0.0, 0.0, 0.0), (0.4, 0.4, 0.4)),
+        boxes=[((0.0, 0.0, 0.0), (0.8, 0.6, 0.6))],
+        spheres=[],
+    ),
+    # DFSPH with a sphere obstacle and XSPH + surface tension + adhesion
+    "dfsph_forces": dict(
+        params=dict(method=2, boundary=2, radius=0.02, visc_method=2, visc=0.01, bvisc=0.01, st_method=3, st=0.5,
+                    adh_method=4, adh=0.1),
+        fluid=lambda: lattice(0.02, (0.05, 0.05, 0.05), (0.35, 0.35, 0.35)),
+        boxes=[((0.0, 0.0, 0.0), (0.6, 0.6, 0.6))],
+        spheres=[((0.3, 0.5, 0.3), 0.08)],
+    ),
+    # DFSPH with artificial viscosity
+    "dfsph_artvisc": dict(
+        params=dict(method=2, boundary=2, radius=0.02, visc_method=1, visc=0.01, bvisc=0.01),
+        fluid=lambda: lattice(0.02, (0.05, 0.05, 0.05), (0.35, 0.3, 0.35)),
+        boxes=[((0.0, 0.0, 0.0), (0.5, 0.5, 0.5))],
+        spheres=[],
+    ),
+    # WCSPH settling block in a cube boundary with XSPH (the CPU-runnable
+    # configuration, scaled down): jitter +-0.01 r, seed 1234
+    "wcsph_cube": dict(
+        params=dict(method=0, boundary=0, radius=0.025, stiffness=1000.0, gamma=7.0, visc_method=2, visc=0.01,
+                    has_cube=1, cube_min=(0.0, 0.0, 0.0), cube_max=(1.0, 1.0, 1.0)),
+        fluid=lambda: jitter(lattice(0.025, (0.0, 0.0, 0.0), (0.5, 0.5, 0.5)), 0.025, 1234),
+        boxes=[],
+        spheres=[],
+    ),
+    # WCSPH with Akinci walls and boundary XSPH
+    "wcsph_akinci": dict(
+        params=dict(method=0, boundary=2, radius=0.02, visc_method=2, visc=0.01, bvisc=0.01),
+        fluid=lambda: lattice(0.02, (0.1, 0.1, 0.1), (0.4, 0.35, 0.4)),
+        boxes=[((0.0, 0.0, 0.0), (0.5, 0.5, 0.5))],
+        spheres=[((0.25, 0.05, 0.25), 0.05)],
+    ),
+    # PCISPH drop with standard viscosity, surface tension, cohesion, adhesion
+    "pcisph_drop": dict(
+        params=dict(method=1, boundary=2, radius=0.02, eta=0.001, min_it=3, max_it=100, visc_method=0, visc=0.01,
+                    bvisc=0.01, st_method=3, st=0.5, adh_method=4, adh=0.1),
+        fluid=lambda: np.concatenate([
+            lattice(0.02, (0.0, 0.0, 0.0), (0.6, 0.08, 0.6)),
+            lattice(0.02, (0.2, 0.2, 0.2), (0.36, 0.36, 0.36)),
+        ]),
+        boxes=[((0.0, 0.0, 0.0), (0.6, 0.6, 0.6))],
+        spheres=[],
+    ),
+    # DFSPH inside a cube boundary (clamp after the divergence solve)
+    "dfsph_cube": dict(
+        params=dict(method=2, boundary=0, radius=0.02, has_cube=1, cube_min=(0.0, 0.0, 0.0),
+                    cube_max=(0.4, 0.4, 0.4)),
+        fluid=lambda: lattice(0.02, (0.0, 0.0, 0.0), (0.3, 0.3, 0.3)),
+        boxes=[],
+        spheres=[],
+    ),
+}
+
+
+def scene(name):
+    s = SCENES[name]
+    return s["params"], s["fluid"](), s["boxes"], s["spheres"]

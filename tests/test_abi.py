@@ -1,0 +1,73 @@
+"""CPU checks of the C ABI: the library loads, exports every function the
+header declares, rejects bad arguments, and its host-side samplers reproduce
+the reference's point sets (no GPU needed for any of these)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import oracle
+import sph_gb300
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def L():
+    sph_gb300.build()
+    return sph_gb300.lib()
+
+
+def header_functions():
+    src = open(os.path.join(ROOT, "include", "sph_gb300.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?[a-z_ ]+\**\s*\**(sph_[a-z0-9_]+)\s*\(", src, flags=re.M)))
+
+
+def test_header_symbols_exported(L):
+    names = header_functions()
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(L, n), n
+    assert {n for n, _, _ in sph_gb300.ABI} == set(names)
+
+
+def test_desc_defaults_follow_reference(L):
+    d = sph_gb300.make_desc()
+    assert d.simulation_method == sph_gb300.DFSPH
+    assert d.time_step == 0.0001 and d.density0 == 1000.0 and d.cfl_factor == 1.0
+    assert d.min_iterations == -1 and d.viscosity_method == -1
+
+
+def test_create_rejects_bad_arguments(L):
+    h = ctypes.c_void_p()
+    for bad in (dict(method=5), dict(boundary=7), dict(radius=0.0), dict(dt=-1.0)):
+        d = sph_gb300.make_desc(**bad)
+        rc = L.sph_ctx_create(ctypes.byref(d), ctypes.byref(h))
+        assert rc == -1
+
+
+def test_step_before_init_is_an_error(L):
+    s = sph_gb300.Scene(method=2, radius=0.02)
+    with pytest.raises(sph_gb300.SPHError):
+        s.step(1)
+    s.close()
+
+
+@pytest.mark.parametrize("r,mn,mx", [(0.02, (0, 0, 0), (0.6, 0.5, 0.5)), (0.005, (0, 0, 0), (1.5, 0.8, 0.8)),
+                                     (0.01, (0.1, 0.2, 0.3), (1.3, 0.7, 0.9))])
+def test_box_sampler_matches_oracle(L, r, mn, mx):
+    assert np.array_equal(sph_gb300.sample_box(4 * r, mn, mx), oracle.sample_box(4 * r, mn, mx))
+
+
+@pytest.mark.parametrize("r,c,R", [(0.01, (0.5, 0.5, 0.5), 0.1), (0.005, (0.3, 0.2, 0.1), 0.2), (0.01, (0, 0, 0), 0.05)])
+def test_sphere_sampler_matches_oracle(L, r, c, R):
+    assert np.array_equal(sph_gb300.sample_sphere(r, c, R), oracle.sample_sphere(r, c, R))
+
+
+def test_fluid_block_matches_oracle(L):
+    a = sph_gb300.fluid_block(0.01, (0, 0, 0), (0.5, 0.5, 0.5))
+    assert a.shape == (15625, 3)
+    assert np.array_equal(a, oracle.fluid_block(0.01, (0, 0, 0), (0.5, 0.5, 0.5)))

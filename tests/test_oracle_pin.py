@@ -1,0 +1,31 @@
+"""Live pin of the C restatement against the reference's own sources, built
+headless (oracle/_ref).  Runs only where the reference tree is available;
+elsewhere the golden fixtures carry the pin."""
+import numpy as np
+import pytest
+
+import oracle
+from scenes import jitter, lattice
+
+pytestmark = pytest.mark.skipif(not oracle.reference_available(), reason="reference build not present")
+
+CASES = [
+    ("dfsph_cube_jitter", dict(method=2, boundary=0, radius=0.02, has_cube=1, cube_min=(0, 0, 0), cube_max=(0.4, 0.5, 0.4)),
+     lambda: jitter(lattice(0.02, (0, 0, 0), (0.3, 0.3, 0.3)), 0.02, 7), [], []),
+    ("pcisph_akinci_xsph", dict(method=1, boundary=2, radius=0.02, visc_method=2, visc=0.02, bvisc=0.01, eta=0.002,
+                                min_it=2, max_it=20),
+     lambda: lattice(0.02, (0.05, 0.05, 0.05), (0.3, 0.4, 0.3)), [((0, 0, 0), (0.5, 0.6, 0.5))], [((0.25, 0.5, 0.25), 0.06)]),
+    ("wcsph_art", dict(method=0, boundary=2, radius=0.02, visc_method=1, visc=0.05, bvisc=0.02, stiffness=500, gamma=7),
+     lambda: jitter(lattice(0.02, (0.02, 0.02, 0.02), (0.3, 0.3, 0.3)), 0.02, 3), [((0, 0, 0), (0.4, 0.4, 0.4))], []),
+]
+
+
+@pytest.mark.parametrize("name,params,fluid,boxes,spheres", CASES, ids=[c[0] for c in CASES])
+def test_oracle_matches_live_reference(name, params, fluid, boxes, spheres):
+    x = fluid()
+    ref = oracle.run_reference(params, x, boxes=boxes, spheres=spheres, steps=4)
+    o = oracle.OracleScene(params, x, boxes=boxes, spheres=spheres)
+    for s in range(1, 5):
+        o.step(1)
+        for f in ("x", "v", "rho", "p"):
+            assert np.array_equal(o.get(f).ravel(), ref[f"s{s}.{f}"]), (name, s, f)
