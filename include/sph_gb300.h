@@ -147,6 +147,9 @@ int sph_ctx_init(sph_ctx* ctx);
  * Asynchronous on the context's stream except where a solver loop needs a
  * convergence test read back (see sph_ctx_set_graph). */
 int sph_ctx_step(sph_ctx* ctx, int nsteps);
+/* sph_ctx_step bracketed by CUDA events on the context's stream; waits for
+ * the steps and returns their device time in *elapsed_ms. */
+int sph_ctx_step_timed(sph_ctx* ctx, int nsteps, float* elapsed_ms);
 /* Wait for the context's stream. */
 int sph_ctx_synchronize(sph_ctx* ctx);
 
@@ -167,6 +170,19 @@ const char* sph_ctx_last_error(const sph_ctx* ctx);
  * totals[1] (boundary pairs) first. */
 int sph_ctx_neighbors(sph_ctx* ctx, int* cells, int* cell_rank, int* nbr_off, int* nbr, int* bnbr_off, int* bnbr,
                       long long* totals);
+
+/* Number of kernels of this library the context has launched (graph steps
+ * counted from the captured graph and the iterations its loops ran). */
+int sph_ctx_get_launch_count(sph_ctx* ctx, unsigned long long* out);
+/* Per-kernel CUDA-event timing of host-driven steps (no effect in graph
+ * mode).  sph_ctx_get_profile writes "name launches total_ms" lines for the
+ * launches since the previous call and returns the text length. */
+int sph_ctx_set_profiling(sph_ctx* ctx, int enable);
+int sph_ctx_get_profile(sph_ctx* ctx, char* buf, unsigned long long len);
+
+/* cudaSetDevice for the calling thread; contexts created afterwards live on
+ * that device. */
+int sph_select_device(int device);
 
 /* Sampling helpers with the reference's point sets, usable without a
  * context; out may be NULL to query the count.  Return the point count. */

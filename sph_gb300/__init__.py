@@ -107,6 +107,7 @@ ABI = [
     ("sph_ctx_add_boundary_points", ctypes.c_int, [_vp, _dp, ctypes.c_uint]),
     ("sph_ctx_init", ctypes.c_int, [_vp]),
     ("sph_ctx_step", ctypes.c_int, [_vp, ctypes.c_int]),
+    ("sph_ctx_step_timed", ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
     ("sph_ctx_synchronize", ctypes.c_int, [_vp]),
     ("sph_ctx_set_graph", ctypes.c_int, [_vp, ctypes.c_int]),
     ("sph_ctx_num_particles", ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_uint), ctypes.POINTER(ctypes.c_uint)]),
@@ -114,6 +115,10 @@ ABI = [
     ("sph_ctx_get_stats", ctypes.c_int, [_vp, ctypes.POINTER(Stats)]),
     ("sph_ctx_last_error", ctypes.c_char_p, [_vp]),
     ("sph_ctx_neighbors", ctypes.c_int, [_vp, _ip, _ip, _ip, _ip, _ip, _ip, ctypes.POINTER(ctypes.c_longlong)]),
+    ("sph_ctx_get_launch_count", ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_ulonglong)]),
+    ("sph_ctx_set_profiling", ctypes.c_int, [_vp, ctypes.c_int]),
+    ("sph_ctx_get_profile", ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_ulonglong]),
+    ("sph_select_device", ctypes.c_int, [ctypes.c_int]),
     ("sph_sample_box", ctypes.c_longlong, [ctypes.c_double, _dp, _dp, _dp]),
     ("sph_sample_sphere", ctypes.c_longlong, [ctypes.c_double, _dp, ctypes.c_double, _dp]),
     ("sph_fluid_block", ctypes.c_longlong, [ctypes.c_double, _dp, _dp, _dp]),
@@ -253,6 +258,12 @@ class Scene:
     def step(self, n=1):
         self._check(lib().sph_ctx_step(self._h, int(n)), "sph_ctx_step")
 
+    def step_timed(self, n=1):
+        """Run n steps; return their device time in ms (CUDA events)."""
+        ms = ctypes.c_float()
+        self._check(lib().sph_ctx_step_timed(self._h, int(n), ctypes.byref(ms)), "sph_ctx_step_timed")
+        return ms.value
+
     def synchronize(self):
         self._check(lib().sph_ctx_synchronize(self._h), "sph_ctx_synchronize")
 
@@ -286,6 +297,26 @@ class Scene:
         self._check(lib().sph_ctx_get_stats(self._h, ctypes.byref(s)), "sph_ctx_get_stats")
         return {name: getattr(s, name) for name, _ in Stats._fields_}
 
+    def launch_count(self):
+        n = ctypes.c_ulonglong()
+        self._check(lib().sph_ctx_get_launch_count(self._h, ctypes.byref(n)), "sph_ctx_get_launch_count")
+        return n.value
+
+    def set_profiling(self, enable=True):
+        self._check(lib().sph_ctx_set_profiling(self._h, int(bool(enable))), "sph_ctx_set_profiling")
+
+    def profile(self):
+        """{kernel name: (launches, total ms)} since the previous call."""
+        buf = ctypes.create_string_buffer(1 << 16)
+        n = lib().sph_ctx_get_profile(self._h, buf, len(buf))
+        if n < 0:
+            self._check(n, "sph_ctx_get_profile")
+        out = {}
+        for line in buf.value.decode().splitlines():
+            name, cnt, ms = line.split()
+            out[name] = (int(cnt), float(ms))
+        return out
+
     def neighbors(self):
         L = lib()
         tot = (ctypes.c_longlong * 2)()
@@ -301,6 +332,12 @@ class Scene:
                     "sph_ctx_neighbors")
         return dict(cell=cells.reshape(n, 3), cell_rank=rank, nbr_off=off, nbr=nbr[: tot[0]], bnbr_off=boff,
                     bnbr=bnbr[: tot[1]])
+
+
+def select_device(device: int):
+    rc = lib().sph_select_device(int(device))
+    if rc != 0:
+        raise SPHError(f"sph_select_device({device}) failed ({rc})")
 
 
 def sample_box(support_radius, mn, mx):

@@ -8,6 +8,8 @@
 #include "../../include/sph_gb300.h"
 #include "sph_scene_base.h"
 
+#include <cuda_runtime.h>
+
 struct sph_ctx {
     sph::SceneBase* scene = nullptr;
     std::string err;
@@ -261,6 +263,12 @@ int sph_ctx_step(sph_ctx* ctx, int nsteps)
     return relay(ctx, ctx->scene->step(nsteps));
 }
 
+int sph_ctx_step_timed(sph_ctx* ctx, int nsteps, float* elapsed_ms)
+{
+    if (!ctx || nsteps < 0 || !elapsed_ms) return bad(ctx, "invalid argument");
+    return relay(ctx, ctx->scene->step_timed(nsteps, elapsed_ms));
+}
+
 int sph_ctx_synchronize(sph_ctx* ctx)
 {
     if (!ctx) return SPH_ERR_INVALID;
@@ -323,6 +331,34 @@ long long sph_fluid_block(double particle_radius, const double mn[3], const doub
 {
     if (!mn || !mx || !(particle_radius > 0.0)) return -1;
     return sph::fluid_block(particle_radius, mn, mx, out);
+}
+
+int sph_ctx_get_launch_count(sph_ctx* ctx, unsigned long long* out)
+{
+    if (!ctx || !out) return bad(ctx, "invalid argument");
+    return relay(ctx, ctx->scene->launch_count(out));
+}
+
+int sph_ctx_set_profiling(sph_ctx* ctx, int enable)
+{
+    if (!ctx) return SPH_ERR_INVALID;
+    return relay(ctx, ctx->scene->set_profiling(enable));
+}
+
+int sph_ctx_get_profile(sph_ctx* ctx, char* buf, unsigned long long len)
+{
+    if (!ctx) return SPH_ERR_INVALID;
+    if (!ctx->scene->inited) return bad(ctx, "not initialised");
+    const int n = ctx->scene->profile(buf, (size_t)len);
+    if (n < 0) return relay(ctx, n);
+    return n;
+}
+
+int sph_select_device(int device)
+{
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) return SPH_ERR_INVALID;
+    return cudaSetDevice(device) == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }
 
 const char* sph_version(void) { return "sph_gb300 0.1 (sm_103a)"; }

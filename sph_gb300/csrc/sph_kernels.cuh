@@ -314,8 +314,8 @@ __device__ __forceinline__ uint32_t final_slot(uint32_t p, const uint32_t* __res
     return s + rank;
 }
 
-// Gather of the state that survives a re-sort (DFSPH: x, v, k, kv; the
-// other fields are recomputed after every build).
+// Gather of the state that survives a re-sort (x, v, DFSPH k, kv and the
+// last predicted density; the other fields are recomputed after every build).
 template <typename R>
 __global__ void k_gather_fluid(uint32_t n, const uint32_t* __restrict__ tmp, const uint32_t* __restrict__ key,
                                const uint32_t* __restrict__ starts, Fluid<R> src, Fluid<R> dst)
@@ -328,6 +328,7 @@ __global__ void k_gather_fluid(uint32_t n, const uint32_t* __restrict__ tmp, con
     dst.vel[d] = src.vel[i];
     dst.kappa[d] = src.kappa[i];
     dst.kappav[d] = src.kappav[i];
+    dst.pred[d] = src.pred[i];
     dst.cell[d] = src.cell[i];
     dst.id[d] = src.id[i];
 }

@@ -48,6 +48,9 @@ public:
         if (st_) cudaStreamDestroy(st_);
         if (st2_) cudaStreamDestroy(st2_);
         if (h_sc_) cudaFreeHost(h_sc_);
+        for (auto& p : pending_) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
+        for (auto e : events_) cudaEventDestroy(e);
+        for (auto e : tev_) if (e) cudaEventDestroy(e);
     }
 
     unsigned nfluid() const override { return inited ? n_ : (unsigned)(hx.size() / 3); }
@@ -137,6 +140,24 @@ public:
         return SPH_OK;
     }
 
+    // nsteps steps bracketed by CUDA events on the scene's stream; waits and
+    // returns the elapsed device time.
+    int step_timed(int nsteps, float* ms) override
+    {
+        if (!inited) { fail("sph_ctx_init has not been called"); return SPH_ERR_INVALID; }
+        if (!tev_[0]) {
+            SPH_CUDA(cudaEventCreate(&tev_[0]));
+            SPH_CUDA(cudaEventCreate(&tev_[1]));
+        }
+        SPH_CUDA(cudaEventRecord(tev_[0], st_));
+        const int rc = step(nsteps);
+        if (rc) return rc;
+        SPH_CUDA(cudaEventRecord(tev_[1], st_));
+        SPH_CUDA(cudaEventSynchronize(tev_[1]));
+        SPH_CUDA(cudaEventElapsedTime(ms, tev_[0], tev_[1]));
+        return SPH_OK;
+    }
+
     int sync() override
     {
         SPH_CUDA(cudaStreamSynchronize(st_));
@@ -145,8 +166,82 @@ public:
 
     int set_graph(int on) override
     {
-        graph_ = on != 0;
+        const bool want = on != 0;
+        if (want == graph_) return SPH_OK;
+        if (inited) {
+            SPH_CUDA(cudaMemcpyAsync(h_sc_, sc_.p, sizeof(DevScalars), cudaMemcpyDeviceToHost, st_));
+            SPH_CUDA(cudaStreamSynchronize(st_));
+            if (want) {
+                snap_it_ = h_sc_->sumIterations;
+                snap_itv_ = h_sc_->sumIterationsV;
+                gsteps_[0] = gsteps_[1] = 0;
+            } else {
+                graph_launches_ += graph_kernels();
+            }
+        }
+        graph_ = want;
         return SPH_OK;
+    }
+
+    // Kernels run by graph steps since the last snapshot: per step the fixed
+    // part of the captured graph, plus each loop body times the iterations it
+    // ran (h_sc_ must be current).
+    unsigned long long graph_kernels() const
+    {
+        unsigned long long k = 0;
+        for (int q = 0; q < 2; ++q) k += gsteps_[q] * (unsigned long long)gshape_[q][0];
+        const unsigned long long b1 = std::max(gshape_[0][1], gshape_[1][1]);
+        const unsigned long long b2 = std::max(gshape_[0][2], gshape_[1][2]);
+        k += b1 * (h_sc_->sumIterations - snap_it_) + b2 * (h_sc_->sumIterationsV - snap_itv_);
+        return k;
+    }
+
+    int launch_count(unsigned long long* out) override
+    {
+        if (!inited) { *out = 0; return SPH_OK; }
+        SPH_CUDA(cudaMemcpyAsync(h_sc_, sc_.p, sizeof(DevScalars), cudaMemcpyDeviceToHost, st_));
+        SPH_CUDA(cudaStreamSynchronize(st_));
+        *out = launches_ + graph_launches_ + (graph_ ? graph_kernels() : 0ull);
+        return SPH_OK;
+    }
+
+    int set_profiling(int on) override
+    {
+        prof_ = on != 0;
+        return SPH_OK;
+    }
+
+    // "name count total_ms" per kernel name, for the launches timed since the
+    // last call (host-driven steps with profiling on).
+    int profile(char* buf, size_t len) override
+    {
+        SPH_CUDA(cudaStreamSynchronize(st_));
+        std::vector<std::string> names;
+        std::vector<double> ms;
+        std::vector<unsigned long long> cnt;
+        for (auto& p : pending_) {
+            float t = 0.f;
+            SPH_CUDA(cudaEventElapsedTime(&t, p.a, p.b));
+            size_t q = 0;
+            while (q < names.size() && names[q] != p.name) ++q;
+            if (q == names.size()) { names.push_back(p.name); ms.push_back(0.0); cnt.push_back(0); }
+            ms[q] += t;
+            cnt[q] += 1;
+            events_.push_back(p.a);
+            events_.push_back(p.b);
+        }
+        pending_.clear();
+        std::string outs;
+        char line[256];
+        for (size_t q = 0; q < names.size(); ++q) {
+            std::snprintf(line, sizeof line, "%s %llu %.6f\n", names[q].c_str(), cnt[q], ms[q]);
+            outs += line;
+        }
+        if (buf && len) {
+            std::strncpy(buf, outs.c_str(), len - 1);
+            buf[len - 1] = 0;
+        }
+        return (int)outs.size();
     }
 
     int download(int field, double* out) override
@@ -452,11 +547,13 @@ private:
         for (int k = 0; k < 2; ++k) {
             SPH_CUDA(pos_[k].alloc(n)); SPH_CUDA(vel_[k].alloc(n)); SPH_CUDA(kappa_[k].alloc(n));
             SPH_CUDA(kappav_[k].alloc(n)); SPH_CUDA(cell_[k].alloc(n)); SPH_CUDA(id_[k].alloc(n));
+            SPH_CUDA(pred_[k].alloc(n));
+            SPH_CUDA(cudaMemsetAsync(pred_[k].p, 0, n * sizeof(R), st_));
             SPH_CUDA(bpos_[k].alloc(nb)); SPH_CUDA(bcell_[k].alloc(nb)); SPH_CUDA(bid_[k].alloc(nb));
         }
         SPH_CUDA(bpsi_.alloc(nb));
         SPH_CUDA(acc_.alloc(n)); SPH_CUDA(xk_.alloc(n)); SPH_CUDA(rho_.alloc(n)); SPH_CUDA(alpha_.alloc(n));
-        SPH_CUDA(pred_.alloc(n)); SPH_CUDA(div_.alloc(n)); SPH_CUDA(press_.alloc(n));
+        SPH_CUDA(div_.alloc(n)); SPH_CUDA(press_.alloc(n));
         const bool pci = d.simulation_method == SPH_PCISPH;
         const bool st = (c_.force_flags & F_SURFACE_TENSION) != 0;
         SPH_CUDA(predR_.alloc(pci ? n : 1)); SPH_CUDA(predV_.alloc(pci ? n : 1)); SPH_CUDA(pacc_.alloc(pci ? n : 1));
@@ -473,14 +570,13 @@ private:
         SPH_CUDA(cudaMemsetAsync(pacc_.p, 0, pacc_.n * sizeof(P4<R>), st_));
         SPH_CUDA(cudaMemsetAsync(alpha_.p, 0, n * sizeof(R), st_));
         SPH_CUDA(cudaMemsetAsync(div_.p, 0, n * sizeof(R), st_));
-        SPH_CUDA(cudaMemsetAsync(pred_.p, 0, n * sizeof(R), st_));
         SPH_CUDA(cudaMemsetAsync(rho_.p, 0, n * sizeof(R), st_));
         for (int k = 0; k < 2; ++k) {
             Fluid<R>& f = fl_[k];
             f.pos = pos_[k].p; f.vel = vel_[k].p; f.kappa = kappa_[k].p; f.kappav = kappav_[k].p;
-            f.cell = cell_[k].p; f.id = id_[k].p;
+            f.cell = cell_[k].p; f.id = id_[k].p; f.pred = pred_[k].p;
             f.acc = acc_.p; f.xk = xk_.p; f.predR = predR_.p; f.predV = predV_.p; f.pacc = pacc_.p; f.normal = normal_.p;
-            f.rho = rho_.p; f.alpha = alpha_.p; f.pred = pred_.p; f.div = div_.p; f.press = press_.p;
+            f.rho = rho_.p; f.alpha = alpha_.p; f.div = div_.p; f.press = press_.p;
             f.n = (uint32_t)n_;
             Boundary<R>& b = bd_[k];
             b.pos = bpos_[k].p; b.cell = bcell_[k].p; b.id = bid_[k].p; b.psi = bpsi_.p; b.n = nb_;
@@ -493,9 +589,9 @@ private:
     int scan(uint32_t* out)
     {
         const unsigned nt = blocks(nkeys_, kScanTile);
-        k_scan_tiles<<<nt, kScanThreads, 0, ls_>>>(nkeys_, count_.p, out, tile_sums_.p);
-        k_scan_tile_sums<<<1, 1024, 0, ls_>>>(nt, tile_sums_.p, out, nkeys_);
-        k_scan_add<<<nt, kScanThreads, 0, ls_>>>(nkeys_, tile_sums_.p, out);
+        run("k_scan_tiles", [&] { k_scan_tiles<<<nt, kScanThreads, 0, ls_>>>(nkeys_, count_.p, out, tile_sums_.p); });
+        run("k_scan_tile_sums", [&] { k_scan_tile_sums<<<1, 1024, 0, ls_>>>(nt, tile_sums_.p, out, nkeys_); });
+        run("k_scan_add", [&] { k_scan_add<<<nt, kScanThreads, 0, ls_>>>(nkeys_, tile_sums_.p, out); });
         SPH_CUDA(cudaGetLastError());
         return SPH_OK;
     }
@@ -507,16 +603,16 @@ private:
     {
         Fluid<R> a = F();
         if (move)
-            k_cell_update<R, true><<<blocks(n_, 256), 256, 0, ls_>>>(n_, a.pos, a.vel, a.cell, key_.p, slot_.p, count_.p, gv_,
-                                                                     c_.h, hd_, sc_.p);
+            run("k_cell_update", [&] { k_cell_update<R, true><<<blocks(n_, 256), 256, 0, ls_>>>(n_, a.pos, a.vel, a.cell, key_.p, slot_.p, count_.p, gv_,
+                                                                     c_.h, hd_, sc_.p); });
         else
-            k_cell_update<R, false><<<blocks(n_, 256), 256, 0, ls_>>>(n_, a.pos, a.vel, a.cell, key_.p, slot_.p, count_.p,
-                                                                      gv_, c_.h, hd_, sc_.p);
+            run("k_cell_update", [&] { k_cell_update<R, false><<<blocks(n_, 256), 256, 0, ls_>>>(n_, a.pos, a.vel, a.cell, key_.p, slot_.p, count_.p,
+                                                                      gv_, c_.h, hd_, sc_.p); });
         SPH_CUDA(cudaGetLastError());
         int rc = scan(starts_.p);
         if (rc) return rc;
-        k_scatter<<<blocks(n_, 256), 256, 0, ls_>>>(n_, key_.p, slot_.p, starts_.p, tmp_.p);
-        k_gather_fluid<R><<<blocks(n_, 256), 256, 0, ls_>>>(n_, tmp_.p, key_.p, starts_.p, fl_[cur_], fl_[1 - cur_]);
+        run("k_scatter", [&] { k_scatter<<<blocks(n_, 256), 256, 0, ls_>>>(n_, key_.p, slot_.p, starts_.p, tmp_.p); });
+        run("k_gather_fluid", [&] { k_gather_fluid<R><<<blocks(n_, 256), 256, 0, ls_>>>(n_, tmp_.p, key_.p, starts_.p, fl_[cur_], fl_[1 - cur_]); });
         SPH_CUDA(cudaGetLastError());
         cur_ = 1 - cur_;
         return SPH_OK;
@@ -544,11 +640,11 @@ private:
         withG([&](auto gt) {
             constexpr int G = decltype(gt)::value;
             if (alpha)
-                k_density<R, G, true, false><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_);
+                run("k_density", [&] { k_density<R, G, true, false><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_); });
             else if (eos)
-                k_density<R, G, false, true><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_);
+                run("k_density", [&] { k_density<R, G, false, true><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_); });
             else
-                k_density<R, G, false, false><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_);
+                run("k_density", [&] { k_density<R, G, false, false><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_); });
         });
         SPH_CUDA(cudaGetLastError());
         return SPH_OK;
@@ -563,8 +659,8 @@ private:
         withG([&](auto gt) {
             constexpr int G = decltype(gt)::value;
             if (c_.force_flags & F_SURFACE_TENSION)
-                k_st_normals<R, G><<<wblocks(), kBlock, 0, ls_>>>(f, gv_, starts_.p, c_);
-            k_npforce<R, G><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_, sc_.p);
+                run("k_st_normals", [&] { k_st_normals<R, G><<<wblocks(), kBlock, 0, ls_>>>(f, gv_, starts_.p, c_); });
+            run("k_npforce", [&] { k_npforce<R, G><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_, sc_.p); });
         });
         SPH_CUDA(cudaGetLastError());
         return SPH_OK;
@@ -574,7 +670,7 @@ private:
     // test, body(h) one iteration whose last kernel sets the next.  Host mode
     // reads the flag back every few iterations (finished-loop kernels exit at
     // once); capture mode makes it a conditional WHILE node.
-    template <typename Init, typename Body> int solve_loop(Init&& init, Body&& body, unsigned minIt, unsigned maxIt)
+    template <typename Init, typename Body> int solve_loop(int loop_id, Init&& init, Body&& body, unsigned minIt, unsigned maxIt)
     {
         if (capturing_) {
             cudaStreamCaptureStatus cs;
@@ -598,7 +694,9 @@ private:
             SPH_CUDA(cudaStreamUpdateCaptureDependencies(st_, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
             SPH_CUDA(cudaStreamBeginCaptureToGraph(st2_, bodyg, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
             ls_ = st2_;
+            loop_ctx_ = loop_id;
             body(h);
+            loop_ctx_ = 0;
             ls_ = st_;
             cudaGraph_t out;
             SPH_CUDA(cudaStreamEndCapture(st2_, &out));
@@ -621,6 +719,29 @@ private:
         return SPH_OK;
     }
 
+    // Every launch of the step path goes through run(): it counts launches
+    // (host mode), records how many kernels a captured step holds per loop
+    // body (graph mode), and brackets the launch with CUDA events when
+    // profiling is on.
+    template <typename Fn> void run(const char* name, Fn&& fn)
+    {
+        if (capturing_) { ++cap_count_[loop_ctx_]; fn(); return; }
+        ++launches_;
+        if (!prof_) { fn(); return; }
+        cudaEvent_t a = take_event(), b = take_event();
+        cudaEventRecord(a, ls_);
+        fn();
+        cudaEventRecord(b, ls_);
+        pending_.push_back({name, a, b});
+    }
+    cudaEvent_t take_event()
+    {
+        if (!events_.empty()) { cudaEvent_t e = events_.back(); events_.pop_back(); return e; }
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        return e;
+    }
+
     // DFSPHSolver::step DFSPHSolver.cpp:38-112
     int dfsph_step()
     {
@@ -628,31 +749,31 @@ private:
         if (rc) return rc;
         {
             Fluid<R> f = F();
-            k_dfsph_cfl<R><<<blocks(n_, 256), 256, 0, ls_>>>(f, c_, sc_.p, lim_, partials_.p);
-            k_dfsph_predict_v_warm<R><<<blocks(n_, 256), 256, 0, ls_>>>(f, c_, sc_.p);
+            run("k_dfsph_cfl", [&] { k_dfsph_cfl<R><<<blocks(n_, 256), 256, 0, ls_>>>(f, c_, sc_.p, lim_, partials_.p); });
+            run("k_dfsph_predict_v_warm", [&] { k_dfsph_predict_v_warm<R><<<blocks(n_, 256), 256, 0, ls_>>>(f, c_, sc_.p); });
             SPH_CUDA(cudaGetLastError());
             const P4<R>* bp = bd_[1].pos;
             withG([&](auto gt) {
                 constexpr int G = decltype(gt)::value;
-                k_dfsph_correct<R, G, 0><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_, sc_.p);
+                run("k_dfsph_correct", [&] { k_dfsph_correct<R, G, 0><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_, sc_.p); });
             });
             SPH_CUDA(cudaGetLastError());
             // correctDensityError DFSPHSolver.cpp:311-406
-            rc = solve_loop(
+            rc = solve_loop(1, 
                 [&](cudaGraphConditionalHandle h) {
                     withG([&](auto gt) {
                         constexpr int G = decltype(gt)::value;
-                        k_dfsph_predict_density<R, G, true><<<wblocks(), kBlock, 0, ls_>>>(
-                            f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_, sc_.p, lim_, partials_.p, h);
+                        run("k_dfsph_predict_density", [&] { k_dfsph_predict_density<R, G, true><<<wblocks(), kBlock, 0, ls_>>>(
+                            f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_, sc_.p, lim_, partials_.p, h); });
                     });
                 },
                 [&](cudaGraphConditionalHandle h) {
                     withG([&](auto gt) {
                         constexpr int G = decltype(gt)::value;
-                        k_dfsph_correct<R, G, 1><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_,
-                                                                                 sc_.p);
-                        k_dfsph_predict_density<R, G, false><<<wblocks(), kBlock, 0, ls_>>>(
-                            f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_, sc_.p, lim_, partials_.p, h);
+                        run("k_dfsph_correct", [&] { k_dfsph_correct<R, G, 1><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_,
+                                                                                 sc_.p); });
+                        run("k_dfsph_predict_density", [&] { k_dfsph_predict_density<R, G, false><<<wblocks(), kBlock, 0, ls_>>>(
+                            f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_, sc_.p, lim_, partials_.p, h); });
                     });
                 },
                 lim_.minIt, lim_.maxIt);
@@ -666,28 +787,28 @@ private:
             Fluid<R> f = F();
             const P4<R>* bp = bd_[1].pos;
             // correctDivergenceError DFSPHSolver.cpp:494-590
-            rc = solve_loop(
+            rc = solve_loop(2, 
                 [&](cudaGraphConditionalHandle h) {
                     withG([&](auto gt) {
                         constexpr int G = decltype(gt)::value;
-                        k_dfsph_divergence<R, G, true><<<wblocks(), kBlock, 0, ls_>>>(
-                            f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_, sc_.p, lim_, partials_.p, h);
+                        run("k_dfsph_divergence", [&] { k_dfsph_divergence<R, G, true><<<wblocks(), kBlock, 0, ls_>>>(
+                            f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_, sc_.p, lim_, partials_.p, h); });
                     });
                 },
                 [&](cudaGraphConditionalHandle h) {
                     withG([&](auto gt) {
                         constexpr int G = decltype(gt)::value;
-                        k_dfsph_correct<R, G, 2><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_,
-                                                                                 sc_.p);
-                        k_dfsph_divergence<R, G, false><<<wblocks(), kBlock, 0, ls_>>>(
-                            f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_, sc_.p, lim_, partials_.p, h);
+                        run("k_dfsph_correct", [&] { k_dfsph_correct<R, G, 2><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_,
+                                                                                 sc_.p); });
+                        run("k_dfsph_divergence", [&] { k_dfsph_divergence<R, G, false><<<wblocks(), kBlock, 0, ls_>>>(
+                            f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_, sc_.p, lim_, partials_.p, h); });
                     });
                 },
                 lim_.minItV, lim_.maxIt);
             if (rc) return rc;
-            if (c_.has_cube) k_dfsph_cube<R><<<blocks(n_, 256), 256, 0, ls_>>>(f, gv_, hd_, c_);
+            if (c_.has_cube) run("k_dfsph_cube", [&] { k_dfsph_cube<R><<<blocks(n_, 256), 256, 0, ls_>>>(f, gv_, hd_, c_); });
         }
-        k_finish_step<<<1, 1, 0, ls_>>>(sc_.p);
+        run("k_finish_step", [&] { k_finish_step<<<1, 1, 0, ls_>>>(sc_.p); });
         SPH_CUDA(cudaGetLastError());
         return SPH_OK;
     }
@@ -703,13 +824,13 @@ private:
         const P4<R>* bp = bd_[1].pos;
         withG([&](auto gt) {
             constexpr int G = decltype(gt)::value;
-            k_wcsph_pressure_force<R, G><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_);
+            run("k_wcsph_pressure_force", [&] { k_wcsph_pressure_force<R, G><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_); });
         });
         SPH_CUDA(cudaGetLastError());
         rc = launch_npforces();
         if (rc) return rc;
-        k_integrate<R, false><<<blocks(n_, 256), 256, 0, ls_>>>(f, gv_, hd_, c_, sc_.p);
-        k_finish_step<<<1, 1, 0, ls_>>>(sc_.p);
+        run("k_integrate", [&] { k_integrate<R, false><<<blocks(n_, 256), 256, 0, ls_>>>(f, gv_, hd_, c_, sc_.p); });
+        run("k_finish_step", [&] { k_finish_step<<<1, 1, 0, ls_>>>(sc_.p); });
         SPH_CUDA(cudaGetLastError());
         return SPH_OK;
     }
@@ -725,24 +846,24 @@ private:
         if (rc) return rc;
         Fluid<R> f = F();
         const P4<R>* bp = bd_[1].pos;
-        k_pcisph_init<R><<<blocks(n_, 256), 256, 0, ls_>>>(f);
-        rc = solve_loop(
-            [&](cudaGraphConditionalHandle h) { k_pcisph_loop_begin<<<1, 1, 0, ls_>>>(sc_.p, lim_, h); },
+        run("k_pcisph_init", [&] { k_pcisph_init<R><<<blocks(n_, 256), 256, 0, ls_>>>(f); });
+        rc = solve_loop(1,
+            [&](cudaGraphConditionalHandle h) { run("k_pcisph_loop_begin", [&] { k_pcisph_loop_begin<<<1, 1, 0, ls_>>>(sc_.p, lim_, h); }); },
             [&](cudaGraphConditionalHandle h) {
-                k_pcisph_predict<R><<<blocks(n_, 256), 256, 0, ls_>>>(f, c_, sc_.p);
+                run("k_pcisph_predict", [&] { k_pcisph_predict<R><<<blocks(n_, 256), 256, 0, ls_>>>(f, c_, sc_.p); });
                 withG([&](auto gt) {
                     constexpr int G = decltype(gt)::value;
-                    k_pcisph_density_pressure<R, G><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_,
-                                                                                   akinci_, sc_.p, lim_, partials_.p);
-                    k_pcisph_pressure_acc<R, G><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_,
-                                                                               sc_.p);
+                    run("k_pcisph_density_pressure", [&] { k_pcisph_density_pressure<R, G><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_,
+                                                                                   akinci_, sc_.p, lim_, partials_.p); });
+                    run("k_pcisph_pressure_acc", [&] { k_pcisph_pressure_acc<R, G><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_,
+                                                                               sc_.p); });
                 });
-                k_pcisph_loop_next<<<1, 1, 0, ls_>>>(sc_.p, lim_, h);
+                run("k_pcisph_loop_next", [&] { k_pcisph_loop_next<<<1, 1, 0, ls_>>>(sc_.p, lim_, h); });
             },
             lim_.minIt, lim_.maxIt);
         if (rc) return rc;
-        k_integrate<R, true><<<blocks(n_, 256), 256, 0, ls_>>>(f, gv_, hd_, c_, sc_.p);
-        k_finish_step<<<1, 1, 0, ls_>>>(sc_.p);
+        run("k_integrate", [&] { k_integrate<R, true><<<blocks(n_, 256), 256, 0, ls_>>>(f, gv_, hd_, c_, sc_.p); });
+        run("k_finish_step", [&] { k_finish_step<<<1, 1, 0, ls_>>>(sc_.p); });
         SPH_CUDA(cudaGetLastError());
         return SPH_OK;
     }
@@ -764,8 +885,10 @@ private:
             cudaGraph_t g;
             SPH_CUDA(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
             capturing_ = true;
+            cap_count_[0] = cap_count_[1] = cap_count_[2] = 0;
             const int rc = one_step();
             capturing_ = false;
+            for (int q = 0; q < 3; ++q) gshape_[k][q] = cap_count_[q];
             cudaError_t e = cudaStreamEndCapture(st_, &g);
             if (rc) { if (e == cudaSuccess) cudaGraphDestroy(g); cur_ = k; return rc; }
             SPH_CUDA(e);
@@ -774,6 +897,7 @@ private:
             cur_ = k;  // capture recorded the swap; the launch performs it
         }
         SPH_CUDA(cudaGraphLaunch(gexec_[k], st_));
+        ++gsteps_[k];
         cur_ = 1 - k;
         return SPH_OK;
     }
@@ -792,13 +916,23 @@ private:
     int cur_ = 0;
     bool graph_ = false, capturing_ = false;
     cudaGraphExec_t gexec_[2] = {nullptr, nullptr};
+    int loop_ctx_ = 0;
+    unsigned cap_count_[3] = {0, 0, 0};
+    unsigned gshape_[2][3] = {{0, 0, 0}, {0, 0, 0}};
+    unsigned long long gsteps_[2] = {0, 0};
+    unsigned long long launches_ = 0, graph_launches_ = 0, snap_it_ = 0, snap_itv_ = 0;
+    bool prof_ = false;
+    cudaEvent_t tev_[2] = {nullptr, nullptr};
+    struct Timed { const char* name; cudaEvent_t a, b; };
+    std::vector<Timed> pending_;
+    std::vector<cudaEvent_t> events_;
     Fluid<R> fl_[2]{};
     Boundary<R> bd_[2]{};
     DevBuf<P4<R>> pos_[2], vel_[2], bpos_[2];
-    DevBuf<R> kappa_[2], kappav_[2];
+    DevBuf<R> kappa_[2], kappav_[2], pred_[2];
     DevBuf<uint32_t> cell_[2], id_[2], bcell_[2], bid_[2];
     DevBuf<P4<R>> acc_, xk_, predR_, predV_, pacc_, normal_;
-    DevBuf<R> rho_, alpha_, pred_, div_, press_, bpsi_;
+    DevBuf<R> rho_, alpha_, div_, press_, bpsi_;
     DevBuf<uint32_t> mortx_, morty_, key_, slot_, tmp_, count_, starts_, bstarts_, tile_sums_;
     DevBuf<double> partials_;
     DevBuf<DevScalars> sc_;

@@ -32,11 +32,15 @@ struct SceneBase {
     void fail(const std::string& m) { err = m; }
     virtual int init() = 0;
     virtual int step(int n) = 0;
+    virtual int step_timed(int n, float* ms) = 0;
     virtual int sync() = 0;
     virtual int set_graph(int on) = 0;
     virtual int download(int field, double* out) = 0;
     virtual int stats(sph_stats* s) = 0;
     virtual int neighbors(int* cells, int* rank, int* off, int* nbr, int* boff, int* bnbr, long long* totals) = 0;
+    virtual int launch_count(unsigned long long* out) = 0;
+    virtual int set_profiling(int on) = 0;
+    virtual int profile(char* buf, size_t len) = 0;
     virtual unsigned nfluid() const = 0;
     virtual unsigned nboundary() const = 0;
 };

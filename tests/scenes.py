@@ -27,19 +27,24 @@ def jitter(x, r, seed):
 
 
 SCENES = {
-    # DFSPH dam break with Akinci walls (the headline solver)
+    # DFSPH dam break with Akinci walls (the headline solver).  The block
+    # starts 2r off the walls: with its first layer at r from an Akinci wall
+    # the reference's DFSPH ejects wall particles at ~500 m/s in step 1.
     "dfsph_akinci": dict(
         params=dict(method=2, boundary=2, radius=0.02, eta=0.001, eta_v=0.001, cfl=1.0, dt=1e-4, min_dt=1e-5,
                     max_dt=5e-3, fps=60.0),
-        fluid=lambda: lattice(0.02, (0.0, 0.0, 0.0), (0.4, 0.4, 0.4)),
+        fluid=lambda: lattice(0.02, (0.04, 0.04, 0.04), (0.44, 0.44, 0.44)),
         boxes=[((0.0, 0.0, 0.0), (0.8, 0.6, 0.6))],
         spheres=[],
     ),
-    # DFSPH with a sphere obstacle and XSPH + surface tension + adhesion
+    # DFSPH with a sphere obstacle and XSPH + surface tension + adhesion.
+    # Jittered: the reference's cohesion kernel jumps by 2x at r = h/2
+    # (Cohesion.h:36-37 leaves valueCoef2 unscaled), exactly the lattice
+    # spacing, so an unjittered lattice makes last-bit rounding pick branches.
     "dfsph_forces": dict(
         params=dict(method=2, boundary=2, radius=0.02, visc_method=2, visc=0.01, bvisc=0.01, st_method=3, st=0.5,
                     adh_method=4, adh=0.1),
-        fluid=lambda: lattice(0.02, (0.05, 0.05, 0.05), (0.35, 0.35, 0.35)),
+        fluid=lambda: jitter(lattice(0.02, (0.05, 0.05, 0.05), (0.35, 0.35, 0.35)), 0.02, 11),
         boxes=[((0.0, 0.0, 0.0), (0.6, 0.6, 0.6))],
         spheres=[((0.3, 0.5, 0.3), 0.08)],
     ),
@@ -66,14 +71,17 @@ SCENES = {
         boxes=[((0.0, 0.0, 0.0), (0.5, 0.5, 0.5))],
         spheres=[((0.25, 0.05, 0.25), 0.05)],
     ),
-    # PCISPH drop with standard viscosity, surface tension, cohesion, adhesion
+    # PCISPH drop with standard viscosity, surface tension, cohesion, adhesion.
+    # The pool starts one lattice spacing off the walls: with its first layer
+    # at r from an Akinci wall the reference's own PCISPH blows up in the
+    # first step (Poly6-derived scaling factor, Spiky pressure gradient).
     "pcisph_drop": dict(
         params=dict(method=1, boundary=2, radius=0.02, eta=0.001, min_it=3, max_it=100, visc_method=0, visc=0.01,
                     bvisc=0.01, st_method=3, st=0.5, adh_method=4, adh=0.1),
-        fluid=lambda: np.concatenate([
-            lattice(0.02, (0.0, 0.0, 0.0), (0.6, 0.08, 0.6)),
+        fluid=lambda: jitter(np.concatenate([
+            lattice(0.02, (0.04, 0.04, 0.04), (0.56, 0.12, 0.56)),
             lattice(0.02, (0.2, 0.2, 0.2), (0.36, 0.36, 0.36)),
-        ]),
+        ]), 0.02, 5),
         boxes=[((0.0, 0.0, 0.0), (0.6, 0.6, 0.6))],
         spheres=[],
     ),
