@@ -160,6 +160,24 @@ int sph_ctx_set_graph(sph_ctx* ctx, int enable);
 int sph_ctx_num_particles(const sph_ctx* ctx, unsigned* num_fluid, unsigned* num_boundary);
 /* Copy a field to host memory in original particle order (FP64). */
 int sph_ctx_download(sph_ctx* ctx, int field, double* out);
+/* Same result as sph_ctx_download, without allocating device memory.  It has
+ * no counterpart in the reference (which keeps its fields in host vectors).
+ * For callers that cannot allocate on the device: a frame-export hook in a
+ * long-running serving process whose device memory is fully reserved for
+ * resident scenes, or a real-time driver that must not call cudaFree (it
+ * waits for the whole device).  sph_ctx_download allocates a staging buffer
+ * per call; this variant stages through one fixed 4 MiB device array inside
+ * the library instead.
+ *   - Limit: a field of at most 524,288 values (174,762 particles for
+ *     3-component fields); larger fields return SPH_ERR_CAPACITY.
+ *   - The array is held by every GPU that loads the library until exit.
+ *   - The first call on a device looks up the array's device address (with
+ *     the context's device current); make that first call before any stream
+ *     capture.
+ *   - All calls share the array: calls that overlap on the GPU (contexts used
+ *     from several host threads at once) race.  Each call writes every value
+ *     it returns, so nothing needs clearing between calls. */
+int sph_ctx_download_noalloc(sph_ctx* ctx, int field, double* out);
 int sph_ctx_get_stats(sph_ctx* ctx, sph_stats* out);
 const char* sph_ctx_last_error(const sph_ctx* ctx);
 

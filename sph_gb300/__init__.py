@@ -112,6 +112,7 @@ ABI = [
     ("sph_ctx_set_graph", ctypes.c_int, [_vp, ctypes.c_int]),
     ("sph_ctx_num_particles", ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_uint), ctypes.POINTER(ctypes.c_uint)]),
     ("sph_ctx_download", ctypes.c_int, [_vp, ctypes.c_int, _dp]),
+    ("sph_ctx_download_noalloc", ctypes.c_int, [_vp, ctypes.c_int, _dp]),
     ("sph_ctx_get_stats", ctypes.c_int, [_vp, ctypes.POINTER(Stats)]),
     ("sph_ctx_last_error", ctypes.c_char_p, [_vp]),
     ("sph_ctx_neighbors", ctypes.c_int, [_vp, _ip, _ip, _ip, _ip, _ip, _ip, ctypes.POINTER(ctypes.c_longlong)]),
@@ -290,6 +291,15 @@ class Scene:
         out = np.zeros((count, 3) if width == 3 else count)
         if count:
             self._check(lib().sph_ctx_download(self._h, fid, _d(out)), f"sph_ctx_download({field})")
+        return out
+
+    def get_noalloc(self, field):
+        """get() through sph_ctx_download_noalloc (fixed device staging array)."""
+        fid, width = FIELDS[field]
+        count = self.nb if field in ("bx", "psi") else self.n
+        out = np.zeros((count, 3) if width == 3 else count)
+        if count:
+            self._check(lib().sph_ctx_download_noalloc(self._h, fid, _d(out)), f"sph_ctx_download_noalloc({field})")
         return out
 
     def stats(self) -> dict:

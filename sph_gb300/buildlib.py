@@ -27,6 +27,7 @@ UNITS = {
     "sph_api.cu": [],
     "sph_scene_f32.cu": [],
     "sph_scene_f64.cu": ["-fmad=false"],
+    "sph_noalloc.cu": [],
 }
 HEADERS = ["sph_device.cuh", "sph_kernels.cuh", "sph_scene.cuh", "sph_scene_base.h"]
 

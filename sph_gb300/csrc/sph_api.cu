@@ -296,6 +296,15 @@ int sph_ctx_download(sph_ctx* ctx, int field, double* out)
     return relay(ctx, ctx->scene->download(field, out));
 }
 
+int sph_ctx_download_noalloc(sph_ctx* ctx, int field, double* out)
+{
+    if (!ctx || !out) return bad(ctx, "invalid argument");
+    std::string err;
+    const int rc = sph::download_noalloc(ctx->scene, field, out, &err);
+    if (rc != SPH_OK) ctx->err = err;
+    return rc;
+}
+
 int sph_ctx_get_stats(sph_ctx* ctx, sph_stats* out)
 {
     if (!ctx || !out) return bad(ctx, "invalid argument");

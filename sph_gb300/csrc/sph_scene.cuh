@@ -63,6 +63,7 @@ public:
         const int G = d.threads_per_particle;
         if (sizeof(R) == 8) G_ = 1;
         else G_ = (G == 2 || G == 4 || G == 8) ? G : 1;
+        SPH_CUDA(cudaGetDevice(&device_));
         SPH_CUDA(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
         SPH_CUDA(cudaStreamCreateWithFlags(&st2_, cudaStreamNonBlocking));
         ls_ = st_;
@@ -283,6 +284,43 @@ public:
         SPH_CUDA(cudaGetLastError());
         SPH_CUDA(cudaMemcpyAsync(out, o.p, count * 8, cudaMemcpyDeviceToHost, st_));
         SPH_CUDA(cudaStreamSynchronize(st_));
+        return SPH_OK;
+    }
+
+    int field_view(int field, FieldView* v) override
+    {
+        if (!inited) { fail("not initialised"); return SPH_ERR_INVALID; }
+        const bool bnd = field == SPH_FIELD_BOUNDARY_POSITION || field == SPH_FIELD_BOUNDARY_VOLUME;
+        Fluid<R> f = F();
+        Boundary<R> b = B(1);
+        FieldView o;
+        o.n = bnd ? nb_ : n_;
+        o.id = bnd ? b.id : f.id;
+        o.cell = bnd ? b.cell : f.cell;
+        switch (field) {
+            case SPH_FIELD_POSITION: o.v4 = f.pos; o.kind = 1; break;
+            case SPH_FIELD_VELOCITY: o.v4 = f.vel; break;
+            case SPH_FIELD_ACCELERATION: o.v4 = f.acc; break;
+            case SPH_FIELD_PRESSURE_ACC: o.v4 = f.pacc; break;
+            case SPH_FIELD_NORMAL: o.v4 = f.normal; break;
+            case SPH_FIELD_DENSITY: o.s = f.rho; o.kind = 2; break;
+            case SPH_FIELD_PRESSURE: o.s = f.press; o.kind = 2; break;
+            case SPH_FIELD_ALPHA: o.s = f.alpha; o.kind = 2; break;
+            case SPH_FIELD_PRED_DENSITY: o.s = f.pred; o.kind = 2; break;
+            case SPH_FIELD_DIV_ERROR: o.s = f.div; o.kind = 2; break;
+            case SPH_FIELD_KAPPA: o.s = f.kappa; o.kind = 2; break;
+            case SPH_FIELD_KAPPA_V: o.s = f.kappav; o.kind = 2; break;
+            case SPH_FIELD_BOUNDARY_POSITION: o.v4 = b.pos; o.kind = 1; break;
+            case SPH_FIELD_BOUNDARY_VOLUME: o.s = b.psi; o.kind = 2; break;
+            default: fail("unknown field"); return SPH_ERR_INVALID;
+        }
+        o.count = (size_t)o.n * (o.kind == 2 ? 1 : 3);
+        o.nx = gv_.nx; o.ny = gv_.ny; o.nz = gv_.nz; o.ox = gv_.ox; o.oy = gv_.oy; o.oz = gv_.oz;
+        o.h = hd_;
+        o.fp64 = sizeof(R) == 8;
+        o.device = device_;
+        o.stream = st_;
+        *v = o;
         return SPH_OK;
     }
 
@@ -911,6 +949,7 @@ private:
     double hd_ = 0, mass_ = 0;
     unsigned n_ = 0, nb_ = 0;
     int akinci_ = 0;
+    int device_ = 0;
     int G_ = 1;
     uint32_t nkeys_ = 0;
     int cur_ = 0;

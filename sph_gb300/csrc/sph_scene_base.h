@@ -2,6 +2,9 @@
 // numeric forms of the scene (sph_scene_f32.cu, sph_scene_f64.cu).
 #pragma once
 
+#include <cuda_runtime.h>
+#include <stdint.h>
+
 #include <string>
 #include <vector>
 
@@ -23,6 +26,23 @@ long long sample_box(double support_radius, const double mn[3], const double mx[
 long long sample_sphere(double particle_radius, const double c[3], double radius, double* out);
 long long fluid_block(double r, const double mn[3], const double mx[3], double* out);
 
+// Where a downloadable field lives on the device (sorted order), for
+// conversion kernels outside the scene's own translation unit.
+struct FieldView {
+    const void* v4 = nullptr;     // P4<R> array, or nullptr for scalar fields
+    const void* s = nullptr;      // R array for scalar fields
+    const uint32_t* id = nullptr;
+    const uint32_t* cell = nullptr;
+    int nx = 0, ny = 0, nz = 0, ox = 0, oy = 0, oz = 0;
+    double h = 0.0;
+    int kind = 0;                 // 0 vector, 1 position, 2 scalar
+    unsigned n = 0;               // points
+    size_t count = 0;             // doubles written
+    bool fp64 = false;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+};
+
 struct SceneBase {
     sph_scene_desc d{};
     std::string err;
@@ -38,6 +58,7 @@ struct SceneBase {
     virtual int download(int field, double* out) = 0;
     virtual int stats(sph_stats* s) = 0;
     virtual int neighbors(int* cells, int* rank, int* off, int* nbr, int* boff, int* bnbr, long long* totals) = 0;
+    virtual int field_view(int field, FieldView* v) = 0;
     virtual int launch_count(unsigned long long* out) = 0;
     virtual int set_profiling(int on) = 0;
     virtual int profile(char* buf, size_t len) = 0;
@@ -46,6 +67,8 @@ struct SceneBase {
 };
 
 SceneBase* make_scene_f32(const sph_scene_desc& d);
+// sph_noalloc.cu
+int download_noalloc(SceneBase* scene, int field, double* out, std::string* err);
 SceneBase* make_scene_f64(const sph_scene_desc& d);
 
 }  // namespace sph
