@@ -51,22 +51,26 @@ WORKLOADS = {
     ),
 }
 
-# Compulsory bytes per fluid particle of each kernel as implemented (FP32
-# form: float4 = 16 B, scalar = 4 B; each array read once and written once,
-# neighbour re-reads not counted); walks that visit boundary particles add
-# 16 B per boundary particle.
+# Compulsory bytes of each kernel as implemented (FP32 form: float4 = 16 B,
+# scalar = 4 B; each array read once and written once, neighbour re-reads not
+# counted): (bytes per fluid particle, bytes per stored pair, touches the
+# boundary particles at 16 B each).
 ALGO_BYTES = {
-    "k_cell_update": (64, False),
-    "k_scatter": (16, False),
-    "k_gather_fluid": (108, False),
-    "k_density": (32, True),
-    "k_dfsph_cfl": (32, False),
-    "k_dfsph_predict_v_warm": (108, False),
-    "k_dfsph_correct": (68, True),
-    "k_dfsph_predict_density": (64, True),
-    "k_dfsph_divergence": (64, True),
-    "k_npforce": (68, True),
-    "k_st_normals": (36, False),
+    "k_cell_update": (64, 0, False),
+    "k_scatter": (16, 0, False),
+    "k_gather_fluid": (108, 0, False),
+    "k_density": (32, 0, True),
+    "k_dfsph_cfl": (32, 0, False),
+    "k_dfsph_predict_v_warm": (108, 0, False),
+    "k_dfsph_correct": (68, 0, True),
+    "k_dfsph_predict_density": (64, 0, True),
+    "k_dfsph_divergence": (64, 0, True),
+    "k_npforce": (68, 0, True),
+    "k_st_normals": (36, 0, False),
+    "k_build_lists": (52, 16, True),
+    "k_dfsph_correct_list": (72, 16, False),
+    "k_dfsph_predict_density_list": (52, 16, False),
+    "k_dfsph_divergence_list": (52, 16, False),
 }
 
 
@@ -166,11 +170,11 @@ def dist_barrier(world):
         dist.barrier()
 
 
-def make_scene(wl, precision="f32", G=0):
+def make_scene(wl, precision="f32", G=0, list_max=64):
     import sph_gb300
 
     w = WORKLOADS[wl]
-    s = sph_gb300.Scene(precision=precision, threads_per_particle=G, **w["params"])
+    s = sph_gb300.Scene(precision=precision, threads_per_particle=G, neighbor_list_max=list_max, **w["params"])
     s.add_fluid_block(*w["block"])
     s.add_boundary_box(*w["box"])
     return s
@@ -230,6 +234,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="dfsph_dam_break_125k", choices=list(WORKLOADS))
     ap.add_argument("--threads-per-particle", type=int, default=0)
+    ap.add_argument("--list-max", type=int, default=64, help="pair-list slots per particle (0: cell walks)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=25.0, help="seconds of CPU baseline work")
     ap.add_argument("--ref-budget", type=float, default=90.0, help="seconds of reference-arm timed work")
@@ -249,7 +254,7 @@ def main():
     G = args.threads_per_particle
 
     # ---- device-resident timed region -------------------------------------
-    s = make_scene(args.workload, G=G)
+    s = make_scene(args.workload, G=G, list_max=args.list_max)
     s.init()
     s.set_graph(True)
     s.step(max(3, args.warmup))
@@ -292,8 +297,9 @@ def main():
     nb = s.nb
     kern = max(prof.items(), key=lambda kv: kv[1][1]) if prof else ("none", (1, 0.0))
     kname, (kcount, kms) = kern
-    per_b, touches_b = ALGO_BYTES.get(kname, (0, False))
-    bytes_launch = n * per_b + (nb * 16 if touches_b else 0)
+    per_b, per_pair, touches_b = ALGO_BYTES.get(kname, (0, 0, False))
+    pairs = s.stats()["list_pairs"]
+    bytes_launch = n * per_b + pairs * per_pair + (nb * 16 if touches_b else 0)
     avg_ms = kms / max(kcount, 1)
     achieved = bytes_launch / (avg_ms / 1000.0) / 1e9 if avg_ms > 0 else 0.0
     peak, peak_kind = load_peaks()
@@ -318,7 +324,7 @@ def main():
         e_steps = args.steps
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        e = sph_gb300.Scene(precision="f32", threads_per_particle=G, **w["params"])
+        e = sph_gb300.Scene(precision="f32", threads_per_particle=G, neighbor_list_max=args.list_max, **w["params"])
         e.set_fluid(x_host, v_host)
         e.add_boundary_box(*w["box"])
         e.init()
@@ -358,7 +364,8 @@ def main():
                        "step_timing": "CUDA events on the scene's stream around each graph-launched step",
                        "mean_density_iterations": its, "mean_divergence_iterations": itsv,
                        "simulated_seconds_per_second": sim_s / (total_ms / 1000.0),
-                       "threads_per_particle": G or 1, "wall_s": wall},
+                       "threads_per_particle": G or 1, "neighbor_list_max": args.list_max,
+                       "list_pairs": st1["list_pairs"], "list_overflow": st1["list_overflow"], "wall_s": wall},
             "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
                          "algorithmic_bytes_per_launch": bytes_launch, "avg_launch_ms": avg_ms,

@@ -101,6 +101,9 @@ typedef struct sph_scene_desc {
     double cube_min[3], cube_max[3];
     double domain_min[3], domain_max[3]; /* grid box; equal min/max: derive from the points */
     int threads_per_particle;     /* 1, 2, 4, 8 (FP32); 0: default */
+    int neighbor_list_max;        /* DFSPH: > 0 builds per-particle pair lists with this many
+                                     slots after each grid build and runs the solver walks over
+                                     them; 0 walks the 27 cells in every pass */
 } sph_scene_desc;
 
 typedef struct sph_stats {
@@ -116,6 +119,8 @@ typedef struct sph_stats {
     unsigned status;              /* SPH_STATUS_* bits, sticky */
     unsigned long long sum_iterations, sum_iterations_v;
     unsigned num_fluid, num_boundary;
+    unsigned long long list_pairs; /* DFSPH pair lists: stored pairs (0 without lists) */
+    unsigned list_overflow;       /* particles whose neighbours exceed neighbor_list_max */
 } sph_stats;
 
 /* Defaults of the reference (SPHSolver.cpp:12-19, DFSPHSolver.cpp:10-22,

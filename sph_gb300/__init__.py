@@ -71,6 +71,7 @@ class SceneDesc(ctypes.Structure):
         ("domain_min", ctypes.c_double * 3),
         ("domain_max", ctypes.c_double * 3),
         ("threads_per_particle", ctypes.c_int),
+        ("neighbor_list_max", ctypes.c_int),
     ]
 
 
@@ -90,6 +91,8 @@ class Stats(ctypes.Structure):
         ("sum_iterations_v", ctypes.c_ulonglong),
         ("num_fluid", ctypes.c_uint),
         ("num_boundary", ctypes.c_uint),
+        ("list_pairs", ctypes.c_ulonglong),
+        ("list_overflow", ctypes.c_uint),
     ]
 
 
@@ -176,6 +179,7 @@ _PARAM_MAP = {
     "visc": "viscosity", "bvisc": "boundary_viscosity", "st_method": "surface_tension_method",
     "st": "surface_tension", "adh_method": "adhesion_method", "adh": "adhesion", "has_cube": "has_cube",
     "precision": "precision", "threads_per_particle": "threads_per_particle",
+    "neighbor_list_max": "neighbor_list_max",
 }
 _VEC = {"gravity", "cube_min", "cube_max", "domain_min", "domain_max"}
 

@@ -139,6 +139,7 @@ int sph_scene_desc_init(sph_scene_desc* d)
     d->adhesion_method = -1;
     d->cube_max[0] = d->cube_max[1] = d->cube_max[2] = 1.0;
     d->threads_per_particle = 0;
+    d->neighbor_list_max = 64;
     return SPH_OK;
 }
 

@@ -126,7 +126,17 @@ __device__ __forceinline__ uint32_t cell_key(const GridView& g, int cx, int cy, 
 
 // Visit every candidate j of the 27 cells around the particle's cell, calling
 // f(j, s) with s the particle's position expressed in the frame of j's cell
-// (so that r_ij = s - pos_j).  Threads of a group of G lanes split each range.
+// (so that r_ij = s - pos_j), in the reference's x -> y -> z cell order.
+//
+// One lane per particle (G == 1): the cell starts of all nine neighbour
+// columns are fetched first (independent loads, one latency instead of nine
+// chained ones), then each column's contiguous particle range is streamed;
+// in the cell-relative form the frame of candidate j (its z cell within the
+// column) is picked by comparing j with the column's two inner cell starts.
+// Columns and z-cells whose box lies farther than h from the particle are
+// skipped: they hold no neighbour, and every smoothing kernel is zero there,
+// so the sums are those of the full 27-cell walk.
+// G > 1 lanes split each cell's range (lane l takes every G-th candidate).
 template <typename R, int G, typename F>
 __device__ __forceinline__ void walk(const GridView& g, const uint32_t* __restrict__ starts, uint32_t pc, V3<R> xi, R h,
                                      int lane, F&& f)
@@ -135,28 +145,80 @@ __device__ __forceinline__ void walk(const GridView& g, const uint32_t* __restri
     const int cx = cell_x(pc), cy = cell_y(pc), cz = cell_z(pc);
     const int z0 = cz > 0 ? cz - 1 : 0;
     const int z1 = cz + 1 < g.nz ? cz + 1 : g.nz - 1;
+    if constexpr (G == 1) {
+        // the particle's offset inside its own cell, and the squared gap from
+        // it to each neighbour layer (0 for its own layer): a cell whose box
+        // is farther than h from the particle holds no neighbour
+        const R ofx = REL ? xi.x : xi.x - (R)(cx + g.ox) * h;
+        const R ofy = REL ? xi.y : xi.y - (R)(cy + g.oy) * h;
+        const R ofz = REL ? xi.z : xi.z - (R)(cz + g.oz) * h;
+        const R gxm = ofx > (R)0 ? ofx * ofx : (R)0, gxp = h - ofx > (R)0 ? (h - ofx) * (h - ofx) : (R)0;
+        const R gym = ofy > (R)0 ? ofy * ofy : (R)0, gyp = h - ofy > (R)0 ? (h - ofy) * (h - ofy) : (R)0;
+        const R gzm = ofz > (R)0 ? ofz * ofz : (R)0, gzp = h - ofz > (R)0 ? (h - ofz) * (h - ofz) : (R)0;
+        const R lim = h * h * (R)(1.0 + 1e-5);
+        uint32_t b[9], m0[9], m1[9], e[9];
 #pragma unroll
-    for (int dx = -1; dx <= 1; ++dx) {
-        const int x = cx + dx;
-        if (x < 0 || x >= g.nx) continue;
-        const uint32_t mx = __ldg(g.mortx + x);
+        for (int dx = -1; dx <= 1; ++dx) {
+            const int x = cx + dx;
+            const bool okx = x >= 0 && x < g.nx;
+            const uint32_t mx = okx ? __ldg(g.mortx + x) : 0u;
+            const R gx = dx < 0 ? gxm : (dx > 0 ? gxp : (R)0);
 #pragma unroll
-        for (int dy = -1; dy <= 1; ++dy) {
-            const int y = cy + dy;
-            if (y < 0 || y >= g.ny) continue;
-            const uint32_t base = (mx | __ldg(g.morty + y)) * (uint32_t)g.nz;
-            if constexpr (REL) {
-                const R sx = xi.x - (R)dx * h, sy = xi.y - (R)dy * h;
-                uint32_t b = __ldg(starts + base + z0);
-                for (int z = z0; z <= z1; ++z) {
-                    const uint32_t e = __ldg(starts + base + z + 1);
-                    const V3<R> s = {sx, sy, xi.z - (R)(z - cz) * h};
-                    for (uint32_t j = b + lane; j < e; j += G) f(j, s);
-                    b = e;
+            for (int dy = -1; dy <= 1; ++dy) {
+                const int c = (dx + 1) * 3 + (dy + 1);
+                const int y = cy + dy;
+                const R gxy = gx + (dy < 0 ? gym : (dy > 0 ? gyp : (R)0));
+                const bool ok = okx && y >= 0 && y < g.ny && gxy <= lim;
+                const uint32_t base = ok ? (mx | __ldg(g.morty + y)) * (uint32_t)g.nz : 0u;
+                if (ok) {
+                    const uint32_t s0 = __ldg(starts + base + z0), sm = __ldg(starts + base + cz);
+                    const uint32_t sp = __ldg(starts + base + cz + 1), s1 = __ldg(starts + base + z1 + 1);
+                    b[c] = gxy + gzm <= lim ? s0 : sm;   // cell cz-1 only if within reach
+                    e[c] = gxy + gzp <= lim ? s1 : sp;   // cell cz+1 only if within reach
+                    m0[c] = sm;
+                    m1[c] = sp;
+                } else {
+                    b[c] = 0u; e[c] = 0u; m0[c] = 0u; m1[c] = 0u;
                 }
-            } else {
-                const uint32_t b = __ldg(starts + base + z0), e = __ldg(starts + base + z1 + 1);
-                for (uint32_t j = b + lane; j < e; j += G) f(j, xi);
+            }
+        }
+        const R szm = xi.z + h, sz0 = xi.z, szp = xi.z - h;  // frames of cells cz-1, cz, cz+1
+#pragma unroll
+        for (int c = 0; c < 9; ++c) {
+            const int dx = c / 3 - 1, dy = c % 3 - 1;
+            // absolute form: every candidate is compared with xi itself
+            V3<R> s = REL ? V3<R>{xi.x - (R)dx * h, xi.y - (R)dy * h, xi.z} : xi;
+            const uint32_t bb = b[c], ee = e[c];
+#pragma unroll 2
+            for (uint32_t j = bb; j < ee; ++j) {
+                if (REL) s.z = j < m0[c] ? szm : (j < m1[c] ? sz0 : szp);
+                f(j, s);
+            }
+        }
+    } else {
+#pragma unroll
+        for (int dx = -1; dx <= 1; ++dx) {
+            const int x = cx + dx;
+            if (x < 0 || x >= g.nx) continue;
+            const uint32_t mx = __ldg(g.mortx + x);
+#pragma unroll
+            for (int dy = -1; dy <= 1; ++dy) {
+                const int y = cy + dy;
+                if (y < 0 || y >= g.ny) continue;
+                const uint32_t base = (mx | __ldg(g.morty + y)) * (uint32_t)g.nz;
+                if constexpr (REL) {
+                    const R sx = xi.x - (R)dx * h, sy = xi.y - (R)dy * h;
+                    uint32_t bz = __ldg(starts + base + z0);
+                    for (int z = z0; z <= z1; ++z) {
+                        const uint32_t ez = __ldg(starts + base + z + 1);
+                        const V3<R> s = {sx, sy, xi.z - (R)(z - cz) * h};
+                        for (uint32_t j = bz + lane; j < ez; j += G) f(j, s);
+                        bz = ez;
+                    }
+                } else {
+                    const uint32_t bz = __ldg(starts + base + z0), ez = __ldg(starts + base + z1 + 1);
+                    for (uint32_t j = bz + lane; j < ez; j += G) f(j, xi);
+                }
             }
         }
     }

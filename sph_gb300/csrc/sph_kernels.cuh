@@ -1077,6 +1077,17 @@ static __global__ void k_pcisph_loop_next(DevScalars* sc, LoopLimits lim, cudaGr
     if (cond) cudaGraphSetConditional(cond, sc->active);
 }
 
+// Pair-list occupancy for the statistics: stored pairs and overflowing particles.
+static __global__ void k_list_stats(uint32_t n, const uint32_t* __restrict__ count, uint32_t kmax,
+                                    unsigned long long* out)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t c = count[i];
+    atomicAdd(out, (unsigned long long)(c < kmax ? c : kmax));
+    if (c > kmax) atomicAdd(out + 1, 1ull);
+}
+
 // Simulation::step bookkeeping: time += dt, steps++ (DFSPHSolver.cpp:111).
 static __global__ void k_finish_step(DevScalars* sc)
 {

@@ -1,0 +1,378 @@
+// Pair lists for the DFSPH solves.
+//
+// Between two grid builds the DFSPH step never moves a particle: the
+// divergence solve, the next step's warm start and its density solve all run
+// at the positions of the last build (DFSPHSolver.cpp:63-97).  So right after
+// each build one 27-cell walk computes the densities and alpha factors
+// (SPHSolver.cpp:44-91, DFSPHSolver.cpp:114-189) and records, per particle,
+// every fluid neighbour with a non-zero kernel gradient together with
+// m * gradW_ij, plus the summed Akinci boundary gradient
+// sum_b rho0 psi_b gradW_ib.  The solver walks then read those lists instead
+// of rescanning ~216 candidates and re-evaluating the kernel per pair.
+//
+// Layout: slot-major, pairs[k * n + i] = {m gradW_ij, as_float(j)}, so the
+// threads of a warp (consecutive particles) read one contiguous 16-byte line
+// per slot.  A particle with more than kmax neighbours keeps its count and
+// falls back to the cell walk in every list kernel.
+//
+// Neighbours are listed in the cell walk's order, so each fluid sum adds the
+// same non-zero terms in the same order as the reference; the boundary sum is
+// pre-added once per build (a re-association of the reference's boundary
+// terms, which all share the factor of particle i).
+#pragma once
+
+#include "sph_kernels.cuh"
+
+namespace sph {
+
+template <typename R> struct Lists {
+    P4<R>* pairs;       // kmax * n, slot-major: {m gradW_ij, as-bits j}
+    uint32_t* count;    // neighbours with a non-zero gradient (may exceed kmax)
+    P4<R>* bgrad;       // xyz: sum_b rho0 psi_b gradW_ib
+    R* kbuf;            // k (or kv) of the pass in progress
+    uint32_t kmax;
+};
+
+__device__ __forceinline__ float idx_as(float, uint32_t j) { return __uint_as_float(j); }
+__device__ __forceinline__ double idx_as(double, uint32_t j) { return __longlong_as_double((long long)j); }
+__device__ __forceinline__ uint32_t as_idx(float w) { return __float_as_uint(w); }
+__device__ __forceinline__ uint32_t as_idx(double w) { return (uint32_t)__double_as_longlong(w); }
+
+// Densities + alpha + the lists, one thread per particle, in two phases:
+// the cell walk only culls candidates (distance test) and queues the
+// accepted indices in shared memory; the kernel values are then evaluated in
+// a dense loop over the queue.  (Evaluating inside the walk makes each warp
+// execute the expensive branch on nearly every candidate, since some lane
+// almost always accepts.)  A particle whose queue overflows is evaluated
+// inside the walk instead.
+constexpr uint32_t kQueue = 64;
+
+template <typename R>
+__device__ __forceinline__ V3<R> pair_vec(V3<R> xi, uint32_t ci, const P4<R>& pj, uint32_t cj, R h)
+{
+    if constexpr (sizeof(R) == 4) {
+        const V3<R> s = {xi.x - (R)(cell_x(cj) - cell_x(ci)) * h, xi.y - (R)(cell_y(cj) - cell_y(ci)) * h,
+                         xi.z - (R)(cell_z(cj) - cell_z(ci)) * h};
+        return s - xyz(pj);
+    } else {
+        return xi - xyz(pj);
+    }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kBlock, 7) k_build_lists(Fluid<R> f, const P4<R>* __restrict__ bpos, GridView g,
+                                                        const uint32_t* __restrict__ cs, const uint32_t* __restrict__ bs,
+                                                        Consts<R> c, int akinci, Lists<R> L)
+{
+    __shared__ uint32_t q[kQueue * kBlock];
+    const uint32_t i = gtid();
+    if (i >= f.n) return;
+    const uint32_t n = f.n;
+    const V3<R> xi = xyz(f.pos[i]);
+    const uint32_t pc = f.cell[i];
+    const uint32_t qcap = L.kmax < kQueue ? L.kmax : kQueue;
+    R density = 0, sumSq = 0;
+    V3<R> sumGrad = {0, 0, 0};
+    uint32_t cnt = 0;
+    auto accept = [&](uint32_t j, V3<R> r, R r2) {
+        density += c.mass * cubic_W(c, sqrt(r2));
+        const V3<R> mg = c.mass * cubic_gradW(c, r, r2);
+        const R mg2 = dot3(mg, mg);
+        if (mg2 > (R)0) {
+            sumGrad = sumGrad + mg;
+            if constexpr (sizeof(R) == 8) {
+                const R m = sqrt(mg2);
+                sumSq += m * m;
+            } else {
+                sumSq += mg2;
+            }
+            if (cnt < L.kmax) L.pairs[(size_t)cnt * n + i] = P4<R>{mg.x, mg.y, mg.z, idx_as(R(0), j)};
+            ++cnt;
+        }
+    };
+    // phase 1: cull
+    uint32_t nq = 0;
+    walk<R, 1>(g, cs, pc, xi, c.h, 0, [&](uint32_t j, V3<R> s) {
+        const V3<R> r = s - xyz(ldg4(f.pos + j));
+        if (dot3(r, r) <= c.cull2) {
+            if (nq < qcap) q[nq * kBlock + threadIdx.x] = j;
+            ++nq;
+        }
+    });
+    if (nq <= qcap) {
+        // phase 2: evaluate the queued candidates in walk order
+        for (uint32_t k = 0; k < nq; ++k) {
+            const uint32_t j = q[k * kBlock + threadIdx.x];
+            const V3<R> r = pair_vec(xi, pc, ldg4(f.pos + j), __ldg(f.cell + j), c.h);
+            accept(j, r, dot3(r, r));
+        }
+    } else {
+        walk<R, 1>(g, cs, pc, xi, c.h, 0, [&](uint32_t j, V3<R> s) {
+            const V3<R> r = s - xyz(ldg4(f.pos + j));
+            const R r2 = dot3(r, r);
+            if (r2 <= c.cull2) accept(j, r, r2);
+        });
+    }
+    V3<R> bg = {0, 0, 0};
+    if (akinci)
+        walk<R, 1>(g, bs, pc, xi, c.h, 0, [&](uint32_t j, V3<R> s) {
+            const P4<R> pb = ldg4(bpos + j);
+            const V3<R> r = s - xyz(pb);
+            const R r2 = dot3(r, r);
+            if (!(r2 <= c.cull2)) return;
+            density += pb.w * cubic_W(c, sqrt(r2));
+            bg = bg + pb.w * cubic_gradW(c, r, r2);
+        });
+    sumGrad = sumGrad + bg;
+    f.rho[i] = density;
+    f.vel[i].w = density;
+    R den;
+    if constexpr (sizeof(R) == 8) {
+        const R m = sqrt(dot3(sumGrad, sumGrad));
+        den = m * m + sumSq;
+    } else {
+        den = dot3(sumGrad, sumGrad) + sumSq;
+    }
+    f.alpha[i] = (fabs(den) > c.eps) ? density / den : (R)0;
+    L.count[i] = cnt;
+    L.bgrad[i] = P4<R>{bg.x, bg.y, bg.z, 0};
+}
+
+// ---- cell-walk fallbacks for particles whose list overflowed -------------
+
+template <typename R, int MODE>
+__device__ V3<R> correct_sum_cells(const Fluid<R>& f, const P4<R>* __restrict__ bpos, const GridView& g,
+                                   const uint32_t* __restrict__ cs, const uint32_t* __restrict__ bs, const Consts<R>& c,
+                                   int akinci, uint32_t i, R ki, const R* __restrict__ kbuf)
+{
+    V3<R> sum = {0, 0, 0};
+    const V3<R> xi = xyz(f.pos[i]);
+    const uint32_t pc = f.cell[i];
+    walk<R, 1>(g, cs, pc, xi, c.h, 0, [&](uint32_t j, V3<R> s) {
+        const R kSum = ki + kbuf[j];
+        if (!(fabs(kSum) > c.eps)) return;
+        const V3<R> r = s - xyz(ldg4(f.pos + j));
+        const R r2 = dot3(r, r);
+        if (r2 <= c.cull2) sum = sum + (c.mass * kSum) * cubic_gradW(c, r, r2);
+    });
+    const R kb = MODE == 0 ? (R)2 * ki : ki;
+    if (akinci && fabs(kb) > c.eps)
+        walk<R, 1>(g, bs, pc, xi, c.h, 0, [&](uint32_t j, V3<R> s) {
+            const P4<R> pb = ldg4(bpos + j);
+            const V3<R> r = s - xyz(pb);
+            const R r2 = dot3(r, r);
+            if (r2 <= c.cull2) sum = sum + (pb.w * kb) * cubic_gradW(c, r, r2);
+        });
+    return sum;
+}
+
+template <typename R>
+__device__ R velocity_div_cells(const Fluid<R>& f, const P4<R>* __restrict__ bpos, const GridView& g,
+                                const uint32_t* __restrict__ cs, const uint32_t* __restrict__ bs, const Consts<R>& c,
+                                int akinci, uint32_t i, V3<R> vi, uint32_t* nn)
+{
+    R dv = 0;
+    unsigned cnt = 0;
+    const V3<R> xi = xyz(f.pos[i]);
+    const uint32_t pc = f.cell[i];
+    walk<R, 1>(g, cs, pc, xi, c.h, 0, [&](uint32_t j, V3<R> s) {
+        const V3<R> r = s - xyz(ldg4(f.pos + j));
+        const R r2 = dot3(r, r);
+        if (r2 <= c.cull2) {
+            const V3<R> gr = cubic_gradW(c, r, r2);
+            dv += c.mass * dot3(vi - xyz(ldg4(f.vel + j)), gr);
+            if (dot3(gr, gr) > (R)0) cnt++;
+        }
+    });
+    if (akinci)
+        walk<R, 1>(g, bs, pc, xi, c.h, 0, [&](uint32_t j, V3<R> s) {
+            const P4<R> pb = ldg4(bpos + j);
+            const V3<R> r = s - xyz(pb);
+            const R r2 = dot3(r, r);
+            if (r2 <= c.cull2) dv += pb.w * dot3(vi, cubic_gradW(c, r, r2));
+        });
+    *nn = cnt;
+    return dv;
+}
+
+// ---- list walks ------------------------------------------------------------
+
+// DFSPH velocity corrections (MODE 0 warm start, 1 density, 2 divergence),
+// as k_dfsph_correct but over the pair lists; kbuf holds this pass's k.
+template <typename R, int MODE>
+__global__ void __launch_bounds__(kBlock, 8) k_dfsph_correct_list(Fluid<R> f, const P4<R>* __restrict__ bpos, GridView g,
+                                                               const uint32_t* __restrict__ cs, const uint32_t* __restrict__ bs,
+                                                               Consts<R> c, int akinci, const DevScalars* __restrict__ sc,
+                                                               Lists<R> L)
+{
+    if (MODE != 0 && !sc->active) return;
+    const uint32_t i = gtid();
+    if (i >= f.n) return;
+    const uint32_t n = f.n;
+    const R* __restrict__ kb_ = L.kbuf;
+    const R ki = kb_[i];
+    const uint32_t cnt = L.count[i];
+    V3<R> sum = {0, 0, 0};
+    if (cnt <= L.kmax) {
+        const P4<R>* __restrict__ p = L.pairs + i;
+#pragma unroll 4
+        for (uint32_t k = 0; k < cnt; ++k) {
+            const P4<R> q = ldg4(p + (size_t)k * n);
+            const R kSum = ki + __ldg(kb_ + as_idx(q.w));
+            if (fabs(kSum) > c.eps) sum = sum + kSum * xyz(q);
+        }
+        const R kb = MODE == 0 ? (R)2 * ki : ki;
+        if (akinci && fabs(kb) > c.eps) sum = sum + kb * xyz(L.bgrad[i]);
+    } else {
+        sum = correct_sum_cells<R, MODE>(f, bpos, g, cs, bs, c, akinci, i, ki, kb_);
+    }
+    const R dt = (R)sc->dt;
+    if (MODE == 1) f.kappa[i] += (f.pred[i] - c.density0) * f.alpha[i];
+    if (MODE == 2) f.kappav[i] += f.div[i] * f.alpha[i];
+    P4<R> v = f.vel[i];
+    if (MODE == 0) { v.x -= sum.x * dt; v.y -= sum.y * dt; v.z -= sum.z * dt; }
+    else { v.x -= dt * sum.x; v.y -= dt * sum.y; v.z -= dt * sum.z; }
+    f.vel[i] = v;
+}
+
+// Sum over the list of m (v_i - v_j) . gradW_ij plus the boundary term.
+template <typename R>
+__device__ __forceinline__ R velocity_div_list(const Fluid<R>& f, const Lists<R>& L, uint32_t i, V3<R> vi, int akinci)
+{
+    const uint32_t n = f.n;
+    const uint32_t cnt = L.count[i];
+    const P4<R>* __restrict__ p = L.pairs + i;
+    R d = 0;
+#pragma unroll 4
+    for (uint32_t k = 0; k < cnt; ++k) {
+        const P4<R> q = ldg4(p + (size_t)k * n);
+        d += dot3(vi - xyz(ldg4(f.vel + as_idx(q.w))), xyz(q));
+    }
+    if (akinci) d += dot3(vi, xyz(L.bgrad[i]));
+    return d;
+}
+
+// DFSPHSolver::predictDensities over the lists (+ loop control, as
+// k_dfsph_predict_density).
+template <typename R, bool INITIAL>
+__global__ void __launch_bounds__(kBlock, 8) k_dfsph_predict_density_list(Fluid<R> f, const P4<R>* __restrict__ bpos, GridView g,
+                                                                       const uint32_t* __restrict__ cs, const uint32_t* __restrict__ bs,
+                                                                       Consts<R> c, int akinci, DevScalars* sc, LoopLimits lim,
+                                                                       double* partials, cudaGraphConditionalHandle cond,
+                                                                       Lists<R> L)
+{
+    __shared__ double sh[33];
+    if (!INITIAL && !sc->active) return;
+    const uint32_t i = gtid();
+    double err = 0.0;
+    if (i < f.n) {
+        const V3<R> vi = xyz(f.vel[i]);
+        R dc;
+        if (L.count[i] <= L.kmax) {
+            dc = velocity_div_list(f, L, i, vi, akinci);
+        } else {
+            uint32_t nn;
+            dc = velocity_div_cells(f, bpos, g, cs, bs, c, akinci, i, vi, &nn);
+        }
+        const R dt = (R)sc->dt;
+        const R rho = f.rho[i];
+        R pred = rho + dc * dt;
+        pred = pred < c.density0 ? c.density0 : pred;
+        f.pred[i] = pred;
+        L.kbuf[i] = (pred - c.density0) * f.alpha[i] / ((dt * dt) * rho);
+        err = ((double)pred - (double)c.density0) / (double)c.density0;
+    }
+    double total;
+    if (finish_reduction<false>(err, partials, &sc->block_counter, sh, &total) && threadIdx.x == 0) {
+        const double avg = f.n ? total / (double)f.n : 0.0;
+        if (!(avg == avg)) sc->status |= ST_NONFINITE;
+        if (INITIAL) {
+            sc->iterations = 0;
+            sc->avgDensError = avg;
+            sc->active = (lim.minIt > 0u) && (lim.maxIt > 0u);
+            if (!sc->active) sc->avgDensError = 0.0;
+        } else {
+            const unsigned it = ++sc->iterations;
+            sc->avgDensError = avg;
+            const unsigned act = ((avg > lim.maxError) || (it < lim.minIt)) && (it < lim.maxIt);
+            sc->active = act;
+            if (!act) {
+                sc->sumIterations += it;
+                if (it >= lim.maxIt && avg > lim.maxError) sc->status |= ST_ITER_CAP;
+            }
+        }
+        if (cond) cudaGraphSetConditional(cond, sc->active);
+    }
+}
+
+// DFSPHSolver::computeDivergenceError over the lists (+ loop control).
+template <typename R, bool INITIAL>
+__global__ void __launch_bounds__(kBlock, 8) k_dfsph_divergence_list(Fluid<R> f, const P4<R>* __restrict__ bpos, GridView g,
+                                                                  const uint32_t* __restrict__ cs, const uint32_t* __restrict__ bs,
+                                                                  Consts<R> c, int akinci, DevScalars* sc, LoopLimits lim,
+                                                                  double* partials, cudaGraphConditionalHandle cond,
+                                                                  Lists<R> L)
+{
+    __shared__ double sh[33];
+    if (!INITIAL && !sc->active) return;
+    const uint32_t i = gtid();
+    double err = 0.0;
+    if (i < f.n) {
+        const V3<R> vi = xyz(f.vel[i]);
+        const uint32_t cnt = L.count[i];
+        R dv;
+        uint32_t nn = cnt;
+        if (cnt <= L.kmax) dv = velocity_div_list(f, L, i, vi, akinci);
+        else dv = velocity_div_cells(f, bpos, g, cs, bs, c, akinci, i, vi, &nn);
+        const R dt = (R)sc->dt;
+        dv = nn < 20u ? (R)0 : (dv < (R)0 ? (R)0 : dv);
+        f.div[i] = dv;
+        L.kbuf[i] = dv * f.alpha[i] / (dt * f.rho[i]);
+        err = (double)dv / (double)c.density0;
+    }
+    double total;
+    if (finish_reduction<false>(err, partials, &sc->block_counter, sh, &total) && threadIdx.x == 0) {
+        const double avg = total / (double)f.n;
+        const double lim_v = lim.maxErrorV / sc->dt;
+        if (!(avg == avg)) sc->status |= ST_NONFINITE;
+        if (INITIAL) {
+            sc->iterationsV = 0;
+            sc->avgDivError = avg;
+            sc->active = (lim.minItV > 0u) && (lim.maxIt > 0u);
+            if (!sc->active) sc->avgDivError = 0.0;
+        } else {
+            const unsigned it = ++sc->iterationsV;
+            sc->avgDivError = avg;
+            const unsigned act = ((avg > lim_v) || (it < lim.minItV)) && (it < lim.maxIt);
+            sc->active = act;
+            if (!act) {
+                sc->sumIterationsV += it;
+                if (it >= lim.maxIt && avg > lim_v) sc->status |= ST_ITER_CAP_V;
+            }
+        }
+        if (cond) cudaGraphSetConditional(cond, sc->active);
+    }
+}
+
+// Warm-start scaling (as k_dfsph_predict_v_warm) writing k to the list
+// pass's kbuf.
+template <typename R>
+__global__ void k_dfsph_predict_v_warm_list(Fluid<R> f, Consts<R> c, const DevScalars* __restrict__ sc, R* __restrict__ kbuf)
+{
+    const uint32_t i = gtid();
+    if (i >= f.n) return;
+    const R dt = (R)sc->dt;
+    P4<R> v = f.vel[i];
+    const P4<R> a = f.acc[i];
+    v.x = v.x + (a.x + c.gx) * dt; v.y = v.y + (a.y + c.gy) * dt; v.z = v.z + (a.z + c.gz) * dt;
+    f.vel[i] = v;
+    f.acc[i] = P4<R>{0, 0, 0, 0};
+    const R dens = f.rho[i];
+    const R ts2 = dt * dt;
+    const R t = -f.kappa[i] / dens;
+    const R mx = t < (R)-0.000000001 ? (R)-0.000000001 : t;
+    kbuf[i] = -mx / ts2;
+    f.kappa[i] = 0;
+}
+
+}  // namespace sph

@@ -22,6 +22,7 @@
 
 #include "sph_scene_base.h"
 #include "sph_kernels.cuh"
+#include "sph_lists.cuh"
 
 namespace sph {
 
@@ -118,7 +119,7 @@ public:
         if (rc) return rc;
         if (d.simulation_method == SPH_DFSPH) {
             // DFSPHSolver::init DFSPHSolver.cpp:24-36
-            rc = launch_density(true, false);
+            rc = lists_ ? launch_build_lists() : launch_density(true, false);
             if (rc) return rc;
         }
         SPH_CUDA(cudaStreamSynchronize(st_));
@@ -327,10 +328,19 @@ public:
     int stats(sph_stats* out) override
     {
         if (!inited) { fail("not initialised"); return SPH_ERR_INVALID; }
+        unsigned long long ls[2] = {0, 0};
+        if (lists_) {
+            SPH_CUDA(cudaMemsetAsync(lstat_.p, 0, 2 * sizeof(unsigned long long), st_));
+            k_list_stats<<<blocks(n_, 256), 256, 0, st_>>>(n_, lcount_.p, kmax_, lstat_.p);
+            SPH_CUDA(cudaGetLastError());
+            SPH_CUDA(cudaMemcpyAsync(ls, lstat_.p, sizeof ls, cudaMemcpyDeviceToHost, st_));
+        }
         SPH_CUDA(cudaMemcpyAsync(h_sc_, sc_.p, sizeof(DevScalars), cudaMemcpyDeviceToHost, st_));
         SPH_CUDA(cudaStreamSynchronize(st_));
         const DevScalars& s = *h_sc_;
         std::memset(out, 0, sizeof *out);
+        out->list_pairs = ls[0];
+        out->list_overflow = (unsigned)ls[1];
         out->time = s.time;
         out->dt = s.dt;
         out->avg_density_error = s.avgDensError;
@@ -401,6 +411,7 @@ private:
     static unsigned blocks(size_t n, unsigned b) { return (unsigned)std::max<size_t>(1, (n + b - 1) / b); }
 
     Fluid<R> F() const { return fl_[cur_]; }
+    Lists<R> LS() const { return Lists<R>{pairs_.p, lcount_.p, bgrad_.p, kbuf_.p, kmax_}; }
     Boundary<R> B(int k) const { return bd_[k]; }
 
     // Kernel coefficients, evaluated in double as each reference kernel's
@@ -596,6 +607,15 @@ private:
         const bool st = (c_.force_flags & F_SURFACE_TENSION) != 0;
         SPH_CUDA(predR_.alloc(pci ? n : 1)); SPH_CUDA(predV_.alloc(pci ? n : 1)); SPH_CUDA(pacc_.alloc(pci ? n : 1));
         SPH_CUDA(normal_.alloc(st ? n : 1));
+        lists_ = d.simulation_method == SPH_DFSPH && d.neighbor_list_max > 0;
+        kmax_ = lists_ ? (uint32_t)d.neighbor_list_max : 0u;
+        SPH_CUDA(pairs_.alloc(lists_ ? (size_t)kmax_ * n : 1));
+        SPH_CUDA(lcount_.alloc(lists_ ? n : 1));
+        SPH_CUDA(bgrad_.alloc(lists_ ? n : 1));
+        SPH_CUDA(kbuf_.alloc(n));
+        SPH_CUDA(cudaMemsetAsync(lcount_.p, 0, lcount_.n * sizeof(uint32_t), st_));
+        SPH_CUDA(cudaMemsetAsync(kbuf_.p, 0, n * sizeof(R), st_));
+        SPH_CUDA(lstat_.alloc(2));
         const size_t nmax = std::max(n, nb);
         SPH_CUDA(key_.alloc(nmax)); SPH_CUDA(slot_.alloc(nmax)); SPH_CUDA(tmp_.alloc(nmax));
         SPH_CUDA(count_.alloc(nkeys_)); SPH_CUDA(starts_.alloc(nkeys_ + 1)); SPH_CUDA(bstarts_.alloc(nkeys_ + 1));
@@ -684,6 +704,73 @@ private:
             else
                 run("k_density", [&] { k_density<R, G, false, false><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_); });
         });
+        SPH_CUDA(cudaGetLastError());
+        return SPH_OK;
+    }
+
+    // Densities, alpha and the DFSPH pair lists after a grid build.
+    int launch_build_lists()
+    {
+        Fluid<R> f = F();
+        const P4<R>* bp = bd_[1].pos;
+        Lists<R> L = LS();
+        run("k_build_lists", [&] { k_build_lists<R><<<blocks(n_, kBlock), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_, L); });
+        SPH_CUDA(cudaGetLastError());
+        return SPH_OK;
+    }
+
+    // DFSPHSolver::step DFSPHSolver.cpp:38-112 over the pair lists.
+    int dfsph_step_lists()
+    {
+        int rc = launch_npforces();
+        if (rc) return rc;
+        const unsigned nb = blocks(n_, kBlock);
+        {
+            Fluid<R> f = F();
+            const P4<R>* bp = bd_[1].pos;
+            Lists<R> L = LS();
+            run("k_dfsph_cfl", [&] { k_dfsph_cfl<R><<<blocks(n_, 256), 256, 0, ls_>>>(f, c_, sc_.p, lim_, partials_.p); });
+            run("k_dfsph_predict_v_warm", [&] { k_dfsph_predict_v_warm_list<R><<<blocks(n_, 256), 256, 0, ls_>>>(f, c_, sc_.p, L.kbuf); });
+            run("k_dfsph_correct_list", [&] { k_dfsph_correct_list<R, 0><<<nb, kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_, sc_.p, L); });
+            SPH_CUDA(cudaGetLastError());
+            // correctDensityError DFSPHSolver.cpp:311-406
+            rc = solve_loop(1,
+                [&](cudaGraphConditionalHandle h) {
+                    run("k_dfsph_predict_density_list", [&] { k_dfsph_predict_density_list<R, true><<<nb, kBlock, 0, ls_>>>(
+                        f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_, sc_.p, lim_, partials_.p, h, L); });
+                },
+                [&](cudaGraphConditionalHandle h) {
+                    run("k_dfsph_correct_list", [&] { k_dfsph_correct_list<R, 1><<<nb, kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_, sc_.p, L); });
+                    run("k_dfsph_predict_density_list", [&] { k_dfsph_predict_density_list<R, false><<<nb, kBlock, 0, ls_>>>(
+                        f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_, sc_.p, lim_, partials_.p, h, L); });
+                },
+                lim_.minIt, lim_.maxIt);
+            if (rc) return rc;
+        }
+        rc = build_grid(true);  // updatePositions + fill grid + neighbour search
+        if (rc) return rc;
+        rc = launch_build_lists();  // computeDensities + computeAlpha + pair lists
+        if (rc) return rc;
+        {
+            Fluid<R> f = F();
+            const P4<R>* bp = bd_[1].pos;
+            Lists<R> L = LS();
+            // correctDivergenceError DFSPHSolver.cpp:494-590
+            rc = solve_loop(2,
+                [&](cudaGraphConditionalHandle h) {
+                    run("k_dfsph_divergence_list", [&] { k_dfsph_divergence_list<R, true><<<nb, kBlock, 0, ls_>>>(
+                        f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_, sc_.p, lim_, partials_.p, h, L); });
+                },
+                [&](cudaGraphConditionalHandle h) {
+                    run("k_dfsph_correct_list", [&] { k_dfsph_correct_list<R, 2><<<nb, kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_, sc_.p, L); });
+                    run("k_dfsph_divergence_list", [&] { k_dfsph_divergence_list<R, false><<<nb, kBlock, 0, ls_>>>(
+                        f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_, sc_.p, lim_, partials_.p, h, L); });
+                },
+                lim_.minItV, lim_.maxIt);
+            if (rc) return rc;
+            if (c_.has_cube) run("k_dfsph_cube", [&] { k_dfsph_cube<R><<<blocks(n_, 256), 256, 0, ls_>>>(f, gv_, hd_, c_); });
+        }
+        run("k_finish_step", [&] { k_finish_step<<<1, 1, 0, ls_>>>(sc_.p); });
         SPH_CUDA(cudaGetLastError());
         return SPH_OK;
     }
@@ -911,7 +998,7 @@ private:
         switch (d.simulation_method) {
             case SPH_WCSPH: return wcsph_step();
             case SPH_PCISPH: return pcisph_step();
-            default: return dfsph_step();
+            default: return lists_ ? dfsph_step_lists() : dfsph_step();
         }
     }
 
@@ -974,6 +1061,12 @@ private:
     DevBuf<R> rho_, alpha_, div_, press_, bpsi_;
     DevBuf<uint32_t> mortx_, morty_, key_, slot_, tmp_, count_, starts_, bstarts_, tile_sums_;
     DevBuf<double> partials_;
+    DevBuf<P4<R>> pairs_, bgrad_;
+    DevBuf<uint32_t> lcount_;
+    DevBuf<R> kbuf_;
+    DevBuf<unsigned long long> lstat_;
+    bool lists_ = false;
+    uint32_t kmax_ = 0;
     DevBuf<DevScalars> sc_;
 };
 

@@ -24,9 +24,9 @@ DFSPH_SCENES = [n for n in SCENES if SCENES[n]["params"]["method"] == 2]
 STEP_FIELDS = ("x", "v", "rho", "p", "alpha", "div", "pred", "k", "kv", "pacc")
 
 
-def gpu_scene(name, precision="f64", G=0, graph=False):
+def gpu_scene(name, precision="f64", G=0, graph=False, lists=64):
     params, x, boxes, spheres = scene(name)
-    s = sph_gb300.Scene(precision=precision, threads_per_particle=G, **params)
+    s = sph_gb300.Scene(precision=precision, threads_per_particle=G, neighbor_list_max=lists, **params)
     s.set_fluid(x)
     for mn, mx in boxes:
         s.add_boundary_box(mn, mx)
@@ -65,10 +65,11 @@ def test_neighbour_sets_bit_exact(gpu_lib, name):
         assert np.array_equal(nb["bnbr"], g["init.bnbr"])
 
 
+@pytest.mark.parametrize("lists", [64, 0], ids=["pairlists", "cellwalk"])
 @pytest.mark.parametrize("name", list(SCENES))
-def test_f64_steps_match_reference(gpu_lib, name):
+def test_f64_steps_match_reference(gpu_lib, name, lists):
     g = golden(name)
-    s = gpu_scene(name)
+    s = gpu_scene(name, lists=lists)
     step = 1
     while f"s{step}.x" in g:
         s.step(1)
@@ -85,15 +86,16 @@ def test_f64_steps_match_reference(gpu_lib, name):
         step += 1
 
 
+@pytest.mark.parametrize("lists", [64, 0], ids=["pairlists", "cellwalk"])
 @pytest.mark.parametrize("name", list(SCENES))
-def test_f32_error_against_reference(gpu_lib, name):
+def test_f32_error_against_reference(gpu_lib, name, lists):
     """FP32 production form against the reference's FP64 results, 3 steps.
     Measured on GB300: positions <= 6e-8 rel, densities <= 1e-6 rel,
     alpha <= 2e-6 rel, WCSPH/PCISPH pressures <= 1e-4 rel, velocities
     <= 2.5e-4 m/s abs (particles near the rho* >= rho0 clamp flip sides), and
     identical iteration counts.  Bounds below leave ~10x headroom."""
     g = golden(name)
-    s = gpu_scene(name, precision="f32")
+    s = gpu_scene(name, precision="f32", lists=lists)
     for step in (1, 2, 3):
         s.step(1)
         assert relerr(s.get("x"), g[f"s{step}.x"]) <= 1e-6
@@ -132,9 +134,24 @@ def test_graph_mode_equals_stream_mode(gpu_lib, name):
 
 @pytest.mark.parametrize("G", [2, 4, 8])
 def test_threads_per_particle_variants(gpu_lib, G):
-    a = gpu_scene("dfsph_forces", precision="f32", G=1)
-    b = gpu_scene("dfsph_forces", precision="f32", G=G)
+    a = gpu_scene("dfsph_forces", precision="f32", G=1, lists=0)
+    b = gpu_scene("dfsph_forces", precision="f32", G=G, lists=0)
     a.step(2)
     b.step(2)
     assert relerr(b.get("rho"), a.get("rho")) <= 1e-4
     assert relerr(b.get("x"), a.get("x")) <= 1e-5
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_pair_list_overflow_falls_back_to_cell_walk(gpu_lib, precision):
+    """With 8 slots every particle overflows its pair list and every solver
+    walk takes the cell-walk fallback; results must agree with the full lists."""
+    a = gpu_scene("dfsph_akinci", precision=precision, lists=64)
+    b = gpu_scene("dfsph_akinci", precision=precision, lists=8)
+    a.step(3)
+    b.step(3)
+    tol = 1e-12 if precision == "f64" else 1e-5
+    for f in ("x", "rho", "alpha"):
+        assert relerr(b.get(f), a.get(f)) <= tol, f
+    assert b.stats()["list_overflow"] > 0 and a.stats()["list_overflow"] == 0
+    assert a.stats()["list_pairs"] > 20 * a.n
