@@ -207,6 +207,52 @@ int sph_ctx_get_profile(sph_ctx* ctx, char* buf, unsigned long long len);
  * that device. */
 int sph_select_device(int device);
 
+/* ------------------------------------------------------------------------
+ * Batched pool: many independent DFSPH scenes (Akinci boundaries, FP32, pair
+ * lists) resident on one GPU and advanced together.  No counterpart in the
+ * reference, which holds one scene per process (Simulation singleton,
+ * src/Simulation.cpp:84-90); each pooled scene runs the same per-step loop as
+ * sph_ctx_step, and its results do not depend on which other scenes share
+ * the pool.  Scenes are admitted and removed between steps.
+ * ------------------------------------------------------------------------ */
+typedef struct sph_pool sph_pool;
+
+typedef struct sph_pool_desc {
+    unsigned long long max_particles;   /* fluid particles resident at once */
+    unsigned long long max_boundary;    /* boundary particles resident at once */
+    unsigned long long max_keys;        /* total grid key space of resident scenes */
+    unsigned max_scenes;
+    int neighbor_list_max;              /* pair-list slots per particle */
+} sph_pool_desc;
+
+/* Capacities that fit a device-memory budget in bytes. */
+int sph_pool_desc_from_budget(unsigned long long hbm_bytes, int neighbor_list_max, sph_pool_desc* out);
+int sph_pool_create(const sph_pool_desc* desc, sph_pool** out);
+int sph_pool_destroy(sph_pool* pool);
+/* Queue a scene (fluid x/v and Akinci boundary points, xyz FP64) to run for
+ * `steps` steps; it becomes resident at the next sph_pool_step.  Returns
+ * SPH_ERR_CAPACITY when it does not fit beside the resident and queued
+ * scenes (admission control). */
+int sph_pool_add_scene(sph_pool* pool, const sph_scene_desc* desc, const double* x, const double* v, unsigned n,
+                       const double* boundary_x, unsigned nb, unsigned steps, int* scene_id);
+/* Release a scene (finished or not) at the next step. */
+int sph_pool_remove_scene(sph_pool* pool, int scene_id);
+/* nsteps steps of every resident scene that still has steps to run. */
+int sph_pool_step(sph_pool* pool, int nsteps);
+/* Whole pool steps as one CUDA graph with device-side solver loops. */
+int sph_pool_set_graph(sph_pool* pool, int enable);
+int sph_pool_synchronize(sph_pool* pool);
+/* Statistics of one scene; *done = 1 once its steps have completed. */
+int sph_pool_query(sph_pool* pool, int scene_id, sph_stats* out, int* done);
+/* Ids of resident scenes whose steps have completed (up to max_ids). */
+int sph_pool_poll(sph_pool* pool, int* done_ids, int max_ids, int* num_done);
+/* A field of one resident scene (original particle order, FP64). */
+int sph_pool_download(sph_pool* pool, int scene_id, int field, double* out);
+int sph_pool_usage(sph_pool* pool, unsigned long long* particles, unsigned long long* boundary,
+                   unsigned long long* keys, unsigned* scenes);
+int sph_pool_get_launch_count(sph_pool* pool, unsigned long long* out);
+const char* sph_pool_last_error(const sph_pool* pool);
+
 /* Sampling helpers with the reference's point sets, usable without a
  * context; out may be NULL to query the count.  Return the point count. */
 long long sph_sample_box(double support_radius, const double min[3], const double max[3], double* out);

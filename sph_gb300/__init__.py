@@ -96,6 +96,16 @@ class Stats(ctypes.Structure):
     ]
 
 
+class PoolDesc(ctypes.Structure):
+    _fields_ = [
+        ("max_particles", ctypes.c_ulonglong),
+        ("max_boundary", ctypes.c_ulonglong),
+        ("max_keys", ctypes.c_ulonglong),
+        ("max_scenes", ctypes.c_uint),
+        ("neighbor_list_max", ctypes.c_int),
+    ]
+
+
 # The C ABI, as (name, restype, argtypes); the CPU tests check that the
 # library exports each of these.
 _vp, _dp, _ip = ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)
@@ -127,6 +137,22 @@ ABI = [
     ("sph_sample_sphere", ctypes.c_longlong, [ctypes.c_double, _dp, ctypes.c_double, _dp]),
     ("sph_fluid_block", ctypes.c_longlong, [ctypes.c_double, _dp, _dp, _dp]),
     ("sph_version", ctypes.c_char_p, []),
+    ("sph_pool_desc_from_budget", ctypes.c_int, [ctypes.c_ulonglong, ctypes.c_int, ctypes.POINTER(PoolDesc)]),
+    ("sph_pool_create", ctypes.c_int, [ctypes.POINTER(PoolDesc), ctypes.POINTER(_vp)]),
+    ("sph_pool_destroy", ctypes.c_int, [_vp]),
+    ("sph_pool_add_scene", ctypes.c_int, [_vp, ctypes.POINTER(SceneDesc), _dp, _dp, ctypes.c_uint, _dp, ctypes.c_uint,
+                                          ctypes.c_uint, ctypes.POINTER(ctypes.c_int)]),
+    ("sph_pool_remove_scene", ctypes.c_int, [_vp, ctypes.c_int]),
+    ("sph_pool_step", ctypes.c_int, [_vp, ctypes.c_int]),
+    ("sph_pool_set_graph", ctypes.c_int, [_vp, ctypes.c_int]),
+    ("sph_pool_synchronize", ctypes.c_int, [_vp]),
+    ("sph_pool_query", ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(Stats), ctypes.POINTER(ctypes.c_int)]),
+    ("sph_pool_poll", ctypes.c_int, [_vp, _ip, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
+    ("sph_pool_download", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _dp]),
+    ("sph_pool_usage", ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(ctypes.c_ulonglong),
+                                      ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(ctypes.c_uint)]),
+    ("sph_pool_get_launch_count", ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_ulonglong)]),
+    ("sph_pool_last_error", ctypes.c_char_p, [_vp]),
 ]
 
 _lib = None
@@ -376,3 +402,107 @@ def fluid_block(particle_radius, mn, mx):
     out = np.zeros((m, 3))
     L.sph_fluid_block(particle_radius, _d(_v3(mn)), _d(_v3(mx)), _d(out))
     return out
+
+
+class PoolFull(SPHError):
+    """The scene does not fit beside the resident and queued scenes."""
+
+
+class Pool:
+    """Many independent DFSPH scenes resident on the GPU, advanced together."""
+
+    def __init__(self, budget_bytes=None, max_particles=None, max_boundary=None, max_keys=None, max_scenes=4096,
+                 neighbor_list_max=64):
+        L = lib()
+        d = PoolDesc()
+        if budget_bytes is not None:
+            L.sph_pool_desc_from_budget(int(budget_bytes), int(neighbor_list_max), ctypes.byref(d))
+        else:
+            d.max_particles = int(max_particles)
+            d.max_boundary = int(max_boundary if max_boundary is not None else max_particles)
+            d.max_keys = int(max_keys if max_keys is not None else 16 * max_particles)
+            d.max_scenes = int(max_scenes)
+            d.neighbor_list_max = int(neighbor_list_max)
+        self.desc = d
+        self._h = ctypes.c_void_p()
+        rc = L.sph_pool_create(ctypes.byref(d), ctypes.byref(self._h))
+        if rc != 0:
+            raise SPHError(f"sph_pool_create failed ({rc})")
+        self._n = {}
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            lib().sph_pool_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc, what):
+        if rc != 0:
+            msg = lib().sph_pool_last_error(self._h)
+            text = f"{what} failed ({rc}): {msg.decode() if msg else ''}"
+            raise (PoolFull if rc == -4 else SPHError)(text)
+
+    def add_scene(self, x, v=None, boundary_points=None, steps=1, **params):
+        x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, 3)
+        vv = None if v is None else np.ascontiguousarray(v, dtype=np.float64).reshape(-1, 3)
+        b = None if boundary_points is None else np.ascontiguousarray(boundary_points, dtype=np.float64).reshape(-1, 3)
+        d = make_desc(**params)
+        sid = ctypes.c_int()
+        rc = lib().sph_pool_add_scene(self._h, ctypes.byref(d), _d(x), None if vv is None else _d(vv), x.shape[0],
+                                      None if b is None else _d(b), 0 if b is None else b.shape[0], int(steps),
+                                      ctypes.byref(sid))
+        self._check(rc, "sph_pool_add_scene")
+        self._n[sid.value] = (x.shape[0], 0 if b is None else b.shape[0])
+        return sid.value
+
+    def remove(self, sid):
+        self._check(lib().sph_pool_remove_scene(self._h, int(sid)), "sph_pool_remove_scene")
+
+    def step(self, n=1):
+        self._check(lib().sph_pool_step(self._h, int(n)), "sph_pool_step")
+
+    def set_graph(self, enable=True):
+        self._check(lib().sph_pool_set_graph(self._h, int(bool(enable))), "sph_pool_set_graph")
+
+    def synchronize(self):
+        self._check(lib().sph_pool_synchronize(self._h), "sph_pool_synchronize")
+
+    def query(self, sid):
+        st = Stats()
+        done = ctypes.c_int()
+        self._check(lib().sph_pool_query(self._h, int(sid), ctypes.byref(st), ctypes.byref(done)), "sph_pool_query")
+        return {name: getattr(st, name) for name, _ in Stats._fields_}, bool(done.value)
+
+    def poll(self):
+        n = ctypes.c_int()
+        self._check(lib().sph_pool_poll(self._h, None, 0, ctypes.byref(n)), "sph_pool_poll")
+        if n.value == 0:
+            return []
+        ids = np.zeros(n.value, np.int32)
+        self._check(lib().sph_pool_poll(self._h, _i(ids), n.value, ctypes.byref(n)), "sph_pool_poll")
+        return [int(t) for t in ids[: n.value]]
+
+    def get(self, sid, field):
+        fid, width = FIELDS[field]
+        nf, nb = self._n[sid]
+        count = nb if field in ("bx", "psi") else nf
+        out = np.zeros((count, 3) if width == 3 else count)
+        if count:
+            self._check(lib().sph_pool_download(self._h, int(sid), fid, _d(out)), f"sph_pool_download({field})")
+        return out
+
+    def usage(self):
+        p, b, k = ctypes.c_ulonglong(), ctypes.c_ulonglong(), ctypes.c_ulonglong()
+        s = ctypes.c_uint()
+        lib().sph_pool_usage(self._h, ctypes.byref(p), ctypes.byref(b), ctypes.byref(k), ctypes.byref(s))
+        return dict(particles=p.value, boundary=b.value, keys=k.value, scenes=s.value)
+
+    def launch_count(self):
+        n = ctypes.c_ulonglong()
+        self._check(lib().sph_pool_get_launch_count(self._h, ctypes.byref(n)), "sph_pool_get_launch_count")
+        return n.value

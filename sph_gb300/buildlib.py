@@ -28,8 +28,9 @@ UNITS = {
     "sph_scene_f32.cu": [],
     "sph_scene_f64.cu": ["-fmad=false"],
     "sph_noalloc.cu": [],
+    "sph_pool.cu": [],
 }
-HEADERS = ["sph_device.cuh", "sph_kernels.cuh", "sph_scene.cuh", "sph_scene_base.h"]
+HEADERS = ["sph_device.cuh", "sph_kernels.cuh", "sph_lists.cuh", "sph_scene.cuh", "sph_scene_base.h"]
 
 
 def nvcc() -> str:

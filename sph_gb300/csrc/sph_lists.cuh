@@ -59,14 +59,14 @@ __device__ __forceinline__ V3<R> pair_vec(V3<R> xi, uint32_t ci, const P4<R>& pj
     }
 }
 
+// Per-particle body shared by the single-scene and the pool kernels; q is
+// the block's shared queue (kQueue x kBlock).
 template <typename R>
-__global__ void __launch_bounds__(kBlock, 7) k_build_lists(Fluid<R> f, const P4<R>* __restrict__ bpos, GridView g,
-                                                        const uint32_t* __restrict__ cs, const uint32_t* __restrict__ bs,
-                                                        Consts<R> c, int akinci, Lists<R> L)
+__device__ __forceinline__ void build_lists_one(uint32_t i, const Fluid<R>& f, const P4<R>* __restrict__ bpos,
+                                                const GridView& g, const uint32_t* __restrict__ cs,
+                                                const uint32_t* __restrict__ bs, const Consts<R>& c, int akinci,
+                                                const Lists<R>& L, uint32_t* q)
 {
-    __shared__ uint32_t q[kQueue * kBlock];
-    const uint32_t i = gtid();
-    if (i >= f.n) return;
     const uint32_t n = f.n;
     const V3<R> xi = xyz(f.pos[i]);
     const uint32_t pc = f.cell[i];
@@ -138,6 +138,17 @@ __global__ void __launch_bounds__(kBlock, 7) k_build_lists(Fluid<R> f, const P4<
     L.bgrad[i] = P4<R>{bg.x, bg.y, bg.z, 0};
 }
 
+template <typename R>
+__global__ void __launch_bounds__(kBlock, 7) k_build_lists(Fluid<R> f, const P4<R>* __restrict__ bpos, GridView g,
+                                                           const uint32_t* __restrict__ cs, const uint32_t* __restrict__ bs,
+                                                           Consts<R> c, int akinci, Lists<R> L)
+{
+    __shared__ uint32_t q[kQueue * kBlock];
+    const uint32_t i = gtid();
+    if (i >= f.n) return;
+    build_lists_one(i, f, bpos, g, cs, bs, c, akinci, L, q);
+}
+
 // ---- cell-walk fallbacks for particles whose list overflowed -------------
 
 template <typename R, int MODE>
@@ -200,14 +211,11 @@ __device__ R velocity_div_cells(const Fluid<R>& f, const P4<R>* __restrict__ bpo
 // DFSPH velocity corrections (MODE 0 warm start, 1 density, 2 divergence),
 // as k_dfsph_correct but over the pair lists; kbuf holds this pass's k.
 template <typename R, int MODE>
-__global__ void __launch_bounds__(kBlock, 8) k_dfsph_correct_list(Fluid<R> f, const P4<R>* __restrict__ bpos, GridView g,
-                                                               const uint32_t* __restrict__ cs, const uint32_t* __restrict__ bs,
-                                                               Consts<R> c, int akinci, const DevScalars* __restrict__ sc,
-                                                               Lists<R> L)
+__device__ __forceinline__ V3<R> correct_sum_one(uint32_t i, const Fluid<R>& f, const P4<R>* __restrict__ bpos,
+                                                 const GridView& g, const uint32_t* __restrict__ cs,
+                                                 const uint32_t* __restrict__ bs, const Consts<R>& c, int akinci,
+                                                 const Lists<R>& L)
 {
-    if (MODE != 0 && !sc->active) return;
-    const uint32_t i = gtid();
-    if (i >= f.n) return;
     const uint32_t n = f.n;
     const R* __restrict__ kb_ = L.kbuf;
     const R ki = kb_[i];
@@ -226,13 +234,34 @@ __global__ void __launch_bounds__(kBlock, 8) k_dfsph_correct_list(Fluid<R> f, co
     } else {
         sum = correct_sum_cells<R, MODE>(f, bpos, g, cs, bs, c, akinci, i, ki, kb_);
     }
-    const R dt = (R)sc->dt;
+    return sum;
+}
+
+// Velocity update after a correction sum (and the k / kv accumulation).
+template <typename R, int MODE>
+__device__ __forceinline__ void correct_apply(uint32_t i, const Fluid<R>& f, const Consts<R>& c, R dt, V3<R> sum)
+{
     if (MODE == 1) f.kappa[i] += (f.pred[i] - c.density0) * f.alpha[i];
     if (MODE == 2) f.kappav[i] += f.div[i] * f.alpha[i];
     P4<R> v = f.vel[i];
     if (MODE == 0) { v.x -= sum.x * dt; v.y -= sum.y * dt; v.z -= sum.z * dt; }
     else { v.x -= dt * sum.x; v.y -= dt * sum.y; v.z -= dt * sum.z; }
     f.vel[i] = v;
+}
+
+// DFSPH velocity corrections (MODE 0 warm start, 1 density, 2 divergence),
+// as k_dfsph_correct but over the pair lists; kbuf holds this pass's k.
+template <typename R, int MODE>
+__global__ void __launch_bounds__(kBlock, 8) k_dfsph_correct_list(Fluid<R> f, const P4<R>* __restrict__ bpos, GridView g,
+                                                                  const uint32_t* __restrict__ cs, const uint32_t* __restrict__ bs,
+                                                                  Consts<R> c, int akinci, const DevScalars* __restrict__ sc,
+                                                                  Lists<R> L)
+{
+    if (MODE != 0 && !sc->active) return;
+    const uint32_t i = gtid();
+    if (i >= f.n) return;
+    const V3<R> sum = correct_sum_one<R, MODE>(i, f, bpos, g, cs, bs, c, akinci, L);
+    correct_apply<R, MODE>(i, f, c, (R)sc->dt, sum);
 }
 
 // Sum over the list of m (v_i - v_j) . gradW_ij plus the boundary term.
@@ -252,6 +281,22 @@ __device__ __forceinline__ R velocity_div_list(const Fluid<R>& f, const Lists<R>
     return d;
 }
 
+// m (v_i - v_j) . gradW summed over the neighbours (list or fallback walk);
+// *nn receives the number of neighbours with a non-zero gradient.
+template <typename R>
+__device__ __forceinline__ R velocity_div_one(uint32_t i, const Fluid<R>& f, const P4<R>* __restrict__ bpos,
+                                              const GridView& g, const uint32_t* __restrict__ cs,
+                                              const uint32_t* __restrict__ bs, const Consts<R>& c, int akinci,
+                                              const Lists<R>& L, V3<R> vi, uint32_t* nn)
+{
+    const uint32_t cnt = L.count[i];
+    if (cnt <= L.kmax) {
+        *nn = cnt;
+        return velocity_div_list(f, L, i, vi, akinci);
+    }
+    return velocity_div_cells(f, bpos, g, cs, bs, c, akinci, i, vi, nn);
+}
+
 // DFSPHSolver::predictDensities over the lists (+ loop control, as
 // k_dfsph_predict_density).
 template <typename R, bool INITIAL>
@@ -267,13 +312,8 @@ __global__ void __launch_bounds__(kBlock, 8) k_dfsph_predict_density_list(Fluid<
     double err = 0.0;
     if (i < f.n) {
         const V3<R> vi = xyz(f.vel[i]);
-        R dc;
-        if (L.count[i] <= L.kmax) {
-            dc = velocity_div_list(f, L, i, vi, akinci);
-        } else {
-            uint32_t nn;
-            dc = velocity_div_cells(f, bpos, g, cs, bs, c, akinci, i, vi, &nn);
-        }
+        uint32_t nn;
+        const R dc = velocity_div_one(i, f, bpos, g, cs, bs, c, akinci, L, vi, &nn);
         const R dt = (R)sc->dt;
         const R rho = f.rho[i];
         R pred = rho + dc * dt;
@@ -319,11 +359,8 @@ __global__ void __launch_bounds__(kBlock, 8) k_dfsph_divergence_list(Fluid<R> f,
     double err = 0.0;
     if (i < f.n) {
         const V3<R> vi = xyz(f.vel[i]);
-        const uint32_t cnt = L.count[i];
-        R dv;
-        uint32_t nn = cnt;
-        if (cnt <= L.kmax) dv = velocity_div_list(f, L, i, vi, akinci);
-        else dv = velocity_div_cells(f, bpos, g, cs, bs, c, akinci, i, vi, &nn);
+        uint32_t nn;
+        R dv = velocity_div_one(i, f, bpos, g, cs, bs, c, akinci, L, vi, &nn);
         const R dt = (R)sc->dt;
         dv = nn < 20u ? (R)0 : (dv < (R)0 ? (R)0 : dv);
         f.div[i] = dv;

@@ -1,0 +1,1268 @@
+// Batched multi-scene pool: many independent DFSPH scenes advanced together.
+//
+// All resident scenes share one set of device arrays.  Each scene keeps its
+// own dense cell box and a disjoint range of grid keys, so one counting sort
+// per step sorts every scene at once and leaves each scene's particles
+// contiguous (scenes are laid out in key order).  Per-scene constants, time
+// step, solver scalars and loop flags live in a device scene table; every
+// kernel looks up its particle's scene.  The solver loops run while any
+// scene's loop is active; a scene whose loop has converged skips the
+// remaining iterations, exactly as if it ran alone.  Per-scene error sums
+// are accumulated as 64-bit fixed-point integers (integer addition is
+// associative), so a scene's results do not depend on which other scenes
+// share the pool or how its particles fall into blocks.
+//
+// The scene set changes only between steps (continuous batching): pending
+// admissions and removals are applied by a re-layout that repacks the
+// resident scenes' state, uploads the new scenes, sorts the boundary and
+// rebuilds the grids and pair lists; the per-step CUDA graph is then
+// re-captured.
+//
+// Scenes use the DFSPH solver (DFSPHSolver.cpp) with Akinci boundaries and
+// optional XSPH / standard / artificial viscosity, in the FP32 form with pair
+// lists (sph_lists.cuh).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstddef>
+#include <cstring>
+#include <list>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "sph_scene.cuh"
+
+struct sph_pool;
+
+namespace sph {
+
+constexpr double kFixScale = 268435456.0;  // 2^28: per-particle error quantum 3.7e-9
+
+struct PoolScene {
+    Consts<float> c;
+    GridView g;
+    LoopLimits lim;
+    DevScalars s;
+    unsigned long long acc;   // fixed-point error sum of the reduction in progress
+    uint32_t key_base, n, nb, pbase, bbase;
+    uint32_t running;         // steps left > 0
+    uint32_t loop_active;     // this scene's solver loop is still iterating
+    uint32_t steps_left;
+    uint32_t vmax_bits;       // CFL: max of sqrt(|v|) as float bits
+    int akinci;
+};
+
+struct PoolCounters {
+    unsigned any;                       // some scene's loop is active
+    unsigned pad;
+    unsigned long long body_d, body_v;  // loop bodies executed (density / divergence)
+};
+
+__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Adds v to scene s's accumulator; all lanes of the warp must call it
+// (s = ~0u: nothing to add).  Warps whose lanes share one scene add once.
+__device__ __forceinline__ void seg_add(uint32_t s, unsigned long long v, PoolScene* T)
+{
+    const uint32_t s0 = __shfl_sync(0xffffffffu, s, 0);
+    if (__all_sync(0xffffffffu, s == s0)) {
+        v = warp_sum_u64(v);
+        if ((threadIdx.x & 31) == 0 && s0 != ~0u && v) atomicAdd(&T[s0].acc, v);
+    } else if (s != ~0u && v) {
+        atomicAdd(&T[s].acc, v);
+    }
+}
+
+__device__ __forceinline__ unsigned long long to_fixed(double e) { return (unsigned long long)(e * kFixScale + 0.5); }
+
+__device__ __forceinline__ uint32_t find_segment(const uint32_t* __restrict__ base, uint32_t S, uint32_t i)
+{
+    uint32_t lo = 0, hi = S;  // last segment whose base <= i
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (base[mid] <= i) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+// Scene id of every particle of a layout: segments [base[s], base[s] + len[s]).
+__global__ void k_fill_sid(uint32_t N, const uint32_t* __restrict__ base, uint32_t S, uint32_t* __restrict__ sid)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < N) sid[i] = find_segment(base, S, i);
+}
+
+// Copy of the state carried across a re-layout: scene k's segment moves from
+// src_base[k] to dst_base[k] (dst bases ascending).
+__global__ void k_repack_fluid(uint32_t N, const uint32_t* __restrict__ dst_base, const uint32_t* __restrict__ src_base,
+                               const uint32_t* __restrict__ len, uint32_t S, Fluid<float> src, Fluid<float> dst)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N || S == 0) return;
+    const uint32_t k = find_segment(dst_base, S, i);
+    const uint32_t off = i - dst_base[k];
+    if (off >= len[k]) return;
+    const uint32_t j = src_base[k] + off;
+    dst.pos[i] = src.pos[j];
+    dst.vel[i] = src.vel[j];
+    dst.kappa[i] = src.kappa[j];
+    dst.kappav[i] = src.kappav[j];
+    dst.pred[i] = src.pred[j];
+    dst.cell[i] = src.cell[j];
+    dst.id[i] = src.id[j];
+}
+
+__global__ void k_repack_boundary(uint32_t N, const uint32_t* __restrict__ dst_base, const uint32_t* __restrict__ src_base,
+                                  const uint32_t* __restrict__ len, uint32_t S, Boundary<float> src, Boundary<float> dst)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N || S == 0) return;
+    const uint32_t k = find_segment(dst_base, S, i);
+    const uint32_t off = i - dst_base[k];
+    if (off >= len[k]) return;
+    const uint32_t j = src_base[k] + off;
+    dst.pos[i] = src.pos[j];
+    dst.cell[i] = src.cell[j];
+    dst.id[i] = src.id[j];
+}
+
+// Cells and keys (scene key base + column-Morton key) of every particle;
+// MOVE first advances positions of running scenes (updatePositions).
+template <bool MOVE>
+__global__ void k_pool_cell_update(uint32_t N, Fluid<float> f, const uint32_t* __restrict__ sid, PoolScene* T,
+                                   uint32_t* __restrict__ key, uint32_t* __restrict__ slot, uint32_t* __restrict__ count)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    PoolScene& sd = T[sid[i]];
+    P4<float> p = f.pos[i];
+    if (MOVE && sd.running) {
+        const float dt = (float)sd.s.dt;
+        const P4<float> v = f.vel[i];
+        p.x = p.x + v.x * dt; p.y = p.y + v.y * dt; p.z = p.z + v.z * dt;
+    }
+    const GridView& g = sd.g;
+    const float h = sd.c.h;
+    const uint32_t c0 = f.cell[i];
+    const int x0 = cell_x(c0), y0 = cell_y(c0), z0 = cell_z(c0);
+    const int cx = x0 + (int)floorf(p.x / h), cy = y0 + (int)floorf(p.y / h), cz = z0 + (int)floorf(p.z / h);
+    const int ccx = min(max(cx, 0), g.nx - 1), ccy = min(max(cy, 0), g.ny - 1), ccz = min(max(cz, 0), g.nz - 1);
+    if (ccx != cx || ccy != cy || ccz != cz) atomicOr(&sd.s.status, (unsigned)ST_OUT_OF_GRID);
+    p.x -= (float)(ccx - x0) * h; p.y -= (float)(ccy - y0) * h; p.z -= (float)(ccz - z0) * h;
+    if (ccx == cx) p.x = fminf(fmaxf(p.x, 0.f), __int_as_float(__float_as_int(h) - 1));
+    if (ccy == cy) p.y = fminf(fmaxf(p.y, 0.f), __int_as_float(__float_as_int(h) - 1));
+    if (ccz == cz) p.z = fminf(fmaxf(p.z, 0.f), __int_as_float(__float_as_int(h) - 1));
+    f.pos[i] = p;
+    f.cell[i] = pack_cell(ccx, ccy, ccz);
+    const uint32_t k = sd.key_base + cell_key(g, ccx, ccy, ccz);
+    key[i] = k;
+    slot[i] = atomicAdd(count + k, 1u);
+}
+
+__global__ void k_pool_bcount(uint32_t N, Boundary<float> b, const uint32_t* __restrict__ bsid, const PoolScene* T,
+                              uint32_t* __restrict__ key, uint32_t* __restrict__ slot, uint32_t* __restrict__ count)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const PoolScene& sd = T[bsid[i]];
+    const uint32_t c = b.cell[i];
+    const uint32_t k = sd.key_base + cell_key(sd.g, cell_x(c), cell_y(c), cell_z(c));
+    key[i] = k;
+    slot[i] = atomicAdd(count + k, 1u);
+}
+
+// AkinciBoundaryModel::computeVolume (AkinciBoundayModel.cpp:11-40) per scene.
+__global__ void k_pool_psi(uint32_t N, Boundary<float> b, const uint32_t* __restrict__ bsid, const PoolScene* T,
+                           const uint32_t* __restrict__ bstarts)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const PoolScene& sd = T[bsid[i]];
+    const Consts<float>& c = sd.c;
+    float delta = 0.f;
+    walk<float, 1>(sd.g, bstarts + sd.key_base, b.cell[i], xyz(b.pos[i]), c.h, 0, [&](uint32_t j, V3<float> s) {
+        const V3<float> r = s - xyz(ldg4(b.pos + j));
+        const float r2 = dot3(r, r);
+        if (r2 <= c.cull2) delta += cubic_W(c, sqrtf(r2));
+    });
+    const float psi = 1.f / delta;
+    b.psi[i] = psi;
+    b.pos[i].w = c.density0 * psi;
+}
+
+__global__ void __launch_bounds__(kBlock, 7) k_pool_build_lists(Fluid<float> f, const P4<float>* __restrict__ bpos,
+                                                                const uint32_t* __restrict__ sid, const PoolScene* T,
+                                                                const uint32_t* __restrict__ cs, const uint32_t* __restrict__ bs,
+                                                                Lists<float> L)
+{
+    __shared__ uint32_t q[kQueue * kBlock];
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= f.n) return;
+    const PoolScene& sd = T[sid[i]];
+    if (!sd.running) return;
+    build_lists_one(i, f, bpos, sd.g, cs + sd.key_base, bs + sd.key_base, sd.c, sd.akinci, L, q);
+}
+
+// Non-pressure forces of the scene (XSPH / standard / artificial viscosity;
+// k_npforce's arithmetic) over the cell walk.
+__global__ void __launch_bounds__(kBlock) k_pool_npforce(Fluid<float> f, const P4<float>* __restrict__ bpos,
+                                                         const uint32_t* __restrict__ sid, const PoolScene* T,
+                                                         const uint32_t* __restrict__ cs, const uint32_t* __restrict__ bs)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= f.n) return;
+    const PoolScene& sd = T[sid[i]];
+    const Consts<float>& c = sd.c;
+    const int fl = c.force_flags;
+    if (!sd.running || !(fl & (F_XSPH | F_STD_VISC | F_ART_VISC))) return;
+    const float dt = (float)sd.s.dt;
+    const V3<float> xi = xyz(f.pos[i]);
+    const P4<float> vi4 = f.vel[i];
+    const V3<float> vi = xyz(vi4);
+    const float rho_i = vi4.w;
+    const uint32_t pc = f.cell[i];
+    const float h2 = c.h * c.h;
+    V3<float> av = {0, 0, 0}, avb = {0, 0, 0};
+    walk<float, 1>(sd.g, cs + sd.key_base, pc, xi, c.h, 0, [&](uint32_t j, V3<float> s) {
+        const V3<float> r = s - xyz(ldg4(f.pos + j));
+        const float r2 = dot3(r, r);
+        if (!(r2 <= c.cull2)) return;
+        const P4<float> vj4 = ldg4(f.vel + j);
+        const V3<float> vj = xyz(vj4);
+        const float rho_j = vj4.w;
+        const float rl = sqrtf(r2);
+        if (fl & F_XSPH) av = av + (((c.visc * (c.mass / rho_j)) * (vj - vi)) * cubic_W(c, rl)) / dt;
+        if (fl & F_STD_VISC) av = av + ((c.mass * (vj - vi)) / rho_j) * visc_laplW(c, r2);
+        if (fl & F_ART_VISC) {
+            const float kij = 2.f * c.density0 / (rho_i + rho_j);
+            av = av + (kij * 10.f * 0.1f * c.visc * (c.mass / rho_j) * dot3(vi - vj, r) / (rl * rl + 0.01f * h2)) *
+                          cubic_gradW(c, r, r2);
+        }
+    });
+    if ((fl & F_BVISC) && sd.akinci)
+        walk<float, 1>(sd.g, bs + sd.key_base, pc, xi, c.h, 0, [&](uint32_t j, V3<float> s) {
+            const P4<float> pb = ldg4(bpos + j);
+            const V3<float> r = s - xyz(pb);
+            const float r2 = dot3(r, r);
+            if (!(r2 <= c.cull2)) return;
+            const float rl = sqrtf(r2);
+            if (fl & F_XSPH) avb = avb + (((c.bvisc * (pb.w / rho_i)) * (-vi)) * cubic_W(c, rl)) / dt;
+            if (fl & F_STD_VISC) avb = avb + ((pb.w * (-vi)) / rho_i) * visc_laplW(c, r2);
+            if (fl & F_ART_VISC)
+                avb = avb + (10.f * 0.1f * c.bvisc * (pb.w / rho_i) * dot3(vi, r) / (rl * rl + 0.01f * h2)) *
+                                cubic_gradW(c, r, r2);
+        });
+    if (fl & F_STD_VISC) { av = av * (c.visc / c.density0); avb = avb * (c.bvisc / c.density0); }
+    P4<float> a = f.acc[i];
+    a.x += av.x; a.y += av.y; a.z += av.z;
+    a.x += avb.x; a.y += avb.y; a.z += avb.z;
+    f.acc[i] = a;
+}
+
+// DFSPHSolver::updateTimeStep per scene: max of sqrt(|v + (a + g) dt|).
+__global__ void k_pool_cfl_accum(Fluid<float> f, const uint32_t* __restrict__ sid, PoolScene* T)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t s = ~0u;
+    float m = 0.f;
+    if (i < f.n) {
+        const uint32_t k = sid[i];
+        const PoolScene& sd = T[k];
+        if (sd.running) {
+            const float dt = (float)sd.s.dt;
+            const P4<float> v = f.vel[i], a = f.acc[i];
+            const V3<float> cur = {v.x + (a.x + sd.c.gx) * dt, v.y + (a.y + sd.c.gy) * dt, v.z + (a.z + sd.c.gz) * dt};
+            m = sqrtf(sqrtf(dot3(cur, cur)));
+            s = k;
+        }
+    }
+    const uint32_t s0 = __shfl_sync(0xffffffffu, s, 0);
+    if (__all_sync(0xffffffffu, s == s0)) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
+        if ((threadIdx.x & 31) == 0 && s0 != ~0u) atomicMax(&T[s0].vmax_bits, __float_as_uint(m));
+    } else if (s != ~0u) {
+        atomicMax(&T[s].vmax_bits, __float_as_uint(m));
+    }
+}
+
+__global__ void k_pool_cfl_control(PoolScene* T, uint32_t S)
+{
+    for (uint32_t k = threadIdx.x; k < S; k += blockDim.x) {
+        PoolScene& sd = T[k];
+        if (!sd.running) continue;
+        const double maxVel = fmax(0.1, (double)__uint_as_float(sd.vmax_bits));
+        sd.vmax_bits = 0u;
+        const double ts = sd.s.dt;
+        const double cflTs = sd.lim.cflFactor * 0.4 * 2.0 * sd.lim.particleRadius / maxVel;
+        double newTs;
+        if (cflTs < ts) newTs = cflTs;
+        else if (sd.s.iterations > 3) newTs = ts * 0.99;
+        else newTs = ts * 1.001;
+        newTs = fmax(newTs, sd.lim.minTs);
+        newTs = fmin(newTs, sd.lim.maxTs);
+        sd.s.dt = newTs;
+        sd.s.maxVel = maxVel;
+    }
+}
+
+__global__ void k_pool_predict_v_warm(Fluid<float> f, const uint32_t* __restrict__ sid, const PoolScene* T,
+                                      float* __restrict__ kbuf)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= f.n) return;
+    const PoolScene& sd = T[sid[i]];
+    if (!sd.running) return;
+    const Consts<float>& c = sd.c;
+    const float dt = (float)sd.s.dt;
+    P4<float> v = f.vel[i];
+    const P4<float> a = f.acc[i];
+    v.x = v.x + (a.x + c.gx) * dt; v.y = v.y + (a.y + c.gy) * dt; v.z = v.z + (a.z + c.gz) * dt;
+    f.vel[i] = v;
+    f.acc[i] = P4<float>{0, 0, 0, 0};
+    const float t = -f.kappa[i] / f.rho[i];
+    const float mx = t < -0.000000001f ? -0.000000001f : t;
+    kbuf[i] = -mx / (dt * dt);
+    f.kappa[i] = 0.f;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kBlock, 8) k_pool_correct(Fluid<float> f, const P4<float>* __restrict__ bpos,
+                                                            const uint32_t* __restrict__ sid, const PoolScene* T,
+                                                            const uint32_t* __restrict__ cs, const uint32_t* __restrict__ bs,
+                                                            Lists<float> L)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= f.n) return;
+    const PoolScene& sd = T[sid[i]];
+    if (!sd.running || (MODE != 0 && !sd.loop_active)) return;
+    const V3<float> sum = correct_sum_one<float, MODE>(i, f, bpos, sd.g, cs + sd.key_base, bs + sd.key_base, sd.c,
+                                                       sd.akinci, L);
+    correct_apply<float, MODE>(i, f, sd.c, (float)sd.s.dt, sum);
+}
+
+// DIV = false: DFSPHSolver::predictDensities; DIV = true:
+// DFSPHSolver::computeDivergenceError.  Adds each scene's error sum.
+template <bool DIV, bool INITIAL>
+__global__ void __launch_bounds__(kBlock, 8) k_pool_errors(Fluid<float> f, const P4<float>* __restrict__ bpos,
+                                                           const uint32_t* __restrict__ sid, PoolScene* T,
+                                                           const uint32_t* __restrict__ cs, const uint32_t* __restrict__ bs,
+                                                           Lists<float> L)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t s = ~0u;
+    unsigned long long contrib = 0ull;
+    if (i < f.n) {
+        const uint32_t k = sid[i];
+        PoolScene& sd = T[k];
+        if (sd.running && (INITIAL || sd.loop_active)) {
+            const Consts<float>& c = sd.c;
+            const float dt = (float)sd.s.dt;
+            const V3<float> vi = xyz(f.vel[i]);
+            uint32_t nn;
+            float d = velocity_div_one(i, f, bpos, sd.g, cs + sd.key_base, bs + sd.key_base, c, sd.akinci, L, vi, &nn);
+            double e;
+            if (DIV) {
+                d = nn < 20u ? 0.f : (d < 0.f ? 0.f : d);
+                f.div[i] = d;
+                L.kbuf[i] = d * f.alpha[i] / (dt * f.rho[i]);
+                e = (double)d / (double)c.density0;
+            } else {
+                const float rho = f.rho[i];
+                float pred = rho + d * dt;
+                pred = pred < c.density0 ? c.density0 : pred;
+                f.pred[i] = pred;
+                L.kbuf[i] = (pred - c.density0) * f.alpha[i] / ((dt * dt) * rho);
+                e = ((double)pred - (double)c.density0) / (double)c.density0;
+            }
+            if (e == e && e < 1e9) {
+                contrib = to_fixed(e);
+            } else {
+                atomicOr(&sd.s.status, (unsigned)ST_NONFINITE);
+            }
+            s = k;
+        }
+    }
+    seg_add(s, contrib, T);
+}
+
+// Loop control per scene after an error reduction (DFSPHSolver.cpp:325-401
+// and :505-585): PHASE 0 density init, 1 density loop, 2 divergence init,
+// 3 divergence loop.  Sets the "any scene still iterating" flag.
+template <int PHASE>
+__global__ void k_pool_control(PoolScene* T, uint32_t S, PoolCounters* pc, cudaGraphConditionalHandle cond)
+{
+    unsigned any = 0;
+    for (uint32_t k = threadIdx.x; k < S; k += blockDim.x) {
+        PoolScene& sd = T[k];
+        const unsigned long long acc = sd.acc;
+        sd.acc = 0ull;
+        if (!sd.running) { sd.loop_active = 0; continue; }
+        const double avg = sd.n ? (double)acc / kFixScale / (double)sd.n : 0.0;
+        const LoopLimits& lim = sd.lim;
+        unsigned act;
+        if (PHASE == 0) {
+            sd.s.iterations = 0;
+            sd.s.avgDensError = avg;
+            act = (lim.minIt > 0u) && (lim.maxIt > 0u);
+        } else if (PHASE == 2) {
+            sd.s.iterationsV = 0;
+            sd.s.avgDivError = avg;
+            act = (lim.minItV > 0u) && (lim.maxIt > 0u);
+        } else {
+            if (!sd.loop_active) continue;
+            if (PHASE == 1) {
+                const unsigned it = ++sd.s.iterations;
+                sd.s.avgDensError = avg;
+                act = ((avg > lim.maxError) || (it < lim.minIt)) && (it < lim.maxIt);
+                if (!act) {
+                    sd.s.sumIterations += it;
+                    if (it >= lim.maxIt && avg > lim.maxError) sd.s.status |= ST_ITER_CAP;
+                }
+            } else {
+                const unsigned it = ++sd.s.iterationsV;
+                const double lim_v = lim.maxErrorV / sd.s.dt;
+                sd.s.avgDivError = avg;
+                act = ((avg > lim_v) || (it < lim.minItV)) && (it < lim.maxIt);
+                if (!act) {
+                    sd.s.sumIterationsV += it;
+                    if (it >= lim.maxIt && avg > lim_v) sd.s.status |= ST_ITER_CAP_V;
+                }
+            }
+        }
+        sd.loop_active = act;
+        any |= act;
+    }
+    any = __syncthreads_or(any);
+    if (threadIdx.x == 0) {
+        if (PHASE == 1 || PHASE == 3) {
+            if (PHASE == 1) pc->body_d += 1;
+            else pc->body_v += 1;
+        }
+        pc->any = any;
+        if (cond) cudaGraphSetConditional(cond, any);
+    }
+}
+
+__global__ void k_pool_finish(PoolScene* T, uint32_t S)
+{
+    for (uint32_t k = threadIdx.x; k < S; k += blockDim.x) {
+        PoolScene& sd = T[k];
+        if (!sd.running) continue;
+        sd.s.time = sd.s.time + sd.s.dt;
+        sd.s.steps += 1;
+        sd.steps_left -= 1;
+        sd.running = sd.steps_left > 0;
+    }
+}
+
+// ===========================================================================
+// Host side
+// ===========================================================================
+
+struct PoolEntry {
+    int id = -1;
+    sph_scene_desc d{};
+    std::vector<double> x, v, b;  // staged until resident
+    unsigned n = 0, nb = 0, steps = 0;
+    GridPlan plan;
+    PoolScene t{};                // last known device entry (layout fields kept by the host)
+    bool resident = false;
+    bool removed = false;
+};
+
+class Pool {
+public:
+    std::string err;
+
+    ~Pool()
+    {
+        for (auto& e : gexec_) if (e) cudaGraphExecDestroy(e);
+        if (st_) cudaStreamDestroy(st_);
+        if (st2_) cudaStreamDestroy(st2_);
+        if (h_pc_) cudaFreeHost(h_pc_);
+    }
+
+    void fail(const std::string& m) { err = m; }
+
+    int create(const sph_pool_desc& d)
+    {
+        pd_ = d;
+        if (d.max_particles == 0 || d.max_scenes == 0 || d.max_keys == 0) { fail("empty pool capacity"); return SPH_ERR_INVALID; }
+        if (d.max_particles >= (1ull << 31) || d.max_boundary >= (1ull << 31) || d.max_keys >= (1ull << 31)) {
+            fail("pool capacity above 2^31");
+            return SPH_ERR_CAPACITY;
+        }
+        kmax_ = d.neighbor_list_max > 0 ? (uint32_t)d.neighbor_list_max : 64u;
+        SPH_CUDA(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
+        SPH_CUDA(cudaStreamCreateWithFlags(&st2_, cudaStreamNonBlocking));
+        ls_ = st_;
+        SPH_CUDA(cudaMallocHost((void**)&h_pc_, sizeof(PoolCounters)));
+        const size_t P = d.max_particles, B = std::max<size_t>(d.max_boundary, 1), K = d.max_keys;
+        for (int k = 0; k < 2; ++k) {
+            SPH_CUDA(pos_[k].alloc(P)); SPH_CUDA(vel_[k].alloc(P)); SPH_CUDA(kappa_[k].alloc(P));
+            SPH_CUDA(kappav_[k].alloc(P)); SPH_CUDA(pred_[k].alloc(P)); SPH_CUDA(cell_[k].alloc(P)); SPH_CUDA(id_[k].alloc(P));
+            SPH_CUDA(bpos_[k].alloc(B)); SPH_CUDA(bcell_[k].alloc(B)); SPH_CUDA(bid_[k].alloc(B));
+        }
+        SPH_CUDA(acc_.alloc(P)); SPH_CUDA(rho_.alloc(P)); SPH_CUDA(alpha_.alloc(P)); SPH_CUDA(div_.alloc(P));
+        SPH_CUDA(press_.alloc(P)); SPH_CUDA(kbuf_.alloc(P)); SPH_CUDA(sid_.alloc(P)); SPH_CUDA(bsid_.alloc(B));
+        SPH_CUDA(bpsi_.alloc(B)); SPH_CUDA(dummy4_.alloc(1));
+        SPH_CUDA(pairs_.alloc(P * kmax_)); SPH_CUDA(lcount_.alloc(P)); SPH_CUDA(bgrad_.alloc(P));
+        const size_t M = std::max(P, B);
+        SPH_CUDA(key_.alloc(M)); SPH_CUDA(slot_.alloc(M)); SPH_CUDA(tmp_.alloc(M));
+        SPH_CUDA(count_.alloc(K)); SPH_CUDA(starts_.alloc(K + 1)); SPH_CUDA(bstarts_.alloc(K + 1));
+        SPH_CUDA(tile_sums_.alloc((K + kScanTile - 1) / kScanTile + 1));
+        SPH_CUDA(cudaMemsetAsync(count_.p, 0, K * sizeof(uint32_t), st_));
+        SPH_CUDA(table_.alloc(d.max_scenes));
+        SPH_CUDA(seg_a_.alloc(d.max_scenes)); SPH_CUDA(seg_b_.alloc(d.max_scenes)); SPH_CUDA(seg_n_.alloc(d.max_scenes));
+        SPH_CUDA(pc_.alloc(1));
+        SPH_CUDA(cudaMemsetAsync(pc_.p, 0, sizeof(PoolCounters), st_));
+        SPH_CUDA(cudaStreamSynchronize(st_));
+        return SPH_OK;
+    }
+
+    // Admission (applied at the next step).  SPH_ERR_CAPACITY: does not fit now.
+    int add(const sph_scene_desc& d, const double* x, const double* v, unsigned n, const double* b, unsigned nb,
+            unsigned steps, int* id)
+    {
+        if (d.simulation_method != SPH_DFSPH || d.boundary_method != SPH_BOUNDARY_AKINCI) {
+            fail("the pool runs DFSPH scenes with Akinci boundaries");
+            return SPH_ERR_UNSUPPORTED;
+        }
+        if (d.surface_tension_method > -1 && d.surface_tension != 0.0) { fail("surface tension is not pooled"); return SPH_ERR_UNSUPPORTED; }
+        if (d.adhesion_method > -1 && d.adhesion != 0.0) { fail("adhesion is not pooled"); return SPH_ERR_UNSUPPORTED; }
+        if (n == 0 || !x) { fail("no fluid particles"); return SPH_ERR_INVALID; }
+        PoolEntry e;
+        e.d = d;
+        e.n = n;
+        e.nb = nb;
+        e.steps = steps;
+        try {
+            e.x.assign(x, x + 3 * (size_t)n);
+            if (v) e.v.assign(v, v + 3 * (size_t)n); else e.v.assign(3 * (size_t)n, 0.0);
+            if (nb) e.b.assign(b, b + 3 * (size_t)nb);
+        } catch (...) {
+            fail("out of host memory");
+            return SPH_ERR_INVALID;
+        }
+        double hh, mass;
+        scene_constants<float>(d, &e.t.c, &e.t.lim, &hh, &mass);
+        int rc = grid_plan(d, e.x, e.b, true, hh, &e.plan, &err);
+        if (rc) return rc;
+        // capacity check against everything resident or pending
+        uint64_t P = 0, B = 0, K = 0;
+        unsigned S = 0;
+        for (auto& q : entries_) {
+            if (q.removed) continue;
+            P += q.n; B += q.nb; K += q.plan.nkeys; ++S;
+        }
+        if (P + n > pd_.max_particles || B + nb > pd_.max_boundary || K + e.plan.nkeys > pd_.max_keys || S + 1 > pd_.max_scenes) {
+            fail("pool full");
+            return SPH_ERR_CAPACITY;
+        }
+        e.id = next_id_++;
+        *id = e.id;
+        entries_.push_back(std::move(e));
+        dirty_ = true;
+        return SPH_OK;
+    }
+
+    int remove(int id)
+    {
+        for (auto& e : entries_)
+            if (e.id == id && !e.removed) {
+                e.removed = true;
+                dirty_ = true;
+                return SPH_OK;
+            }
+        fail("unknown scene id");
+        return SPH_ERR_INVALID;
+    }
+
+    int step(int nsteps)
+    {
+        for (int k = 0; k < nsteps; ++k) {
+            if (dirty_) {
+                const int rc = relayout();
+                if (rc) return rc;
+            }
+            if (S_ == 0) return SPH_OK;
+            const int rc = graph_ ? graph_step() : one_step();
+            if (rc) return rc;
+        }
+        return SPH_OK;
+    }
+
+    int set_graph(int on) { graph_ = on != 0; return SPH_OK; }
+
+    int sync()
+    {
+        SPH_CUDA(cudaStreamSynchronize(st_));
+        return SPH_OK;
+    }
+
+    // Statistics of one scene; *done = its steps have completed.
+    int query(int id, sph_stats* out, int* done)
+    {
+        PoolEntry* e = find(id);
+        if (!e) { fail("unknown scene id"); return SPH_ERR_INVALID; }
+        std::memset(out, 0, sizeof *out);
+        if (!e->resident) {
+            if (done) *done = 0;
+            out->num_fluid = e->n;
+            out->num_boundary = e->nb;
+            return SPH_OK;
+        }
+        PoolScene t;
+        SPH_CUDA(cudaMemcpyAsync(&t, table_.p + slot_of(id), sizeof t, cudaMemcpyDeviceToHost, st_));
+        SPH_CUDA(cudaStreamSynchronize(st_));
+        const DevScalars& s = t.s;
+        out->time = s.time; out->dt = s.dt; out->avg_density_error = s.avgDensError;
+        out->avg_divergence_error = s.avgDivError; out->max_velocity = s.maxVel; out->iterations = s.iterations;
+        out->iterations_v = s.iterationsV; out->steps = s.steps; out->status = s.status;
+        out->sum_iterations = s.sumIterations; out->sum_iterations_v = s.sumIterationsV;
+        out->num_fluid = t.n; out->num_boundary = t.nb;
+        if (done) *done = t.running ? 0 : 1;
+        return SPH_OK;
+    }
+
+    // Ids of resident scenes whose steps have completed (one table read).
+    int poll(int* ids, int max, int* ndone)
+    {
+        std::vector<PoolScene> t(S_);
+        if (S_) SPH_CUDA(cudaMemcpyAsync(t.data(), table_.p, S_ * sizeof(PoolScene), cudaMemcpyDeviceToHost, st_));
+        SPH_CUDA(cudaStreamSynchronize(st_));
+        int k = 0;
+        for (uint32_t s = 0; s < S_; ++s)
+            if (!t[s].running && !order_[s]->removed) {
+                if (ids && k < max) ids[k] = order_[s]->id;
+                ++k;
+            }
+        *ndone = k;
+        return SPH_OK;
+    }
+
+    int download(int id, int field, double* out)
+    {
+        PoolEntry* e = find(id);
+        if (!e || !e->resident) { fail("scene is not resident"); return SPH_ERR_INVALID; }
+        const uint32_t s = slot_of(id);
+        PoolScene t;
+        SPH_CUDA(cudaMemcpyAsync(&t, table_.p + s, sizeof t, cudaMemcpyDeviceToHost, st_));
+        SPH_CUDA(cudaStreamSynchronize(st_));
+        const bool bnd = field == SPH_FIELD_BOUNDARY_POSITION || field == SPH_FIELD_BOUNDARY_VOLUME;
+        const uint32_t n = bnd ? t.nb : t.n, base = bnd ? t.bbase : t.pbase;
+        const bool vec = field == SPH_FIELD_POSITION || field == SPH_FIELD_VELOCITY || field == SPH_FIELD_ACCELERATION ||
+                         field == SPH_FIELD_BOUNDARY_POSITION;
+        const P4<float>* v4 = nullptr;
+        const float* sc = nullptr;
+        int kind = 0;
+        switch (field) {
+            case SPH_FIELD_POSITION: v4 = pos_[cur_].p + base; kind = 1; break;
+            case SPH_FIELD_VELOCITY: v4 = vel_[cur_].p + base; break;
+            case SPH_FIELD_ACCELERATION: v4 = acc_.p + base; break;
+            case SPH_FIELD_DENSITY: sc = rho_.p + base; kind = 2; break;
+            case SPH_FIELD_ALPHA: sc = alpha_.p + base; kind = 2; break;
+            case SPH_FIELD_PRED_DENSITY: sc = pred_[cur_].p + base; kind = 2; break;
+            case SPH_FIELD_DIV_ERROR: sc = div_.p + base; kind = 2; break;
+            case SPH_FIELD_KAPPA: sc = kappa_[cur_].p + base; kind = 2; break;
+            case SPH_FIELD_KAPPA_V: sc = kappav_[cur_].p + base; kind = 2; break;
+            case SPH_FIELD_BOUNDARY_POSITION: v4 = bpos_[bcur_].p + base; kind = 1; break;
+            case SPH_FIELD_BOUNDARY_VOLUME: sc = bpsi_.p + base; kind = 2; break;
+            default: fail("field not available in the pool"); return SPH_ERR_INVALID;
+        }
+        const size_t count = (size_t)n * (vec ? 3 : 1);
+        if (!count) return SPH_OK;
+        DevBuf<double> o;
+        SPH_CUDA(o.alloc(count));
+        const uint32_t* idp = bnd ? bid_[bcur_].p + base : id_[cur_].p + base;
+        const uint32_t* cellp = bnd ? bcell_[bcur_].p + base : cell_[cur_].p + base;
+        k_download<float><<<(n + 255) / 256, 256, 0, st_>>>(n, v4, sc, idp, cellp, t.g, (double)t.c.h, kind, o.p);
+        SPH_CUDA(cudaGetLastError());
+        SPH_CUDA(cudaMemcpyAsync(out, o.p, count * 8, cudaMemcpyDeviceToHost, st_));
+        SPH_CUDA(cudaStreamSynchronize(st_));
+        return SPH_OK;
+    }
+
+    int usage(unsigned long long* p, unsigned long long* b, unsigned long long* k, unsigned* s)
+    {
+        uint64_t P = 0, B = 0, K = 0;
+        unsigned S = 0;
+        for (auto& q : entries_) {
+            if (q.removed) continue;
+            P += q.n; B += q.nb; K += q.plan.nkeys; ++S;
+        }
+        if (p) *p = P;
+        if (b) *b = B;
+        if (k) *k = K;
+        if (s) *s = S;
+        return SPH_OK;
+    }
+
+    // Kernels of this library launched by steps so far.
+    int launches(unsigned long long* out)
+    {
+        SPH_CUDA(cudaMemcpyAsync(h_pc_, pc_.p, sizeof(PoolCounters), cudaMemcpyDeviceToHost, st_));
+        SPH_CUDA(cudaStreamSynchronize(st_));
+        *out = host_launches_ + graph_launches_ + graph_period_kernels();
+        return SPH_OK;
+    }
+
+private:
+    PoolEntry* find(int id)
+    {
+        for (auto& e : entries_)
+            if (e.id == id && !e.removed) return &e;
+        return nullptr;
+    }
+    uint32_t slot_of(int id) const
+    {
+        for (uint32_t s = 0; s < S_; ++s)
+            if (order_[s]->id == id) return s;
+        return 0;
+    }
+    static unsigned blocks(size_t n, unsigned b) { return (unsigned)std::max<size_t>(1, (n + b - 1) / b); }
+
+    Fluid<float> F(int k) const
+    {
+        Fluid<float> f{};
+        f.pos = pos_[k].p; f.vel = vel_[k].p; f.kappa = kappa_[k].p; f.kappav = kappav_[k].p; f.pred = pred_[k].p;
+        f.cell = cell_[k].p; f.id = id_[k].p;
+        f.acc = acc_.p; f.xk = dummy4_.p; f.predR = dummy4_.p; f.predV = dummy4_.p; f.pacc = dummy4_.p;
+        f.normal = dummy4_.p; f.rho = rho_.p; f.alpha = alpha_.p; f.div = div_.p; f.press = press_.p;
+        f.n = N_;
+        return f;
+    }
+    Boundary<float> B(int k) const { return Boundary<float>{bpos_[k].p, bpsi_.p, bcell_[k].p, bid_[k].p, NB_}; }
+    Lists<float> LS() const { return Lists<float>{pairs_.p, lcount_.p, bgrad_.p, kbuf_.p, kmax_}; }
+
+    int scan(uint32_t* out)
+    {
+        const unsigned nt = blocks(K_, kScanTile);
+        run([&] { k_scan_tiles<<<nt, kScanThreads, 0, ls_>>>(K_, count_.p, out, tile_sums_.p); });
+        run([&] { k_scan_tile_sums<<<1, 1024, 0, ls_>>>(nt, tile_sums_.p, out, K_); });
+        run([&] { k_scan_add<<<nt, kScanThreads, 0, ls_>>>(K_, tile_sums_.p, out); });
+        SPH_CUDA(cudaGetLastError());
+        return SPH_OK;
+    }
+
+    // Launch accounting: kernels of host-driven steps are counted as they
+    // are launched, those of a captured step graph per loop part.
+    template <typename Fn> void run(Fn&& fn)
+    {
+        if (capturing_) ++cap_[loop_ctx_];
+        else if (counting_) ++host_launches_;
+        fn();
+    }
+    DevScalars* scalars_of(uint32_t s) const
+    {
+        return reinterpret_cast<DevScalars*>(reinterpret_cast<char*>(table_.p + s) + offsetof(PoolScene, s));
+    }
+
+    // Applies admissions and removals: repack, upload, sort, lists.
+    int relayout()
+    {
+        SPH_CUDA(cudaStreamSynchronize(st_));
+        graph_period_end();
+        counting_ = false;
+        // device-side scene state of the resident scenes back to the host
+        if (S_) {
+            std::vector<PoolScene> t(S_);
+            SPH_CUDA(cudaMemcpy(t.data(), table_.p, S_ * sizeof(PoolScene), cudaMemcpyDeviceToHost));
+            for (uint32_t s = 0; s < S_; ++s) order_[s]->t = t[s];
+        }
+        std::vector<PoolEntry*> keep, fresh;
+        for (auto& e : entries_) {
+            if (e.removed) continue;
+            (e.resident ? keep : fresh).push_back(&e);
+        }
+        std::vector<PoolEntry*> order = keep;
+        order.insert(order.end(), fresh.begin(), fresh.end());
+        // layout: packed in order
+        std::vector<uint32_t> pb(order.size()), bb(order.size()), kb(order.size()), mxo(order.size()), myo(order.size());
+        uint64_t P = 0, Bn = 0, K = 0, MX = 0;
+        for (size_t s = 0; s < order.size(); ++s) {
+            pb[s] = (uint32_t)P; bb[s] = (uint32_t)Bn; kb[s] = (uint32_t)K;
+            mxo[s] = (uint32_t)MX; MX += order[s]->plan.nn[0];
+            myo[s] = (uint32_t)MX; MX += order[s]->plan.nn[1];
+            P += order[s]->n; Bn += order[s]->nb; K += order[s]->plan.nkeys;
+        }
+        // morton tables of every resident scene
+        std::vector<uint32_t> mort(std::max<uint64_t>(MX, 1));
+        for (size_t s = 0; s < order.size(); ++s) {
+            std::copy(order[s]->plan.mx.begin(), order[s]->plan.mx.end(), mort.begin() + mxo[s]);
+            std::copy(order[s]->plan.my.begin(), order[s]->plan.my.end(), mort.begin() + myo[s]);
+        }
+        SPH_CUDA(mort_.alloc(mort.size()));
+        SPH_CUDA(cudaMemcpyAsync(mort_.p, mort.data(), mort.size() * 4, cudaMemcpyHostToDevice, st_));
+        const int nc = 1 - cur_, nbc = 1 - bcur_;
+        // repack kept scenes into the other buffers
+        if (!keep.empty()) {
+            std::vector<uint32_t> a(keep.size()), b(keep.size()), l(keep.size()), ba(keep.size()), bbb(keep.size()),
+                bl(keep.size());
+            for (size_t s = 0; s < keep.size(); ++s) {
+                a[s] = pb[s]; b[s] = keep[s]->t.pbase; l[s] = keep[s]->n;
+                ba[s] = bb[s]; bbb[s] = keep[s]->t.bbase; bl[s] = keep[s]->nb;
+            }
+            const uint32_t Sk = (uint32_t)keep.size();
+            uint32_t Pk = 0, Bk = 0;
+            for (auto* e : keep) { Pk += e->n; Bk += e->nb; }
+            SPH_CUDA(cudaMemcpyAsync(seg_a_.p, a.data(), Sk * 4, cudaMemcpyHostToDevice, st_));
+            SPH_CUDA(cudaMemcpyAsync(seg_b_.p, b.data(), Sk * 4, cudaMemcpyHostToDevice, st_));
+            SPH_CUDA(cudaMemcpyAsync(seg_n_.p, l.data(), Sk * 4, cudaMemcpyHostToDevice, st_));
+            k_repack_fluid<<<blocks(Pk, 256), 256, 0, st_>>>(Pk, seg_a_.p, seg_b_.p, seg_n_.p, Sk, F(cur_), F(nc));
+            SPH_CUDA(cudaGetLastError());
+            SPH_CUDA(cudaStreamSynchronize(st_));
+            if (Bk) {
+                SPH_CUDA(cudaMemcpyAsync(seg_a_.p, ba.data(), Sk * 4, cudaMemcpyHostToDevice, st_));
+                SPH_CUDA(cudaMemcpyAsync(seg_b_.p, bbb.data(), Sk * 4, cudaMemcpyHostToDevice, st_));
+                SPH_CUDA(cudaMemcpyAsync(seg_n_.p, bl.data(), Sk * 4, cudaMemcpyHostToDevice, st_));
+                k_repack_boundary<<<blocks(Bk, 256), 256, 0, st_>>>(Bk, seg_a_.p, seg_b_.p, seg_n_.p, Sk, B(bcur_), B(nbc));
+                SPH_CUDA(cudaGetLastError());
+                SPH_CUDA(cudaStreamSynchronize(st_));
+            }
+        }
+        N_ = (uint32_t)P;
+        NB_ = (uint32_t)Bn;
+        K_ = (uint32_t)K;
+        // scene table
+        std::vector<PoolScene> tab(order.size());
+        for (size_t s = 0; s < order.size(); ++s) {
+            PoolEntry* e = order[s];
+            PoolScene t = e->t;
+            if (!e->resident) {
+                t.s = DevScalars{};
+                t.s.dt = e->d.time_step;
+                t.acc = 0;
+                t.steps_left = e->steps;
+                t.running = e->steps > 0;
+                t.loop_active = 0;
+                t.vmax_bits = 0;
+                t.akinci = 1;
+            }
+            t.g.nx = e->plan.nn[0]; t.g.ny = e->plan.nn[1]; t.g.nz = e->plan.nn[2];
+            t.g.ox = e->plan.o[0]; t.g.oy = e->plan.o[1]; t.g.oz = e->plan.o[2];
+            t.g.mortx = mort_.p + mxo[s];
+            t.g.morty = mort_.p + myo[s];
+            t.key_base = kb[s]; t.n = e->n; t.nb = e->nb; t.pbase = pb[s]; t.bbase = bb[s];
+            tab[s] = t;
+        }
+        S_ = (uint32_t)order.size();
+        SPH_CUDA(cudaMemcpyAsync(table_.p, tab.data(), S_ * sizeof(PoolScene), cudaMemcpyHostToDevice, st_));
+        // upload the new scenes into their segments
+        for (size_t s = keep.size(); s < order.size(); ++s) {
+            PoolEntry* e = order[s];
+            DevBuf<double> tx, tv, tb;
+            SPH_CUDA(tx.alloc(e->x.size()));
+            SPH_CUDA(tv.alloc(e->v.size()));
+            SPH_CUDA(cudaMemcpyAsync(tx.p, e->x.data(), e->x.size() * 8, cudaMemcpyHostToDevice, st_));
+            SPH_CUDA(cudaMemcpyAsync(tv.p, e->v.data(), e->v.size() * 8, cudaMemcpyHostToDevice, st_));
+            Fluid<float> f = F(nc);
+            f.pos += pb[s]; f.vel += pb[s]; f.kappa += pb[s]; f.kappav += pb[s]; f.cell += pb[s]; f.id += pb[s];
+            f.acc += pb[s]; f.press += pb[s];
+            DevScalars* sst = scalars_of(s);
+            k_upload_fluid<float><<<blocks(e->n, 256), 256, 0, st_>>>(tx.p, tv.p, e->n, 0, f, tab[s].g, 4.0 * e->d.particle_radius, sst);
+            SPH_CUDA(cudaMemsetAsync(pred_[nc].p + pb[s], 0, e->n * sizeof(float), st_));
+            if (e->nb) {
+                SPH_CUDA(tb.alloc(e->b.size()));
+                SPH_CUDA(cudaMemcpyAsync(tb.p, e->b.data(), e->b.size() * 8, cudaMemcpyHostToDevice, st_));
+                Boundary<float> bo = B(nbc);
+                bo.pos += bb[s]; bo.cell += bb[s]; bo.id += bb[s];
+                k_upload_boundary<float><<<blocks(e->nb, 256), 256, 0, st_>>>(tb.p, e->nb, bo, tab[s].g, 4.0 * e->d.particle_radius, sst);
+            }
+            SPH_CUDA(cudaGetLastError());
+            SPH_CUDA(cudaStreamSynchronize(st_));
+            e->resident = true;
+            std::vector<double>().swap(e->x);
+            std::vector<double>().swap(e->v);
+            std::vector<double>().swap(e->b);
+        }
+        cur_ = nc;
+        bcur_ = nbc;
+        // drop removed entries; the resident order is the layout order
+        entries_.remove_if([](const PoolEntry& e) { return e.removed; });
+        order_ = order;
+        any_forces_ = false;
+        for (uint32_t s = 0; s < S_; ++s) {
+            order_[s]->t = tab[s];
+            any_forces_ |= (tab[s].c.force_flags & (F_XSPH | F_STD_VISC | F_ART_VISC)) != 0;
+        }
+        // scene ids of fluid and boundary particles
+        std::vector<uint32_t> pbv(pb.begin(), pb.end()), bbv(bb.begin(), bb.end());
+        SPH_CUDA(cudaMemcpyAsync(seg_a_.p, pbv.data(), S_ * 4, cudaMemcpyHostToDevice, st_));
+        k_fill_sid<<<blocks(N_, 256), 256, 0, st_>>>(N_, seg_a_.p, S_, sid_.p);
+        SPH_CUDA(cudaStreamSynchronize(st_));
+        if (NB_) {
+            SPH_CUDA(cudaMemcpyAsync(seg_a_.p, bbv.data(), S_ * 4, cudaMemcpyHostToDevice, st_));
+            k_fill_sid<<<blocks(NB_, 256), 256, 0, st_>>>(NB_, seg_a_.p, S_, bsid_.p);
+            SPH_CUDA(cudaStreamSynchronize(st_));
+        }
+        // boundary: sort by (key, id) -- kept scenes are already in order -- and volumes
+        if (NB_) {
+            k_pool_bcount<<<blocks(NB_, 256), 256, 0, st_>>>(NB_, B(bcur_), bsid_.p, table_.p, key_.p, slot_.p, count_.p);
+            int rc = scan(bstarts_.p);
+            if (rc) return rc;
+            k_scatter<<<blocks(NB_, 256), 256, 0, st_>>>(NB_, key_.p, slot_.p, bstarts_.p, tmp_.p);
+            k_gather_boundary<float><<<blocks(NB_, 256), 256, 0, st_>>>(NB_, tmp_.p, key_.p, bstarts_.p, B(bcur_), B(1 - bcur_));
+            SPH_CUDA(cudaGetLastError());
+            bcur_ = 1 - bcur_;
+            k_pool_psi<<<blocks(NB_, 128), 128, 0, st_>>>(NB_, B(bcur_), bsid_.p, table_.p, bstarts_.p);
+            SPH_CUDA(cudaGetLastError());
+        } else {
+            SPH_CUDA(cudaMemsetAsync(bstarts_.p, 0, (K_ + 1) * sizeof(uint32_t), st_));
+        }
+        // fluid grid and lists (DFSPHSolver::init for new scenes; identical
+        // recomputation for the kept ones, whose positions have not moved)
+        int rc = build_grid(false);
+        if (rc) return rc;
+        run([&] { k_pool_build_lists<<<blocks(N_, kBlock), kBlock, 0, ls_>>>(F(cur_), bpos_[bcur_].p, sid_.p, table_.p, starts_.p,
+                                                                           bstarts_.p, LS()); });
+        SPH_CUDA(cudaGetLastError());
+        SPH_CUDA(cudaStreamSynchronize(st_));
+        counting_ = true;
+        for (auto& e : gexec_) if (e) { cudaGraphExecDestroy(e); e = nullptr; }
+        dirty_ = false;
+        graph_period_begin();
+        return SPH_OK;
+    }
+
+    int build_grid(bool move)
+    {
+        Fluid<float> a = F(cur_);
+        if (move)
+            run([&] { k_pool_cell_update<true><<<blocks(N_, 256), 256, 0, ls_>>>(N_, a, sid_.p, table_.p, key_.p, slot_.p, count_.p); });
+        else
+            run([&] { k_pool_cell_update<false><<<blocks(N_, 256), 256, 0, ls_>>>(N_, a, sid_.p, table_.p, key_.p, slot_.p, count_.p); });
+        SPH_CUDA(cudaGetLastError());
+        int rc = scan(starts_.p);
+        if (rc) return rc;
+        run([&] { k_scatter<<<blocks(N_, 256), 256, 0, ls_>>>(N_, key_.p, slot_.p, starts_.p, tmp_.p); });
+        run([&] { k_gather_fluid<float><<<blocks(N_, 256), 256, 0, ls_>>>(N_, tmp_.p, key_.p, starts_.p, F(cur_), F(1 - cur_)); });
+        SPH_CUDA(cudaGetLastError());
+        cur_ = 1 - cur_;
+        return SPH_OK;
+    }
+
+    template <typename Init, typename Body> int solve_loop(int loop_id, Init&& init, Body&& body)
+    {
+        if (capturing_) {
+            cudaStreamCaptureStatus cs;
+            cudaGraph_t g;
+            const cudaGraphNode_t* deps = nullptr;
+            size_t ndeps = 0;
+            SPH_CUDA(cudaStreamGetCaptureInfo(st_, &cs, nullptr, &g, nullptr, nullptr, nullptr));
+            cudaGraphConditionalHandle h;
+            SPH_CUDA(cudaGraphConditionalHandleCreate(&h, g, 0, 0));
+            init(h);
+            SPH_CUDA(cudaGetLastError());
+            SPH_CUDA(cudaStreamGetCaptureInfo(st_, &cs, nullptr, &g, &deps, nullptr, &ndeps));
+            cudaGraphNodeParams p{};
+            p.type = cudaGraphNodeTypeConditional;
+            p.conditional.handle = h;
+            p.conditional.type = cudaGraphCondTypeWhile;
+            p.conditional.size = 1;
+            cudaGraphNode_t node;
+            SPH_CUDA(cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &p));
+            cudaGraph_t bodyg = p.conditional.phGraph_out[0];
+            SPH_CUDA(cudaStreamUpdateCaptureDependencies(st_, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+            SPH_CUDA(cudaStreamBeginCaptureToGraph(st2_, bodyg, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+            ls_ = st2_;
+            loop_ctx_ = loop_id;
+            body(h);
+            loop_ctx_ = 0;
+            ls_ = st_;
+            cudaGraph_t out;
+            SPH_CUDA(cudaStreamEndCapture(st2_, &out));
+            return SPH_OK;
+        }
+        init((cudaGraphConditionalHandle)0);
+        SPH_CUDA(cudaGetLastError());
+        for (unsigned it = 0; it < 1000u; ++it) {
+            SPH_CUDA(cudaMemcpyAsync(h_pc_, pc_.p, sizeof(PoolCounters), cudaMemcpyDeviceToHost, st_));
+            SPH_CUDA(cudaStreamSynchronize(st_));
+            if (!h_pc_->any) break;
+            if (loop_id == 1) ++host_body_d_; else ++host_body_v_;
+            body((cudaGraphConditionalHandle)0);
+            SPH_CUDA(cudaGetLastError());
+        }
+        return SPH_OK;
+    }
+
+    // DFSPHSolver::step (DFSPHSolver.cpp:38-112) for every running scene.
+    int one_step()
+    {
+        const unsigned nb = blocks(N_, kBlock);
+        const unsigned nb256 = blocks(N_, 256);
+        {
+            Fluid<float> f = F(cur_);
+            const P4<float>* bp = bpos_[bcur_].p;
+            Lists<float> L = LS();
+            if (any_forces_)
+                run([&] { k_pool_npforce<<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p); });
+            run([&] { k_pool_cfl_accum<<<nb256, 256, 0, ls_>>>(f, sid_.p, table_.p); });
+            run([&] { k_pool_cfl_control<<<1, 256, 0, ls_>>>(table_.p, S_); });
+            run([&] { k_pool_predict_v_warm<<<nb256, 256, 0, ls_>>>(f, sid_.p, table_.p, L.kbuf); });
+            run([&] { k_pool_correct<0><<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
+            SPH_CUDA(cudaGetLastError());
+            int rc = solve_loop(
+                1,
+                [&](cudaGraphConditionalHandle h) {
+                    run([&] { k_pool_errors<false, true><<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
+                    run([&] { k_pool_control<0><<<1, 256, 0, ls_>>>(table_.p, S_, pc_.p, h); });
+                },
+                [&](cudaGraphConditionalHandle h) {
+                    run([&] { k_pool_correct<1><<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
+                    run([&] { k_pool_errors<false, false><<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
+                    run([&] { k_pool_control<1><<<1, 256, 0, ls_>>>(table_.p, S_, pc_.p, h); });
+                });
+            if (rc) return rc;
+        }
+        int rc = build_grid(true);
+        if (rc) return rc;
+        {
+            Fluid<float> f = F(cur_);
+            const P4<float>* bp = bpos_[bcur_].p;
+            Lists<float> L = LS();
+            run([&] { k_pool_build_lists<<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
+            SPH_CUDA(cudaGetLastError());
+            rc = solve_loop(
+                2,
+                [&](cudaGraphConditionalHandle h) {
+                    run([&] { k_pool_errors<true, true><<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
+                    run([&] { k_pool_control<2><<<1, 256, 0, ls_>>>(table_.p, S_, pc_.p, h); });
+                },
+                [&](cudaGraphConditionalHandle h) {
+                    run([&] { k_pool_correct<2><<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
+                    run([&] { k_pool_errors<true, false><<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
+                    run([&] { k_pool_control<3><<<1, 256, 0, ls_>>>(table_.p, S_, pc_.p, h); });
+                });
+            if (rc) return rc;
+        }
+        run([&] { k_pool_finish<<<1, 256, 0, ls_>>>(table_.p, S_); });
+        SPH_CUDA(cudaGetLastError());
+        return SPH_OK;
+    }
+
+    int graph_step()
+    {
+        const int k = cur_;
+        if (!gexec_[k]) {
+            cudaGraph_t g;
+            SPH_CUDA(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
+            capturing_ = true;
+            cap_[0] = cap_[1] = cap_[2] = 0;
+            const int rc = one_step();
+            capturing_ = false;
+            cudaError_t e = cudaStreamEndCapture(st_, &g);
+            if (rc) { if (e == cudaSuccess) cudaGraphDestroy(g); cur_ = k; return rc; }
+            SPH_CUDA(e);
+            SPH_CUDA(cudaGraphInstantiate(&gexec_[k], g, 0));
+            cudaGraphDestroy(g);
+            cur_ = k;
+            // the loop-control kernel is part of each body and of the fixed part
+            fixed_ = cap_[0];
+            body_d_size_ = cap_[1];
+            body_v_size_ = cap_[2];
+        }
+        SPH_CUDA(cudaGraphLaunch(gexec_[k], st_));
+        ++gsteps_;
+        cur_ = 1 - k;
+        return SPH_OK;
+    }
+
+    // Graph kernels of the current layout (h_pc_ must be current).  Loop
+    // bodies are counted from the device's body counters, which host-driven
+    // steps advance too; those are subtracted via host_body_*.
+    unsigned long long graph_period_kernels() const
+    {
+        if (!gsteps_) return 0ull;
+        return gsteps_ * fixed_ + body_d_size_ * (h_pc_->body_d - snap_d_ - host_body_d_) +
+               body_v_size_ * (h_pc_->body_v - snap_v_ - host_body_v_);
+    }
+    void graph_period_begin()
+    {
+        cudaMemcpy(h_pc_, pc_.p, sizeof(PoolCounters), cudaMemcpyDeviceToHost);
+        snap_d_ = h_pc_->body_d;
+        snap_v_ = h_pc_->body_v;
+        host_body_d_ = host_body_v_ = 0;
+        gsteps_ = 0;
+    }
+    void graph_period_end()
+    {
+        cudaMemcpy(h_pc_, pc_.p, sizeof(PoolCounters), cudaMemcpyDeviceToHost);
+        graph_launches_ += graph_period_kernels();
+    }
+
+public:
+    unsigned long long total_launches()
+    {
+        unsigned long long k = 0;
+        launches(&k);
+        return k;
+    }
+
+private:
+    sph_pool_desc pd_{};
+    cudaStream_t st_ = nullptr, st2_ = nullptr, ls_ = nullptr;
+    PoolCounters* h_pc_ = nullptr;
+    std::list<PoolEntry> entries_;  // stable addresses: order_ points into it
+    std::vector<PoolEntry*> order_;
+    int next_id_ = 1;
+    bool dirty_ = false, graph_ = false, capturing_ = false;
+    uint32_t S_ = 0, N_ = 0, NB_ = 0, K_ = 0, kmax_ = 64;
+    int cur_ = 0, bcur_ = 0;
+    int loop_ctx_ = 0;
+    unsigned cap_[3] = {0, 0, 0};
+    unsigned long long fixed_ = 0, body_d_size_ = 0, body_v_size_ = 0, gsteps_ = 0, snap_d_ = 0, snap_v_ = 0;
+    unsigned long long host_launches_ = 0, graph_launches_ = 0, host_body_d_ = 0, host_body_v_ = 0;
+    bool counting_ = true, any_forces_ = false;
+    cudaGraphExec_t gexec_[2] = {nullptr, nullptr};
+    DevBuf<P4<float>> pos_[2], vel_[2], bpos_[2];
+    DevBuf<float> kappa_[2], kappav_[2], pred_[2];
+    DevBuf<uint32_t> cell_[2], id_[2], bcell_[2], bid_[2];
+    DevBuf<P4<float>> acc_, dummy4_, pairs_, bgrad_;
+    DevBuf<float> rho_, alpha_, div_, press_, kbuf_, bpsi_;
+    DevBuf<uint32_t> sid_, bsid_, lcount_, key_, slot_, tmp_, count_, starts_, bstarts_, tile_sums_, mort_;
+    DevBuf<uint32_t> seg_a_, seg_b_, seg_n_;
+    DevBuf<PoolScene> table_;
+    DevBuf<PoolCounters> pc_;
+};
+
+}  // namespace sph
+
+struct sph_pool {
+    sph::Pool pool;
+};
+
+static int pool_bad(sph_pool* p, const char* m)
+{
+    if (p) p->pool.err = m;
+    return SPH_ERR_INVALID;
+}
+
+extern "C" {
+
+int sph_pool_desc_from_budget(unsigned long long hbm_bytes, int neighbor_list_max, sph_pool_desc* out)
+{
+    if (!out || hbm_bytes < (1ull << 20)) return SPH_ERR_INVALID;
+    const unsigned long long kmax = neighbor_list_max > 0 ? (unsigned long long)neighbor_list_max : 64ull;
+    // bytes per fluid particle (double-buffered carried state, shared fields,
+    // sort scratch, pair-list slots), per boundary particle and per grid key,
+    // with one boundary particle and sixteen keys budgeted per fluid particle
+    const unsigned long long per_p = 2 * (16 + 16 + 4 + 4 + 4 + 4 + 4) + (16 + 4 + 4 + 4 + 4 + 4 + 4 + 4 + 16) +
+                                     3 * 4 + kmax * 16;
+    const unsigned long long per_b = 2 * (16 + 4 + 4) + 4 + 4;
+    const unsigned long long per_k = 3 * 4;
+    const unsigned long long unit = per_p + per_b + 16 * per_k;
+    std::memset(out, 0, sizeof *out);
+    out->max_particles = hbm_bytes / unit;
+    out->max_boundary = out->max_particles;
+    out->max_keys = 16 * out->max_particles;
+    out->max_scenes = 4096;
+    out->neighbor_list_max = (int)kmax;
+    if (out->max_particles >= (1ull << 31)) {
+        out->max_particles = (1ull << 31) - 1;
+        out->max_boundary = out->max_particles;
+        out->max_keys = (1ull << 31) - 1;
+    }
+    return SPH_OK;
+}
+
+int sph_pool_create(const sph_pool_desc* desc, sph_pool** out)
+{
+    if (!desc || !out) return SPH_ERR_INVALID;
+    *out = nullptr;
+    sph_pool* p = new (std::nothrow) sph_pool();
+    if (!p) return SPH_ERR_INVALID;
+    const int rc = p->pool.create(*desc);
+    if (rc) {
+        delete p;
+        return rc;
+    }
+    *out = p;
+    return SPH_OK;
+}
+
+int sph_pool_destroy(sph_pool* p)
+{
+    if (!p) return SPH_ERR_INVALID;
+    delete p;
+    return SPH_OK;
+}
+
+int sph_pool_add_scene(sph_pool* p, const sph_scene_desc* d, const double* x, const double* v, unsigned n,
+                       const double* bx, unsigned nb, unsigned steps, int* scene_id)
+{
+    if (!p || !d || !scene_id || (nb && !bx)) return pool_bad(p, "invalid argument");
+    return p->pool.add(*d, x, v, n, bx, nb, steps, scene_id);
+}
+
+int sph_pool_remove_scene(sph_pool* p, int scene_id)
+{
+    if (!p) return SPH_ERR_INVALID;
+    return p->pool.remove(scene_id);
+}
+
+int sph_pool_step(sph_pool* p, int nsteps)
+{
+    if (!p || nsteps < 0) return pool_bad(p, "invalid argument");
+    return p->pool.step(nsteps);
+}
+
+int sph_pool_set_graph(sph_pool* p, int enable)
+{
+    if (!p) return SPH_ERR_INVALID;
+    return p->pool.set_graph(enable);
+}
+
+int sph_pool_synchronize(sph_pool* p)
+{
+    if (!p) return SPH_ERR_INVALID;
+    return p->pool.sync();
+}
+
+int sph_pool_query(sph_pool* p, int scene_id, sph_stats* out, int* done)
+{
+    if (!p || !out) return pool_bad(p, "invalid argument");
+    return p->pool.query(scene_id, out, done);
+}
+
+int sph_pool_poll(sph_pool* p, int* done_ids, int max_ids, int* num_done)
+{
+    if (!p || !num_done) return pool_bad(p, "invalid argument");
+    return p->pool.poll(done_ids, max_ids, num_done);
+}
+
+int sph_pool_download(sph_pool* p, int scene_id, int field, double* out)
+{
+    if (!p || !out) return pool_bad(p, "invalid argument");
+    return p->pool.download(scene_id, field, out);
+}
+
+int sph_pool_usage(sph_pool* p, unsigned long long* particles, unsigned long long* boundary, unsigned long long* keys,
+                   unsigned* scenes)
+{
+    if (!p) return SPH_ERR_INVALID;
+    return p->pool.usage(particles, boundary, keys, scenes);
+}
+
+int sph_pool_get_launch_count(sph_pool* p, unsigned long long* out)
+{
+    if (!p || !out) return pool_bad(p, "invalid argument");
+    *out = p->pool.total_launches();
+    return SPH_OK;
+}
+
+const char* sph_pool_last_error(const sph_pool* p)
+{
+    if (!p) return "null pool";
+    return p->pool.err.c_str();
+}
+
+}  // extern "C"

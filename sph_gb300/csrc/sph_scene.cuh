@@ -26,6 +26,151 @@
 
 namespace sph {
 
+// Kernel coefficients, evaluated in double as each reference kernel's
+// setSupportRadius does (CubicSpline.h:18-26, Poly6.h:19-28, Spiky.h:18-27,
+// ViscoK.h:18-26, Cohesion.h:20-27), the particle mass of
+// Simulation::initMasses (Simulation.cpp:134-146), the plugin selection of
+// FluidModel::set*Force (FluidModel.cpp:73-122) and the solver limits
+// (defaults SPHSolver.cpp:12-19, DFSPHSolver.cpp:10-22).
+template <typename R>
+void scene_constants(const sph_scene_desc& d, Consts<R>* out_c, LoopLimits* out_l, double* out_h, double* out_mass)
+{
+    const double r = d.particle_radius;
+    const double sr = 4.0 * r;
+    const double pi = M_PI;
+    const double h3 = sr * sr * sr;
+    const double h6 = sr * sr * sr * sr * sr * sr;
+    const double h9 = sr * sr * sr * sr * sr * sr * sr * sr * sr;
+    const double diameter = 2.0 * r;
+    const double mass = d.density0 * std::pow(diameter, 3.0);
+    Consts<R> c{};
+    c.h = (R)sr;
+    c.inv_h = (R)(1.0 / sr);
+    c.h2 = (R)(sr * sr);
+    c.cull2 = (R)(sr * sr * (sizeof(R) == 8 ? (1.0 + 1e-12) : (1.0 + 1e-6)));
+    c.cs_k = (R)(8.0 / (pi * h3));
+    c.cs_l = (R)(48.0 / (pi * h3));
+    c.p6_h2 = (R)(sr * sr);
+    c.p6_value = (R)(315.0 / (64.0 * M_PI * h9));
+    c.p6_grad = (R)(945.0 / (32.0 * M_PI * h9));
+    c.sp_value = (R)(15.0 / (M_PI * h6));
+    c.sp_grad = (R)(45.0 / (M_PI * h6));
+    c.vk_lapl = (R)(45 / (M_PI * h6));
+    c.co_c1 = (R)(32.0 / (M_PI * h9));
+    c.co_c2 = (R)(h6 / 64.0);
+    c.mass = (R)mass;
+    c.density0 = (R)d.density0;
+    c.eps = (R)1e-5;
+    c.gx = (R)d.gravity[0]; c.gy = (R)d.gravity[1]; c.gz = (R)d.gravity[2];
+    c.stiffness = (R)d.stiffness;
+    c.gamma = (R)d.gamma;
+    c.k_eos = (R)(d.stiffness * d.density0 / d.gamma);
+    c.visc = (R)d.viscosity;
+    c.bvisc = (R)d.boundary_viscosity;
+    c.st = (R)d.surface_tension;
+    c.adh = (R)d.adhesion;
+    for (int k = 0; k < 3; ++k) { c.cube_min[k] = (R)d.cube_min[k]; c.cube_max[k] = (R)d.cube_max[k]; }
+    c.has_cube = (d.boundary_method == SPH_BOUNDARY_CUBE && d.has_cube) ? 1 : 0;
+    int fl = 0;
+    if (d.viscosity_method > -1 && d.viscosity != 0.0) {
+        if (d.viscosity_method == SPH_VISCOSITY_STANDARD) fl |= F_STD_VISC;
+        else if (d.viscosity_method == SPH_VISCOSITY_ARTIFICIAL) fl |= F_ART_VISC;
+        else if (d.viscosity_method == SPH_VISCOSITY_XSPH) fl |= F_XSPH;
+        if (d.boundary_viscosity != 0.0) fl |= F_BVISC;
+    }
+    if (d.surface_tension_method == SPH_SURFACE_TENSION_AKINCI && d.surface_tension != 0.0) fl |= F_SURFACE_TENSION;
+    if (d.adhesion_method == SPH_ADHESION_AKINCI && d.adhesion != 0.0) fl |= F_ADHESION;
+    c.force_flags = fl;
+    LoopLimits l{};
+    l.maxError = 0.01; l.minIt = 3; l.maxIt = 100; l.maxErrorV = 0.001; l.minItV = 1; l.maxItV = 100;
+    l.cflFactor = 1.0;
+    if (d.simulation_method == SPH_DFSPH) { l.minIt = 2; l.maxIt = 100; }
+    if (d.simulation_method != SPH_WCSPH) l.maxError = d.max_error;
+    if (d.simulation_method == SPH_DFSPH) { l.maxErrorV = d.max_error_v; l.cflFactor = d.cfl_factor; }
+    if (d.min_iterations >= 0) l.minIt = (unsigned)d.min_iterations;
+    if (d.max_iterations >= 0) l.maxIt = (unsigned)d.max_iterations;
+    if (d.min_iterations_v >= 0) l.minItV = (unsigned)d.min_iterations_v;
+    if (d.max_iterations_v >= 0) l.maxItV = (unsigned)d.max_iterations_v;
+    l.particleRadius = d.particle_radius;
+    // TimeManager::setMinTimeStep keeps min(minTs, 1/fps) (TimeManager.h:55)
+    const double minFPSTimeStep = 1.0 / d.fps;
+    l.minTs = minFPSTimeStep < d.min_time_step ? minFPSTimeStep : d.min_time_step;
+    l.maxTs = d.max_time_step;
+    *out_c = c;
+    *out_l = l;
+    *out_h = sr;
+    *out_mass = mass;
+}
+
+// Dense cell box over the domain (given, or the points' bounds + 5 %) with a
+// two-cell margin, and the column-Morton tables of its key space.
+struct GridPlan {
+    int o[3] = {0, 0, 0}, nn[3] = {0, 0, 0};
+    std::vector<uint32_t> mx, my;
+    uint64_t nkeys = 0;
+};
+
+inline int grid_plan(const sph_scene_desc& d, const std::vector<double>& hx, const std::vector<double>& hb, bool akinci,
+                     double h, GridPlan* out, std::string* err)
+{
+    double lo[3], hi[3];
+    bool given = false;
+    for (int k = 0; k < 3; ++k) given |= d.domain_max[k] > d.domain_min[k];
+    if (given) {
+        for (int k = 0; k < 3; ++k) { lo[k] = d.domain_min[k]; hi[k] = d.domain_max[k]; }
+    } else {
+        for (int k = 0; k < 3; ++k) { lo[k] = 1e300; hi[k] = -1e300; }
+        auto acc = [&](const std::vector<double>& v) {
+            for (size_t i = 0; i + 2 < v.size(); i += 3)
+                for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], v[i + k]); hi[k] = std::max(hi[k], v[i + k]); }
+        };
+        acc(hx);
+        if (akinci) acc(hb);
+        if (d.boundary_method == SPH_BOUNDARY_CUBE && d.has_cube)
+            for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], d.cube_min[k]); hi[k] = std::max(hi[k], d.cube_max[k]); }
+        for (int k = 0; k < 3; ++k) {
+            const double ext = hi[k] - lo[k];
+            lo[k] -= 0.05 * ext;
+            hi[k] += 0.05 * ext;
+        }
+    }
+    GridPlan p;
+    for (int k = 0; k < 3; ++k) {
+        p.o[k] = (int)std::floor(lo[k] / h) - 2;
+        p.nn[k] = (int)std::floor(hi[k] / h) + 3 - p.o[k];
+    }
+    if (p.nn[0] > 2048 || p.nn[1] > 2048 || p.nn[2] > 1024 || p.nn[0] < 1 || p.nn[1] < 1 || p.nn[2] < 1) {
+        *err = "grid box too large for the cell packing (max 2048 x 2048 x 1024 cells)";
+        return SPH_ERR_CAPACITY;
+    }
+    int bx = 0, by = 0;
+    while ((1 << bx) < p.nn[0]) ++bx;
+    while ((1 << by) < p.nn[1]) ++by;
+    p.mx.assign(p.nn[0], 0u);
+    p.my.assign(p.nn[1], 0u);
+    // interleave bit k of x and y (x first) while both have bits left
+    int pos = 0;
+    std::vector<int> px(bx), py(by);
+    for (int k = 0; k < std::max(bx, by); ++k) {
+        if (k < bx) px[k] = pos++;
+        if (k < by) py[k] = pos++;
+    }
+    for (int v = 0; v < p.nn[0]; ++v) {
+        uint32_t m = 0;
+        for (int k = 0; k < bx; ++k) if (v >> k & 1) m |= 1u << px[k];
+        p.mx[v] = m;
+    }
+    for (int v = 0; v < p.nn[1]; ++v) {
+        uint32_t m = 0;
+        for (int k = 0; k < by; ++k) if (v >> k & 1) m |= 1u << py[k];
+        p.my[v] = m;
+    }
+    p.nkeys = (1ull << (bx + by)) * (uint64_t)p.nn[2];
+    if (p.nkeys > (1ull << 30)) { *err = "grid key space too large"; return SPH_ERR_CAPACITY; }
+    *out = std::move(p);
+    return SPH_OK;
+}
+
 template <typename T> struct DevBuf {
     T* p = nullptr;
     size_t n = 0;
@@ -420,74 +565,7 @@ private:
     // mass of Simulation::initMasses (Simulation.cpp:134-146).
     void setup_constants()
     {
-        const double r = d.particle_radius;
-        const double sr = 4.0 * r;
-        hd_ = sr;
-        const double pi = M_PI;
-        const double h3 = sr * sr * sr;
-        const double h6 = sr * sr * sr * sr * sr * sr;
-        const double h9 = sr * sr * sr * sr * sr * sr * sr * sr * sr;
-        const double diameter = 2.0 * r;
-        mass_ = d.density0 * std::pow(diameter, 3.0);
-        Consts<R> c{};
-        c.h = (R)sr;
-        c.inv_h = (R)(1.0 / sr);
-        c.h2 = (R)(sr * sr);
-        c.cull2 = (R)(sr * sr * (sizeof(R) == 8 ? (1.0 + 1e-12) : (1.0 + 1e-6)));
-        c.cs_k = (R)(8.0 / (pi * h3));
-        c.cs_l = (R)(48.0 / (pi * h3));
-        c.p6_h2 = (R)(sr * sr);
-        c.p6_value = (R)(315.0 / (64.0 * M_PI * h9));
-        c.p6_grad = (R)(945.0 / (32.0 * M_PI * h9));
-        c.sp_value = (R)(15.0 / (M_PI * h6));
-        c.sp_grad = (R)(45.0 / (M_PI * h6));
-        c.vk_lapl = (R)(45 / (M_PI * h6));
-        c.co_c1 = (R)(32.0 / (M_PI * h9));
-        c.co_c2 = (R)(h6 / 64.0);
-        c.mass = (R)mass_;
-        c.density0 = (R)d.density0;
-        c.eps = (R)1e-5;
-        c.gx = (R)d.gravity[0]; c.gy = (R)d.gravity[1]; c.gz = (R)d.gravity[2];
-        c.stiffness = (R)d.stiffness;
-        c.gamma = (R)d.gamma;
-        c.k_eos = (R)(d.stiffness * d.density0 / d.gamma);
-        c.visc = (R)d.viscosity;
-        c.bvisc = (R)d.boundary_viscosity;
-        c.st = (R)d.surface_tension;
-        c.adh = (R)d.adhesion;
-        for (int k = 0; k < 3; ++k) { c.cube_min[k] = (R)d.cube_min[k]; c.cube_max[k] = (R)d.cube_max[k]; }
-        c.has_cube = (d.boundary_method == SPH_BOUNDARY_CUBE && d.has_cube) ? 1 : 0;
-        int fl = 0;
-        // plugin selection of FluidModel::setViscosityForce / setSurfaceTensionForce /
-        // setAdhesionForce (FluidModel.cpp:73-122) as called by Simulation::importScene
-        // (Simulation.cpp:423-430)
-        if (d.viscosity_method > -1 && d.viscosity != 0.0) {
-            if (d.viscosity_method == SPH_VISCOSITY_STANDARD) fl |= F_STD_VISC;
-            else if (d.viscosity_method == SPH_VISCOSITY_ARTIFICIAL) fl |= F_ART_VISC;
-            else if (d.viscosity_method == SPH_VISCOSITY_XSPH) fl |= F_XSPH;
-            if (d.boundary_viscosity != 0.0) fl |= F_BVISC;
-        }
-        if (d.surface_tension_method == SPH_SURFACE_TENSION_AKINCI && d.surface_tension != 0.0) fl |= F_SURFACE_TENSION;
-        if (d.adhesion_method == SPH_ADHESION_AKINCI && d.adhesion != 0.0) fl |= F_ADHESION;
-        c.force_flags = fl;
-        c_ = c;
-        // solver limits (defaults SPHSolver.cpp:12-19, DFSPHSolver.cpp:10-22)
-        LoopLimits l{};
-        l.maxError = 0.01; l.minIt = 3; l.maxIt = 100; l.maxErrorV = 0.001; l.minItV = 1; l.maxItV = 100;
-        l.cflFactor = 1.0;
-        if (d.simulation_method == SPH_DFSPH) { l.minIt = 2; l.maxIt = 100; }
-        if (d.simulation_method != SPH_WCSPH) l.maxError = d.max_error;
-        if (d.simulation_method == SPH_DFSPH) { l.maxErrorV = d.max_error_v; l.cflFactor = d.cfl_factor; }
-        if (d.min_iterations >= 0) l.minIt = (unsigned)d.min_iterations;
-        if (d.max_iterations >= 0) l.maxIt = (unsigned)d.max_iterations;
-        if (d.min_iterations_v >= 0) l.minItV = (unsigned)d.min_iterations_v;
-        if (d.max_iterations_v >= 0) l.maxItV = (unsigned)d.max_iterations_v;
-        l.particleRadius = d.particle_radius;
-        // TimeManager::setMinTimeStep keeps min(minTs, 1/fps) (TimeManager.h:55)
-        const double minFPSTimeStep = 1.0 / d.fps;
-        l.minTs = minFPSTimeStep < d.min_time_step ? minFPSTimeStep : d.min_time_step;
-        l.maxTs = d.max_time_step;
-        lim_ = l;
+        scene_constants<R>(d, &c_, &lim_, &hd_, &mass_);
     }
 
     // PCISPHSolver::computeScalingFactor PCISPHSolver.cpp:389-421 (Poly6
@@ -523,68 +601,16 @@ private:
     // Dense cell box over the domain with a margin; column-Morton key space.
     int setup_grid()
     {
-        double lo[3], hi[3];
-        bool given = false;
-        for (int k = 0; k < 3; ++k) given |= d.domain_max[k] > d.domain_min[k];
-        if (given) {
-            for (int k = 0; k < 3; ++k) { lo[k] = d.domain_min[k]; hi[k] = d.domain_max[k]; }
-        } else {
-            for (int k = 0; k < 3; ++k) { lo[k] = 1e300; hi[k] = -1e300; }
-            auto acc = [&](const std::vector<double>& v) {
-                for (size_t i = 0; i + 2 < v.size(); i += 3)
-                    for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], v[i + k]); hi[k] = std::max(hi[k], v[i + k]); }
-            };
-            acc(hx);
-            if (akinci_) acc(hb);
-            if (d.boundary_method == SPH_BOUNDARY_CUBE && d.has_cube)
-                for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], d.cube_min[k]); hi[k] = std::max(hi[k], d.cube_max[k]); }
-            for (int k = 0; k < 3; ++k) {
-                const double ext = hi[k] - lo[k];
-                lo[k] -= 0.05 * ext;
-                hi[k] += 0.05 * ext;
-            }
-        }
-        const double h = hd_;
-        int o[3], nn[3];
-        for (int k = 0; k < 3; ++k) {
-            o[k] = (int)std::floor(lo[k] / h) - 2;
-            nn[k] = (int)std::floor(hi[k] / h) + 3 - o[k];
-        }
-        if (nn[0] > 2048 || nn[1] > 2048 || nn[2] > 1024 || nn[0] < 1 || nn[1] < 1 || nn[2] < 1) {
-            fail("grid box too large for the cell packing (max 2048 x 2048 x 1024 cells)");
-            return SPH_ERR_CAPACITY;
-        }
-        int bx = 0, by = 0;
-        while ((1 << bx) < nn[0]) ++bx;
-        while ((1 << by) < nn[1]) ++by;
-        std::vector<uint32_t> mx(nn[0]), my(nn[1]);
-        // interleave bit k of x and y (x first) while both have bits left
-        int pos = 0;
-        std::vector<int> px(bx), py(by);
-        for (int k = 0; k < std::max(bx, by); ++k) {
-            if (k < bx) px[k] = pos++;
-            if (k < by) py[k] = pos++;
-        }
-        for (int v = 0; v < nn[0]; ++v) {
-            uint32_t m = 0;
-            for (int k = 0; k < bx; ++k) if (v >> k & 1) m |= 1u << px[k];
-            mx[v] = m;
-        }
-        for (int v = 0; v < nn[1]; ++v) {
-            uint32_t m = 0;
-            for (int k = 0; k < by; ++k) if (v >> k & 1) m |= 1u << py[k];
-            my[v] = m;
-        }
-        const uint64_t ncols = 1ull << (bx + by);
-        const uint64_t nkeys = ncols * (uint64_t)nn[2];
-        if (nkeys > (1ull << 30)) { fail("grid key space too large"); return SPH_ERR_CAPACITY; }
-        nkeys_ = (uint32_t)nkeys;
-        SPH_CUDA(mortx_.alloc(nn[0]));
-        SPH_CUDA(morty_.alloc(nn[1]));
-        SPH_CUDA(cudaMemcpy(mortx_.p, mx.data(), nn[0] * 4, cudaMemcpyHostToDevice));
-        SPH_CUDA(cudaMemcpy(morty_.p, my.data(), nn[1] * 4, cudaMemcpyHostToDevice));
-        gv_.nx = nn[0]; gv_.ny = nn[1]; gv_.nz = nn[2];
-        gv_.ox = o[0]; gv_.oy = o[1]; gv_.oz = o[2];
+        GridPlan p;
+        const int rc = grid_plan(d, hx, hb, akinci_ != 0, hd_, &p, &err);
+        if (rc) return rc;
+        nkeys_ = (uint32_t)p.nkeys;
+        SPH_CUDA(mortx_.alloc(p.nn[0]));
+        SPH_CUDA(morty_.alloc(p.nn[1]));
+        SPH_CUDA(cudaMemcpy(mortx_.p, p.mx.data(), p.nn[0] * 4, cudaMemcpyHostToDevice));
+        SPH_CUDA(cudaMemcpy(morty_.p, p.my.data(), p.nn[1] * 4, cudaMemcpyHostToDevice));
+        gv_.nx = p.nn[0]; gv_.ny = p.nn[1]; gv_.nz = p.nn[2];
+        gv_.ox = p.o[0]; gv_.oy = p.o[1]; gv_.oz = p.o[2];
         gv_.mortx = mortx_.p;
         gv_.morty = morty_.p;
         return SPH_OK;

@@ -1,0 +1,118 @@
+"""Batched pool: scenes resident together on one GPU.
+
+* a scene's results are the same alone and in a mix of other scenes, and when
+  other scenes are admitted or removed while it runs (bit-exact: per-scene
+  reductions use fixed-point integer sums, so nothing depends on the mix);
+* a pooled scene matches the one-scene solver (same FP32 pair-list
+  arithmetic) within the FP32 tolerance of the parity tests;
+* graph-captured pool steps equal host-driven ones; step counts complete;
+  admission respects capacity.
+"""
+import numpy as np
+import pytest
+
+import sph_gb300
+from scenes import jitter, lattice
+from util import relerr
+
+pytestmark = pytest.mark.gpu
+
+
+def mk(seed, n_side=8, r=0.02, box=0.5, spheres=()):
+    lo = 2 * r + 0.01 * (seed % 3)
+    x = jitter(lattice(r, (lo, lo, lo), (lo + 2 * r * n_side, lo + 2 * r * n_side * 0.8, lo + 2 * r * n_side)), r, seed)
+    b = [sph_gb300.sample_box(4 * r, (0, 0, 0), (box, box, box))]
+    for c, rad in spheres:
+        b.append(sph_gb300.sample_sphere(r, c, rad))
+    params = dict(method=2, boundary=2, radius=r, eta=0.001, eta_v=0.001, precision="f32")
+    return x, np.concatenate(b), params
+
+
+A = mk(1, 9, spheres=[((0.3, 0.4, 0.3), 0.06)])
+OTHERS = [mk(2, 6), mk(3, 11, box=0.6), mk(4, 5, r=0.025, box=0.4)]
+
+
+def pool_run(scenes, steps, graph=False, admit_later=(), later_at=0):
+    P = sph_gb300.Pool(max_particles=200_000, max_boundary=400_000, max_keys=4_000_000, max_scenes=64)
+    if graph:
+        P.set_graph(True)
+    ids = [P.add_scene(x, boundary_points=b, steps=1000, **p) for x, b, p in scenes]
+    if admit_later:
+        P.step(later_at)
+        ids += [P.add_scene(x, boundary_points=b, steps=1000, **p) for x, b, p in admit_later]
+        P.step(steps - later_at)
+    else:
+        P.step(steps)
+    P.synchronize()
+    return P, ids
+
+
+def test_scene_alone_equals_scene_in_mix(gpu_lib):
+    P1, (a1,) = pool_run([A], 8)
+    P2, ids = pool_run([OTHERS[0], A, OTHERS[1], OTHERS[2]], 8)
+    a2 = ids[1]
+    for f in ("x", "v", "rho", "alpha"):
+        assert np.array_equal(P1.get(a1, f), P2.get(a2, f)), f
+    s1, _ = P1.query(a1)
+    s2, _ = P2.query(a2)
+    assert s1["sum_iterations"] == s2["sum_iterations"] and s1["dt"] == s2["dt"] and s1["time"] == s2["time"]
+
+
+def test_admission_and_removal_mid_run_do_not_change_a_scene(gpu_lib):
+    P1, (a1,) = pool_run([A], 8)
+    P2, ids = pool_run([A, OTHERS[0]], 8, admit_later=[OTHERS[1], OTHERS[2]], later_at=3)
+    a2 = ids[0]
+    assert np.array_equal(P1.get(a1, "x"), P2.get(a2, "x"))
+    # remove a neighbour and keep going
+    P2.remove(ids[1])
+    P1.step(4)
+    P2.step(4)
+    assert np.array_equal(P1.get(a1, "x"), P2.get(a2, "x"))
+    assert np.array_equal(P1.get(a1, "v"), P2.get(a2, "v"))
+
+
+def test_pooled_scene_matches_one_scene_solver(gpu_lib):
+    x, b, p = A
+    P, (a,) = pool_run([A], 6)
+    s = sph_gb300.Scene(neighbor_list_max=64, **p)
+    s.set_fluid(x)
+    s.add_boundary_points(b)
+    s.init()
+    s.step(6)
+    assert relerr(P.get(a, "x"), s.get("x")) <= 1e-6
+    assert relerr(P.get(a, "rho"), s.get("rho")) <= 1e-5
+    assert np.abs(P.get(a, "v") - s.get("v")).max() <= 2.5e-3
+    assert P.query(a)[0]["sum_iterations"] == s.stats()["sum_iterations"]
+
+
+def test_graph_pool_equals_host_pool(gpu_lib):
+    P1, ids1 = pool_run([A] + OTHERS, 6, graph=False)
+    P2, ids2 = pool_run([A] + OTHERS, 6, graph=True)
+    for i1, i2 in zip(ids1, ids2):
+        assert np.array_equal(P1.get(i1, "x"), P2.get(i2, "x"))
+    assert P2.launch_count() > 0
+
+
+def test_step_counts_complete_and_poll(gpu_lib):
+    P = sph_gb300.Pool(max_particles=100_000, max_boundary=200_000, max_keys=2_000_000, max_scenes=8)
+    x, b, p = A
+    short = P.add_scene(x, boundary_points=b, steps=3, **p)
+    long = P.add_scene(OTHERS[0][0], boundary_points=OTHERS[0][1], steps=6, **OTHERS[0][2])
+    P.step(4)
+    assert P.poll() == [short]
+    st, done = P.query(short)
+    assert done and st["steps"] == 3
+    P.remove(short)
+    P.step(3)
+    st, done = P.query(long)
+    assert done and st["steps"] == 6
+    assert P.poll() == [long]
+
+
+def test_admission_respects_capacity(gpu_lib):
+    x, b, p = A
+    P = sph_gb300.Pool(max_particles=x.shape[0] + 10, max_boundary=400_000, max_keys=4_000_000, max_scenes=8)
+    P.add_scene(x, boundary_points=b, steps=5, **p)
+    with pytest.raises(sph_gb300.PoolFull):
+        P.add_scene(x, boundary_points=b, steps=5, **p)
+    assert P.usage()["particles"] == x.shape[0]
