@@ -1,32 +1,54 @@
-"""Benchmark of the per-step SPH particle loop on GB300.
+"""Benchmark of the per-step SPH particle loop on GB300: DFSPH particle-steps/s
+at 0.1 % average density error, batched/served versus the plain one-scene GPU
+solver, with p50/p99 scene latency.
 
-Workload (default): the DFSPH dam break with Akinci boundaries -- a
-50 x 50 x 50 = 125,000-particle fluid block at r = 0.005 m in the corner of a
-1.5 x 0.8 x 0.8 m box whose walls are sampled as Akinci boundary particles
-(60,802 points), CFL-adaptive dt in [1e-5, 5e-3] s, 0.1 % average density
-error, 0.1 %/s divergence error, at most 100 iterations, 2000 steps.  (At
-r = 0.01 m the 50^3 block would be 1 m tall and not fit the 0.8 m box;
-r = 0.005 m keeps the particle count and the box.  The block starts 2r off
-the walls: with its first layer at r from an Akinci wall the reference's DFSPH
-ejects the wall-adjacent particles at hundreds of m/s in the first step.)  A "step" is one DFSPHSolver::step of that scene
-(one time step: non-pressure forces, CFL, density solve, neighbour grid,
-densities/alpha, divergence solve); the metric is particle-steps/s.
+Workloads (seeded, synthetic; sph_gb300/workloads.py):
+  batched_mix_256  (headline) 256 independent DFSPH scenes, fluid counts
+                   log-uniform in [2k, 64k] (seed 42; 4,151,352 fluid and
+                   4,127,798 Akinci boundary particles in all), block aspect
+                   ratios U(0.5, 2), 0-3 Akinci sphere obstacles of radius
+                   0.05-0.2 m in a 1 m Akinci box, r = 0.01 m, CFL-adaptive
+                   dt in [1e-5, 5e-3] s, 0.1 % density / 0.1 %/s divergence
+                   error, FP32 bulk with FP64 reductions.  Every scene runs
+                   W + K steps (the 500-step scenes at the defaults).
+  dam_break_125k   one 50^3 = 125,000-particle dam break at r = 0.005 m in a
+                   1.5 x 0.8 x 0.8 m Akinci box (60,802 boundary points).
+                   (At r = 0.01 m the 50^3 block is 1 m tall and does not
+                   fit the 0.8 m box; r = 0.005 m keeps count and box.)
+
+One "step" of the headline is one step of every scene of the mix: the pool
+advances all resident scenes with one CUDA graph launch per step (segmented
+grid, per-scene CFL, per-scene solver loops as device-side conditional
+nodes).  value = sum over scenes of fluid particles x K / device time of the
+K timed steps.  Beside it, on the same mix and the same steps:
+  plain      each scene alone through the plain one-scene solver (the same
+             kernels, one scene per graph);
+  served     the request loop (continuous batching, admission by an 80 GB
+             HBM budget) on a Poisson stream of mixed scenes at 200 scenes/s
+             (saturating) and at a sub-saturation rate, with a 4M-particle
+             dam break every 10 s: aggregate particle-steps/s, p50/p99 scene
+             latency;
+  dam_break_125k  the plain solver on the single large scene;
+  e2e        the mix through the pool's C ABI with host buffers: scenes
+             uploaded from pinned host memory, per-step status read back,
+             final positions and velocities downloaded, all timed;
+  cpu_baseline  the reference's algorithm (the C restatement in oracle/,
+             OpenMP on every host core) on a seeded 16-scene sample of the mix.
 
 Arms:
-  default            the CUDA path (FP32 bulk, FP64 reductions), whole steps as
-                     CUDA graphs with device-side solver loops
-  --impl reference   the reference's CPU algorithm on the host cores (the C
-                     restatement in oracle/, OpenMP, every host thread), a
-                     bounded number of steps of the same scene
+  default            the CUDA path
+  --impl reference   the reference's CPU algorithm on the host cores on the
+                     16-scene sample of the mix, bounded in time
 
 Prints one JSON line (rank 0).  Multi-GPU (torchrun): every rank runs its own
-replica of the scene (scenes are independent; no collective on the data
-path); value = all ranks' particle-steps / the slowest rank's time.
+replica of the mix (scenes are independent; no collective on the data path);
+value = all ranks' particle-steps / the slowest rank's time.
 """
 from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -39,38 +61,38 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "DFSPH particle-steps/s @0.1% density err"
+METRIC = "DFSPH particle-steps/s @0.1% density err, served vs plain GPU; p50/p99 latency"
 UNIT = "particle-steps/s"
-
-WORKLOADS = {
-    "dfsph_dam_break_125k": dict(
-        params=dict(method=2, boundary=2, radius=0.005, eta=0.001, eta_v=0.001, cfl=1.0, max_it=100, dt=1e-4,
-                    min_dt=1e-5, max_dt=5e-3, fps=60.0),
-        block=((0.01, 0.01, 0.01), (0.51, 0.51, 0.51)),
-        box=((0.0, 0.0, 0.0), (1.5, 0.8, 0.8)),
-    ),
-}
+WORKLOAD = "batched_mix_256"
+CPU_SAMPLE_SCENES = 16
 
 # Compulsory bytes of each kernel as implemented (FP32 form: float4 = 16 B,
-# scalar = 4 B; each array read once and written once, neighbour re-reads not
-# counted): (bytes per fluid particle, bytes per stored pair, touches the
-# boundary particles at 16 B each).
+# scalar = 4 B, scene id 4 B; each array read once and written once,
+# neighbour re-reads not counted): (bytes per fluid particle, bytes per stored
+# pair, touches the boundary particles at 16 B each).
 ALGO_BYTES = {
     "k_cell_update": (64, 0, False),
+    "k_pool_cell_update": (68, 0, False),
     "k_scatter": (16, 0, False),
     "k_gather_fluid": (108, 0, False),
     "k_density": (32, 0, True),
     "k_dfsph_cfl": (32, 0, False),
+    "k_pool_cfl_accum": (36, 0, False),
     "k_dfsph_predict_v_warm": (108, 0, False),
+    "k_pool_predict_v_warm": (112, 0, False),
     "k_dfsph_correct": (68, 0, True),
     "k_dfsph_predict_density": (64, 0, True),
     "k_dfsph_divergence": (64, 0, True),
     "k_npforce": (68, 0, True),
+    "k_pool_npforce": (72, 0, True),
     "k_st_normals": (36, 0, False),
     "k_build_lists": (52, 16, True),
+    "k_pool_build_lists": (56, 16, True),
     "k_dfsph_correct_list": (72, 16, False),
+    "k_pool_correct": (76, 16, False),
     "k_dfsph_predict_density_list": (52, 16, False),
     "k_dfsph_divergence_list": (52, 16, False),
+    "k_pool_errors": (56, 16, False),
 }
 
 
@@ -170,75 +192,295 @@ def dist_barrier(world):
         dist.barrier()
 
 
-def make_scene(wl, precision="f32", G=0, list_max=64):
-    import sph_gb300
+def mix(steps):
+    from sph_gb300 import workloads
 
-    w = WORKLOADS[wl]
-    s = sph_gb300.Scene(precision=precision, threads_per_particle=G, neighbor_list_max=list_max, **w["params"])
-    s.add_fluid_block(*w["block"])
-    s.add_boundary_box(*w["box"])
-    return s
+    return workloads.batched_mix(n_scenes=256, seed=42, steps=steps, r=0.01)
 
 
-def cpu_reference(wl, steps, warmup, threads, budget_s):
-    """The reference's algorithm on the host (C restatement, OpenMP)."""
+# ---- CPU: the reference's algorithm on a sample of the mix -----------------
+
+def cpu_mix_sample(scenes, steps_each, threads, budget_s):
+    """The first CPU_SAMPLE_SCENES scenes of the mix through the C restatement
+    (OpenMP on `threads` host threads), one untimed warm-up step each, then up
+    to `steps_each` timed steps each within budget_s / #scenes seconds."""
     os.environ["OMP_NUM_THREADS"] = str(threads)
     import oracle
 
-    w = WORKLOADS[wl]
-    r = w["params"]["radius"]
-    x = oracle.fluid_block(r, *w["block"])
-    o = oracle.OracleScene(w["params"], x, boxes=[w["box"]])
-    for _ in range(max(0, warmup)):
+    sample = scenes[:CPU_SAMPLE_SCENES]
+    per = budget_s / len(sample)
+    work, el, done_steps, its = 0, 0.0, 0, 0
+    for x, b, params, _ in sample:
+        p = {k: v for k, v in params.items() if k != "precision"}
+        o = oracle.OracleScene(p, x, points=b)
         o.step(1)
-    done, its, t0 = 0, 0, time.perf_counter()
-    while done < max(1, steps):
-        o.step(1)
-        its += o.scalar("iterations")
-        done += 1
-        if time.perf_counter() - t0 > budget_s:
-            break
-    el = time.perf_counter() - t0
-    return o.n * done / el, done, its / done, o.n
+        t0 = time.perf_counter()
+        k = 0
+        while k < steps_each:
+            o.step(1)
+            its += o.scalar("iterations")
+            k += 1
+            if time.perf_counter() - t0 > per:
+                break
+        el += time.perf_counter() - t0
+        work += o.n * k
+        done_steps += k
+        del o
+    desc = (f"first {len(sample)} scenes of the mix (seed 42; {sum(s[0].shape[0] for s in sample)} fluid particles), "
+            f"1 untimed warm-up step each, then {done_steps} timed steps in all "
+            f"(at most {steps_each} per scene, {per:.1f} s per scene); reference algorithm restated in C "
+            f"(oracle/sph_oracle.c), FP64, OpenMP; mean {its / max(done_steps, 1):.1f} density iterations/step")
+    return work / el, desc, done_steps
 
 
 def run_reference_arm(args, world, rank):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    warm = min(args.warmup, 1)
-    v, done, mean_it, n = cpu_reference(args.workload, args.steps, warm, threads, args.ref_budget)
-    sample = f"{done} DFSPH steps of the {n}-particle scene after {warm} warm-up step(s)"
+    scenes = mix(args.warmup + args.steps)
+    v, desc, done = cpu_mix_sample(scenes, max(1, args.steps), threads, args.ref_budget)
     line = {
-        "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": done, "warmup": warm,
-        "ms_per_step": 1000.0 * n / v, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic", "impl": "reference",
-        "config": {"workload": args.workload, "fluid_particles": n, "mean_iterations": mean_it,
+        "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+        "config": {"workload": WORKLOAD, "sample": desc,
                    "implementation": "reference algorithm restated in C (oracle/sph_oracle.c), OpenMP"},
-        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
-def flush_l2(buf):
-    # write a buffer larger than L2 (126 MB) between timed steps
-    buf.fill_(1.0)
+# ---- GPU pieces --------------------------------------------------------------
+
+def make_pool(scenes, kmax):
+    import sph_gb300
+
+    n = sum(s[0].shape[0] for s in scenes)
+    nb = sum(s[1].shape[0] for s in scenes)
+    return sph_gb300.Pool(max_particles=n, max_boundary=nb, max_keys=16 * n, max_scenes=len(scenes) + 1,
+                          neighbor_list_max=kmax)
+
+
+def scene_stats(pool, ids):
+    out = []
+    for sid in ids:
+        st, done = pool.query(sid)
+        out.append((st["sum_iterations"], st["sum_iterations_v"], st["time"], st["steps"], done))
+    return out
+
+
+def run_batched(scenes, args, world, local):
+    """Headline: the mix resident in one pool, K graph-launched steps timed
+    with CUDA events on the pool's stream, then a host-driven profiled pass."""
+    import torch
+
+    W, K, P = args.warmup, args.steps, args.profile_steps
+    pool = make_pool(scenes, args.list_max)
+    ids = [pool.add_scene(x, boundary_points=b, steps=W + K + P, **params) for x, b, params, _ in scenes]
+    n = sum(s[0].shape[0] for s in scenes)
+    nb = sum(s[1].shape[0] for s in scenes)
+    pool.set_graph(True)
+    pool.step(W)
+    pool.synchronize()
+    s0 = scene_stats(pool, ids)
+    l0 = pool.launch_count()
+    dist_barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        ms = pool.step_timed(K)
+    torch.cuda.synchronize()
+    l1 = pool.launch_count()
+    s1 = scene_stats(pool, ids)
+    finished_early = sum(1 for q in s1 if q[4])
+    its = sum(b[0] - a[0] for a, b in zip(s0, s1)) / (len(ids) * K)
+    itsv = sum(b[1] - a[1] for a, b in zip(s0, s1)) / (len(ids) * K)
+    sim = sum(b[2] - a[2] for a, b in zip(s0, s1)) / len(ids)
+    pairs, overflow = pool.list_pairs()
+
+    # per-kernel CUDA-event timing over P host-driven steps of the same pool
+    pool.set_graph(False)
+    pool.set_profiling(True)
+    pool.profile()
+    pool.step(P)
+    prof = pool.profile()
+    pool.set_profiling(False)
+    pool.close()
+    return dict(ms=ms, n=n, nb=nb, launches=l1 - l0, clocks=clocks.summary(), its=its, itsv=itsv,
+                sim_s_per_scene=sim, pairs=pairs, overflow=overflow, prof=prof, finished_early=finished_early)
+
+
+def run_plain(scenes, args):
+    """The same mix, each scene alone through the plain one-scene solver
+    (graph mode), W untimed then K_plain timed steps per scene."""
+    import sph_gb300
+
+    W = args.warmup
+    Kp = args.plain_steps if args.plain_steps > 0 else args.steps
+    work, ms_total, its, steps_total = 0, 0.0, 0, 0
+    for x, b, params, _ in scenes:
+        s = sph_gb300.Scene(neighbor_list_max=args.list_max, **params)
+        s.set_fluid(x)
+        s.add_boundary_points(b)
+        s.init()
+        s.set_graph(True)
+        s.step(W)
+        s.synchronize()
+        st0 = s.stats()
+        ms_total += s.step_timed(Kp)
+        st1 = s.stats()
+        its += st1["sum_iterations"] - st0["sum_iterations"]
+        work += s.n * Kp
+        steps_total += Kp
+        s.close()
+    return dict(value=work / (ms_total / 1000.0), ms=ms_total, steps_per_scene=Kp, mean_iterations=its / steps_total)
+
+
+def run_dam_break(args):
+    """The 125k dam break alone, plain solver, L2 flushed between steps."""
+    import torch
+
+    import sph_gb300
+    from sph_gb300 import workloads
+
+    x, b, params, _ = workloads.dam_break()
+    s = sph_gb300.Scene(neighbor_list_max=args.list_max, **params)
+    s.set_fluid(x)
+    s.add_boundary_points(b)
+    s.init()
+    s.set_graph(True)
+    s.step(max(3, args.warmup))
+    s.synchronize()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
+    st0 = s.stats()
+    ms = 0.0
+    K = args.dam_steps
+    for _ in range(K):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        ms += s.step_timed(1)
+    st1 = s.stats()
+    out = dict(value=s.n * K / (ms / 1000.0), ms_per_step=ms / K, steps=K, fluid_particles=s.n,
+               boundary_particles=s.nb,
+               mean_density_iterations=(st1["sum_iterations"] - st0["sum_iterations"]) / K,
+               mean_divergence_iterations=(st1["sum_iterations_v"] - st0["sum_iterations_v"]) / K,
+               l2="flushed between timed steps (256 MB write)")
+    s.close()
+    return out
+
+
+def run_e2e(scenes, args):
+    """The mix through the pool's C ABI with host buffers, all of it timed:
+    pool creation, upload of every scene from pinned host memory, W + K steps
+    with each step's per-scene completion flags read back, and the download of
+    every scene's final positions and velocities into pinned host memory."""
+    import torch
+
+    import sph_gb300
+
+    def pinned(a):
+        t = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+        return t, t.numpy()
+
+    hold, xs, bs, outs = [], [], [], []
+    for x, b, _, _ in scenes:
+        tx, ax = pinned(x)
+        tb, ab = pinned(b)
+        to, ao = pinned(np.empty_like(x))
+        tv, av = pinned(np.empty_like(x))
+        hold += [tx, tb, to, tv]
+        xs.append(ax)
+        bs.append(ab)
+        outs.append((ao, av))
+    T = args.warmup + args.steps
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    pool = make_pool(scenes, args.list_max)
+    ids = [pool.add_scene(x, boundary_points=b, steps=T, **params) for x, b, (_, _, params, _) in zip(xs, bs, scenes)]
+    pool.set_graph(True)
+    polled = 0
+    for _ in range(T):
+        pool.step(1)
+        polled += len(pool.poll())
+    for sid, (ox, ov) in zip(ids, outs):
+        pool.get(sid, "x", out=ox)
+        pool.get(sid, "v", out=ov)
+    wall = time.perf_counter() - t0
+    pool.close()
+    n = sum(x.shape[0] for x in xs)
+    h2d = sum(x.nbytes + b.nbytes for x, b in zip(xs, bs))
+    d2h = sum(ox.nbytes + ov.nbytes for ox, ov in outs) + T * len(ids) * 4
+    return {"value": n * T / wall, "unit": UNIT, "h2d_bytes_per_step": h2d / T, "d2h_bytes_per_step": d2h / T,
+            "wall_s": wall, "scenes_completed": polled,
+            "scope": "pool create + upload from pinned host + W+K steps (completion flags read back each step) "
+                     "+ download x, v of every scene into pinned host memory"}
+
+
+def stream_mean_work(r=0.01):
+    """E[N * steps] of the stream's regular scenes (N log-uniform in [1k, 200k],
+    steps uniform in {200..2000})."""
+    en = (200000 - 1000) / math.log(200000 / 1000)
+    return en * 1100.0
+
+
+def run_served(args, rate, seconds, big_every):
+    import sph_gb300
+    from sph_gb300 import serve, workloads
+
+    pool = sph_gb300.Pool(budget_bytes=int(args.serve_budget_gb * 1e9), neighbor_list_max=args.list_max)
+    pool.set_graph(True)
+    reqs = workloads.request_stream(rate=rate, duration=seconds, seed=7, big_every=big_every)
+    out = serve.serve(pool, reqs, seconds, epoch_steps=args.epoch_steps)
+    out.pop("results", None)
+    out["rate_per_s"] = rate
+    out["budget_gb"] = args.serve_budget_gb
+    out["big_dam_break_every_s"] = big_every
+    pool.close()
+    return out
+
+
+def roofline(prof, n, nb, pairs):
+    kern = max(prof.items(), key=lambda kv: kv[1][1]) if prof else ("none", (1, 0.0))
+    kname, (kcount, kms) = kern
+    per_b, per_pair, touches_b = ALGO_BYTES.get(kname, (0, 0, False))
+    bytes_launch = n * per_b + pairs * per_pair + (nb * 16 if touches_b else 0)
+    avg_ms = kms / max(kcount, 1)
+    achieved = bytes_launch / (avg_ms / 1000.0) / 1e9 if avg_ms > 0 else 0.0
+    peak, peak_kind = load_peaks()
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", f"ncu_{kname}_{WORKLOAD}.md")
+    if os.path.exists(tp):
+        for ln in open(tp):
+            if ln.startswith("dram_bytes_per_launch:"):
+                traffic = float(ln.split(":", 1)[1])
+    total = sum(v[1] for v in prof.values())
+    return {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_kind": f"of {peak_kind}", "traffic": traffic,
+            "algorithmic_bytes_per_launch": bytes_launch, "avg_launch_ms": avg_ms,
+            "kernel_share": kms / total if total else None}
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--steps", type=int, default=495)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="dfsph_dam_break_125k", choices=list(WORKLOADS))
-    ap.add_argument("--threads-per-particle", type=int, default=0)
-    ap.add_argument("--list-max", type=int, default=64, help="pair-list slots per particle (0: cell walks)")
+    ap.add_argument("--list-max", type=int, default=64, help="pair-list slots per particle")
+    ap.add_argument("--profile-steps", type=int, default=10, help="host-driven steps timed per kernel")
+    ap.add_argument("--plain-steps", type=int, default=0, help="timed steps per scene for the plain arm (0: --steps)")
+    ap.add_argument("--dam-steps", type=int, default=500)
+    ap.add_argument("--serve-seconds", type=float, default=30.0)
+    ap.add_argument("--serve-budget-gb", type=float, default=80.0)
+    ap.add_argument("--epoch-steps", type=int, default=10)
+    ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=25.0, help="seconds of CPU baseline work")
     ap.add_argument("--ref-budget", type=float, default=90.0, help="seconds of reference-arm timed work")
     args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference_arm(args, world, rank)
@@ -251,131 +493,61 @@ def main():
     sph_gb300.build()
     sph_gb300.select_device(local)
     torch.cuda.set_device(local)
-    G = args.threads_per_particle
-
-    # ---- device-resident timed region -------------------------------------
-    s = make_scene(args.workload, G=G, list_max=args.list_max)
-    s.init()
-    s.set_graph(True)
-    s.step(max(3, args.warmup))
-    s.synchronize()
-    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
-    st0 = s.stats()
-    l0 = s.launch_count()
-    n = s.n
-    step_ms = []
-    dist_barrier(world)
-    torch.cuda.synchronize()
     wall0 = time.perf_counter()
-    with ClockSampler(local) as clocks:
-        for _ in range(args.steps):
-            flush_l2(flush)
-            torch.cuda.synchronize()
-            step_ms.append(s.step_timed(1))
-    torch.cuda.synchronize()
-    wall = time.perf_counter() - wall0
-    st1 = s.stats()
-    l1 = s.launch_count()
-    total_ms = float(np.sum(step_ms))
-    t_max = dist_max(total_ms, world)
-    value = world * n * args.steps / (t_max / 1000.0)
-    its = (st1["sum_iterations"] - st0["sum_iterations"]) / args.steps
-    itsv = (st1["sum_iterations_v"] - st0["sum_iterations_v"]) / args.steps
-    sim_s = st1["time"] - st0["time"]
 
-    # ---- per-kernel event timing (same scene, host-driven steps) ----------
-    s.set_graph(False)
-    s.set_profiling(True)
-    s.profile()
-    prof_steps = min(args.steps, 20)
-    for _ in range(prof_steps):
-        flush_l2(flush)
-        torch.cuda.synchronize()
-        s.step(1)
-    prof = s.profile()
-    s.set_profiling(False)
-    nb = s.nb
-    kern = max(prof.items(), key=lambda kv: kv[1][1]) if prof else ("none", (1, 0.0))
-    kname, (kcount, kms) = kern
-    per_b, per_pair, touches_b = ALGO_BYTES.get(kname, (0, 0, False))
-    pairs = s.stats()["list_pairs"]
-    bytes_launch = n * per_b + pairs * per_pair + (nb * 16 if touches_b else 0)
-    avg_ms = kms / max(kcount, 1)
-    achieved = bytes_launch / (avg_ms / 1000.0) / 1e9 if avg_ms > 0 else 0.0
-    peak, peak_kind = load_peaks()
-    traffic = None
-    tp = os.path.join(ROOT, "profiles", f"ncu_{kname}_{args.workload}.md")
-    if os.path.exists(tp):
-        for ln in open(tp):
-            if ln.startswith("dram_bytes_per_launch:"):
-                traffic = float(ln.split(":", 1)[1])
-    total_prof_ms = sum(v[1] for v in prof.values())
+    scenes = mix(args.warmup + args.steps)
+    B = run_batched(scenes, args, world, local)
+    t_max = dist_max(B["ms"], world)
+    value = world * B["n"] * args.steps / (t_max / 1000.0)
+    roof = roofline(B["prof"], B["n"], B["nb"], B["pairs"])
+    roof["timing"] = f"CUDA events around each launch, {args.profile_steps} host-driven pool steps"
 
-    # ---- end to end through the C ABI with host buffers --------------------
-    e2e = None
-    if rank == 0 or world > 1:
-        import ctypes
+    plain = None if args.no_plain else run_plain(scenes, args)
+    dam = run_dam_break(args)
+    e2e = None if args.no_e2e else run_e2e(scenes, args)
+    if e2e is not None:
+        e2e["value"] = world * e2e["value"] * e2e["wall_s"] / dist_max(e2e["wall_s"], world)
 
-        w = WORKLOADS[args.workload]
-        x_host = torch.from_numpy(sph_gb300.fluid_block(w["params"]["radius"], *w["block"])).pin_memory().numpy()
-        v_host = torch.zeros_like(torch.from_numpy(x_host)).pin_memory().numpy()
-        out_x = torch.empty(x_host.shape, dtype=torch.float64).pin_memory().numpy()
-        out_v = torch.empty(x_host.shape, dtype=torch.float64).pin_memory().numpy()
-        e_steps = args.steps
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        e = sph_gb300.Scene(precision="f32", threads_per_particle=G, neighbor_list_max=args.list_max, **w["params"])
-        e.set_fluid(x_host, v_host)
-        e.add_boundary_box(*w["box"])
-        e.init()
-        e.set_graph(True)
-        for _ in range(args.warmup + e_steps):
-            e.step(1)
-            e.stats()  # the step's result (dt, iterations, errors) read back every step
-        out_x[:] = e.get("x")
-        out_v[:] = e.get("v")
-        e_wall = time.perf_counter() - t0
-        e_n = e.n
-        h2d = x_host.nbytes + v_host.nbytes + e.nb * 24
-        d2h = out_x.nbytes + out_v.nbytes + (args.warmup + e_steps) * ctypes.sizeof(sph_gb300.Stats)
-        tot_steps = args.warmup + e_steps
-        e_wall_max = dist_max(e_wall, world)
-        e2e = {"value": world * e_n * tot_steps / e_wall_max, "unit": UNIT,
-               "h2d_bytes_per_step": h2d / tot_steps, "d2h_bytes_per_step": d2h / tot_steps,
-               "scope": "create + upload from pinned host + init + steps (stats read back each step) + download x, v"}
-        e.close()
+    served = None
+    if not args.no_served and world == 1:
+        big_load = 4_000_000 * 200 / 10.0
+        sub_rate = max(0.5, (0.5 * value - big_load) / stream_mean_work())
+        served = {
+            "saturated": run_served(args, 200.0, args.serve_seconds, 10.0),
+            "sub_saturation": run_served(args, round(sub_rate, 2), args.serve_seconds, 10.0),
+            "sub_saturation_rate_rule": "offered load = half the batched value, 4M dam break included",
+        }
 
-    # ---- CPU baseline (rank 0, N = 1) ---------------------------------------
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        v, done, mean_it, nn = cpu_reference(args.workload, 3, 1, threads, args.cpu_budget)
-        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"{done} DFSPH steps of the {nn}-particle scene after 1 warm-up step, "
-                         f"reference algorithm restated in C (oracle/), OpenMP, mean {mean_it:.1f} iterations/step"}
+        v, desc, _ = cpu_mix_sample(scenes, 50, threads, args.cpu_budget)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc}
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": max(3, args.warmup), "ms_per_step": t_max / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": args.workload, "fluid_particles": n, "boundary_particles": nb,
-                       "parallelism": f"replicas x{world}", "l2": "flushed between timed steps (256 MB write)",
-                       "step_timing": "CUDA events on the scene's stream around each graph-launched step",
-                       "mean_density_iterations": its, "mean_divergence_iterations": itsv,
-                       "simulated_seconds_per_second": sim_s / (total_ms / 1000.0),
-                       "threads_per_particle": G or 1, "neighbor_list_max": args.list_max,
-                       "list_pairs": st1["list_pairs"], "list_overflow": st1["list_overflow"], "wall_s": wall},
-            "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
-                         "algorithmic_bytes_per_launch": bytes_launch, "avg_launch_ms": avg_ms,
-                         "kernel_share": kms / total_prof_ms if total_prof_ms else None,
-                         "timing": f"CUDA events around each launch, {prof_steps} host-driven steps"},
-            "clocks": clocks.summary(),
-            "gpu_launches": l1 - l0,
+            "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scenes)",
+            "config": {"workload": WORKLOAD, "scenes": len(scenes), "fluid_particles": B["n"],
+                       "boundary_particles": B["nb"], "steps_per_scene": args.warmup + args.steps,
+                       "parallelism": f"replicas x{world}",
+                       "l2": "not flushed: the resident working set (pair lists ~4 GB) is far larger than L2",
+                       "step_timing": "CUDA events on the pool's stream around the K graph-launched steps",
+                       "mean_density_iterations": B["its"], "mean_divergence_iterations": B["itsv"],
+                       "simulated_seconds_per_scene": B["sim_s_per_scene"],
+                       "neighbor_list_max": args.list_max, "list_pairs": B["pairs"],
+                       "list_overflow": B["overflow"], "scenes_finished_early": B["finished_early"],
+                       "plain_gpu": plain,
+                       "batched_over_plain": value / plain["value"] if plain else None,
+                       "served": served, "dam_break_125k": dam,
+                       "wall_s": time.perf_counter() - wall0},
+            "roofline": roof,
+            "clocks": B["clocks"],
+            "gpu_launches": B["launches"],
             "e2e": e2e,
             "cpu_baseline": cpu,
-            "kernels": {k: {"launches": c, "ms": round(ms, 4)} for k, (c, ms) in sorted(prof.items(),
+            "kernels": {k: {"launches": c, "ms": round(ms, 4)} for k, (c, ms) in sorted(B["prof"].items(),
                                                                                       key=lambda kv: -kv[1][1])},
         }
         print(json.dumps(line), flush=True)

@@ -251,6 +251,15 @@ int sph_pool_download(sph_pool* pool, int scene_id, int field, double* out);
 int sph_pool_usage(sph_pool* pool, unsigned long long* particles, unsigned long long* boundary,
                    unsigned long long* keys, unsigned* scenes);
 int sph_pool_get_launch_count(sph_pool* pool, unsigned long long* out);
+/* sph_pool_step bracketed by CUDA events on the pool's stream (admissions are
+ * applied before the first event); returns the device time in *elapsed_ms. */
+int sph_pool_step_timed(sph_pool* pool, int nsteps, float* elapsed_ms);
+/* Per-kernel CUDA-event timing of host-driven pool steps, reported as
+ * "name launches total_ms" lines (as sph_ctx_get_profile). */
+int sph_pool_set_profiling(sph_pool* pool, int enable);
+int sph_pool_get_profile(sph_pool* pool, char* buf, unsigned long long len);
+/* Pair-list occupancy: stored pairs and particles whose neighbours overflow. */
+int sph_pool_list_pairs(sph_pool* pool, unsigned long long* pairs, unsigned* overflow);
 const char* sph_pool_last_error(const sph_pool* pool);
 
 /* Sampling helpers with the reference's point sets, usable without a

@@ -96,6 +96,7 @@ def lib():
         L.orc_set_fluid.argtypes = [vp, dp, dp, ctypes.c_uint]
         L.orc_add_box.argtypes = [vp, dp, dp]
         L.orc_add_sphere.argtypes = [vp, dp, ctypes.c_double]
+        L.orc_add_points.argtypes = [vp, dp, ctypes.c_uint]
         L.orc_init.argtypes = [vp]
         L.orc_step.argtypes = [vp, ctypes.c_int]
         L.orc_num_fluid.argtypes = [vp]
@@ -173,7 +174,7 @@ def sample_sphere(particle_radius, c, radius):
 class OracleScene:
     """One scene of the C restatement (one fluid model, one boundary model)."""
 
-    def __init__(self, params: dict, x, v=None, boxes=(), spheres=()):
+    def __init__(self, params: dict, x, v=None, boxes=(), spheres=(), points=None):
         L = lib()
         self.params = dict(params)
         self._p = make_params(**params)
@@ -188,6 +189,9 @@ class OracleScene:
             L.orc_add_box(self.h, _dptr(_vec3(mn)), _dptr(_vec3(mx)))
         for c, r in spheres:
             L.orc_add_sphere(self.h, _dptr(_vec3(c)), float(r))
+        if points is not None and len(points):
+            pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
+            L.orc_add_points(self.h, _dptr(pts), pts.shape[0])
         if L.orc_init(self.h) != 0:
             raise RuntimeError("orc_init failed")
 

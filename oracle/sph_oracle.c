@@ -1288,6 +1288,16 @@ int orc_add_sphere(orc_scene* s, const double c[3], double radius)
     return 0;
 }
 
+/* Pre-sampled points appended to the boundary model, as the reference's
+ * BoundaryModel::addPoints-style setup fills its position vector directly
+ * (AkinciBoundaryModel.h:13-31 keeps positions in one vector per model). */
+int orc_add_points(orc_scene* s, const double* pts, unsigned m)
+{
+    if (!s || s->inited || (m && !pts)) return -1;
+    boundary_append(s, pts, (long long)m);
+    return 0;
+}
+
 /* Simulation::init -> solver->init (Simulation.cpp:102-110; SPHSolver.cpp:
  * 22-39; DFSPHSolver.cpp:24-36; PCISPHSolver.cpp:12-19; WCSPHSolver.cpp:9) */
 int orc_init(orc_scene* s)

@@ -43,6 +43,7 @@ void orc_destroy(orc_scene* s);
 int orc_set_fluid(orc_scene* s, const double* x, const double* v, unsigned n);
 int orc_add_box(orc_scene* s, const double mn[3], const double mx[3]);
 int orc_add_sphere(orc_scene* s, const double c[3], double radius);
+int orc_add_points(orc_scene* s, const double* pts, unsigned m);
 int orc_init(orc_scene* s);
 int orc_step(orc_scene* s, int nsteps);
 unsigned orc_num_fluid(const orc_scene* s);

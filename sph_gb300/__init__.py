@@ -152,6 +152,10 @@ ABI = [
     ("sph_pool_usage", ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(ctypes.c_ulonglong),
                                       ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(ctypes.c_uint)]),
     ("sph_pool_get_launch_count", ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_ulonglong)]),
+    ("sph_pool_step_timed", ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
+    ("sph_pool_set_profiling", ctypes.c_int, [_vp, ctypes.c_int]),
+    ("sph_pool_get_profile", ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_ulonglong]),
+    ("sph_pool_list_pairs", ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(ctypes.c_uint)]),
     ("sph_pool_last_error", ctypes.c_char_p, [_vp]),
 ]
 
@@ -487,11 +491,15 @@ class Pool:
         self._check(lib().sph_pool_poll(self._h, _i(ids), n.value, ctypes.byref(n)), "sph_pool_poll")
         return [int(t) for t in ids[: n.value]]
 
-    def get(self, sid, field):
+    def get(self, sid, field, out=None):
         fid, width = FIELDS[field]
         nf, nb = self._n[sid]
         count = nb if field in ("bx", "psi") else nf
-        out = np.zeros((count, 3) if width == 3 else count)
+        shape = (count, 3) if width == 3 else (count,)
+        if out is None:
+            out = np.zeros(shape)
+        elif out.shape != shape or out.dtype != np.float64 or not out.flags.c_contiguous:
+            raise ValueError(f"out must be a C-contiguous float64 array of shape {shape}")
         if count:
             self._check(lib().sph_pool_download(self._h, int(sid), fid, _d(out)), f"sph_pool_download({field})")
         return out
@@ -506,3 +514,27 @@ class Pool:
         n = ctypes.c_ulonglong()
         self._check(lib().sph_pool_get_launch_count(self._h, ctypes.byref(n)), "sph_pool_get_launch_count")
         return n.value
+
+    def step_timed(self, n=1):
+        ms = ctypes.c_float()
+        self._check(lib().sph_pool_step_timed(self._h, int(n), ctypes.byref(ms)), "sph_pool_step_timed")
+        return ms.value
+
+    def set_profiling(self, enable=True):
+        self._check(lib().sph_pool_set_profiling(self._h, int(bool(enable))), "sph_pool_set_profiling")
+
+    def profile(self):
+        buf = ctypes.create_string_buffer(1 << 16)
+        n = lib().sph_pool_get_profile(self._h, buf, len(buf))
+        if n < 0:
+            self._check(n, "sph_pool_get_profile")
+        out = {}
+        for line in buf.value.decode().splitlines():
+            name, cnt, ms = line.split()
+            out[name] = (int(cnt), float(ms))
+        return out
+
+    def list_pairs(self):
+        p, o = ctypes.c_ulonglong(), ctypes.c_uint()
+        self._check(lib().sph_pool_list_pairs(self._h, ctypes.byref(p), ctypes.byref(o)), "sph_pool_list_pairs")
+        return p.value, o.value

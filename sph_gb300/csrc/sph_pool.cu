@@ -484,6 +484,9 @@ public:
     ~Pool()
     {
         for (auto& e : gexec_) if (e) cudaGraphExecDestroy(e);
+        for (auto& q : pending_) { cudaEventDestroy(q.a); cudaEventDestroy(q.b); }
+        for (auto e : events_) cudaEventDestroy(e);
+        for (auto e : tev_) if (e) cudaEventDestroy(e);
         if (st_) cudaStreamDestroy(st_);
         if (st2_) cudaStreamDestroy(st2_);
         if (h_pc_) cudaFreeHost(h_pc_);
@@ -600,6 +603,76 @@ public:
     }
 
     int set_graph(int on) { graph_ = on != 0; return SPH_OK; }
+    int set_profiling(int on) { prof_ = on != 0; return SPH_OK; }
+
+    // "name launches total_ms" per kernel for the host-driven steps timed
+    // since the previous call.
+    int profile(char* buf, size_t len)
+    {
+        SPH_CUDA(cudaStreamSynchronize(st_));
+        std::vector<std::string> names;
+        std::vector<double> ms;
+        std::vector<unsigned long long> cnt;
+        for (auto& q : pending_) {
+            float t = 0.f;
+            SPH_CUDA(cudaEventElapsedTime(&t, q.a, q.b));
+            size_t k = 0;
+            while (k < names.size() && names[k] != q.name) ++k;
+            if (k == names.size()) { names.push_back(q.name); ms.push_back(0.0); cnt.push_back(0); }
+            ms[k] += t;
+            cnt[k] += 1;
+            events_.push_back(q.a);
+            events_.push_back(q.b);
+        }
+        pending_.clear();
+        std::string outs;
+        char line[256];
+        for (size_t k = 0; k < names.size(); ++k) {
+            std::snprintf(line, sizeof line, "%s %llu %.6f\n", names[k].c_str(), cnt[k], ms[k]);
+            outs += line;
+        }
+        if (buf && len) {
+            std::strncpy(buf, outs.c_str(), len - 1);
+            buf[len - 1] = 0;
+        }
+        return (int)outs.size();
+    }
+
+    // nsteps steps bracketed by CUDA events on the pool's stream.
+    int step_timed(int nsteps, float* ms)
+    {
+        if (!tev_[0]) {
+            SPH_CUDA(cudaEventCreate(&tev_[0]));
+            SPH_CUDA(cudaEventCreate(&tev_[1]));
+        }
+        if (dirty_) {
+            const int rc = relayout();
+            if (rc) return rc;
+        }
+        SPH_CUDA(cudaEventRecord(tev_[0], st_));
+        const int rc = step(nsteps);
+        if (rc) return rc;
+        SPH_CUDA(cudaEventRecord(tev_[1], st_));
+        SPH_CUDA(cudaEventSynchronize(tev_[1]));
+        SPH_CUDA(cudaEventElapsedTime(ms, tev_[0], tev_[1]));
+        return SPH_OK;
+    }
+
+    // Stored pairs and overflowing particles of the running scenes' lists.
+    int list_pairs(unsigned long long* pairs, unsigned* overflow)
+    {
+        DevBuf<unsigned long long> o;
+        SPH_CUDA(o.alloc(2));
+        SPH_CUDA(cudaMemsetAsync(o.p, 0, 2 * sizeof(unsigned long long), st_));
+        if (N_) k_list_stats<<<blocks(N_, 256), 256, 0, st_>>>(N_, lcount_.p, kmax_, o.p);
+        SPH_CUDA(cudaGetLastError());
+        unsigned long long h[2];
+        SPH_CUDA(cudaMemcpyAsync(h, o.p, sizeof h, cudaMemcpyDeviceToHost, st_));
+        SPH_CUDA(cudaStreamSynchronize(st_));
+        *pairs = h[0];
+        *overflow = (unsigned)h[1];
+        return SPH_OK;
+    }
 
     int sync()
     {
@@ -745,20 +818,32 @@ private:
     int scan(uint32_t* out)
     {
         const unsigned nt = blocks(K_, kScanTile);
-        run([&] { k_scan_tiles<<<nt, kScanThreads, 0, ls_>>>(K_, count_.p, out, tile_sums_.p); });
-        run([&] { k_scan_tile_sums<<<1, 1024, 0, ls_>>>(nt, tile_sums_.p, out, K_); });
-        run([&] { k_scan_add<<<nt, kScanThreads, 0, ls_>>>(K_, tile_sums_.p, out); });
+        run("k_scan_tiles", [&] { k_scan_tiles<<<nt, kScanThreads, 0, ls_>>>(K_, count_.p, out, tile_sums_.p); });
+        run("k_scan_tile_sums", [&] { k_scan_tile_sums<<<1, 1024, 0, ls_>>>(nt, tile_sums_.p, out, K_); });
+        run("k_scan_add", [&] { k_scan_add<<<nt, kScanThreads, 0, ls_>>>(K_, tile_sums_.p, out); });
         SPH_CUDA(cudaGetLastError());
         return SPH_OK;
     }
 
     // Launch accounting: kernels of host-driven steps are counted as they
     // are launched, those of a captured step graph per loop part.
-    template <typename Fn> void run(Fn&& fn)
+    template <typename Fn> void run(const char* name, Fn&& fn)
     {
-        if (capturing_) ++cap_[loop_ctx_];
-        else if (counting_) ++host_launches_;
+        if (capturing_) { ++cap_[loop_ctx_]; fn(); return; }
+        if (counting_) ++host_launches_;
+        if (!prof_ || !counting_) { fn(); return; }
+        cudaEvent_t a = take_event(), b = take_event();
+        cudaEventRecord(a, ls_);
         fn();
+        cudaEventRecord(b, ls_);
+        pending_.push_back({name, a, b});
+    }
+    cudaEvent_t take_event()
+    {
+        if (!events_.empty()) { cudaEvent_t e = events_.back(); events_.pop_back(); return e; }
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        return e;
     }
     DevScalars* scalars_of(uint32_t s) const
     {
@@ -921,7 +1006,7 @@ private:
         // recomputation for the kept ones, whose positions have not moved)
         int rc = build_grid(false);
         if (rc) return rc;
-        run([&] { k_pool_build_lists<<<blocks(N_, kBlock), kBlock, 0, ls_>>>(F(cur_), bpos_[bcur_].p, sid_.p, table_.p, starts_.p,
+        run("k_pool_build_lists", [&] { k_pool_build_lists<<<blocks(N_, kBlock), kBlock, 0, ls_>>>(F(cur_), bpos_[bcur_].p, sid_.p, table_.p, starts_.p,
                                                                            bstarts_.p, LS()); });
         SPH_CUDA(cudaGetLastError());
         SPH_CUDA(cudaStreamSynchronize(st_));
@@ -936,14 +1021,14 @@ private:
     {
         Fluid<float> a = F(cur_);
         if (move)
-            run([&] { k_pool_cell_update<true><<<blocks(N_, 256), 256, 0, ls_>>>(N_, a, sid_.p, table_.p, key_.p, slot_.p, count_.p); });
+            run("k_pool_cell_update", [&] { k_pool_cell_update<true><<<blocks(N_, 256), 256, 0, ls_>>>(N_, a, sid_.p, table_.p, key_.p, slot_.p, count_.p); });
         else
-            run([&] { k_pool_cell_update<false><<<blocks(N_, 256), 256, 0, ls_>>>(N_, a, sid_.p, table_.p, key_.p, slot_.p, count_.p); });
+            run("k_pool_cell_update", [&] { k_pool_cell_update<false><<<blocks(N_, 256), 256, 0, ls_>>>(N_, a, sid_.p, table_.p, key_.p, slot_.p, count_.p); });
         SPH_CUDA(cudaGetLastError());
         int rc = scan(starts_.p);
         if (rc) return rc;
-        run([&] { k_scatter<<<blocks(N_, 256), 256, 0, ls_>>>(N_, key_.p, slot_.p, starts_.p, tmp_.p); });
-        run([&] { k_gather_fluid<float><<<blocks(N_, 256), 256, 0, ls_>>>(N_, tmp_.p, key_.p, starts_.p, F(cur_), F(1 - cur_)); });
+        run("k_scatter", [&] { k_scatter<<<blocks(N_, 256), 256, 0, ls_>>>(N_, key_.p, slot_.p, starts_.p, tmp_.p); });
+        run("k_gather_fluid", [&] { k_gather_fluid<float><<<blocks(N_, 256), 256, 0, ls_>>>(N_, tmp_.p, key_.p, starts_.p, F(cur_), F(1 - cur_)); });
         SPH_CUDA(cudaGetLastError());
         cur_ = 1 - cur_;
         return SPH_OK;
@@ -1004,22 +1089,22 @@ private:
             const P4<float>* bp = bpos_[bcur_].p;
             Lists<float> L = LS();
             if (any_forces_)
-                run([&] { k_pool_npforce<<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p); });
-            run([&] { k_pool_cfl_accum<<<nb256, 256, 0, ls_>>>(f, sid_.p, table_.p); });
-            run([&] { k_pool_cfl_control<<<1, 256, 0, ls_>>>(table_.p, S_); });
-            run([&] { k_pool_predict_v_warm<<<nb256, 256, 0, ls_>>>(f, sid_.p, table_.p, L.kbuf); });
-            run([&] { k_pool_correct<0><<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
+                run("k_pool_npforce", [&] { k_pool_npforce<<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p); });
+            run("k_pool_cfl_accum", [&] { k_pool_cfl_accum<<<nb256, 256, 0, ls_>>>(f, sid_.p, table_.p); });
+            run("k_pool_cfl_control", [&] { k_pool_cfl_control<<<1, 256, 0, ls_>>>(table_.p, S_); });
+            run("k_pool_predict_v_warm", [&] { k_pool_predict_v_warm<<<nb256, 256, 0, ls_>>>(f, sid_.p, table_.p, L.kbuf); });
+            run("k_pool_correct", [&] { k_pool_correct<0><<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
             SPH_CUDA(cudaGetLastError());
             int rc = solve_loop(
                 1,
                 [&](cudaGraphConditionalHandle h) {
-                    run([&] { k_pool_errors<false, true><<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
-                    run([&] { k_pool_control<0><<<1, 256, 0, ls_>>>(table_.p, S_, pc_.p, h); });
+                    run("k_pool_errors", [&] { k_pool_errors<false, true><<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
+                    run("k_pool_control", [&] { k_pool_control<0><<<1, 256, 0, ls_>>>(table_.p, S_, pc_.p, h); });
                 },
                 [&](cudaGraphConditionalHandle h) {
-                    run([&] { k_pool_correct<1><<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
-                    run([&] { k_pool_errors<false, false><<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
-                    run([&] { k_pool_control<1><<<1, 256, 0, ls_>>>(table_.p, S_, pc_.p, h); });
+                    run("k_pool_correct", [&] { k_pool_correct<1><<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
+                    run("k_pool_errors", [&] { k_pool_errors<false, false><<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
+                    run("k_pool_control", [&] { k_pool_control<1><<<1, 256, 0, ls_>>>(table_.p, S_, pc_.p, h); });
                 });
             if (rc) return rc;
         }
@@ -1029,22 +1114,22 @@ private:
             Fluid<float> f = F(cur_);
             const P4<float>* bp = bpos_[bcur_].p;
             Lists<float> L = LS();
-            run([&] { k_pool_build_lists<<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
+            run("k_pool_build_lists", [&] { k_pool_build_lists<<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
             SPH_CUDA(cudaGetLastError());
             rc = solve_loop(
                 2,
                 [&](cudaGraphConditionalHandle h) {
-                    run([&] { k_pool_errors<true, true><<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
-                    run([&] { k_pool_control<2><<<1, 256, 0, ls_>>>(table_.p, S_, pc_.p, h); });
+                    run("k_pool_errors", [&] { k_pool_errors<true, true><<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
+                    run("k_pool_control", [&] { k_pool_control<2><<<1, 256, 0, ls_>>>(table_.p, S_, pc_.p, h); });
                 },
                 [&](cudaGraphConditionalHandle h) {
-                    run([&] { k_pool_correct<2><<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
-                    run([&] { k_pool_errors<true, false><<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
-                    run([&] { k_pool_control<3><<<1, 256, 0, ls_>>>(table_.p, S_, pc_.p, h); });
+                    run("k_pool_correct", [&] { k_pool_correct<2><<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
+                    run("k_pool_errors", [&] { k_pool_errors<true, false><<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
+                    run("k_pool_control", [&] { k_pool_control<3><<<1, 256, 0, ls_>>>(table_.p, S_, pc_.p, h); });
                 });
             if (rc) return rc;
         }
-        run([&] { k_pool_finish<<<1, 256, 0, ls_>>>(table_.p, S_); });
+        run("k_pool_finish", [&] { k_pool_finish<<<1, 256, 0, ls_>>>(table_.p, S_); });
         SPH_CUDA(cudaGetLastError());
         return SPH_OK;
     }
@@ -1121,7 +1206,11 @@ private:
     unsigned cap_[3] = {0, 0, 0};
     unsigned long long fixed_ = 0, body_d_size_ = 0, body_v_size_ = 0, gsteps_ = 0, snap_d_ = 0, snap_v_ = 0;
     unsigned long long host_launches_ = 0, graph_launches_ = 0, host_body_d_ = 0, host_body_v_ = 0;
-    bool counting_ = true, any_forces_ = false;
+    bool counting_ = true, any_forces_ = false, prof_ = false;
+    struct Timed { const char* name; cudaEvent_t a, b; };
+    std::vector<Timed> pending_;
+    std::vector<cudaEvent_t> events_;
+    cudaEvent_t tev_[2] = {nullptr, nullptr};
     cudaGraphExec_t gexec_[2] = {nullptr, nullptr};
     DevBuf<P4<float>> pos_[2], vel_[2], bpos_[2];
     DevBuf<float> kappa_[2], kappav_[2], pred_[2];
@@ -1257,6 +1346,30 @@ int sph_pool_get_launch_count(sph_pool* p, unsigned long long* out)
     if (!p || !out) return pool_bad(p, "invalid argument");
     *out = p->pool.total_launches();
     return SPH_OK;
+}
+
+int sph_pool_step_timed(sph_pool* p, int nsteps, float* elapsed_ms)
+{
+    if (!p || nsteps < 0 || !elapsed_ms) return pool_bad(p, "invalid argument");
+    return p->pool.step_timed(nsteps, elapsed_ms);
+}
+
+int sph_pool_set_profiling(sph_pool* p, int enable)
+{
+    if (!p) return SPH_ERR_INVALID;
+    return p->pool.set_profiling(enable);
+}
+
+int sph_pool_get_profile(sph_pool* p, char* buf, unsigned long long len)
+{
+    if (!p) return SPH_ERR_INVALID;
+    return p->pool.profile(buf, (size_t)len);
+}
+
+int sph_pool_list_pairs(sph_pool* p, unsigned long long* pairs, unsigned* overflow)
+{
+    if (!p || !pairs || !overflow) return pool_bad(p, "invalid argument");
+    return p->pool.list_pairs(pairs, overflow);
 }
 
 const char* sph_pool_last_error(const sph_pool* p)

@@ -116,3 +116,27 @@ def test_admission_respects_capacity(gpu_lib):
     with pytest.raises(sph_gb300.PoolFull):
         P.add_scene(x, boundary_points=b, steps=5, **p)
     assert P.usage()["particles"] == x.shape[0]
+
+
+def test_timed_profiled_steps_and_list_stats(gpu_lib):
+    """step_timed advances like step; the per-kernel profile covers the
+    pool's kernels; list occupancy is reported; results are unchanged by
+    profiling."""
+    scenes = [A] + OTHERS
+    P1, ids1 = pool_run(scenes, 3, graph=True)
+    ms = P1.step_timed(4)
+    assert ms > 0
+    P2, ids2 = pool_run(scenes, 3)
+    P2.set_profiling(True)
+    P2.step(4)
+    prof = P2.profile()
+    assert "k_pool_build_lists" in prof and "k_pool_correct" in prof and "k_pool_errors" in prof
+    assert all(c > 0 and t >= 0 for c, t in prof.values())
+    for s1, s2 in zip(ids1, ids2):
+        assert np.array_equal(P1.get(s1, "x"), P2.get(s2, "x"))
+        assert P1.query(s1)[0]["steps"] == 7
+    pairs, overflow = P1.list_pairs()
+    n = sum(x.shape[0] for x, _, _ in scenes)
+    assert 10 * n < pairs < 64 * n and overflow == 0
+    out = np.empty((A[0].shape[0], 3))
+    assert P1.get(ids1[0], "v", out=out) is out
