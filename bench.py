@@ -66,33 +66,36 @@ UNIT = "particle-steps/s"
 WORKLOAD = "batched_mix_256"
 CPU_SAMPLE_SCENES = 16
 
-# Compulsory bytes of each kernel as implemented (FP32 form: float4 = 16 B,
-# scalar = 4 B, scene id 4 B; each array read once and written once,
-# neighbour re-reads not counted): (bytes per fluid particle, bytes per stored
-# pair, touches the boundary particles at 16 B each).
+# Algorithmic bytes of each kernel: the compulsory field traffic per fluid
+# particle of the reference's pass it implements (FP32 SoA: float4 = 16 B,
+# scalar = 4 B; each array read once and written once, neighbour re-reads not
+# counted; walks that touch the boundary add 16 B per boundary particle).
+# (bytes per fluid particle, touches the boundary, pair-list bytes per stored
+# pair that the kernel streams as implemented).
 ALGO_BYTES = {
-    "k_cell_update": (64, 0, False),
-    "k_pool_cell_update": (68, 0, False),
-    "k_scatter": (16, 0, False),
-    "k_gather_fluid": (108, 0, False),
-    "k_density": (32, 0, True),
-    "k_dfsph_cfl": (32, 0, False),
-    "k_pool_cfl_accum": (36, 0, False),
-    "k_dfsph_predict_v_warm": (108, 0, False),
-    "k_pool_predict_v_warm": (112, 0, False),
-    "k_dfsph_correct": (68, 0, True),
-    "k_dfsph_predict_density": (64, 0, True),
-    "k_dfsph_divergence": (64, 0, True),
-    "k_npforce": (68, 0, True),
-    "k_pool_npforce": (72, 0, True),
-    "k_st_normals": (36, 0, False),
-    "k_build_lists": (52, 16, True),
-    "k_pool_build_lists": (56, 16, True),
-    "k_dfsph_correct_list": (72, 16, False),
-    "k_pool_correct": (76, 16, False),
-    "k_dfsph_predict_density_list": (52, 16, False),
-    "k_dfsph_divergence_list": (52, 16, False),
-    "k_pool_errors": (56, 16, False),
+    "k_cell_update": (64, False, 0),
+    "k_pool_cell_update": (64, False, 0),
+    "k_scatter": (16, False, 0),
+    "k_gather_fluid": (108, False, 0),
+    "k_density": (28, True, 0),
+    "k_build_lists": (28, True, 16),
+    "k_pool_build_lists": (28, True, 16),
+    "k_dfsph_cfl": (32, False, 0),
+    "k_pool_cfl_accum": (32, False, 0),
+    "k_dfsph_predict_v_warm": (76, False, 0),
+    "k_pool_predict_v_warm": (76, False, 0),
+    "k_dfsph_correct": (68, True, 0),
+    "k_dfsph_correct_list": (68, False, 16),
+    "k_pool_correct": (68, False, 16),
+    "k_dfsph_predict_density": (40, True, 0),
+    "k_dfsph_predict_density_list": (40, False, 16),
+    "k_pool_errors_density": (40, False, 16),
+    "k_dfsph_divergence": (36, True, 0),
+    "k_dfsph_divergence_list": (36, False, 16),
+    "k_pool_errors_div": (36, False, 16),
+    "k_npforce": (68, True, 0),
+    "k_pool_npforce": (68, True, 0),
+    "k_st_normals": (36, False, 0),
 }
 
 
@@ -439,16 +442,18 @@ def run_served(args, rate, seconds, big_every):
     return out
 
 
-def roofline(prof, n, nb, pairs):
+def roofline(prof, n, nb, pairs, workload):
     kern = max(prof.items(), key=lambda kv: kv[1][1]) if prof else ("none", (1, 0.0))
     kname, (kcount, kms) = kern
-    per_b, per_pair, touches_b = ALGO_BYTES.get(kname, (0, 0, False))
-    bytes_launch = n * per_b + pairs * per_pair + (nb * 16 if touches_b else 0)
+    per_p, touches_b, per_pair = ALGO_BYTES.get(kname, (0, False, 0))
+    bytes_launch = n * per_p + (nb * 16 if touches_b else 0)
+    stream_launch = bytes_launch + pairs * per_pair
     avg_ms = kms / max(kcount, 1)
     achieved = bytes_launch / (avg_ms / 1000.0) / 1e9 if avg_ms > 0 else 0.0
+    streamed = stream_launch / (avg_ms / 1000.0) / 1e9 if avg_ms > 0 else 0.0
     peak, peak_kind = load_peaks()
     traffic = None
-    tp = os.path.join(ROOT, "profiles", f"ncu_{kname}_{WORKLOAD}.md")
+    tp = os.path.join(ROOT, "profiles", f"ncu_{kname}_{workload}.md")
     if os.path.exists(tp):
         for ln in open(tp):
             if ln.startswith("dram_bytes_per_launch:"):
@@ -457,7 +462,9 @@ def roofline(prof, n, nb, pairs):
     return {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "peak_kind": f"of {peak_kind}", "traffic": traffic,
             "algorithmic_bytes_per_launch": bytes_launch, "avg_launch_ms": avg_ms,
-            "kernel_share": kms / total if total else None}
+            "kernel_share": kms / total if total else None,
+            "with_pair_lists": {"bytes_per_launch": stream_launch, "achieved": streamed, "frac": streamed / peak,
+                                "note": "field bytes plus the 16-byte pair records the kernel writes or reads"}}
 
 
 def main():
@@ -467,6 +474,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--list-max", type=int, default=64, help="pair-list slots per particle")
+    ap.add_argument("--scenes", type=int, default=256, help="first N scenes of the mix (256: the full workload)")
     ap.add_argument("--profile-steps", type=int, default=10, help="host-driven steps timed per kernel")
     ap.add_argument("--plain-steps", type=int, default=0, help="timed steps per scene for the plain arm (0: --steps)")
     ap.add_argument("--dam-steps", type=int, default=500)
@@ -495,11 +503,12 @@ def main():
     torch.cuda.set_device(local)
     wall0 = time.perf_counter()
 
-    scenes = mix(args.warmup + args.steps)
+    scenes = mix(args.warmup + args.steps)[: args.scenes]
+    workload = WORKLOAD if args.scenes == 256 else f"batched_mix_{args.scenes}"
     B = run_batched(scenes, args, world, local)
     t_max = dist_max(B["ms"], world)
     value = world * B["n"] * args.steps / (t_max / 1000.0)
-    roof = roofline(B["prof"], B["n"], B["nb"], B["pairs"])
+    roof = roofline(B["prof"], B["n"], B["nb"], B["pairs"], workload)
     roof["timing"] = f"CUDA events around each launch, {args.profile_steps} host-driven pool steps"
 
     plain = None if args.no_plain else run_plain(scenes, args)
@@ -529,7 +538,7 @@ def main():
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scenes)",
-            "config": {"workload": WORKLOAD, "scenes": len(scenes), "fluid_particles": B["n"],
+            "config": {"workload": workload, "scenes": len(scenes), "fluid_particles": B["n"],
                        "boundary_particles": B["nb"], "steps_per_scene": args.warmup + args.steps,
                        "parallelism": f"replicas x{world}",
                        "l2": "not flushed: the resident working set (pair lists ~4 GB) is far larger than L2",

@@ -97,6 +97,7 @@ def lib():
         L.orc_add_box.argtypes = [vp, dp, dp]
         L.orc_add_sphere.argtypes = [vp, dp, ctypes.c_double]
         L.orc_add_points.argtypes = [vp, dp, ctypes.c_uint]
+        L.orc_perturb.argtypes = [vp, ctypes.c_double, ctypes.c_double, ctypes.c_ulonglong]
         L.orc_init.argtypes = [vp]
         L.orc_step.argtypes = [vp, ctypes.c_int]
         L.orc_num_fluid.argtypes = [vp]
@@ -220,6 +221,11 @@ class OracleScene:
         if rc != 0:
             raise KeyError(field)
         return out
+
+    def perturb(self, dx, dv, seed):
+        """Test instrument: add U(-dx, dx) to positions, U(-dv, dv) to velocities."""
+        if lib().orc_perturb(self.h, float(dx), float(dv), int(seed)) != 0:
+            raise RuntimeError("orc_perturb failed")
 
     def scalar(self, name):
         out = ctypes.c_double()

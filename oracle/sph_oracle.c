@@ -1333,6 +1333,30 @@ int orc_step(orc_scene* s, int nsteps)
     return 0;
 }
 
+/* Test instrument, not part of the reference: adds U(-dx, dx) to every
+ * position component and U(-dv, dv) to every velocity component (splitmix64
+ * stream from `seed`).  Used to measure how far the reference's own
+ * trajectories spread under rounding-sized noise injected every step. */
+static double orc_unit(uint64_t* st)
+{
+    uint64_t z = (*st += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return (double)(z >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0;
+}
+
+int orc_perturb(orc_scene* s, double dx, double dv, unsigned long long seed)
+{
+    if (!s || !s->inited) return -1;
+    uint64_t st = seed;
+    for (unsigned i = 0; i < s->n; ++i) {
+        s->x[i].x += dx * orc_unit(&st); s->x[i].y += dx * orc_unit(&st); s->x[i].z += dx * orc_unit(&st);
+        s->v[i].x += dv * orc_unit(&st); s->v[i].y += dv * orc_unit(&st); s->v[i].z += dv * orc_unit(&st);
+    }
+    return 0;
+}
+
 unsigned orc_num_fluid(const orc_scene* s) { return s ? s->n : 0; }
 unsigned orc_num_boundary(const orc_scene* s) { return s ? s->nb : 0; }
 

@@ -46,6 +46,8 @@ int orc_add_sphere(orc_scene* s, const double c[3], double radius);
 int orc_add_points(orc_scene* s, const double* pts, unsigned m);
 int orc_init(orc_scene* s);
 int orc_step(orc_scene* s, int nsteps);
+/* test instrument: uniform noise on positions and velocities */
+int orc_perturb(orc_scene* s, double dx, double dv, unsigned long long seed);
 unsigned orc_num_fluid(const orc_scene* s);
 unsigned orc_num_boundary(const orc_scene* s);
 /* field: x v a rho p alpha div pred k kv pacc normal bx psi */

@@ -1098,12 +1098,12 @@ private:
             int rc = solve_loop(
                 1,
                 [&](cudaGraphConditionalHandle h) {
-                    run("k_pool_errors", [&] { k_pool_errors<false, true><<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
+                    run("k_pool_errors_density", [&] { k_pool_errors<false, true><<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
                     run("k_pool_control", [&] { k_pool_control<0><<<1, 256, 0, ls_>>>(table_.p, S_, pc_.p, h); });
                 },
                 [&](cudaGraphConditionalHandle h) {
                     run("k_pool_correct", [&] { k_pool_correct<1><<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
-                    run("k_pool_errors", [&] { k_pool_errors<false, false><<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
+                    run("k_pool_errors_density", [&] { k_pool_errors<false, false><<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
                     run("k_pool_control", [&] { k_pool_control<1><<<1, 256, 0, ls_>>>(table_.p, S_, pc_.p, h); });
                 });
             if (rc) return rc;
@@ -1119,12 +1119,12 @@ private:
             rc = solve_loop(
                 2,
                 [&](cudaGraphConditionalHandle h) {
-                    run("k_pool_errors", [&] { k_pool_errors<true, true><<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
+                    run("k_pool_errors_div", [&] { k_pool_errors<true, true><<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
                     run("k_pool_control", [&] { k_pool_control<2><<<1, 256, 0, ls_>>>(table_.p, S_, pc_.p, h); });
                 },
                 [&](cudaGraphConditionalHandle h) {
                     run("k_pool_correct", [&] { k_pool_correct<2><<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
-                    run("k_pool_errors", [&] { k_pool_errors<true, false><<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
+                    run("k_pool_errors_div", [&] { k_pool_errors<true, false><<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
                     run("k_pool_control", [&] { k_pool_control<3><<<1, 256, 0, ls_>>>(table_.p, S_, pc_.p, h); });
                 });
             if (rc) return rc;

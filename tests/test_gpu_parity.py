@@ -15,7 +15,7 @@ import pytest
 
 import oracle
 import sph_gb300
-from scenes import SCENES, scene
+from scenes import SCENES, jitter, scene
 from util import golden, relerr
 
 pytestmark = pytest.mark.gpu
@@ -92,8 +92,13 @@ def test_f32_error_against_reference(gpu_lib, name, lists):
     """FP32 production form against the reference's FP64 results, 3 steps.
     Measured on GB300: positions <= 6e-8 rel, densities <= 1e-6 rel,
     alpha <= 2e-6 rel, WCSPH/PCISPH pressures <= 1e-4 rel, velocities
-    <= 2.5e-4 m/s abs (particles near the rho* >= rho0 clamp flip sides), and
-    identical iteration counts.  Bounds below leave ~10x headroom."""
+    <= 2.5e-4 m/s abs, and identical iteration counts.  Bounds below leave
+    ~10x headroom.  The velocity bound is loose because most of these scenes
+    are exact lattices: neighbours at exactly h make the reference's
+    20-neighbour rule and rho* >= rho0 clamp depend on the last bit, so
+    single wall-layer particles get or miss a divergence correction; the
+    jittered test below holds FP32 velocities to 1e-3 of the largest speed
+    (measured 7e-5 for DFSPH, 1e-6 for WCSPH)."""
     g = golden(name)
     s = gpu_scene(name, precision="f32", lists=lists)
     for step in (1, 2, 3):
@@ -106,6 +111,40 @@ def test_f32_error_against_reference(gpu_lib, name, lists):
         if SCENES[name]["params"]["method"] != 2:
             assert relerr(s.get("p"), g[f"s{step}.p"]) <= 1e-3
         assert s.stats()["iterations"] == int(g[f"s{step}.iterations"][0])
+
+
+@pytest.mark.parametrize("name", ["dfsph_akinci", "dfsph_artvisc", "dfsph_cube", "wcsph_akinci"])
+def test_f32_error_on_jittered_lattice(gpu_lib, name):
+    """FP32 against the oracle on the exact-lattice scenes jittered by
+    U(-0.01 r, 0.01 r).  An exact lattice of spacing 2r with h = 4r puts
+    neighbours at exactly h, where the reference's 20-neighbour rule and the
+    rho* >= rho0 clamp let the last bit decide, so the bounds of the test
+    above are loose; off the lattice FP32 must track the FP64 reference
+    closely: velocities within 1e-3 of the largest speed, positions 1e-6
+    and densities 1e-5 relative, equal iteration counts, 3 steps."""
+    params, x, boxes, spheres = scene(name)
+    x = jitter(x, params["radius"], 7)
+    o = oracle.OracleScene(params, x, boxes=boxes, spheres=spheres)
+    s = sph_gb300.Scene(precision="f32", **params)
+    s.set_fluid(x)
+    for mn, mx in boxes:
+        s.add_boundary_box(mn, mx)
+    for c, r in spheres:
+        s.add_boundary_sphere(c, r)
+    s.init()
+    for step in (1, 2, 3):
+        o.step(1)
+        s.step(1)
+        vr = o.get("v")
+        dv = np.abs(s.get("v") - vr).max()
+        vmax = np.sqrt((vr * vr).sum(1)).max()
+        print(f"{name} step {step}: |dv| {dv:.3e} of |v|max {vmax:.3e}")
+        assert dv <= 1e-3 * vmax
+        assert relerr(s.get("x"), o.get("x")) <= 1e-6
+        assert relerr(s.get("rho"), o.get("rho")) <= 1e-5
+        if params["method"] == 2:
+            assert s.stats()["iterations"] == int(o.scalar("iterations"))
+            assert s.stats()["iterations_v"] == int(o.scalar("iterationsV"))
 
 
 def test_f64_twenty_steps_match_oracle(gpu_lib):
