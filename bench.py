@@ -10,7 +10,9 @@ Workloads (seeded, synthetic; sph_gb300/workloads.py):
                    0.05-0.2 m in a 1 m Akinci box, r = 0.01 m, CFL-adaptive
                    dt in [1e-5, 5e-3] s, 0.1 % density / 0.1 %/s divergence
                    error, FP32 bulk with FP64 reductions.  Every scene runs
-                   W + K steps (the 500-step scenes at the defaults).
+                   the autotuner's measuring steps (18, ordinary steps that
+                   pick the launch shapes), W warm-up and K timed steps
+                   (about 500 at the defaults).
   dam_break_125k   one 50^3 = 125,000-particle dam break at r = 0.005 m in a
                    1.5 x 0.8 x 0.8 m Akinci box (60,802 boundary points).
                    (At r = 0.01 m the 50^3 block is 1 m tall and does not
@@ -65,6 +67,7 @@ METRIC = "DFSPH particle-steps/s @0.1% density err, served vs plain GPU; p50/p99
 UNIT = "particle-steps/s"
 WORKLOAD = "batched_mix_256"
 CPU_SAMPLE_SCENES = 16
+TUNE_STEPS = 19  # at most: the autotuner's 18 measuring steps + the admitting step
 
 # Algorithmic bytes of each kernel: the compulsory field traffic per fluid
 # particle of the reference's pass it implements (FP32 SoA: float4 = 16 B,
@@ -280,10 +283,13 @@ def run_batched(scenes, args, world, local):
 
     W, K, P = args.warmup, args.steps, args.profile_steps
     pool = make_pool(scenes, args.list_max)
-    ids = [pool.add_scene(x, boundary_points=b, steps=W + K + P, **params) for x, b, params, _ in scenes]
+    pool.set_autotune(2)  # measure launch shapes on this mix (cached afterwards)
+    ids = [pool.add_scene(x, boundary_points=b, steps=TUNE_STEPS + W + K + P, **params) for x, b, params, _ in scenes]
     n = sum(s[0].shape[0] for s in scenes)
     nb = sum(s[1].shape[0] for s in scenes)
     pool.set_graph(True)
+    tune_steps = pool.tune()
+    tuning = dict(pool.tuning(), steps=tune_steps, log=pool.tuning_log().strip().splitlines())
     pool.step(W)
     pool.synchronize()
     s0 = scene_stats(pool, ids)
@@ -310,7 +316,8 @@ def run_batched(scenes, args, world, local):
     pool.set_profiling(False)
     pool.close()
     return dict(ms=ms, n=n, nb=nb, launches=l1 - l0, clocks=clocks.summary(), its=its, itsv=itsv,
-                sim_s_per_scene=sim, pairs=pairs, overflow=overflow, prof=prof, finished_early=finished_early)
+                sim_s_per_scene=sim, pairs=pairs, overflow=overflow, prof=prof, finished_early=finished_early,
+                tuning=tuning)
 
 
 def run_plain(scenes, args):
@@ -539,7 +546,10 @@ def main():
             "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scenes)",
             "config": {"workload": workload, "scenes": len(scenes), "fluid_particles": B["n"],
-                       "boundary_particles": B["nb"], "steps_per_scene": args.warmup + args.steps,
+                       "boundary_particles": B["nb"],
+                       "steps_per_scene": f"{B['tuning']['steps']} autotuning + {args.warmup} warm-up + {args.steps} "
+                                          f"timed + {args.profile_steps} profiled",
+                       "autotuner": B["tuning"],
                        "parallelism": f"replicas x{world}",
                        "l2": "not flushed: the resident working set (pair lists ~4 GB) is far larger than L2",
                        "step_timing": "CUDA events on the pool's stream around the K graph-launched steps",

@@ -258,6 +258,28 @@ int sph_pool_step_timed(sph_pool* pool, int nsteps, float* elapsed_ms);
  * "name launches total_ms" lines (as sph_ctx_get_profile). */
 int sph_pool_set_profiling(sph_pool* pool, int enable);
 int sph_pool_get_profile(sph_pool* pool, char* buf, unsigned long long len);
+/* Launch shapes of the pool's hot kernels.  Results do not depend on them. */
+typedef struct sph_pool_tuning {
+    int build_block;  /* threads per block of the pair-list build: 64, 128 or 256 */
+    int queue_depth;  /* candidates staged per particle in shared memory by the build: 32, 48 or 64 */
+    int solver_block; /* threads per block of the solver passes: 128, 256 or 512 */
+    int scan_width;   /* grid keys per thread of the cell-count scan (sort width): 4, 8 or 16 */
+    int source;       /* 0 defaults or set by the caller, 1 tuning cache, 2 measured */
+    int steps_left;   /* tuning steps still to run (read only) */
+} sph_pool_tuning;
+/* Autotuner (no reference counterpart): mode 0 off (keep the current
+ * shapes), 1 (default) after each re-layout use the cached shapes for this
+ * GPU model / particle-count bucket / list width or measure them over the
+ * next 18 steps (ordinary steps of every resident scene, host-driven), 2 as 1
+ * but measure again.  The cache is a text file (SPH_GB300_TUNE_FILE, default
+ * ~/.cache/sph_gb300_tune.txt). */
+int sph_pool_set_autotune(sph_pool* pool, int mode);
+int sph_pool_get_tuning(sph_pool* pool, sph_pool_tuning* out);
+/* Fixed shapes (turns the autotuner off); values outside the sets above are
+ * rejected with SPH_ERR_INVALID. */
+int sph_pool_set_tuning(sph_pool* pool, const sph_pool_tuning* tuning);
+/* The last measurement, one "candidate: ms" line per candidate. */
+int sph_pool_get_tuning_log(sph_pool* pool, char* buf, unsigned long long len);
 /* Pair-list occupancy: stored pairs and particles whose neighbours overflow. */
 int sph_pool_list_pairs(sph_pool* pool, unsigned long long* pairs, unsigned* overflow);
 const char* sph_pool_last_error(const sph_pool* pool);

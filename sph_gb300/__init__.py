@@ -106,6 +106,17 @@ class PoolDesc(ctypes.Structure):
     ]
 
 
+class PoolTuning(ctypes.Structure):
+    _fields_ = [
+        ("build_block", ctypes.c_int),
+        ("queue_depth", ctypes.c_int),
+        ("solver_block", ctypes.c_int),
+        ("scan_width", ctypes.c_int),
+        ("source", ctypes.c_int),
+        ("steps_left", ctypes.c_int),
+    ]
+
+
 # The C ABI, as (name, restype, argtypes); the CPU tests check that the
 # library exports each of these.
 _vp, _dp, _ip = ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)
@@ -155,6 +166,10 @@ ABI = [
     ("sph_pool_step_timed", ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
     ("sph_pool_set_profiling", ctypes.c_int, [_vp, ctypes.c_int]),
     ("sph_pool_get_profile", ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_ulonglong]),
+    ("sph_pool_set_autotune", ctypes.c_int, [_vp, ctypes.c_int]),
+    ("sph_pool_get_tuning", ctypes.c_int, [_vp, ctypes.POINTER(PoolTuning)]),
+    ("sph_pool_set_tuning", ctypes.c_int, [_vp, ctypes.POINTER(PoolTuning)]),
+    ("sph_pool_get_tuning_log", ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_ulonglong]),
     ("sph_pool_list_pairs", ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(ctypes.c_uint)]),
     ("sph_pool_last_error", ctypes.c_char_p, [_vp]),
 ]
@@ -533,6 +548,35 @@ class Pool:
             name, cnt, ms = line.split()
             out[name] = (int(cnt), float(ms))
         return out
+
+    def set_autotune(self, mode=1):
+        """0 off, 1 cached-or-measured after each re-layout (default), 2 measure again."""
+        self._check(lib().sph_pool_set_autotune(self._h, int(mode)), "sph_pool_set_autotune")
+
+    def tuning(self):
+        t = PoolTuning()
+        self._check(lib().sph_pool_get_tuning(self._h, ctypes.byref(t)), "sph_pool_get_tuning")
+        return {name: getattr(t, name) for name, _ in PoolTuning._fields_}
+
+    def set_tuning(self, build_block=128, queue_depth=64, solver_block=128, scan_width=8):
+        t = PoolTuning(build_block, queue_depth, solver_block, scan_width, 0, 0)
+        self._check(lib().sph_pool_set_tuning(self._h, ctypes.byref(t)), "sph_pool_set_tuning")
+
+    def tuning_log(self):
+        buf = ctypes.create_string_buffer(1 << 14)
+        lib().sph_pool_get_tuning_log(self._h, buf, len(buf))
+        return buf.value.decode()
+
+    def tune(self):
+        """Run the pending tuning steps now (ordinary steps of every resident
+        scene); returns how many steps were taken."""
+        k = 0
+        self.step(1)
+        k += 1
+        while self.tuning()["steps_left"] > 0:
+            self.step(1)
+            k += 1
+        return k
 
     def list_pairs(self):
         p, o = ctypes.c_ulonglong(), ctypes.c_uint()

@@ -238,27 +238,55 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* sh, ui
     return r;
 }
 
+// Each thread owns PER consecutive keys moved as 16-byte vectors when the
+// run lies inside the key range (count and starts are 256-byte aligned
+// allocations and PER is a multiple of 4, so every run is 16-byte aligned).
+// PER (the scan width) is a tuning parameter of the pool; the result does
+// not depend on it.
+template <unsigned PER = kScanPer>
 static __global__ void __launch_bounds__(kScanThreads) k_scan_tiles(uint32_t nkeys, uint32_t* __restrict__ count,
                                                              uint32_t* __restrict__ starts, uint32_t* __restrict__ tile_sums)
 {
+    static_assert(PER % 4 == 0, "whole uint4 per thread");
     __shared__ uint32_t sh[33];
-    const uint32_t base = blockIdx.x * kScanTile + threadIdx.x * kScanPer;
-    uint32_t v[kScanPer];
+    const uint32_t base = blockIdx.x * (kScanThreads * PER) + threadIdx.x * PER;
+    uint32_t v[PER];
+    const bool full = base + PER <= nkeys;
+    if (full) {
+        uint4* c4 = reinterpret_cast<uint4*>(count + base);
+#pragma unroll
+        for (unsigned q = 0; q < PER / 4; ++q) {
+            const uint4 a = c4[q];
+            v[4 * q] = a.x; v[4 * q + 1] = a.y; v[4 * q + 2] = a.z; v[4 * q + 3] = a.w;
+            c4[q] = make_uint4(0u, 0u, 0u, 0u);
+        }
+    } else {
+#pragma unroll
+        for (unsigned k = 0; k < PER; ++k) {
+            const uint32_t idx = base + k;
+            v[k] = idx < nkeys ? count[idx] : 0u;
+            if (idx < nkeys) count[idx] = 0u;
+        }
+    }
     uint32_t s = 0;
 #pragma unroll
-    for (int k = 0; k < (int)kScanPer; ++k) {
-        const uint32_t idx = base + k;
-        v[k] = idx < nkeys ? count[idx] : 0u;
-        if (idx < nkeys) count[idx] = 0u;
-        s += v[k];
-    }
+    for (unsigned k = 0; k < PER; ++k) s += v[k];
     uint32_t total;
     uint32_t run = block_excl_scan(s, sh, &total);
 #pragma unroll
-    for (int k = 0; k < (int)kScanPer; ++k) {
-        const uint32_t idx = base + k;
-        if (idx < nkeys) starts[idx] = run;
-        run += v[k];
+    for (unsigned k = 0; k < PER; ++k) {
+        const uint32_t t = v[k];
+        v[k] = run;
+        run += t;
+    }
+    if (full) {
+        uint4* s4 = reinterpret_cast<uint4*>(starts + base);
+#pragma unroll
+        for (unsigned q = 0; q < PER / 4; ++q) s4[q] = make_uint4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+    } else {
+#pragma unroll
+        for (unsigned k = 0; k < PER; ++k)
+            if (base + k < nkeys) starts[base + k] = v[k];
     }
     if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
 }
@@ -279,14 +307,23 @@ static __global__ void __launch_bounds__(1024) k_scan_tile_sums(uint32_t ntiles,
     if (threadIdx.x == 0) starts[nkeys] = carry;
 }
 
+template <unsigned PER = kScanPer>
 static __global__ void __launch_bounds__(kScanThreads) k_scan_add(uint32_t nkeys, const uint32_t* __restrict__ tile_sums,
                                                            uint32_t* __restrict__ starts)
 {
     const uint32_t add = tile_sums[blockIdx.x];
-    const uint32_t base = blockIdx.x * kScanTile;
-    for (uint32_t k = threadIdx.x; k < kScanTile; k += blockDim.x) {
-        const uint32_t idx = base + k;
-        if (idx < nkeys) starts[idx] += add;
+    const uint32_t base = blockIdx.x * (kScanThreads * PER) + threadIdx.x * PER;
+    if (base + PER <= nkeys) {
+        uint4* s4 = reinterpret_cast<uint4*>(starts + base);
+#pragma unroll
+        for (unsigned q = 0; q < PER / 4; ++q) {
+            uint4 a = s4[q];
+            a.x += add; a.y += add; a.z += add; a.w += add;
+            s4[q] = a;
+        }
+    } else {
+        for (uint32_t k = 0; k < PER; ++k)
+            if (base + k < nkeys) starts[base + k] += add;
     }
 }
 

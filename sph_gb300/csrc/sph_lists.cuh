@@ -65,12 +65,13 @@ template <typename R>
 __device__ __forceinline__ void build_lists_one(uint32_t i, const Fluid<R>& f, const P4<R>* __restrict__ bpos,
                                                 const GridView& g, const uint32_t* __restrict__ cs,
                                                 const uint32_t* __restrict__ bs, const Consts<R>& c, int akinci,
-                                                const Lists<R>& L, uint32_t* q)
+                                                const Lists<R>& L, uint32_t* q, uint32_t qstride = kBlock,
+                                                uint32_t qdepth = kQueue)
 {
     const uint32_t n = f.n;
     const V3<R> xi = xyz(f.pos[i]);
     const uint32_t pc = f.cell[i];
-    const uint32_t qcap = L.kmax < kQueue ? L.kmax : kQueue;
+    const uint32_t qcap = L.kmax < qdepth ? L.kmax : qdepth;
     R density = 0, sumSq = 0;
     V3<R> sumGrad = {0, 0, 0};
     uint32_t cnt = 0;
@@ -95,14 +96,14 @@ __device__ __forceinline__ void build_lists_one(uint32_t i, const Fluid<R>& f, c
     walk<R, 1>(g, cs, pc, xi, c.h, 0, [&](uint32_t j, V3<R> s) {
         const V3<R> r = s - xyz(ldg4(f.pos + j));
         if (dot3(r, r) <= c.cull2) {
-            if (nq < qcap) q[nq * kBlock + threadIdx.x] = j;
+            if (nq < qcap) q[nq * qstride + threadIdx.x] = j;
             ++nq;
         }
     });
     if (nq <= qcap) {
         // phase 2: evaluate the queued candidates in walk order
         for (uint32_t k = 0; k < nq; ++k) {
-            const uint32_t j = q[k * kBlock + threadIdx.x];
+            const uint32_t j = q[k * qstride + threadIdx.x];
             const V3<R> r = pair_vec(xi, pc, ldg4(f.pos + j), __ldg(f.cell + j), c.h);
             accept(j, r, dot3(r, r));
         }

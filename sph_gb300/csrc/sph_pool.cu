@@ -23,8 +23,12 @@
 // lists (sph_lists.cuh).
 #include <cuda_runtime.h>
 
+#include <sys/stat.h>
+
 #include <algorithm>
 #include <cstddef>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <list>
 #include <new>
@@ -196,17 +200,24 @@ __global__ void k_pool_psi(uint32_t N, Boundary<float> b, const uint32_t* __rest
     b.pos[i].w = c.density0 * psi;
 }
 
-__global__ void __launch_bounds__(kBlock, 7) k_pool_build_lists(Fluid<float> f, const P4<float>* __restrict__ bpos,
-                                                                const uint32_t* __restrict__ sid, const PoolScene* T,
-                                                                const uint32_t* __restrict__ cs, const uint32_t* __restrict__ bs,
-                                                                Lists<float> L)
+// Pair-list build (k_build_lists per scene).  BLOCK threads per block and a
+// shared candidate queue of qdepth entries per thread (dynamic shared
+// memory, qdepth * BLOCK * 4 bytes): both tuning parameters; the lists do not
+// depend on them (queued and re-walked candidates are accepted in the same
+// walk order).
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK, 896 / BLOCK) k_pool_build_lists(Fluid<float> f, const P4<float>* __restrict__ bpos,
+                                                                         const uint32_t* __restrict__ sid, const PoolScene* T,
+                                                                         const uint32_t* __restrict__ cs,
+                                                                         const uint32_t* __restrict__ bs, Lists<float> L,
+                                                                         uint32_t qdepth)
 {
-    __shared__ uint32_t q[kQueue * kBlock];
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    extern __shared__ uint32_t q[];
+    const uint32_t i = blockIdx.x * BLOCK + threadIdx.x;
     if (i >= f.n) return;
     const PoolScene& sd = T[sid[i]];
     if (!sd.running) return;
-    build_lists_one(i, f, bpos, sd.g, cs + sd.key_base, bs + sd.key_base, sd.c, sd.akinci, L, q);
+    build_lists_one(i, f, bpos, sd.g, cs + sd.key_base, bs + sd.key_base, sd.c, sd.akinci, L, q, (uint32_t)BLOCK, qdepth);
 }
 
 // Non-pressure forces of the scene (XSPH / standard / artificial viscosity;
@@ -332,8 +343,8 @@ __global__ void k_pool_predict_v_warm(Fluid<float> f, const uint32_t* __restrict
     f.kappa[i] = 0.f;
 }
 
-template <int MODE>
-__global__ void __launch_bounds__(kBlock, 8) k_pool_correct(Fluid<float> f, const P4<float>* __restrict__ bpos,
+template <int BLOCK, int MODE>
+__global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) k_pool_correct(Fluid<float> f, const P4<float>* __restrict__ bpos,
                                                             const uint32_t* __restrict__ sid, const PoolScene* T,
                                                             const uint32_t* __restrict__ cs, const uint32_t* __restrict__ bs,
                                                             Lists<float> L)
@@ -349,8 +360,8 @@ __global__ void __launch_bounds__(kBlock, 8) k_pool_correct(Fluid<float> f, cons
 
 // DIV = false: DFSPHSolver::predictDensities; DIV = true:
 // DFSPHSolver::computeDivergenceError.  Adds each scene's error sum.
-template <bool DIV, bool INITIAL>
-__global__ void __launch_bounds__(kBlock, 8) k_pool_errors(Fluid<float> f, const P4<float>* __restrict__ bpos,
+template <int BLOCK, bool DIV, bool INITIAL>
+__global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) k_pool_errors(Fluid<float> f, const P4<float>* __restrict__ bpos,
                                                            const uint32_t* __restrict__ sid, PoolScene* T,
                                                            const uint32_t* __restrict__ cs, const uint32_t* __restrict__ bs,
                                                            Lists<float> L)
@@ -479,12 +490,14 @@ struct PoolEntry {
 
 class Pool {
 public:
+    struct Tune { int build_block = 128, queue = 64, solver_block = 128, scan_per = 8; };
     std::string err;
 
     ~Pool()
     {
         for (auto& e : gexec_) if (e) cudaGraphExecDestroy(e);
         for (auto& q : pending_) { cudaEventDestroy(q.a); cudaEventDestroy(q.b); }
+        for (auto& q : tpending_) { cudaEventDestroy(q.a); cudaEventDestroy(q.b); }
         for (auto e : events_) cudaEventDestroy(e);
         for (auto e : tev_) if (e) cudaEventDestroy(e);
         if (st_) cudaStreamDestroy(st_);
@@ -520,7 +533,9 @@ public:
         const size_t M = std::max(P, B);
         SPH_CUDA(key_.alloc(M)); SPH_CUDA(slot_.alloc(M)); SPH_CUDA(tmp_.alloc(M));
         SPH_CUDA(count_.alloc(K)); SPH_CUDA(starts_.alloc(K + 1)); SPH_CUDA(bstarts_.alloc(K + 1));
-        SPH_CUDA(tile_sums_.alloc((K + kScanTile - 1) / kScanTile + 1));
+        SPH_CUDA(tile_sums_.alloc((K + kScanThreads * 4 - 1) / (kScanThreads * 4) + 1));
+        SPH_CUDA(cudaFuncSetAttribute(k_pool_build_lists<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      64 * 256 * (int)sizeof(uint32_t)));
         SPH_CUDA(cudaMemsetAsync(count_.p, 0, K * sizeof(uint32_t), st_));
         SPH_CUDA(table_.alloc(d.max_scenes));
         SPH_CUDA(seg_a_.alloc(d.max_scenes)); SPH_CUDA(seg_b_.alloc(d.max_scenes)); SPH_CUDA(seg_n_.alloc(d.max_scenes));
@@ -596,13 +611,204 @@ public:
                 if (rc) return rc;
             }
             if (S_ == 0) return SPH_OK;
-            const int rc = graph_ ? graph_step() : one_step();
+            const int rc = tune_left_ > 0 ? tuning_step() : graph_ ? graph_step() : one_step();
             if (rc) return rc;
         }
         return SPH_OK;
     }
 
     int set_graph(int on) { graph_ = on != 0; return SPH_OK; }
+
+    // ---- autotuner --------------------------------------------------------
+    // Candidates: pair-list build block x queue depth, solver-pass block,
+    // scan width.  Each family's kernels are timed separately (CUDA events)
+    // over 2 x 9 host-driven steps that cycle through the candidates, and the
+    // fastest candidate of each family is kept.  Tuning steps are ordinary
+    // steps of every resident scene: no candidate changes any result.  The
+    // choice is cached per GPU model, particle-count bucket (next power of
+    // two) and list width in a text file (SPH_GB300_TUNE_FILE, default
+    // ~/.cache/sph_gb300_tune.txt) and re-measured only for a new bucket.
+    static constexpr int kBB[3] = {64, 128, 256}, kQD[3] = {32, 48, 64}, kSB[3] = {128, 256, 512},
+                         kSW[3] = {4, 8, 16};
+    static constexpr int kTuneSteps = 18;
+
+    int set_autotune(int mode)
+    {
+        if (mode < 0 || mode > 2) { fail("autotune mode is 0, 1 or 2"); return SPH_ERR_INVALID; }
+        tune_mode_ = mode;
+        tune_bucket_ = 0;  // decide again at the next re-layout
+        if (mode == 0) tune_left_ = 0;
+        dirty_ = dirty_ || (mode != 0 && S_ > 0);
+        return SPH_OK;
+    }
+
+    int set_tuning(const sph_pool_tuning& t)
+    {
+        auto in = [](int v, const int* c) { return v == c[0] || v == c[1] || v == c[2]; };
+        if (!in(t.build_block, kBB) || !in(t.queue_depth, kQD) || !in(t.solver_block, kSB) || !in(t.scan_width, kSW)) {
+            fail("tuning values outside the candidate sets");
+            return SPH_ERR_INVALID;
+        }
+        tune_ = Tune{t.build_block, t.queue_depth, t.solver_block, t.scan_width};
+        tune_source_ = 0;
+        tune_mode_ = 0;
+        tune_left_ = 0;
+        drop_graphs();
+        return SPH_OK;
+    }
+
+    void get_tuning(sph_pool_tuning* t) const
+    {
+        t->build_block = tune_.build_block;
+        t->queue_depth = tune_.queue;
+        t->solver_block = tune_.solver_block;
+        t->scan_width = tune_.scan_per;
+        t->source = tune_source_;
+        t->steps_left = tune_left_;
+    }
+
+    const std::string& tuning_log() const { return tune_log_; }
+
+    static void tune_family(const char* name, int* fam, int* sub)
+    {
+        if (!std::strcmp(name, "k_pool_build_lists")) { *fam = 0; *sub = 0; }
+        else if (!std::strcmp(name, "k_pool_correct")) { *fam = 1; *sub = 0; }
+        else if (!std::strcmp(name, "k_pool_errors_density")) { *fam = 1; *sub = 1; }
+        else if (!std::strcmp(name, "k_pool_errors_div")) { *fam = 1; *sub = 2; }
+        else if (!std::strcmp(name, "k_scan_tiles")) { *fam = 2; *sub = 0; }
+        else if (!std::strcmp(name, "k_scan_add")) { *fam = 2; *sub = 1; }
+    }
+
+    std::string tune_key() const
+    {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceProp prop;
+        std::memset(&prop, 0, sizeof prop);
+        cudaGetDeviceProperties(&prop, dev);
+        char k[320];
+        std::snprintf(k, sizeof k, "%s|sm%d%d|n%llu|k%u", prop.name, prop.major, prop.minor,
+                      (unsigned long long)tune_bucket_, kmax_);
+        std::string out = k;
+        for (auto& ch : out) if (ch == ' ') ch = '_';
+        return out;
+    }
+
+    static std::string tune_path()
+    {
+        const char* e = std::getenv("SPH_GB300_TUNE_FILE");
+        if (e && *e) return e;
+        const char* home = std::getenv("HOME");
+        if (!home || !*home) return "";
+        std::string d = std::string(home) + "/.cache";
+        mkdir(d.c_str(), 0755);
+        return d + "/sph_gb300_tune.txt";
+    }
+
+    bool cache_lookup(const std::string& key, Tune* t) const
+    {
+        const std::string path = tune_path();
+        if (path.empty()) return false;
+        FILE* fp = std::fopen(path.c_str(), "r");
+        if (!fp) return false;
+        char line[512], k[400];
+        int a, b, c, d;
+        bool hit = false;
+        while (std::fgets(line, sizeof line, fp))
+            if (std::sscanf(line, "%399s %d %d %d %d", k, &a, &b, &c, &d) == 5 && key == k) {
+                auto in = [](int v, const int* cs) { return v == cs[0] || v == cs[1] || v == cs[2]; };
+                if (in(a, kBB) && in(b, kQD) && in(c, kSB) && in(d, kSW)) { *t = Tune{a, b, c, d}; hit = true; }
+            }
+        std::fclose(fp);
+        return hit;
+    }
+
+    void cache_store(const std::string& key, const Tune& t) const
+    {
+        const std::string path = tune_path();
+        if (path.empty()) return;
+        FILE* fp = std::fopen(path.c_str(), "a");
+        if (!fp) return;
+        std::fprintf(fp, "%s %d %d %d %d\n", key.c_str(), t.build_block, t.queue, t.solver_block, t.scan_per);
+        std::fclose(fp);
+    }
+
+    // After a re-layout: use the cached choice for this bucket, or measure.
+    void tune_after_relayout()
+    {
+        if (tune_mode_ == 0 || N_ == 0) return;
+        unsigned long long b = 1;
+        while (b < N_) b <<= 1;
+        if (b == tune_bucket_ && tune_mode_ == 1) return;
+        tune_bucket_ = b;
+        Tune t;
+        if (tune_mode_ == 1 && cache_lookup(tune_key(), &t)) {
+            tune_ = t;
+            tune_source_ = 1;
+            return;
+        }
+        std::memset(tacc_ms_, 0, sizeof tacc_ms_);
+        std::memset(tacc_n_, 0, sizeof tacc_n_);
+        tune_left_ = kTuneSteps;
+        tune_step_ = 0;
+    }
+
+    int tuning_step()
+    {
+        const int t = tune_step_++;
+        const int bc = t % 9, sc = t % 3, wc = (t / 3) % 3;
+        cand_[0] = bc; cand_[1] = sc; cand_[2] = wc;
+        tune_ = Tune{kBB[bc / 3], kQD[bc % 3], kSB[sc], kSW[wc]};
+        tuning_ = true;
+        const int rc = one_step();
+        tuning_ = false;
+        SPH_CUDA(cudaStreamSynchronize(st_));
+        for (auto& q : tpending_) {
+            float ms = 0.f;
+            if (rc == SPH_OK) SPH_CUDA(cudaEventElapsedTime(&ms, q.a, q.b));
+            tacc_ms_[q.fam][cand_[q.fam]][q.sub] += ms;
+            tacc_n_[q.fam][cand_[q.fam]][q.sub] += 1;
+            events_.push_back(q.a);
+            events_.push_back(q.b);
+        }
+        tpending_.clear();
+        if (rc) return rc;
+        if (--tune_left_ == 0) finish_tuning();
+        return SPH_OK;
+    }
+
+    void finish_tuning()
+    {
+        const int ncand[3] = {9, 3, 3};
+        int best[3] = {1 * 3 + 2, 0, 1};
+        char line[160];
+        tune_log_.clear();
+        for (int fam = 0; fam < 3; ++fam) {
+            double bestc = 1e300;
+            for (int c = 0; c < ncand[fam]; ++c) {
+                double cost = 0.0;
+                bool any = false;
+                for (int sub = 0; sub < 3; ++sub)
+                    if (tacc_n_[fam][c][sub]) { cost += tacc_ms_[fam][c][sub] / tacc_n_[fam][c][sub]; any = true; }
+                if (!any) continue;
+                if (fam == 0) std::snprintf(line, sizeof line, "build block %d queue %d: %.4f ms\n", kBB[c / 3], kQD[c % 3], cost);
+                else if (fam == 1) std::snprintf(line, sizeof line, "solver block %d: %.4f ms\n", kSB[c], cost);
+                else std::snprintf(line, sizeof line, "scan width %d: %.4f ms\n", kSW[c], cost);
+                tune_log_ += line;
+                if (cost < bestc) { bestc = cost; best[fam] = c; }
+            }
+        }
+        tune_ = Tune{kBB[best[0] / 3], kQD[best[0] % 3], kSB[best[1]], kSW[best[2]]};
+        tune_source_ = 2;
+        if (tune_mode_ == 2) tune_mode_ = 1;
+        cache_store(tune_key(), tune_);
+        drop_graphs();
+    }
+
+    void drop_graphs()
+    {
+        for (auto& e : gexec_) if (e) { cudaGraphExecDestroy(e); e = nullptr; }
+    }
     int set_profiling(int on) { prof_ = on != 0; return SPH_OK; }
 
     // "name launches total_ms" per kernel for the host-driven steps timed
@@ -817,12 +1023,55 @@ private:
 
     int scan(uint32_t* out)
     {
-        const unsigned nt = blocks(K_, kScanTile);
-        run("k_scan_tiles", [&] { k_scan_tiles<<<nt, kScanThreads, 0, ls_>>>(K_, count_.p, out, tile_sums_.p); });
+        const unsigned per = (unsigned)tune_.scan_per;
+        const unsigned nt = blocks(K_, kScanThreads * per);
+        run("k_scan_tiles", [&] {
+            if (per == 4) k_scan_tiles<4><<<nt, kScanThreads, 0, ls_>>>(K_, count_.p, out, tile_sums_.p);
+            else if (per == 16) k_scan_tiles<16><<<nt, kScanThreads, 0, ls_>>>(K_, count_.p, out, tile_sums_.p);
+            else k_scan_tiles<8><<<nt, kScanThreads, 0, ls_>>>(K_, count_.p, out, tile_sums_.p);
+        });
         run("k_scan_tile_sums", [&] { k_scan_tile_sums<<<1, 1024, 0, ls_>>>(nt, tile_sums_.p, out, K_); });
-        run("k_scan_add", [&] { k_scan_add<<<nt, kScanThreads, 0, ls_>>>(K_, tile_sums_.p, out); });
+        run("k_scan_add", [&] {
+            if (per == 4) k_scan_add<4><<<nt, kScanThreads, 0, ls_>>>(K_, tile_sums_.p, out);
+            else if (per == 16) k_scan_add<16><<<nt, kScanThreads, 0, ls_>>>(K_, tile_sums_.p, out);
+            else k_scan_add<8><<<nt, kScanThreads, 0, ls_>>>(K_, tile_sums_.p, out);
+        });
         SPH_CUDA(cudaGetLastError());
         return SPH_OK;
+    }
+
+    // ---- tuned launches ---------------------------------------------------
+    void launch_build(Fluid<float> f, const P4<float>* bp, Lists<float> L)
+    {
+        const int bb = tune_.build_block;
+        const uint32_t qd = (uint32_t)tune_.queue;
+        const size_t smem = (size_t)qd * (size_t)bb * sizeof(uint32_t);
+        const unsigned nb = blocks(N_, (unsigned)bb);
+        if (bb == 64)
+            k_pool_build_lists<64><<<nb, 64, smem, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L, qd);
+        else if (bb == 256)
+            k_pool_build_lists<256><<<nb, 256, smem, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L, qd);
+        else
+            k_pool_build_lists<128><<<nb, 128, smem, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L, qd);
+    }
+    template <int MODE> void launch_correct(Fluid<float> f, const P4<float>* bp, Lists<float> L)
+    {
+        const int sb = tune_.solver_block;
+        const unsigned nb = blocks(N_, (unsigned)sb);
+        if (sb == 256) k_pool_correct<256, MODE><<<nb, 256, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L);
+        else if (sb == 512) k_pool_correct<512, MODE><<<nb, 512, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L);
+        else k_pool_correct<128, MODE><<<nb, 128, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L);
+    }
+    template <bool DIV, bool INITIAL> void launch_errors(Fluid<float> f, const P4<float>* bp, Lists<float> L)
+    {
+        const int sb = tune_.solver_block;
+        const unsigned nb = blocks(N_, (unsigned)sb);
+        if (sb == 256)
+            k_pool_errors<256, DIV, INITIAL><<<nb, 256, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L);
+        else if (sb == 512)
+            k_pool_errors<512, DIV, INITIAL><<<nb, 512, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L);
+        else
+            k_pool_errors<128, DIV, INITIAL><<<nb, 128, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L);
     }
 
     // Launch accounting: kernels of host-driven steps are counted as they
@@ -831,12 +1080,20 @@ private:
     {
         if (capturing_) { ++cap_[loop_ctx_]; fn(); return; }
         if (counting_) ++host_launches_;
-        if (!prof_ || !counting_) { fn(); return; }
+        int fam = -1, sub = 0;
+        if (tuning_) tune_family(name, &fam, &sub);
+        const bool prof = prof_ && counting_;
+        if (fam < 0 && !prof) { fn(); return; }
         cudaEvent_t a = take_event(), b = take_event();
+        cudaEvent_t c = prof && fam >= 0 ? take_event() : nullptr, d = c ? take_event() : nullptr;
         cudaEventRecord(a, ls_);
+        if (c) cudaEventRecord(c, ls_);
         fn();
+        if (d) cudaEventRecord(d, ls_);
         cudaEventRecord(b, ls_);
-        pending_.push_back({name, a, b});
+        if (fam >= 0) tpending_.push_back({fam, sub, a, b});
+        else pending_.push_back({name, a, b});
+        if (c) pending_.push_back({name, c, d});
     }
     cudaEvent_t take_event()
     {
@@ -1006,14 +1263,14 @@ private:
         // recomputation for the kept ones, whose positions have not moved)
         int rc = build_grid(false);
         if (rc) return rc;
-        run("k_pool_build_lists", [&] { k_pool_build_lists<<<blocks(N_, kBlock), kBlock, 0, ls_>>>(F(cur_), bpos_[bcur_].p, sid_.p, table_.p, starts_.p,
-                                                                           bstarts_.p, LS()); });
+        run("k_pool_build_lists", [&] { launch_build(F(cur_), bpos_[bcur_].p, LS()); });
         SPH_CUDA(cudaGetLastError());
         SPH_CUDA(cudaStreamSynchronize(st_));
         counting_ = true;
-        for (auto& e : gexec_) if (e) { cudaGraphExecDestroy(e); e = nullptr; }
+        drop_graphs();
         dirty_ = false;
         graph_period_begin();
+        tune_after_relayout();
         return SPH_OK;
     }
 
@@ -1093,17 +1350,17 @@ private:
             run("k_pool_cfl_accum", [&] { k_pool_cfl_accum<<<nb256, 256, 0, ls_>>>(f, sid_.p, table_.p); });
             run("k_pool_cfl_control", [&] { k_pool_cfl_control<<<1, 256, 0, ls_>>>(table_.p, S_); });
             run("k_pool_predict_v_warm", [&] { k_pool_predict_v_warm<<<nb256, 256, 0, ls_>>>(f, sid_.p, table_.p, L.kbuf); });
-            run("k_pool_correct", [&] { k_pool_correct<0><<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
+            run("k_pool_correct", [&] { launch_correct<0>(f, bp, L); });
             SPH_CUDA(cudaGetLastError());
             int rc = solve_loop(
                 1,
                 [&](cudaGraphConditionalHandle h) {
-                    run("k_pool_errors_density", [&] { k_pool_errors<false, true><<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
+                    run("k_pool_errors_density", [&] { launch_errors<false, true>(f, bp, L); });
                     run("k_pool_control", [&] { k_pool_control<0><<<1, 256, 0, ls_>>>(table_.p, S_, pc_.p, h); });
                 },
                 [&](cudaGraphConditionalHandle h) {
-                    run("k_pool_correct", [&] { k_pool_correct<1><<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
-                    run("k_pool_errors_density", [&] { k_pool_errors<false, false><<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
+                    run("k_pool_correct", [&] { launch_correct<1>(f, bp, L); });
+                    run("k_pool_errors_density", [&] { launch_errors<false, false>(f, bp, L); });
                     run("k_pool_control", [&] { k_pool_control<1><<<1, 256, 0, ls_>>>(table_.p, S_, pc_.p, h); });
                 });
             if (rc) return rc;
@@ -1114,17 +1371,17 @@ private:
             Fluid<float> f = F(cur_);
             const P4<float>* bp = bpos_[bcur_].p;
             Lists<float> L = LS();
-            run("k_pool_build_lists", [&] { k_pool_build_lists<<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
+            run("k_pool_build_lists", [&] { launch_build(f, bp, L); });
             SPH_CUDA(cudaGetLastError());
             rc = solve_loop(
                 2,
                 [&](cudaGraphConditionalHandle h) {
-                    run("k_pool_errors_div", [&] { k_pool_errors<true, true><<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
+                    run("k_pool_errors_div", [&] { launch_errors<true, true>(f, bp, L); });
                     run("k_pool_control", [&] { k_pool_control<2><<<1, 256, 0, ls_>>>(table_.p, S_, pc_.p, h); });
                 },
                 [&](cudaGraphConditionalHandle h) {
-                    run("k_pool_correct", [&] { k_pool_correct<2><<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
-                    run("k_pool_errors_div", [&] { k_pool_errors<true, false><<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L); });
+                    run("k_pool_correct", [&] { launch_correct<2>(f, bp, L); });
+                    run("k_pool_errors_div", [&] { launch_errors<true, false>(f, bp, L); });
                     run("k_pool_control", [&] { k_pool_control<3><<<1, 256, 0, ls_>>>(table_.p, S_, pc_.p, h); });
                 });
             if (rc) return rc;
@@ -1206,7 +1463,16 @@ private:
     unsigned cap_[3] = {0, 0, 0};
     unsigned long long fixed_ = 0, body_d_size_ = 0, body_v_size_ = 0, gsteps_ = 0, snap_d_ = 0, snap_v_ = 0;
     unsigned long long host_launches_ = 0, graph_launches_ = 0, host_body_d_ = 0, host_body_v_ = 0;
-    bool counting_ = true, any_forces_ = false, prof_ = false;
+    bool counting_ = true, any_forces_ = false, prof_ = false, tuning_ = false;
+    Tune tune_;
+    int tune_mode_ = 1, tune_source_ = 0, tune_left_ = 0, tune_step_ = 0;
+    unsigned long long tune_bucket_ = 0;
+    int cand_[3] = {0, 0, 0};
+    double tacc_ms_[3][9][3];
+    unsigned tacc_n_[3][9][3];
+    std::string tune_log_;
+    struct TTimed { int fam, sub; cudaEvent_t a, b; };
+    std::vector<TTimed> tpending_;
     struct Timed { const char* name; cudaEvent_t a, b; };
     std::vector<Timed> pending_;
     std::vector<cudaEvent_t> events_;
@@ -1364,6 +1630,36 @@ int sph_pool_get_profile(sph_pool* p, char* buf, unsigned long long len)
 {
     if (!p) return SPH_ERR_INVALID;
     return p->pool.profile(buf, (size_t)len);
+}
+
+int sph_pool_set_autotune(sph_pool* p, int mode)
+{
+    if (!p) return SPH_ERR_INVALID;
+    return p->pool.set_autotune(mode);
+}
+
+int sph_pool_get_tuning(sph_pool* p, sph_pool_tuning* out)
+{
+    if (!p || !out) return pool_bad(p, "invalid argument");
+    p->pool.get_tuning(out);
+    return SPH_OK;
+}
+
+int sph_pool_set_tuning(sph_pool* p, const sph_pool_tuning* t)
+{
+    if (!p || !t) return pool_bad(p, "invalid argument");
+    return p->pool.set_tuning(*t);
+}
+
+int sph_pool_get_tuning_log(sph_pool* p, char* buf, unsigned long long len)
+{
+    if (!p) return SPH_ERR_INVALID;
+    const std::string& s = p->pool.tuning_log();
+    if (buf && len) {
+        std::strncpy(buf, s.c_str(), (size_t)len - 1);
+        buf[len - 1] = 0;
+    }
+    return (int)s.size();
 }
 
 int sph_pool_list_pairs(sph_pool* p, unsigned long long* pairs, unsigned* overflow)

@@ -140,3 +140,45 @@ def test_timed_profiled_steps_and_list_stats(gpu_lib):
     assert 10 * n < pairs < 64 * n and overflow == 0
     out = np.empty((A[0].shape[0], 3))
     assert P1.get(ids1[0], "v", out=out) is out
+
+
+def test_autotuned_shapes_do_not_change_results(gpu_lib, tmp_path, monkeypatch):
+    """The tuner's measurement steps are ordinary steps; any launch shape it
+    may pick gives bit-identical results."""
+    monkeypatch.setenv("SPH_GB300_TUNE_FILE", str(tmp_path / "tune.txt"))
+    scenes = [A] + OTHERS
+
+    def run(tuning=None, mode=0, steps=22):
+        P = sph_gb300.Pool(max_particles=200_000, max_boundary=400_000, max_keys=4_000_000, max_scenes=64)
+        P.set_autotune(mode)
+        if tuning:
+            P.set_tuning(**tuning)
+        ids = [P.add_scene(x, boundary_points=b, steps=1000, **p) for x, b, p in scenes]
+        P.set_graph(True)
+        P.step(steps)
+        P.synchronize()
+        return P, ids
+
+    ref, rids = run()
+    variants = [dict(build_block=64, queue_depth=32, solver_block=512, scan_width=16),
+                dict(build_block=256, queue_depth=48, solver_block=256, scan_width=4)]
+    for t in variants:
+        P, ids = run(tuning=t)
+        assert P.tuning()["build_block"] == t["build_block"]
+        for a, b in zip(rids, ids):
+            for f in ("x", "v", "rho"):
+                assert np.array_equal(ref.get(a, f), P.get(b, f)), (t, f)
+    P, ids = run(mode=2)
+    tu = P.tuning()
+    assert tu["source"] == 2 and tu["steps_left"] == 0
+    assert "build block" in P.tuning_log() and "solver block" in P.tuning_log()
+    for a, b in zip(rids, ids):
+        assert np.array_equal(ref.get(a, "x"), P.get(b, "x"))
+    # a second pool of the same size takes the cached shapes without measuring
+    Q, _ = run(mode=1, steps=1)
+    q = Q.tuning()
+    assert q["source"] == 1 and q["steps_left"] == 0
+    assert (q["build_block"], q["queue_depth"], q["solver_block"], q["scan_width"]) == (
+        tu["build_block"], tu["queue_depth"], tu["solver_block"], tu["scan_width"])
+    with pytest.raises(sph_gb300.SPHError):
+        Q.set_tuning(build_block=96)
