@@ -10,7 +10,7 @@ Workloads (seeded, synthetic; sph_gb300/workloads.py):
                    0.05-0.2 m in a 1 m Akinci box, r = 0.01 m, CFL-adaptive
                    dt in [1e-5, 5e-3] s, 0.1 % density / 0.1 %/s divergence
                    error, FP32 bulk with FP64 reductions.  Every scene runs
-                   the autotuner's measuring steps (18, ordinary steps that
+                   the autotuner's measuring steps (24, ordinary steps that
                    pick the launch shapes), W warm-up and K timed steps
                    (about 500 at the defaults).
   dam_break_125k   one 50^3 = 125,000-particle dam break at r = 0.005 m in a
@@ -67,7 +67,7 @@ METRIC = "DFSPH particle-steps/s @0.1% density err, served vs plain GPU; p50/p99
 UNIT = "particle-steps/s"
 WORKLOAD = "batched_mix_256"
 CPU_SAMPLE_SCENES = 16
-TUNE_STEPS = 19  # at most: the autotuner's 18 measuring steps + the admitting step
+TUNE_STEPS = 25  # at most: the autotuner's 24 measuring steps + the admitting step
 
 # Algorithmic bytes of each kernel: the compulsory field traffic per fluid
 # particle of the reference's pass it implements (FP32 SoA: float4 = 16 B,
@@ -283,7 +283,12 @@ def run_batched(scenes, args, world, local):
 
     W, K, P = args.warmup, args.steps, args.profile_steps
     pool = make_pool(scenes, args.list_max)
-    pool.set_autotune(2)  # measure launch shapes on this mix (cached afterwards)
+    if args.tuning:
+        b, bo, q, sb, so, w = (int(t) for t in args.tuning.split(","))
+        pool.set_tuning(build_block=b, build_occupancy=bo, queue_depth=q, solver_block=sb, solver_occupancy=so,
+                        scan_width=w)
+    else:
+        pool.set_autotune(2)  # measure launch shapes on this mix (cached afterwards)
     ids = [pool.add_scene(x, boundary_points=b, steps=TUNE_STEPS + W + K + P, **params) for x, b, params, _ in scenes]
     n = sum(s[0].shape[0] for s in scenes)
     nb = sum(s[1].shape[0] for s in scenes)
@@ -481,6 +486,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--list-max", type=int, default=64, help="pair-list slots per particle")
+    ap.add_argument("--tuning", default="", help="fixed launch shapes: build block,build occupancy,queue,solver block,"
+                                                 "solver occupancy,scan width (skips the autotuner)")
     ap.add_argument("--scenes", type=int, default=256, help="first N scenes of the mix (256: the full workload)")
     ap.add_argument("--profile-steps", type=int, default=10, help="host-driven steps timed per kernel")
     ap.add_argument("--plain-steps", type=int, default=0, help="timed steps per scene for the plain arm (0: --steps)")
@@ -491,6 +498,7 @@ def main():
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-dam", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=25.0, help="seconds of CPU baseline work")
     ap.add_argument("--ref-budget", type=float, default=90.0, help="seconds of reference-arm timed work")
@@ -519,7 +527,7 @@ def main():
     roof["timing"] = f"CUDA events around each launch, {args.profile_steps} host-driven pool steps"
 
     plain = None if args.no_plain else run_plain(scenes, args)
-    dam = run_dam_break(args)
+    dam = None if args.no_dam else run_dam_break(args)
     e2e = None if args.no_e2e else run_e2e(scenes, args)
     if e2e is not None:
         e2e["value"] = world * e2e["value"] * e2e["wall_s"] / dist_max(e2e["wall_s"], world)

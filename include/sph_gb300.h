@@ -260,17 +260,19 @@ int sph_pool_set_profiling(sph_pool* pool, int enable);
 int sph_pool_get_profile(sph_pool* pool, char* buf, unsigned long long len);
 /* Launch shapes of the pool's hot kernels.  Results do not depend on them. */
 typedef struct sph_pool_tuning {
-    int build_block;  /* threads per block of the pair-list build: 64, 128 or 256 */
-    int queue_depth;  /* candidates staged per particle in shared memory by the build: 32, 48 or 64 */
-    int solver_block; /* threads per block of the solver passes: 128, 256 or 512 */
-    int scan_width;   /* grid keys per thread of the cell-count scan (sort width): 4, 8 or 16 */
-    int source;       /* 0 defaults or set by the caller, 1 tuning cache, 2 measured */
-    int steps_left;   /* tuning steps still to run (read only) */
+    int build_block;      /* pair-list build: threads per block and threads per SM */
+    int build_occupancy;  /* the register budget allows: (128, 896), (128, 1024), (256, 768), (256, 1024) */
+    int queue_depth;      /* candidates staged per particle in shared memory by the build: 8..64, multiple of 8 */
+    int solver_block;     /* solver passes: threads per block (128 or 256) and threads per SM */
+    int solver_occupancy; /* the register budget allows (1024, 1536 or 2048) */
+    int scan_width;       /* grid keys per thread of the cell-count scan (sort width): 4, 8 or 16 */
+    int source;           /* 0 defaults or set by the caller, 1 tuning cache, 2 measured */
+    int steps_left;       /* tuning steps still to run (read only) */
 } sph_pool_tuning;
 /* Autotuner (no reference counterpart): mode 0 off (keep the current
  * shapes), 1 (default) after each re-layout use the cached shapes for this
  * GPU model / particle-count bucket / list width or measure them over the
- * next 18 steps (ordinary steps of every resident scene, host-driven), 2 as 1
+ * next 24 steps (ordinary steps of every resident scene, host-driven), 2 as 1
  * but measure again.  The cache is a text file (SPH_GB300_TUNE_FILE, default
  * ~/.cache/sph_gb300_tune.txt). */
 int sph_pool_set_autotune(sph_pool* pool, int mode);

@@ -109,8 +109,10 @@ class PoolDesc(ctypes.Structure):
 class PoolTuning(ctypes.Structure):
     _fields_ = [
         ("build_block", ctypes.c_int),
+        ("build_occupancy", ctypes.c_int),
         ("queue_depth", ctypes.c_int),
         ("solver_block", ctypes.c_int),
+        ("solver_occupancy", ctypes.c_int),
         ("scan_width", ctypes.c_int),
         ("source", ctypes.c_int),
         ("steps_left", ctypes.c_int),
@@ -558,8 +560,9 @@ class Pool:
         self._check(lib().sph_pool_get_tuning(self._h, ctypes.byref(t)), "sph_pool_get_tuning")
         return {name: getattr(t, name) for name, _ in PoolTuning._fields_}
 
-    def set_tuning(self, build_block=128, queue_depth=64, solver_block=128, scan_width=8):
-        t = PoolTuning(build_block, queue_depth, solver_block, scan_width, 0, 0)
+    def set_tuning(self, build_block=256, build_occupancy=768, queue_depth=48, solver_block=128, solver_occupancy=1024,
+                   scan_width=16):
+        t = PoolTuning(build_block, build_occupancy, queue_depth, solver_block, solver_occupancy, scan_width, 0, 0)
         self._check(lib().sph_pool_set_tuning(self._h, ctypes.byref(t)), "sph_pool_set_tuning")
 
     def tuning_log(self):

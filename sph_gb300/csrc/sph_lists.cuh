@@ -61,6 +61,44 @@ __device__ __forceinline__ V3<R> pair_vec(V3<R> xi, uint32_t ci, const P4<R>& pj
 
 // Per-particle body shared by the single-scene and the pool kernels; q is
 // the block's shared queue (kQueue x kBlock).
+template <typename R> struct BuildSums {
+    R density, sumSq;
+    V3<R> sumGrad;
+    uint32_t cnt;
+};
+
+// Particles whose candidates overflow the shared queue: the whole
+// evaluation inside the walk.  Out of line, so the common path's register
+// allocation does not carry it.
+template <typename R>
+__device__ __noinline__ BuildSums<R> build_walk_all(uint32_t i, const Fluid<R>& f, const GridView& g,
+                                                    const uint32_t* __restrict__ cs, const Consts<R>& c, const Lists<R>& L,
+                                                    V3<R> xi, uint32_t pc)
+{
+    const uint32_t n = f.n;
+    BuildSums<R> b{0, 0, {0, 0, 0}, 0};
+    walk<R, 1>(g, cs, pc, xi, c.h, 0, [&](uint32_t j, V3<R> s) {
+        const V3<R> r = s - xyz(ldg4(f.pos + j));
+        const R r2 = dot3(r, r);
+        if (!(r2 <= c.cull2)) return;
+        b.density += c.mass * cubic_W(c, sqrt(r2));
+        const V3<R> mg = c.mass * cubic_gradW(c, r, r2);
+        const R mg2 = dot3(mg, mg);
+        if (mg2 > (R)0) {
+            b.sumGrad = b.sumGrad + mg;
+            if constexpr (sizeof(R) == 8) {
+                const R m = sqrt(mg2);
+                b.sumSq += m * m;
+            } else {
+                b.sumSq += mg2;
+            }
+            if (b.cnt < L.kmax) L.pairs[(size_t)b.cnt * n + i] = P4<R>{mg.x, mg.y, mg.z, idx_as(R(0), j)};
+            ++b.cnt;
+        }
+    });
+    return b;
+}
+
 template <typename R>
 __device__ __forceinline__ void build_lists_one(uint32_t i, const Fluid<R>& f, const P4<R>* __restrict__ bpos,
                                                 const GridView& g, const uint32_t* __restrict__ cs,
@@ -108,11 +146,11 @@ __device__ __forceinline__ void build_lists_one(uint32_t i, const Fluid<R>& f, c
             accept(j, r, dot3(r, r));
         }
     } else {
-        walk<R, 1>(g, cs, pc, xi, c.h, 0, [&](uint32_t j, V3<R> s) {
-            const V3<R> r = s - xyz(ldg4(f.pos + j));
-            const R r2 = dot3(r, r);
-            if (r2 <= c.cull2) accept(j, r, r2);
-        });
+        const BuildSums<R> b = build_walk_all(i, f, g, cs, c, L, xi, pc);
+        density = b.density;
+        sumSq = b.sumSq;
+        sumGrad = b.sumGrad;
+        cnt = b.cnt;
     }
     V3<R> bg = {0, 0, 0};
     if (akinci)
@@ -153,7 +191,7 @@ __global__ void __launch_bounds__(kBlock, 7) k_build_lists(Fluid<R> f, const P4<
 // ---- cell-walk fallbacks for particles whose list overflowed -------------
 
 template <typename R, int MODE>
-__device__ V3<R> correct_sum_cells(const Fluid<R>& f, const P4<R>* __restrict__ bpos, const GridView& g,
+__device__ __noinline__ V3<R> correct_sum_cells(const Fluid<R>& f, const P4<R>* __restrict__ bpos, const GridView& g,
                                    const uint32_t* __restrict__ cs, const uint32_t* __restrict__ bs, const Consts<R>& c,
                                    int akinci, uint32_t i, R ki, const R* __restrict__ kbuf)
 {
@@ -178,10 +216,15 @@ __device__ V3<R> correct_sum_cells(const Fluid<R>& f, const P4<R>* __restrict__ 
     return sum;
 }
 
+template <typename R> struct DivSum {
+    R dv;
+    uint32_t nn;
+};
+
 template <typename R>
-__device__ R velocity_div_cells(const Fluid<R>& f, const P4<R>* __restrict__ bpos, const GridView& g,
-                                const uint32_t* __restrict__ cs, const uint32_t* __restrict__ bs, const Consts<R>& c,
-                                int akinci, uint32_t i, V3<R> vi, uint32_t* nn)
+__device__ __noinline__ DivSum<R> velocity_div_cells(const Fluid<R>& f, const P4<R>* __restrict__ bpos, const GridView& g,
+                                                     const uint32_t* __restrict__ cs, const uint32_t* __restrict__ bs,
+                                                     const Consts<R>& c, int akinci, uint32_t i, V3<R> vi)
 {
     R dv = 0;
     unsigned cnt = 0;
@@ -203,8 +246,7 @@ __device__ R velocity_div_cells(const Fluid<R>& f, const P4<R>* __restrict__ bpo
             const R r2 = dot3(r, r);
             if (r2 <= c.cull2) dv += pb.w * dot3(vi, cubic_gradW(c, r, r2));
         });
-    *nn = cnt;
-    return dv;
+    return DivSum<R>{dv, cnt};
 }
 
 // ---- list walks ------------------------------------------------------------
@@ -295,7 +337,9 @@ __device__ __forceinline__ R velocity_div_one(uint32_t i, const Fluid<R>& f, con
         *nn = cnt;
         return velocity_div_list(f, L, i, vi, akinci);
     }
-    return velocity_div_cells(f, bpos, g, cs, bs, c, akinci, i, vi, nn);
+    const DivSum<R> d = velocity_div_cells(f, bpos, g, cs, bs, c, akinci, i, vi);
+    *nn = d.nn;
+    return d.dv;
 }
 
 // DFSPHSolver::predictDensities over the lists (+ loop control, as

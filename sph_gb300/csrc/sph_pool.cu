@@ -200,13 +200,13 @@ __global__ void k_pool_psi(uint32_t N, Boundary<float> b, const uint32_t* __rest
     b.pos[i].w = c.density0 * psi;
 }
 
-// Pair-list build (k_build_lists per scene).  BLOCK threads per block and a
-// shared candidate queue of qdepth entries per thread (dynamic shared
-// memory, qdepth * BLOCK * 4 bytes): both tuning parameters; the lists do not
-// depend on them (queued and re-walked candidates are accepted in the same
-// walk order).
-template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK, 896 / BLOCK) k_pool_build_lists(Fluid<float> f, const P4<float>* __restrict__ bpos,
+// Pair-list build (k_build_lists per scene).  BLOCK threads per block, a
+// register budget for MINB resident blocks per SM, and a shared candidate
+// queue of qdepth entries per thread (dynamic shared memory, qdepth * BLOCK
+// * 4 bytes) are tuning parameters; the lists do not depend on them (queued
+// and re-walked candidates are accepted in the same walk order).
+template <int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) k_pool_build_lists(Fluid<float> f, const P4<float>* __restrict__ bpos,
                                                                          const uint32_t* __restrict__ sid, const PoolScene* T,
                                                                          const uint32_t* __restrict__ cs,
                                                                          const uint32_t* __restrict__ bs, Lists<float> L,
@@ -343,8 +343,8 @@ __global__ void k_pool_predict_v_warm(Fluid<float> f, const uint32_t* __restrict
     f.kappa[i] = 0.f;
 }
 
-template <int BLOCK, int MODE>
-__global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) k_pool_correct(Fluid<float> f, const P4<float>* __restrict__ bpos,
+template <int BLOCK, int MINB, int MODE>
+__global__ void __launch_bounds__(BLOCK, MINB) k_pool_correct(Fluid<float> f, const P4<float>* __restrict__ bpos,
                                                             const uint32_t* __restrict__ sid, const PoolScene* T,
                                                             const uint32_t* __restrict__ cs, const uint32_t* __restrict__ bs,
                                                             Lists<float> L)
@@ -360,8 +360,8 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) k_pool_correct(Fluid<floa
 
 // DIV = false: DFSPHSolver::predictDensities; DIV = true:
 // DFSPHSolver::computeDivergenceError.  Adds each scene's error sum.
-template <int BLOCK, bool DIV, bool INITIAL>
-__global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) k_pool_errors(Fluid<float> f, const P4<float>* __restrict__ bpos,
+template <int BLOCK, int MINB, bool DIV, bool INITIAL>
+__global__ void __launch_bounds__(BLOCK, MINB) k_pool_errors(Fluid<float> f, const P4<float>* __restrict__ bpos,
                                                            const uint32_t* __restrict__ sid, PoolScene* T,
                                                            const uint32_t* __restrict__ cs, const uint32_t* __restrict__ bs,
                                                            Lists<float> L)
@@ -490,7 +490,7 @@ struct PoolEntry {
 
 class Pool {
 public:
-    struct Tune { int build_block = 128, queue = 64, solver_block = 128, scan_per = 8; };
+    struct Tune { int build_block = 256, build_occ = 768, queue = 48, solver_block = 128, solver_occ = 1024, scan_per = 16; };
     std::string err;
 
     ~Pool()
@@ -534,7 +534,9 @@ public:
         SPH_CUDA(key_.alloc(M)); SPH_CUDA(slot_.alloc(M)); SPH_CUDA(tmp_.alloc(M));
         SPH_CUDA(count_.alloc(K)); SPH_CUDA(starts_.alloc(K + 1)); SPH_CUDA(bstarts_.alloc(K + 1));
         SPH_CUDA(tile_sums_.alloc((K + kScanThreads * 4 - 1) / (kScanThreads * 4) + 1));
-        SPH_CUDA(cudaFuncSetAttribute(k_pool_build_lists<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        SPH_CUDA(cudaFuncSetAttribute(k_pool_build_lists<256, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      64 * 256 * (int)sizeof(uint32_t)));
+        SPH_CUDA(cudaFuncSetAttribute(k_pool_build_lists<256, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       64 * 256 * (int)sizeof(uint32_t)));
         SPH_CUDA(cudaMemsetAsync(count_.p, 0, K * sizeof(uint32_t), st_));
         SPH_CUDA(table_.alloc(d.max_scenes));
@@ -620,17 +622,36 @@ public:
     int set_graph(int on) { graph_ = on != 0; return SPH_OK; }
 
     // ---- autotuner --------------------------------------------------------
-    // Candidates: pair-list build block x queue depth, solver-pass block,
-    // scan width.  Each family's kernels are timed separately (CUDA events)
-    // over 2 x 9 host-driven steps that cycle through the candidates, and the
-    // fastest candidate of each family is kept.  Tuning steps are ordinary
-    // steps of every resident scene: no candidate changes any result.  The
-    // choice is cached per GPU model, particle-count bucket (next power of
-    // two) and list width in a text file (SPH_GB300_TUNE_FILE, default
+    // Candidates: pair-list build shape (block, register budget) x queue
+    // depth, solver-pass shape (block, register budget), scan width.  Each
+    // family's kernels are timed separately (CUDA events) over 2 x 12
+    // host-driven steps that cycle through the candidates, and the fastest
+    // candidate of each family is kept.  Tuning steps are ordinary steps of
+    // every resident scene: no candidate changes any result.  The choice is
+    // cached per GPU model, particle-count bucket (next power of two) and list
+    // width in a text file (SPH_GB300_TUNE_FILE, default
     // ~/.cache/sph_gb300_tune.txt) and re-measured only for a new bucket.
-    static constexpr int kBB[3] = {64, 128, 256}, kQD[3] = {32, 48, 64}, kSB[3] = {128, 256, 512},
-                         kSW[3] = {4, 8, 16};
-    static constexpr int kTuneSteps = 18;
+    struct Shape { int block, occ; };
+    static constexpr Shape kBuild[4] = {{128, 896}, {128, 1024}, {256, 768}, {256, 1024}};
+    static constexpr int kQD[3] = {40, 48, 56};
+    static constexpr Shape kSolver[6] = {{128, 1024}, {128, 1536}, {128, 2048}, {256, 1024}, {256, 1536}, {256, 2048}};
+    static constexpr int kSW[3] = {4, 8, 16};
+    static constexpr int kNBuild = 12, kNSolver = 6, kNScan = 3;
+    static constexpr int kTuneSteps = 2 * kNBuild;
+
+    static bool valid(const Tune& t)
+    {
+        bool b = false, s = false;
+        for (const Shape& q : kBuild) b |= q.block == t.build_block && q.occ == t.build_occ;
+        for (const Shape& q : kSolver) s |= q.block == t.solver_block && q.occ == t.solver_occ;
+        const bool qd = t.queue >= 8 && t.queue <= 64 && t.queue % 8 == 0;
+        const bool w = t.scan_per == 4 || t.scan_per == 8 || t.scan_per == 16;
+        return b && s && qd && w;
+    }
+    static Tune candidate(int bc, int sc, int wc)
+    {
+        return Tune{kBuild[bc / 3].block, kBuild[bc / 3].occ, kQD[bc % 3], kSolver[sc].block, kSolver[sc].occ, kSW[wc]};
+    }
 
     int set_autotune(int mode)
     {
@@ -644,12 +665,12 @@ public:
 
     int set_tuning(const sph_pool_tuning& t)
     {
-        auto in = [](int v, const int* c) { return v == c[0] || v == c[1] || v == c[2]; };
-        if (!in(t.build_block, kBB) || !in(t.queue_depth, kQD) || !in(t.solver_block, kSB) || !in(t.scan_width, kSW)) {
-            fail("tuning values outside the candidate sets");
+        const Tune v{t.build_block, t.build_occupancy, t.queue_depth, t.solver_block, t.solver_occupancy, t.scan_width};
+        if (!valid(v)) {
+            fail("tuning values outside the supported shapes");
             return SPH_ERR_INVALID;
         }
-        tune_ = Tune{t.build_block, t.queue_depth, t.solver_block, t.scan_width};
+        tune_ = v;
         tune_source_ = 0;
         tune_mode_ = 0;
         tune_left_ = 0;
@@ -660,8 +681,10 @@ public:
     void get_tuning(sph_pool_tuning* t) const
     {
         t->build_block = tune_.build_block;
+        t->build_occupancy = tune_.build_occ;
         t->queue_depth = tune_.queue;
         t->solver_block = tune_.solver_block;
+        t->solver_occupancy = tune_.solver_occ;
         t->scan_width = tune_.scan_per;
         t->source = tune_source_;
         t->steps_left = tune_left_;
@@ -712,12 +735,13 @@ public:
         FILE* fp = std::fopen(path.c_str(), "r");
         if (!fp) return false;
         char line[512], k[400];
-        int a, b, c, d;
+        Tune v;
         bool hit = false;
         while (std::fgets(line, sizeof line, fp))
-            if (std::sscanf(line, "%399s %d %d %d %d", k, &a, &b, &c, &d) == 5 && key == k) {
-                auto in = [](int v, const int* cs) { return v == cs[0] || v == cs[1] || v == cs[2]; };
-                if (in(a, kBB) && in(b, kQD) && in(c, kSB) && in(d, kSW)) { *t = Tune{a, b, c, d}; hit = true; }
+            if (std::sscanf(line, "%399s %d %d %d %d %d %d", k, &v.build_block, &v.build_occ, &v.queue, &v.solver_block,
+                            &v.solver_occ, &v.scan_per) == 7 && key == k && valid(v)) {
+                *t = v;
+                hit = true;
             }
         std::fclose(fp);
         return hit;
@@ -729,7 +753,8 @@ public:
         if (path.empty()) return;
         FILE* fp = std::fopen(path.c_str(), "a");
         if (!fp) return;
-        std::fprintf(fp, "%s %d %d %d %d\n", key.c_str(), t.build_block, t.queue, t.solver_block, t.scan_per);
+        std::fprintf(fp, "%s %d %d %d %d %d %d\n", key.c_str(), t.build_block, t.build_occ, t.queue, t.solver_block,
+                     t.solver_occ, t.scan_per);
         std::fclose(fp);
     }
 
@@ -756,9 +781,9 @@ public:
     int tuning_step()
     {
         const int t = tune_step_++;
-        const int bc = t % 9, sc = t % 3, wc = (t / 3) % 3;
+        const int bc = t % kNBuild, sc = t % kNSolver, wc = (t / kNSolver) % kNScan;
         cand_[0] = bc; cand_[1] = sc; cand_[2] = wc;
-        tune_ = Tune{kBB[bc / 3], kQD[bc % 3], kSB[sc], kSW[wc]};
+        tune_ = candidate(bc, sc, wc);
         tuning_ = true;
         const int rc = one_step();
         tuning_ = false;
@@ -779,8 +804,8 @@ public:
 
     void finish_tuning()
     {
-        const int ncand[3] = {9, 3, 3};
-        int best[3] = {1 * 3 + 2, 0, 1};
+        const int ncand[3] = {kNBuild, kNSolver, kNScan};
+        int best[3] = {2 * 3 + 1, 0, 2};
         char line[160];
         tune_log_.clear();
         for (int fam = 0; fam < 3; ++fam) {
@@ -791,14 +816,19 @@ public:
                 for (int sub = 0; sub < 3; ++sub)
                     if (tacc_n_[fam][c][sub]) { cost += tacc_ms_[fam][c][sub] / tacc_n_[fam][c][sub]; any = true; }
                 if (!any) continue;
-                if (fam == 0) std::snprintf(line, sizeof line, "build block %d queue %d: %.4f ms\n", kBB[c / 3], kQD[c % 3], cost);
-                else if (fam == 1) std::snprintf(line, sizeof line, "solver block %d: %.4f ms\n", kSB[c], cost);
-                else std::snprintf(line, sizeof line, "scan width %d: %.4f ms\n", kSW[c], cost);
+                if (fam == 0)
+                    std::snprintf(line, sizeof line, "build block %d occupancy %d queue %d: %.4f ms\n", kBuild[c / 3].block,
+                                  kBuild[c / 3].occ, kQD[c % 3], cost);
+                else if (fam == 1)
+                    std::snprintf(line, sizeof line, "solver block %d occupancy %d: %.4f ms\n", kSolver[c].block,
+                                  kSolver[c].occ, cost);
+                else
+                    std::snprintf(line, sizeof line, "scan width %d: %.4f ms\n", kSW[c], cost);
                 tune_log_ += line;
                 if (cost < bestc) { bestc = cost; best[fam] = c; }
             }
         }
-        tune_ = Tune{kBB[best[0] / 3], kQD[best[0] % 3], kSB[best[1]], kSW[best[2]]};
+        tune_ = candidate(best[0], best[1], best[2]);
         tune_source_ = 2;
         if (tune_mode_ == 2) tune_mode_ = 1;
         cache_store(tune_key(), tune_);
@@ -1041,37 +1071,37 @@ private:
     }
 
     // ---- tuned launches ---------------------------------------------------
+    // Shapes: (threads per block, threads per SM the register budget allows).
     void launch_build(Fluid<float> f, const P4<float>* bp, Lists<float> L)
     {
-        const int bb = tune_.build_block;
+        const int bb = tune_.build_block, bo = tune_.build_occ;
         const uint32_t qd = (uint32_t)tune_.queue;
         const size_t smem = (size_t)qd * (size_t)bb * sizeof(uint32_t);
-        const unsigned nb = blocks(N_, (unsigned)bb);
-        if (bb == 64)
-            k_pool_build_lists<64><<<nb, 64, smem, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L, qd);
-        else if (bb == 256)
-            k_pool_build_lists<256><<<nb, 256, smem, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L, qd);
-        else
-            k_pool_build_lists<128><<<nb, 128, smem, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L, qd);
+#define SPH_BUILD(BL, MB) \
+    k_pool_build_lists<BL, MB><<<blocks(N_, BL), BL, smem, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L, qd)
+        if (bb == 128 && bo == 896) SPH_BUILD(128, 7);
+        else if (bb == 128) SPH_BUILD(128, 8);
+        else if (bo == 1024) SPH_BUILD(256, 4);
+        else SPH_BUILD(256, 3);
+#undef SPH_BUILD
     }
     template <int MODE> void launch_correct(Fluid<float> f, const P4<float>* bp, Lists<float> L)
     {
-        const int sb = tune_.solver_block;
-        const unsigned nb = blocks(N_, (unsigned)sb);
-        if (sb == 256) k_pool_correct<256, MODE><<<nb, 256, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L);
-        else if (sb == 512) k_pool_correct<512, MODE><<<nb, 512, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L);
-        else k_pool_correct<128, MODE><<<nb, 128, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L);
+        const int sb = tune_.solver_block, so = tune_.solver_occ;
+#define SPH_CORR(BL, MB) \
+    k_pool_correct<BL, MB, MODE><<<blocks(N_, BL), BL, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L)
+        if (sb == 128) { if (so == 1536) SPH_CORR(128, 12); else if (so == 2048) SPH_CORR(128, 16); else SPH_CORR(128, 8); }
+        else { if (so == 1536) SPH_CORR(256, 6); else if (so == 2048) SPH_CORR(256, 8); else SPH_CORR(256, 4); }
+#undef SPH_CORR
     }
     template <bool DIV, bool INITIAL> void launch_errors(Fluid<float> f, const P4<float>* bp, Lists<float> L)
     {
-        const int sb = tune_.solver_block;
-        const unsigned nb = blocks(N_, (unsigned)sb);
-        if (sb == 256)
-            k_pool_errors<256, DIV, INITIAL><<<nb, 256, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L);
-        else if (sb == 512)
-            k_pool_errors<512, DIV, INITIAL><<<nb, 512, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L);
-        else
-            k_pool_errors<128, DIV, INITIAL><<<nb, 128, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L);
+        const int sb = tune_.solver_block, so = tune_.solver_occ;
+#define SPH_ERRS(BL, MB) \
+    k_pool_errors<BL, MB, DIV, INITIAL><<<blocks(N_, BL), BL, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L)
+        if (sb == 128) { if (so == 1536) SPH_ERRS(128, 12); else if (so == 2048) SPH_ERRS(128, 16); else SPH_ERRS(128, 8); }
+        else { if (so == 1536) SPH_ERRS(256, 6); else if (so == 2048) SPH_ERRS(256, 8); else SPH_ERRS(256, 4); }
+#undef SPH_ERRS
     }
 
     // Launch accounting: kernels of host-driven steps are counted as they
@@ -1468,8 +1498,8 @@ private:
     int tune_mode_ = 1, tune_source_ = 0, tune_left_ = 0, tune_step_ = 0;
     unsigned long long tune_bucket_ = 0;
     int cand_[3] = {0, 0, 0};
-    double tacc_ms_[3][9][3];
-    unsigned tacc_n_[3][9][3];
+    double tacc_ms_[3][12][3];
+    unsigned tacc_n_[3][12][3];
     std::string tune_log_;
     struct TTimed { int fam, sub; cudaEvent_t a, b; };
     std::vector<TTimed> tpending_;

@@ -148,7 +148,7 @@ def test_autotuned_shapes_do_not_change_results(gpu_lib, tmp_path, monkeypatch):
     monkeypatch.setenv("SPH_GB300_TUNE_FILE", str(tmp_path / "tune.txt"))
     scenes = [A] + OTHERS
 
-    def run(tuning=None, mode=0, steps=22):
+    def run(tuning=None, mode=0, steps=28):
         P = sph_gb300.Pool(max_particles=200_000, max_boundary=400_000, max_keys=4_000_000, max_scenes=64)
         P.set_autotune(mode)
         if tuning:
@@ -160,8 +160,10 @@ def test_autotuned_shapes_do_not_change_results(gpu_lib, tmp_path, monkeypatch):
         return P, ids
 
     ref, rids = run()
-    variants = [dict(build_block=64, queue_depth=32, solver_block=512, scan_width=16),
-                dict(build_block=256, queue_depth=48, solver_block=256, scan_width=4)]
+    variants = [dict(build_block=128, build_occupancy=896, queue_depth=16, solver_block=128, solver_occupancy=2048,
+                     scan_width=4),
+                dict(build_block=256, build_occupancy=1024, queue_depth=64, solver_block=256, solver_occupancy=1536,
+                     scan_width=8)]
     for t in variants:
         P, ids = run(tuning=t)
         assert P.tuning()["build_block"] == t["build_block"]
@@ -178,7 +180,9 @@ def test_autotuned_shapes_do_not_change_results(gpu_lib, tmp_path, monkeypatch):
     Q, _ = run(mode=1, steps=1)
     q = Q.tuning()
     assert q["source"] == 1 and q["steps_left"] == 0
-    assert (q["build_block"], q["queue_depth"], q["solver_block"], q["scan_width"]) == (
-        tu["build_block"], tu["queue_depth"], tu["solver_block"], tu["scan_width"])
+    keys = ("build_block", "build_occupancy", "queue_depth", "solver_block", "solver_occupancy", "scan_width")
+    assert all(q[k] == tu[k] for k in keys)
     with pytest.raises(sph_gb300.SPHError):
         Q.set_tuning(build_block=96)
+    with pytest.raises(sph_gb300.SPHError):
+        Q.set_tuning(solver_occupancy=1000)
