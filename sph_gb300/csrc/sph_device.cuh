@@ -43,6 +43,20 @@ __device__ __forceinline__ P4<double> ldg4(const P4<double>* p)
     return P4<double>{a.x, a.y, b.x, b.y};
 }
 template <typename R> __device__ __forceinline__ R ldg1(const R* p) { return __ldg(p); }
+// Streaming load (evict first): data read exactly once, such as pair-list
+// records, so that it does not displace the neighbour data that the gathers
+// of the same pass re-use from L1.
+__device__ __forceinline__ P4<float> ldcs4(const P4<float>* p)
+{
+    float4 t = __ldcs(reinterpret_cast<const float4*>(p));
+    return P4<float>{t.x, t.y, t.z, t.w};
+}
+__device__ __forceinline__ P4<double> ldcs4(const P4<double>* p)
+{
+    const double2* q = reinterpret_cast<const double2*>(p);
+    double2 a = __ldcs(q), b = __ldcs(q + 1);
+    return P4<double>{a.x, a.y, b.x, b.y};
+}
 
 // Division by the support radius: IEEE division in the parity form (the
 // reference divides), multiplication by 1/h in the production form.

@@ -266,9 +266,9 @@ __device__ __forceinline__ V3<R> correct_sum_one(uint32_t i, const Fluid<R>& f, 
     V3<R> sum = {0, 0, 0};
     if (cnt <= L.kmax) {
         const P4<R>* __restrict__ p = L.pairs + i;
-#pragma unroll 4
+#pragma unroll 8
         for (uint32_t k = 0; k < cnt; ++k) {
-            const P4<R> q = ldg4(p + (size_t)k * n);
+            const P4<R> q = ldcs4(p + (size_t)k * n);
             const R kSum = ki + __ldg(kb_ + as_idx(q.w));
             if (fabs(kSum) > c.eps) sum = sum + kSum * xyz(q);
         }
@@ -315,9 +315,9 @@ __device__ __forceinline__ R velocity_div_list(const Fluid<R>& f, const Lists<R>
     const uint32_t cnt = L.count[i];
     const P4<R>* __restrict__ p = L.pairs + i;
     R d = 0;
-#pragma unroll 4
+#pragma unroll 8
     for (uint32_t k = 0; k < cnt; ++k) {
-        const P4<R> q = ldg4(p + (size_t)k * n);
+        const P4<R> q = ldcs4(p + (size_t)k * n);
         d += dot3(vi - xyz(ldg4(f.vel + as_idx(q.w))), xyz(q));
     }
     if (akinci) d += dot3(vi, xyz(L.bgrad[i]));
