@@ -61,6 +61,8 @@ class OrcParams(ctypes.Structure):
         ("cube_min", ctypes.c_double * 3),
         ("cube_max", ctypes.c_double * 3),
         ("has_cube", ctypes.c_int),
+        ("bh_normal_fct", ctypes.c_double),
+        ("bh_tang_fct", ctypes.c_double),
     ]
 
 
@@ -69,7 +71,7 @@ DEFAULTS = dict(
     max_dt=5e-3, fps=60.0, density0=1000.0, stiffness=1000.0, gamma=7.0, eta=0.001, eta_v=0.001,
     cfl=1.0, min_it=-1, max_it=-1, min_it_v=-1, max_it_v=-1, visc_method=-1, visc=0.0, bvisc=0.0,
     st_method=-1, st=0.0, adh_method=-1, adh=0.0, cube_min=(0.0, 0.0, 0.0), cube_max=(1.0, 1.0, 1.0),
-    has_cube=0,
+    has_cube=0, bh_normal_fct=0.0, bh_tang_fct=1.0,
 )
 
 _lib = None
@@ -97,6 +99,10 @@ def lib():
         L.orc_add_box.argtypes = [vp, dp, dp]
         L.orc_add_sphere.argtypes = [vp, dp, ctypes.c_double]
         L.orc_add_points.argtypes = [vp, dp, ctypes.c_uint]
+        L.orc_add_bh_box.argtypes = [vp, dp, dp, ctypes.c_int]
+        L.orc_add_bh_sphere.argtypes = [vp, dp, ctypes.c_double, ctypes.c_int]
+        L.orc_sample_bh_box.argtypes = [ctypes.c_double, dp, dp, ctypes.c_int, dp, dp]
+        L.orc_sample_bh_box.restype = ctypes.c_longlong
         L.orc_perturb.argtypes = [vp, ctypes.c_double, ctypes.c_double, ctypes.c_ulonglong]
         L.orc_init.argtypes = [vp]
         L.orc_step.argtypes = [vp, ctypes.c_int]
@@ -144,6 +150,17 @@ def make_params(**kw) -> OrcParams:
     return p
 
 
+def sample_bh_box(h, mn, mx, inverted=True):
+    """PCISPHBoundaryModel::sampleCube: (points, normals)."""
+    L = lib()
+    mn, mx = _vec3(mn), _vec3(mx)
+    n = L.orc_sample_bh_box(h, _dptr(mn), _dptr(mx), int(inverted), None, None)
+    pts = np.zeros((n, 3))
+    nrm = np.zeros((n, 3))
+    L.orc_sample_bh_box(h, _dptr(mn), _dptr(mx), int(inverted), _dptr(pts), _dptr(nrm))
+    return pts, nrm
+
+
 def fluid_block(radius, mn, mx):
     """Lattice of Simulation::buildFluidBlock (spacing 2r from min + r)."""
     L = lib()
@@ -175,7 +192,7 @@ def sample_sphere(particle_radius, c, radius):
 class OracleScene:
     """One scene of the C restatement (one fluid model, one boundary model)."""
 
-    def __init__(self, params: dict, x, v=None, boxes=(), spheres=(), points=None):
+    def __init__(self, params: dict, x, v=None, boxes=(), spheres=(), points=None, bh_boxes=(), bh_spheres=()):
         L = lib()
         self.params = dict(params)
         self._p = make_params(**params)
@@ -190,6 +207,12 @@ class OracleScene:
             L.orc_add_box(self.h, _dptr(_vec3(mn)), _dptr(_vec3(mx)))
         for c, r in spheres:
             L.orc_add_sphere(self.h, _dptr(_vec3(c)), float(r))
+        for mn, mx, inv in bh_boxes:
+            if L.orc_add_bh_box(self.h, _dptr(_vec3(mn)), _dptr(_vec3(mx)), int(inv)) != 0:
+                raise RuntimeError("orc_add_bh_box failed (boundary must be 1)")
+        for c, r, inv in bh_spheres:
+            if L.orc_add_bh_sphere(self.h, _dptr(_vec3(c)), float(r), int(inv)) != 0:
+                raise RuntimeError("orc_add_bh_sphere failed (boundary must be 1)")
         if points is not None and len(points):
             pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
             L.orc_add_points(self.h, _dptr(pts), pts.shape[0])
@@ -214,8 +237,8 @@ class OracleScene:
             raise RuntimeError("orc_step failed")
 
     def get(self, field):
-        vec = field in ("x", "v", "a", "pacc", "normal", "bx")
-        count = self.nb if field in ("bx", "psi") else self.n
+        vec = field in ("x", "v", "a", "pacc", "normal", "bx", "bn")
+        count = self.nb if field in ("bx", "psi", "bn", "bdens", "bpress") else self.n
         out = np.zeros((count, 3) if vec else count)
         rc = lib().orc_get(self.h, field.encode(), _dptr(out))
         if rc != 0:

@@ -195,6 +195,7 @@ typedef struct {
     size_t cand_cap, bcand_cap;
     unsigned* fcell;     /* cell of each fluid particle at insertion */
     unsigned* bcell;
+    unsigned nbuilt;     /* cells that have candidate lists (the last build's) */
 } grid;
 
 /* HashTable.h:26-29 (computed in int, as the reference does) */
@@ -277,6 +278,13 @@ struct orc_scene {
     unsigned nb, nb_cap;
     v3* bx;
     double* psi;
+    /* solver weight of each boundary particle: rho0 psi_b (Akinci) or the
+     * PCISPH model's mass (PCISPHBoundaryModel.h:13-24, Simulation.cpp:464-468) */
+    double* bw;
+    /* PCISPH boundary model: normals, densities, pressures */
+    v3* bn;
+    double *bdens, *bpress;
+    double bmass;
     /* TimeManager (TimeManager.h:20-33) */
     double time, ts, minTs, maxTs;
     double maxVel;
@@ -346,6 +354,7 @@ static void grid_build(orc_scene* s)
         g->bcstart[c + 1] = bc;
     }
     for (unsigned c = 0; c < nc; ++c) { g->cstart[c + 1] += g->cstart[c]; g->bcstart[c + 1] += g->bcstart[c]; }
+    g->nbuilt = nc;
     if (g->cstart[nc] > g->cand_cap) { free(g->cand); g->cand_cap = g->cstart[nc]; g->cand = (unsigned*)xcalloc(g->cand_cap, sizeof(unsigned)); }
     if (g->bcstart[nc] > g->bcand_cap) { free(g->bcand); g->bcand_cap = g->bcstart[nc]; g->bcand = (unsigned*)xcalloc(g->bcand_cap, sizeof(unsigned)); }
     #pragma omp parallel for schedule(static)
@@ -373,7 +382,7 @@ static inline cands cands_at(const orc_scene* s, v3 p)
 {
     cands r = {0, 0, 0, 0};
     int c = grid_find(&s->g, cell_of(p.x, p.y, p.z, s->h));
-    if (c >= 0) {
+    if (c >= 0 && (unsigned)c < s->g.nbuilt) {
         r.f = s->g.cand + s->g.cstart[c];
         r.nf = s->g.cstart[c + 1] - s->g.cstart[c];
         r.b = s->g.bcand + s->g.bcstart[c];
@@ -383,6 +392,21 @@ static inline cands cands_at(const orc_scene* s, v3 p)
 }
 
 static int akinci(const orc_scene* s) { return s->prm.boundary == 2; }
+/* PCISPH boundary model (Simulation::PCISPH_BOUNDARY_METHOD) */
+static int bh(const orc_scene* s) { return s->prm.boundary == 1; }
+/* boundary particles take part in the solver sums (Akinci: weight rho0 psi_b,
+ * PCISPH model: the model's mass) */
+static int hasb(const orc_scene* s) { return s->prm.boundary == 1 || s->prm.boundary == 2; }
+
+/* grid->table[cellId] as a lookup that creates the cell when missing
+ * (unordered_map::operator[]): a cell created since the last neighbour
+ * search has no candidates. */
+static cands cands_at_create(orc_scene* s, v3 p)
+{
+    const i3 k = cell_of(p.x, p.y, p.z, s->h);
+    if (grid_find(&s->g, k) < 0) grid_insert(&s->g, k);
+    return cands_at(s, p);
+}
 
 /* ------------------------------------------------------------------------ */
 /* Shared solver passes (src/SPHSolver.cpp)                                  */
@@ -391,8 +415,7 @@ static int akinci(const orc_scene* s) { return s->prm.boundary == 2; }
 /* SPHSolver::computeFluidDensities SPHSolver.cpp:44-91 */
 static void compute_densities(orc_scene* s)
 {
-    const double density0 = s->prm.density0;
-    const int ak = akinci(s);
+    const int hb = hasb(s);
     #pragma omp parallel for
     for (unsigned i = 0; i < s->n; ++i) {
         const v3 ri = s->x[i];
@@ -402,10 +425,10 @@ static void compute_densities(orc_scene* s)
             unsigned j = c.f[q];
             density += s->mass * cubic_Wv(&s->K, vsub(ri, s->x[j]));
         }
-        if (ak)
+        if (hb)
             for (unsigned q = 0; q < c.nbn; ++q) {
                 unsigned b = c.b[q];
-                density += density0 * s->psi[b] * cubic_Wv(&s->K, vsub(ri, s->bx[b]));
+                density += s->bw[b] * cubic_Wv(&s->K, vsub(ri, s->bx[b]));
             }
         s->rho[i] = density;
     }
@@ -636,11 +659,98 @@ static void non_pressure_forces(orc_scene* s)
 /* DFSPH (src/DFSPHSolver.cpp)                                               */
 /* ------------------------------------------------------------------------ */
 
+/* ------------------------------------------------------------------------ */
+/* PCISPH boundary model (src/PCISPHBoundaryModel.cpp, SPHSolver.cpp)         */
+/* ------------------------------------------------------------------------ */
+
+/* SPHSolver::computeBoundaryDensities SPHSolver.cpp:94-127 */
+static void bh_boundary_densities(orc_scene* s)
+{
+    #pragma omp parallel for
+    for (unsigned i = 0; i < s->nb; ++i) {
+        const v3 ri = s->bx[i];
+        cands c = cands_at(s, ri);
+        double density = 0;
+        for (unsigned q = 0; q < c.nf; ++q) density += s->mass * cubic_Wv(&s->K, vsub(ri, s->x[c.f[q]]));
+        for (unsigned q = 0; q < c.nbn; ++q) density += s->bmass * cubic_Wv(&s->K, vsub(ri, s->bx[c.b[q]]));
+        s->bdens[i] = density;
+    }
+}
+
+/* Collision weights of fluid particle i against the boundary points within
+ * restRadius = h/2 of `ri` (PCISPHBoundaryModel.cpp:219-316, 394-448): the
+ * weight uses the distance from `rw` (the current or the predicted position).
+ * Returns 1 and the correction displacement when some weight is positive;
+ * always writes the particle's normal (normalize of the weighted normal sum,
+ * NaN when no point is within restRadius). */
+static int bh_collide(orc_scene* s, unsigned i, v3 ri, v3 rw, v3* disp)
+{
+    const double restRadius = 0.5 * s->h;
+    v3 avg_normal = V(0, 0, 0);
+    double w_sum = 0, w2_sum = 0;
+    /* the loops run serially in the reference: cells are created in order */
+    cands c = cands_at_create(s, ri);
+    for (unsigned q = 0; q < c.nbn; ++q) {
+        const unsigned b = c.b[q];
+        const v3 rb = s->bx[b];
+        const v3 prib = vsub(rw, rb);
+        if (vlen(vsub(ri, rb)) < restRadius) {
+            const double w = dmax(0.0, (restRadius - vlen(prib)) / restRadius);
+            w_sum += w;
+            w2_sum += w * (restRadius - vlen(prib));
+            avg_normal = vadd(avg_normal, smul(w, s->bn[b]));
+        }
+    }
+    const v3 ni = vmul(avg_normal, 1.0 / sqrt(vdot(avg_normal, avg_normal)));
+    s->normal[i] = ni;
+    if (w_sum > 0) {
+        *disp = smul(1.0 / w_sum * w2_sum, ni);
+        return 1;
+    }
+    return 0;
+}
+
+/* PCISPHBoundaryModel::correctPositions :219-316 (pred: the PCISPH form,
+ * weights from the predicted positions) */
+static void bh_correct_positions(orc_scene* s, int pred)
+{
+    for (unsigned i = 0; i < s->n; ++i) {
+        v3 d;
+        if (bh_collide(s, i, s->x[i], pred ? s->predR[i] : s->x[i], &d)) s->x[i] = vadd(s->x[i], d);
+    }
+}
+
+/* PCISPHBoundaryModel::correctPredPositions :394-448 */
+static void bh_correct_pred_positions(orc_scene* s)
+{
+    for (unsigned i = 0; i < s->n; ++i) {
+        v3 d;
+        if (bh_collide(s, i, s->x[i], s->predR[i], &d)) s->predR[i] = vadd(s->predR[i], d);
+    }
+}
+
+/* PCISPHBoundaryModel::correctVelocities :318-392: reflect the normal part
+ * of the velocity (PCISPH: of the predicted velocity) for particles whose
+ * normal is valid */
+static void bh_correct_velocities(orc_scene* s, int pred)
+{
+    const double nf = s->prm.bh_normal_fct, tf = s->prm.bh_tang_fct;
+    #pragma omp parallel for
+    for (unsigned i = 0; i < s->n; ++i) {
+        const v3 ni = s->normal[i];
+        if (vlen(ni) > 0) {
+            const v3 u = pred ? s->predV[i] : s->v[i];
+            const v3 nVel = smul(vdot(u, ni), ni);
+            const v3 tVel = vsub(u, nVel);
+            s->v[i] = vsub(smul(tf, tVel), smul(nf, nVel));
+        }
+    }
+}
+
 /* DFSPHSolver::computeAlpha DFSPHSolver.cpp:114-189 */
 static void dfsph_alpha(orc_scene* s)
 {
-    const double density0 = s->prm.density0;
-    const int ak = akinci(s);
+    const int hb = hasb(s);
     #pragma omp parallel for
     for (unsigned i = 0; i < s->n; ++i) {
         const v3 ri = s->x[i];
@@ -654,10 +764,10 @@ static void dfsph_alpha(orc_scene* s)
             sumGrad = vadd(sumGrad, massGrad);
             sumSqGrad += massGradMag * massGradMag;
         }
-        if (ak)
+        if (hb)
             for (unsigned q = 0; q < c.nbn; ++q) {
                 unsigned b = c.b[q];
-                const v3 massGrad = smul(density0 * s->psi[b], cubic_gradW(&s->K, vsub(ri, s->bx[b])));
+                const v3 massGrad = smul(s->bw[b], cubic_gradW(&s->K, vsub(ri, s->bx[b])));
                 sumGrad = vadd(sumGrad, massGrad);
             }
         const double sumGradMag = vlen(sumGrad);
@@ -692,7 +802,7 @@ static void dfsph_update_positions(orc_scene* s)
 static void dfsph_predict_densities(orc_scene* s)
 {
     const double density0 = s->prm.density0, ts = s->ts;
-    const int ak = akinci(s);
+    const int hb = hasb(s);
     double avgDensError = 0.0;
     #pragma omp parallel for reduction(+ : avgDensError)
     for (unsigned i = 0; i < s->n; ++i) {
@@ -703,10 +813,10 @@ static void dfsph_predict_densities(orc_scene* s)
             unsigned j = c.f[q];
             densityChange += s->mass * vdot(vsub(vi, s->v[j]), cubic_gradW(&s->K, vsub(ri, s->x[j])));
         }
-        if (ak)
+        if (hb)
             for (unsigned q = 0; q < c.nbn; ++q) {
                 unsigned b = c.b[q];
-                densityChange += density0 * s->psi[b] * vdot(vi, cubic_gradW(&s->K, vsub(ri, s->bx[b])));
+                densityChange += s->bw[b] * vdot(vi, cubic_gradW(&s->K, vsub(ri, s->bx[b])));
             }
         double pred = s->rho[i] + densityChange * ts;
         pred = dmax(pred, density0);
@@ -721,8 +831,9 @@ static void dfsph_predict_densities(orc_scene* s)
 /* DFSPHSolver::densityWarmStart DFSPHSolver.cpp:592-690 */
 static void dfsph_density_warm_start(orc_scene* s)
 {
-    const double density0 = s->prm.density0, ts = s->ts, ts2 = ts * ts;
-    const int ak = akinci(s);
+    const double ts = s->ts, ts2 = ts * ts;
+    const int hb = hasb(s);
+    const int bhm = bh(s);
     #pragma omp parallel for
     for (unsigned i = 0; i < s->n; ++i) {
         const double dens_i = s->rho[i];
@@ -739,12 +850,12 @@ static void dfsph_density_warm_start(orc_scene* s)
             const double kSum = (ki + s->k[j]);
             if (fabs(kSum) > s->eps) sum = vadd(sum, smul(s->mass * kSum, cubic_gradW(&s->K, vsub(ri, s->x[j]))));
         }
-        if (ak)
+        if (hb)
             for (unsigned q = 0; q < c.nbn; ++q) {
                 unsigned b = c.b[q];
-                const double kSum = 2.0 * ki;
+                const double kSum = bhm ? ki : 2.0 * ki;   /* DFSPHSolver.cpp:646-672 */
                 if (fabs(kSum) > s->eps)
-                    sum = vadd(sum, smul(density0 * s->psi[b] * kSum, cubic_gradW(&s->K, vsub(ri, s->bx[b]))));
+                    sum = vadd(sum, smul(s->bw[b] * kSum, cubic_gradW(&s->K, vsub(ri, s->bx[b]))));
             }
         s->v[i] = vsub(s->v[i], vmul(sum, ts));
     }
@@ -756,7 +867,7 @@ static void dfsph_density_warm_start(orc_scene* s)
 static void dfsph_correct_density_error(orc_scene* s)
 {
     const double density0 = s->prm.density0, ts = s->ts, ts2 = ts * ts;
-    const int ak = akinci(s);
+    const int hb = hasb(s);
     dfsph_density_warm_start(s);
     dfsph_predict_densities(s);
     s->iterations = 0;
@@ -776,10 +887,10 @@ static void dfsph_correct_density_error(orc_scene* s)
                 const double kSum = (ki + kj);
                 if (fabs(kSum) > s->eps) sum = vadd(sum, smul(s->mass * kSum, cubic_gradW(&s->K, vsub(ri, s->x[j]))));
             }
-            if (fabs(ki) > s->eps && ak)
+            if (fabs(ki) > s->eps && hb)
                 for (unsigned q = 0; q < c.nbn; ++q) {
                     unsigned b = c.b[q];
-                    sum = vadd(sum, smul(density0 * s->psi[b] * ki, cubic_gradW(&s->K, vsub(ri, s->bx[b]))));
+                    sum = vadd(sum, smul(s->bw[b] * ki, cubic_gradW(&s->K, vsub(ri, s->bx[b]))));
                 }
             s->v[i] = vsub(s->v[i], smul(ts, sum));
         }
@@ -793,7 +904,7 @@ static void dfsph_correct_density_error(orc_scene* s)
 static void dfsph_divergence_error(orc_scene* s)
 {
     const double density0 = s->prm.density0;
-    const int ak = akinci(s);
+    const int hb = hasb(s);
     double avgDivError = 0;
     #pragma omp parallel for reduction(+ : avgDivError)
     for (unsigned i = 0; i < s->n; ++i) {
@@ -807,11 +918,11 @@ static void dfsph_divergence_error(orc_scene* s)
             divError += s->mass * vdot(vsub(vi, s->v[j]), grad);
             if (vlen(grad) > 0.0) numNeighbors++;
         }
-        if (ak)
+        if (hb)
             for (unsigned q = 0; q < c.nbn; ++q) {
                 unsigned b = c.b[q];
                 const v3 grad = cubic_gradW(&s->K, vsub(ri, s->bx[b]));
-                divError += density0 * s->psi[b] * vdot(vi, grad);
+                divError += s->bw[b] * vdot(vi, grad);
             }
         if (numNeighbors < 20) divError = 0.0;
         else divError = dmax(divError, 0.0);
@@ -826,8 +937,8 @@ static void dfsph_divergence_error(orc_scene* s)
  * bounded by maxIterations, not maxIterationsV, as the reference writes it) */
 static void dfsph_correct_divergence_error(orc_scene* s)
 {
-    const double density0 = s->prm.density0, ts = s->ts;
-    const int ak = akinci(s);
+    const double ts = s->ts;
+    const int hb = hasb(s);
     dfsph_divergence_error(s);
     s->iterationsV = 0;
     s->avgDivError = 0;
@@ -846,10 +957,10 @@ static void dfsph_correct_divergence_error(orc_scene* s)
                 const double kSumV = (kiv + kjv);
                 if (fabs(kSumV) > s->eps) sum = vadd(sum, smul(s->mass * kSumV, cubic_gradW(&s->K, vsub(ri, s->x[j]))));
             }
-            if (fabs(kiv) > s->eps && ak)
+            if (fabs(kiv) > s->eps && hb)
                 for (unsigned q = 0; q < c.nbn; ++q) {
                     unsigned b = c.b[q];
-                    sum = vadd(sum, smul(density0 * s->psi[b] * kiv, cubic_gradW(&s->K, vsub(ri, s->bx[b]))));
+                    sum = vadd(sum, smul(s->bw[b] * kiv, cubic_gradW(&s->K, vsub(ri, s->bx[b]))));
                 }
             s->v[i] = vsub(s->v[i], smul(ts, sum));
         }
@@ -889,8 +1000,10 @@ static void dfsph_step(orc_scene* s)
     non_pressure_forces(s);
     dfsph_update_time_step(s);
     dfsph_predict_velocities(s);
+    if (bh(s)) bh_correct_velocities(s, 0);      /* DFSPHSolver.cpp:51-57 */
     dfsph_correct_density_error(s);
     dfsph_update_positions(s);
+    if (bh(s)) bh_correct_positions(s, 0);       /* :65-75 */
     grid_build(s);
     compute_densities(s);
     dfsph_alpha(s);
@@ -912,11 +1025,19 @@ static void wcsph_pressures(orc_scene* s)
         s->p[i] = dmax(0.0, stiffness * density0 / gamma * (pow(s->rho[i] / density0, gamma) - 1));
 }
 
+/* WCSPHSolver::computeBoundaryPressures WCSPHSolver.cpp:97-114 */
+static void wcsph_boundary_pressures(orc_scene* s)
+{
+    const double density0 = s->prm.density0, stiffness = s->prm.stiffness, gamma = s->prm.gamma;
+    #pragma omp parallel for
+    for (unsigned i = 0; i < s->nb; ++i)
+        s->bpress[i] = dmax(0.0, stiffness * density0 / gamma * (pow(s->bdens[i] / density0, gamma) - 1));
+}
+
 /* WCSPHSolver::computePressureForce WCSPHSolver.cpp:132-188 */
 static void wcsph_pressure_force(orc_scene* s)
 {
-    const double density0 = s->prm.density0;
-    const int ak = akinci(s);
+    const int ak = akinci(s), bhm = bh(s);
     #pragma omp parallel for
     for (unsigned i = 0; i < s->n; ++i) {
         const v3 ri = s->x[i];
@@ -931,7 +1052,13 @@ static void wcsph_pressure_force(orc_scene* s)
         if (ak)
             for (unsigned q = 0; q < c.nbn; ++q) {
                 unsigned b = c.b[q];
-                ai = vsub(ai, smul(density0 * s->psi[b] * (densPress_i * 1.0), cubic_gradW(&s->K, vsub(ri, s->bx[b]))));
+                ai = vsub(ai, smul(s->bw[b] * (densPress_i * 1.0), cubic_gradW(&s->K, vsub(ri, s->bx[b]))));
+            }
+        else if (bhm)
+            for (unsigned q = 0; q < c.nbn; ++q) {
+                unsigned b = c.b[q];
+                ai = vsub(ai, smul(s->bmass * (densPress_i + s->bpress[b] / (s->bdens[b] * s->bdens[b])),
+                                   cubic_gradW(&s->K, vsub(ri, s->bx[b]))));
             }
         s->a[i] = ai;
     }
@@ -943,11 +1070,17 @@ static void wcsph_step(orc_scene* s)
     ++s->steps;
     grid_build(s);
     compute_densities(s);
+    if (bh(s)) bh_boundary_densities(s);
     wcsph_pressures(s);
+    if (bh(s)) wcsph_boundary_pressures(s);
     wcsph_pressure_force(s);
     non_pressure_forces(s);
     integrate_symplectic(s);
     if (s->prm.boundary == 0 && s->prm.has_cube) cube_correct(s);
+    if (bh(s)) {                                 /* WCSPHSolver.cpp:62-72 */
+        bh_correct_positions(s, 0);
+        bh_correct_velocities(s, 0);
+    }
     s->time = s->time + s->ts;
 }
 
@@ -993,8 +1126,7 @@ static void pcisph_predict(orc_scene* s)
  * positions, candidate lists of the current positions' cells. */
 static void pcisph_predict_densities(orc_scene* s)
 {
-    const double density0 = s->prm.density0;
-    const int ak = akinci(s);
+    const int hb = hasb(s);
     #pragma omp parallel for
     for (unsigned i = 0; i < s->n; ++i) {
         const v3 ri = s->predR[i];
@@ -1004,12 +1136,27 @@ static void pcisph_predict_densities(orc_scene* s)
             unsigned j = c.f[q];
             density += s->mass * cubic_Wv(&s->K, vsub(ri, s->predR[j]));
         }
-        if (ak)
+        if (hb)
             for (unsigned q = 0; q < c.nbn; ++q) {
                 unsigned b = c.b[q];
-                density += density0 * s->psi[b] * cubic_Wv(&s->K, vsub(ri, s->bx[b]));
+                density += s->bw[b] * cubic_Wv(&s->K, vsub(ri, s->bx[b]));
             }
         s->rho[i] = density;
+    }
+}
+
+/* PCISPHSolver::predictBoundaryDensities PCISPHSolver.cpp:214-247 (Poly6,
+ * predicted fluid positions) */
+static void pcisph_predict_boundary_densities(orc_scene* s)
+{
+    #pragma omp parallel for
+    for (unsigned i = 0; i < s->nb; ++i) {
+        const v3 ri = s->bx[i];
+        cands c = cands_at(s, ri);
+        double density = 0;
+        for (unsigned q = 0; q < c.nf; ++q) density += s->mass * poly6_W(&s->K, vsub(ri, s->predR[c.f[q]]));
+        for (unsigned q = 0; q < c.nbn; ++q) density += s->bmass * poly6_W(&s->K, vsub(ri, s->bx[c.b[q]]));
+        s->bdens[i] = density;
     }
 }
 
@@ -1026,13 +1173,16 @@ static void pcisph_update_pressure(orc_scene* s)
         maxDensityError = dmax(maxDensityError, error / density0);
     }
     s->maxDensityError = maxDensityError;
+    if (bh(s)) {
+        #pragma omp parallel for
+        for (unsigned i = 0; i < s->nb; ++i) s->bpress[i] += s->scaling * dmax(0.0, s->bdens[i] - density0);
+    }
 }
 
 /* PCISPHSolver::computePressureAcc PCISPHSolver.cpp:297-358 */
 static void pcisph_pressure_acc(orc_scene* s)
 {
-    const double density0 = s->prm.density0;
-    const int ak = akinci(s);
+    const int ak = akinci(s), bhm = bh(s);
     #pragma omp parallel for
     for (unsigned i = 0; i < s->n; ++i) {
         const v3 ri = s->x[i];
@@ -1047,7 +1197,13 @@ static void pcisph_pressure_acc(orc_scene* s)
         if (ak)
             for (unsigned q = 0; q < c.nbn; ++q) {
                 unsigned b = c.b[q];
-                pacc = vsub(pacc, smul(density0 * s->psi[b] * (densPress_i), spiky_gradW(&s->K, vsub(ri, s->bx[b]))));
+                pacc = vsub(pacc, smul(s->bw[b] * (densPress_i), spiky_gradW(&s->K, vsub(ri, s->bx[b]))));
+            }
+        else if (bhm)
+            for (unsigned q = 0; q < c.nbn; ++q) {
+                unsigned b = c.b[q];
+                pacc = vsub(pacc, smul(s->bmass * (densPress_i + s->bpress[b] / (s->bdens[b] * s->bdens[b])),
+                                       spiky_gradW(&s->K, vsub(ri, s->bx[b]))));
             }
         s->pacc[i] = pacc;
     }
@@ -1060,7 +1216,9 @@ static void pcisph_pressure_solver(orc_scene* s)
     s->iterations = 0;
     while ((s->maxDensityError > s->maxError || s->iterations < s->min_it) && s->iterations < s->max_it) {
         pcisph_predict(s);
+        if (bh(s)) bh_correct_pred_positions(s);    /* PCISPHSolver.cpp:367-377 */
         pcisph_predict_densities(s);
+        if (bh(s)) pcisph_predict_boundary_densities(s);
         pcisph_update_pressure(s);
         pcisph_pressure_acc(s);
         ++s->iterations;
@@ -1089,12 +1247,19 @@ static void pcisph_step(orc_scene* s)
     ++s->steps;
     grid_build(s);
     compute_densities(s);
+    if (bh(s)) bh_boundary_densities(s);
     non_pressure_forces(s);
     /* initPressure PCISPHSolver.cpp:83-120 */
     for (unsigned i = 0; i < s->n; ++i) { s->p[i] = 0.0; s->pacc[i] = V(0.0, 0.0, 0.0); }
+    if (bh(s))
+        for (unsigned i = 0; i < s->nb; ++i) s->bpress[i] = 0.0;
     pcisph_pressure_solver(s);
     pcisph_integrate(s);
     if (s->prm.boundary == 0 && s->prm.has_cube) cube_correct(s);
+    if (bh(s)) {                                 /* PCISPHSolver.cpp:65-75 */
+        bh_correct_positions(s, 1);
+        bh_correct_velocities(s, 1);
+    }
     s->time = s->time + s->ts;
 }
 
@@ -1107,7 +1272,6 @@ static void boundary_append(orc_scene* s, const double* pts, long long m);
 orc_scene* orc_create(const orc_params* p)
 {
     if (!p || p->method < 0 || p->method > 2) return NULL;
-    if (p->boundary == 1) return NULL; /* PCISPH boundary particles: not restated */
     orc_scene* s = (orc_scene*)calloc(1, sizeof(orc_scene));
     s->prm = *p;
     s->h = 4.0 * p->radius;              /* Simulation::setParticleRadius Simulation.cpp:192-199 */
@@ -1117,6 +1281,9 @@ orc_scene* orc_create(const orc_params* p)
         const double particleVolume = pow(diameter, 3.0);
         s->mass = p->density0 * particleVolume;
     }
+    /* PCISPH boundary model mass: density0 * (2r)^3, as the fluid's
+     * (Simulation.cpp:464-468) */
+    s->bmass = s->mass;
     s->ts = p->dt;
     /* TimeManager::setMinTimeStep stores min(minTs, 1/fps) (TimeManager.h:55) */
     {
@@ -1152,7 +1319,7 @@ void orc_destroy(orc_scene* s)
     free(s->x); free(s->v); free(s->a); free(s->rho); free(s->p);
     free(s->alpha); free(s->div); free(s->pred); free(s->k); free(s->kv);
     free(s->predR); free(s->predV); free(s->pacc); free(s->normal);
-    free(s->bx); free(s->psi);
+    free(s->bx); free(s->psi); free(s->bw); free(s->bn); free(s->bdens); free(s->bpress);
     grid_free(&s->g);
     free(s);
 }
@@ -1174,21 +1341,31 @@ int orc_set_fluid(orc_scene* s, const double* x, const double* v, unsigned n)
     return 0;
 }
 
-static void boundary_append(orc_scene* s, const double* pts, long long m)
+static void boundary_append_n(orc_scene* s, const double* pts, const double* nrm, long long m)
 {
     if (s->nb + m > s->nb_cap) {
         unsigned cap = s->nb_cap ? s->nb_cap : 1024;
         while (cap < s->nb + m) cap *= 2;
         s->bx = (v3*)realloc(s->bx, cap * sizeof(v3));
+        s->bn = (v3*)realloc(s->bn, cap * sizeof(v3));
         s->psi = (double*)realloc(s->psi, cap * sizeof(double));
+        s->bw = (double*)realloc(s->bw, cap * sizeof(double));
+        s->bdens = (double*)realloc(s->bdens, cap * sizeof(double));
+        s->bpress = (double*)realloc(s->bpress, cap * sizeof(double));
         s->nb_cap = cap;
     }
     for (long long q = 0; q < m; ++q) {
         s->bx[s->nb] = V(pts[3 * q], pts[3 * q + 1], pts[3 * q + 2]);
+        s->bn[s->nb] = nrm ? V(nrm[3 * q], nrm[3 * q + 1], nrm[3 * q + 2]) : V(0, 0, 0);
         s->psi[s->nb] = 0.0;
+        s->bw[s->nb] = 0.0;
+        s->bdens[s->nb] = 0.0;
+        s->bpress[s->nb] = 0.0;
         s->nb++;
     }
 }
+
+static void boundary_append(orc_scene* s, const double* pts, long long m) { boundary_append_n(s, pts, NULL, m); }
 
 /* AkinciBoundaryModel::sampleCube AkinciBoundayModel.cpp:100-134 */
 long long orc_sample_box(double supportRadius, const double mn[3], const double mx[3], double* out)
@@ -1298,6 +1475,89 @@ int orc_add_points(orc_scene* s, const double* pts, unsigned m)
     return 0;
 }
 
+static v3 unit(v3 a) { return vmul(a, 1.0 / sqrt(vdot(a, a))); }
+
+/* PCISPHBoundaryModel::sampleCube PCISPHBoundaryModel.cpp:56-184: points on
+ * the faces of the box at a spacing of at most 0.45 h, each with the normal of
+ * its face, edge or corner (mean of the faces' normals, normalised), pointing
+ * into the box; `inverted` 0 flips them outwards (addCube :7-30). */
+long long orc_sample_bh_box(double supportRadius, const double mn[3], const double mx[3], int inverted, double* pts,
+                            double* normals)
+{
+    const double lx = fabs(mn[0] - mx[0]), ly = fabs(mn[1] - mx[1]), lz = fabs(mn[2] - mx[2]);
+    const unsigned nx = (unsigned)ceil(lx / (0.45 * supportRadius));
+    const unsigned ny = (unsigned)ceil(ly / (0.45 * supportRadius));
+    const unsigned nz = (unsigned)ceil(lz / (0.45 * supportRadius));
+    const double dx = lx / nx, dy = ly / ny, dz = lz / nz;
+    const v3 L = V(1, 0, 0), R = V(-1, 0, 0), T = V(0, -1, 0), B = V(0, 1, 0), F = V(0, 0, -1), K = V(0, 0, 1);
+    const double inv = inverted ? 1.0 : -1;
+    long long count = 0;
+    for (unsigned i = 0; i <= nx; i++)
+        for (unsigned j = 0; j <= ny; j++)
+            for (unsigned k = 0; k <= nz; k++) {
+                const int xi0 = i == 0, xi1 = i == nx, yj0 = j == 0, yj1 = j == ny, zk0 = k == 0, zk1 = k == nz;
+                if (!(xi0 || xi1 || yj0 || yj1 || zk0 || zk1)) continue;
+                const int xin = !xi0 && !xi1, yin = !yj0 && !yj1, zin = !zk0 && !zk1;
+                v3 n;
+                if (!xin && !yin && !zin) {  /* corner: three faces */
+                    n = unit(vdiv(vadd(vadd(xi0 ? L : R, zk0 ? K : F), yj0 ? B : T), 3.0));
+                } else if (xin + yin + zin == 1) {  /* edge: two faces */
+                    v3 a, b;
+                    if (zin) { a = xi0 ? L : R; b = yj0 ? B : T; }
+                    else if (xin) { a = zk0 ? K : F; b = yj0 ? B : T; }
+                    else { a = xi0 ? L : R; b = zk0 ? K : F; }
+                    n = unit(vmul(vadd(a, b), 0.5));
+                } else {  /* face */
+                    n = !xin ? (xi0 ? L : R) : !yin ? (yj0 ? B : T) : (zk0 ? K : F);
+                }
+                if (pts) {
+                    pts[3 * count] = i * dx + mn[0];
+                    pts[3 * count + 1] = j * dy + mn[1];
+                    pts[3 * count + 2] = k * dz + mn[2];
+                    const v3 o = smul(inv, n);
+                    normals[3 * count] = o.x;
+                    normals[3 * count + 1] = o.y;
+                    normals[3 * count + 2] = o.z;
+                }
+                count++;
+            }
+    return count;
+}
+
+/* PCISPHBoundaryModel::addCube :7-30 */
+int orc_add_bh_box(orc_scene* s, const double mn[3], const double mx[3], int inverted)
+{
+    if (!s || s->inited || !bh(s)) return -1;
+    const long long m = orc_sample_bh_box(s->h, mn, mx, inverted, NULL, NULL);
+    double* pts = (double*)xcalloc((size_t)(3 * m), 8);
+    double* nrm = (double*)xcalloc((size_t)(3 * m), 8);
+    orc_sample_bh_box(s->h, mn, mx, inverted, pts, nrm);
+    boundary_append_n(s, pts, nrm, m);
+    free(pts);
+    free(nrm);
+    return 0;
+}
+
+/* PCISPHBoundaryModel::addSphere :32-54 (normals inv * (centre - point), not
+ * normalised; the Akinci sphere sampler) */
+int orc_add_bh_sphere(orc_scene* s, const double c[3], double radius, int inverted)
+{
+    if (!s || s->inited || !bh(s)) return -1;
+    const long long m = orc_sample_sphere(s->prm.radius, c, radius, NULL);
+    double* pts = (double*)xcalloc((size_t)(3 * m), 8);
+    double* nrm = (double*)xcalloc((size_t)(3 * m), 8);
+    orc_sample_sphere(s->prm.radius, c, radius, pts);
+    const double inv = inverted ? 1.0 : -1;
+    for (long long q = 0; q < m; ++q) {
+        const v3 n = smul(inv, vsub(V(c[0], c[1], c[2]), V(pts[3 * q], pts[3 * q + 1], pts[3 * q + 2])));
+        nrm[3 * q] = n.x; nrm[3 * q + 1] = n.y; nrm[3 * q + 2] = n.z;
+    }
+    boundary_append_n(s, pts, nrm, m);
+    free(pts);
+    free(nrm);
+    return 0;
+}
+
 /* Simulation::init -> solver->init (Simulation.cpp:102-110; SPHSolver.cpp:
  * 22-39; DFSPHSolver.cpp:24-36; PCISPHSolver.cpp:12-19; WCSPHSolver.cpp:9) */
 int orc_init(orc_scene* s)
@@ -1311,7 +1571,10 @@ int orc_init(orc_scene* s)
         grid_build(s);
         s->n = n;
         compute_volume(s);
+        for (unsigned b = 0; b < s->nb; ++b) s->bw[b] = s->prm.density0 * s->psi[b];
     }
+    if (bh(s))
+        for (unsigned b = 0; b < s->nb; ++b) s->bw[b] = s->bmass;
     if (s->prm.method == 2) {
         grid_build(s);
         compute_densities(s);
@@ -1383,6 +1646,9 @@ int orc_get(const orc_scene* s, const char* f, double* out)
     else if (!strcmp(f, "k")) memcpy(out, s->k, n * 8);
     else if (!strcmp(f, "kv")) memcpy(out, s->kv, n * 8);
     else if (!strcmp(f, "psi")) memcpy(out, s->psi, s->nb * 8);
+    else if (!strcmp(f, "bn")) put_v3(s->bn, s->nb, out);
+    else if (!strcmp(f, "bdens")) memcpy(out, s->bdens, s->nb * 8);
+    else if (!strcmp(f, "bpress")) memcpy(out, s->bpress, s->nb * 8);
     else return -2;
     return 0;
 }

@@ -34,6 +34,7 @@ typedef struct orc_params {
     double adh;
     double cube_min[3], cube_max[3];      /* cube boundary (boundary == 0) */
     int has_cube;
+    double bh_normal_fct, bh_tang_fct;    /* PCISPH boundary model (boundary == 1) */
 } orc_params;
 
 typedef struct orc_scene orc_scene;
@@ -44,6 +45,11 @@ int orc_set_fluid(orc_scene* s, const double* x, const double* v, unsigned n);
 int orc_add_box(orc_scene* s, const double mn[3], const double mx[3]);
 int orc_add_sphere(orc_scene* s, const double c[3], double radius);
 int orc_add_points(orc_scene* s, const double* pts, unsigned m);
+/* PCISPH boundary model (boundary == 1): sampled cube / sphere with normals */
+int orc_add_bh_box(orc_scene* s, const double mn[3], const double mx[3], int inverted);
+int orc_add_bh_sphere(orc_scene* s, const double c[3], double radius, int inverted);
+long long orc_sample_bh_box(double supportRadius, const double mn[3], const double mx[3], int inverted, double* pts,
+                            double* normals);
 int orc_init(orc_scene* s);
 int orc_step(orc_scene* s, int nsteps);
 /* test instrument: uniform noise on positions and velocities */
