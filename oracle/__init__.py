@@ -306,7 +306,7 @@ def read_dump(path):
 
 
 def run_reference(params: dict, x, v=None, boxes=(), spheres=(), steps=1, dump_neighbors=False,
-                  dump_every=1, timed=False, threads=1, workdir=None):
+                  dump_every=1, timed=False, threads=1, workdir=None, bh_boxes=(), bh_spheres=()):
     """Run the reference's own solver on the scene and return its dump."""
     exe = REF_TIMED if timed else REF_PARITY
     if not os.path.exists(exe):
@@ -334,6 +334,7 @@ def run_reference(params: dict, x, v=None, boxes=(), spheres=(), steps=1, dump_n
             f"adh_method {d['adh_method']}", f"adh {d['adh']!r}",
             f"fluid {fluid}", f"out {out}", f"steps {steps}", f"dump_neighbors {int(dump_neighbors)}",
             f"dump_every {dump_every}",
+            f"bh_normal_fct {d['bh_normal_fct']!r}", f"bh_tang_fct {d['bh_tang_fct']!r}",
         ]
         if d["has_cube"]:
             lines.append("cube " + " ".join(repr(float(t)) for t in list(d["cube_min"]) + list(d["cube_max"])))
@@ -341,6 +342,10 @@ def run_reference(params: dict, x, v=None, boxes=(), spheres=(), steps=1, dump_n
             lines.append("box " + " ".join(repr(float(t)) for t in list(mn) + list(mx)))
         for c, r in spheres:
             lines.append("sphere " + " ".join(repr(float(t)) for t in list(c) + [r]))
+        for mn, mx, inv in bh_boxes:
+            lines.append("bh_box " + " ".join(repr(float(t)) for t in list(mn) + list(mx)) + f" {int(inv)}")
+        for c, r, inv in bh_spheres:
+            lines.append("bh_sphere " + " ".join(repr(float(t)) for t in list(c) + [r]) + f" {int(inv)}")
         scene = os.path.join(td, "scene.txt")
         with open(scene, "w") as f:
             f.write("\n".join(lines) + "\n")

@@ -24,6 +24,7 @@
 #include "WCSPHSolver.h"
 #include "AkinciBoundaryModel.h"
 #include "CubeBoundaryModel.h"
+#include "PCISPHBoundaryModel.h"
 #include "CubicSpline.h"
 #include "HashTable.h"
 #include "../extern/RegularTriangleSampling.h"
@@ -101,6 +102,8 @@ struct Spec {
     bool has_cube = false;
     double cube[6] = {0, 0, 0, 1, 1, 1};
     std::vector<std::vector<double>> boxes, spheres;
+    std::vector<std::vector<double>> bh_boxes, bh_spheres;  // + inverted flag
+    double bh_normal_fct = 0, bh_tang_fct = 1;
     std::string fluid, out;
     int steps = 1;
     int dump_neighbors = 0;   // 1: neighbour sets after init and after step 1
@@ -145,6 +148,10 @@ static Spec read_spec(const char* path)
         else if (k == "cube") { s.has_cube = true; for (double& c : s.cube) is >> c; }
         else if (k == "box") { std::vector<double> b(6); for (double& c : b) is >> c; s.boxes.push_back(b); }
         else if (k == "sphere") { std::vector<double> b(4); for (double& c : b) is >> c; s.spheres.push_back(b); }
+        else if (k == "bh_box") { std::vector<double> b(7); for (double& c : b) is >> c; s.bh_boxes.push_back(b); }
+        else if (k == "bh_sphere") { std::vector<double> b(5); for (double& c : b) is >> c; s.bh_spheres.push_back(b); }
+        else if (k == "bh_normal_fct") is >> s.bh_normal_fct;
+        else if (k == "bh_tang_fct") is >> s.bh_tang_fct;
         else if (k == "fluid") is >> s.fluid;
         else if (k == "out") is >> s.out;
         else if (k == "steps") is >> s.steps;
@@ -234,6 +241,16 @@ static void dump_state(const std::string& tag, Simulation* sim, const Spec& s)
         putscalar(tag + ".avgDensError", d->*DFSPHAccess::avgDensPtr());
         putscalar(tag + ".avgDivError", d->*DFSPHAccess::avgDivPtr());
     }
+    if (s.boundary == Simulation::PCISPH_BOUNDARY_METHOD && sim->numberBoundaryModels() > 0) {
+        PCISPHBoundaryModel* bm = static_cast<PCISPHBoundaryModel*>(sim->getBoundaryModel(0));
+        std::vector<double> bd(bm->size()), bp(bm->size());
+        for (unsigned i = 0; i < bm->size(); ++i) { bd[i] = bm->getDensity(i); bp[i] = bm->getPressure(i); }
+        std::vector<Vector3r> nrm(n);
+        for (unsigned i = 0; i < n; ++i) nrm[i] = fm->getNormal(i);
+        putd(tag + ".bdens", bd);
+        putd(tag + ".bpress", bp);
+        putd(tag + ".normal", flat(nrm, n));
+    }
     if (s.method == Simulation::PCISPH_METHOD) {
         PCISPHSolver* pc = static_cast<PCISPHSolver*>(solver);
         std::vector<double> pacc(3 * n);
@@ -316,6 +333,18 @@ int main(int argc, char** argv)
         for (auto& b : s.boxes) bm->addCube(Vector3r(b[0], b[1], b[2]), Vector3r(b[3], b[4], b[5]));
         for (auto& b : s.spheres) bm->addSphere(Vector3r(b[0], b[1], b[2]), b[3]);
         sim->addBoundaryModel(bm);
+    } else if (s.boundary == Simulation::PCISPH_BOUNDARY_METHOD) {
+        // as Simulation::importScene builds it (src/Simulation.cpp:459-484)
+        PCISPHBoundaryModel* bm = new PCISPHBoundaryModel();
+        Real density0 = fm->getRefDensity();
+        Real particleVolume = pow(2.0 * sim->getParticleRadius(), 3.0);
+        bm->setMass(density0 * particleVolume);
+        bm->setRefDensity(density0);
+        bm->setNormalFct(s.bh_normal_fct);
+        bm->setTangentialFct(s.bh_tang_fct);
+        for (auto& b : s.bh_boxes) bm->addCube(Vector3r(b[0], b[1], b[2]), Vector3r(b[3], b[4], b[5]), b[6] != 0);
+        for (auto& b : s.bh_spheres) bm->addSphere(Vector3r(b[0], b[1], b[2]), b[3], b[4] != 0);
+        sim->addBoundaryModel(bm);
     } else if (s.boundary == Simulation::CUBE_BOUNDARY_METHOD && s.has_cube) {
         // importScene never creates a CubeBoundaryModel; it is added the way
         // CubeBoundaryModel::init expects: two points, min then max.
@@ -334,6 +363,10 @@ int main(int argc, char** argv)
         for (unsigned i = 0; i < bm->size(); ++i) psi[i] = bm->getVolume(i);
         putd("b.x", flat(bm->getPosition(), bm->size()));
         putd("b.psi", psi);
+    }
+    if (s.boundary == Simulation::PCISPH_BOUNDARY_METHOD && sim->numberBoundaryModels() > 0) {
+        PCISPHBoundaryModel* bm = static_cast<PCISPHBoundaryModel*>(sim->getBoundaryModel(0));
+        putd("b.x", flat(bm->getPosition(), bm->size()));
     }
     putscalar("h", sim->getSupportRadius());
     putscalar("mass", fm->getMass(0));

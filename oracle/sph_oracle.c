@@ -1006,6 +1006,7 @@ static void dfsph_step(orc_scene* s)
     if (bh(s)) bh_correct_positions(s, 0);       /* :65-75 */
     grid_build(s);
     compute_densities(s);
+    if (bh(s)) bh_boundary_densities(s);         /* SPHSolver::computeDensities :129-139 */
     dfsph_alpha(s);
     dfsph_correct_divergence_error(s);
     if (s->prm.boundary == 0 && s->prm.has_cube) cube_correct(s);
@@ -1578,6 +1579,7 @@ int orc_init(orc_scene* s)
     if (s->prm.method == 2) {
         grid_build(s);
         compute_densities(s);
+        if (bh(s)) bh_boundary_densities(s);
         dfsph_alpha(s);
     }
     s->inited = 1;

@@ -20,11 +20,11 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "tests"))
 
 import oracle  # noqa: E402
-from scenes import SCENES, scene  # noqa: E402
+from scenes import SCENES, scene, scene_extra  # noqa: E402
 
 STEPS = 3
 KEEP = ("x", "v", "a", "rho", "p", "alpha", "div", "pred", "k", "kv", "pacc", "time", "dt", "iterations",
-        "iterationsV", "avgDensError", "avgDivError", "maxDensityError", "scaling")
+        "iterationsV", "avgDensError", "avgDivError", "maxDensityError", "scaling", "normal", "bdens", "bpress")
 
 
 def main(ref_tree="/root/reference"):
@@ -34,15 +34,18 @@ def main(ref_tree="/root/reference"):
     here = os.path.dirname(os.path.abspath(__file__))
     for name in SCENES:
         params, x, boxes, spheres = scene(name)
-        dump = oracle.run_reference(params, x, boxes=boxes, spheres=spheres, steps=STEPS,
-                                    dump_neighbors=params["method"] == 2)
+        v, bh_boxes, bh_spheres = scene_extra(name, x)
+        dump = oracle.run_reference(params, x, v, boxes=boxes, spheres=spheres, steps=STEPS,
+                                    dump_neighbors=params["method"] == 2, bh_boxes=bh_boxes, bh_spheres=bh_spheres)
         out = {"input.x": x}
+        if v is not None:
+            out["input.v"] = v
         for k, v in dump.items():
             tag, _, field = k.partition(".")
             if k in ("b.x", "b.psi", "h", "mass") or k.startswith("init.") or field in KEEP:
                 out[k] = v
         np.savez_compressed(os.path.join(here, f"{name}.npz"), **out)
-        print(name, x.shape[0], "fluid,", len(dump.get("b.psi", [])), "boundary")
+        print(name, x.shape[0], "fluid,", len(dump.get("b.x", [])) // 3, "boundary")
 
 
 if __name__ == "__main__":

@@ -96,6 +96,43 @@ SCENES = {
 }
 
 
+def _bh_fluid():
+    """A pool 1.5 r off the floor and walls of the box (inside the PCISPH
+    model's collision radius h/2) plus a falling block, all moving towards
+    the walls, so that every step has colliding particles."""
+    return jitter(np.concatenate([lattice(0.02, (0.01, 0.01, 0.01), (0.3, 0.12, 0.3)),
+                                  lattice(0.02, (0.2, 0.3, 0.2), (0.4, 0.4, 0.4))]), 0.02, 5)
+
+
+def _bh_velocity(x):
+    v = np.zeros_like(x)
+    v[:, 0] = -0.2
+    v[:, 1] = -0.5
+    return v
+
+
+# PCISPH boundary model (boundary 1): a container box (normals inwards) and a
+# solid sphere obstacle (normals outwards), for each solver.
+_BH = dict(bh_boxes=[((0.0, 0.0, 0.0), (0.6, 0.6, 0.6), 1)], bh_spheres=[((0.3, 0.2, 0.3), 0.05, 0)],
+           velocity=_bh_velocity, fluid=_bh_fluid, boxes=[], spheres=[])
+SCENES.update({
+    "wcsph_bh": dict(params=dict(method=0, boundary=1, radius=0.02, bh_normal_fct=0.5, bh_tang_fct=0.9,
+                                 visc_method=2, visc=0.01), **_BH),
+    "pcisph_bh": dict(params=dict(method=1, boundary=1, radius=0.02, bh_normal_fct=0.5, bh_tang_fct=0.9, eta=0.001,
+                                  min_it=3, max_it=100), **_BH),
+    "dfsph_bh": dict(params=dict(method=2, boundary=1, radius=0.02, bh_normal_fct=0.5, bh_tang_fct=0.9, eta=0.001,
+                                 eta_v=0.001), **_BH),
+})
+
+
 def scene(name):
     s = SCENES[name]
     return s["params"], s["fluid"](), s["boxes"], s["spheres"]
+
+
+def scene_extra(name, x):
+    """Initial velocities and PCISPH-model shapes of a scene: (v or None,
+    [(min, max, inverted)], [(centre, radius, inverted)])."""
+    s = SCENES[name]
+    v = s["velocity"](x) if "velocity" in s else None
+    return v, s.get("bh_boxes", []), s.get("bh_spheres", [])
