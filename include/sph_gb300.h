@@ -64,6 +64,8 @@ extern "C" {
 #define SPH_FIELD_NORMAL 11         /* 3 (surface tension) */
 #define SPH_FIELD_BOUNDARY_POSITION 12 /* 3 per boundary particle */
 #define SPH_FIELD_BOUNDARY_VOLUME 13   /* 1 per boundary particle (psi) */
+#define SPH_FIELD_BOUNDARY_DENSITY 14  /* 1 per boundary particle (PCISPH boundary model) */
+#define SPH_FIELD_BOUNDARY_PRESSURE 15 /* 1 per boundary particle (PCISPH boundary model) */
 
 /* Device status bits (sph_stats.status). */
 #define SPH_STATUS_OUT_OF_GRID 1u   /* a particle left the grid box; it was kept in the border cell */
@@ -104,6 +106,8 @@ typedef struct sph_scene_desc {
     int neighbor_list_max;        /* DFSPH: > 0 builds per-particle pair lists with this many
                                      slots after each grid build and runs the solver walks over
                                      them; 0 walks the 27 cells in every pass */
+    double bh_normal_fct;         /* PCISPH boundary model: normal and tangential velocity */
+    double bh_tangential_fct;     /* factors of its collisions (scene "normalFct", "tangFct") */
 } sph_scene_desc;
 
 typedef struct sph_stats {
@@ -142,6 +146,14 @@ int sph_ctx_add_boundary_box(sph_ctx* ctx, const double min[3], const double max
 int sph_ctx_add_boundary_sphere(sph_ctx* ctx, const double center[3], double radius);
 /* Raw boundary points (xyz, FP64). */
 int sph_ctx_add_boundary_points(sph_ctx* ctx, const double* x, unsigned n);
+/* PCISPHBoundaryModel::addCube / ::addSphere (src/PCISPHBoundaryModel.cpp:7-54)
+ * for boundary_method SPH_BOUNDARY_PCISPH: points with normals; `inverted`
+ * non-zero points the normals into the box (a container) or towards the
+ * sphere's centre.  sph_ctx_add_boundary_box / _sphere with this boundary
+ * method add an inverted box and a solid sphere.  Boundary points without
+ * normals (sph_ctx_add_boundary_points) are rejected for this model. */
+int sph_ctx_add_pcisph_box(sph_ctx* ctx, const double mn[3], const double mx[3], int inverted);
+int sph_ctx_add_pcisph_sphere(sph_ctx* ctx, const double c[3], double radius, int inverted);
 
 /* Simulation::init -> solver->init (Simulation.cpp:102-110,
  * SPHSolver.cpp:22-39, DFSPHSolver.cpp:24-36, PCISPHSolver.cpp:12-19):
@@ -289,6 +301,10 @@ const char* sph_pool_last_error(const sph_pool* pool);
 /* Sampling helpers with the reference's point sets, usable without a
  * context; out may be NULL to query the count.  Return the point count. */
 long long sph_sample_box(double support_radius, const double min[3], const double max[3], double* out);
+/* PCISPHBoundaryModel::sampleCube: points and normals (out, normals may be
+ * NULL to count). */
+long long sph_sample_pcisph_box(double support_radius, const double mn[3], const double mx[3], int inverted,
+                                double* out, double* normals);
 long long sph_sample_sphere(double particle_radius, const double center[3], double radius, double* out);
 long long sph_fluid_block(double particle_radius, const double min[3], const double max[3], double* out);
 

@@ -32,6 +32,7 @@ PRECISION_F32, PRECISION_F64 = 0, 1
 FIELDS = {
     "x": (0, 3), "v": (1, 3), "a": (2, 3), "rho": (3, 1), "p": (4, 1), "alpha": (5, 1), "pred": (6, 1),
     "div": (7, 1), "k": (8, 1), "kv": (9, 1), "pacc": (10, 3), "normal": (11, 3), "bx": (12, 3), "psi": (13, 1),
+    "bdens": (14, 1), "bpress": (15, 1),
 }
 
 STATUS_OUT_OF_GRID, STATUS_NONFINITE, STATUS_ITER_CAP, STATUS_ITER_CAP_V = 1, 2, 4, 8
@@ -72,6 +73,8 @@ class SceneDesc(ctypes.Structure):
         ("domain_max", ctypes.c_double * 3),
         ("threads_per_particle", ctypes.c_int),
         ("neighbor_list_max", ctypes.c_int),
+        ("bh_normal_fct", ctypes.c_double),
+        ("bh_tangential_fct", ctypes.c_double),
     ]
 
 
@@ -131,6 +134,8 @@ ABI = [
     ("sph_ctx_add_boundary_box", ctypes.c_int, [_vp, _dp, _dp]),
     ("sph_ctx_add_boundary_sphere", ctypes.c_int, [_vp, _dp, ctypes.c_double]),
     ("sph_ctx_add_boundary_points", ctypes.c_int, [_vp, _dp, ctypes.c_uint]),
+    ("sph_ctx_add_pcisph_box", ctypes.c_int, [_vp, _dp, _dp, ctypes.c_int]),
+    ("sph_ctx_add_pcisph_sphere", ctypes.c_int, [_vp, _dp, ctypes.c_double, ctypes.c_int]),
     ("sph_ctx_init", ctypes.c_int, [_vp]),
     ("sph_ctx_step", ctypes.c_int, [_vp, ctypes.c_int]),
     ("sph_ctx_step_timed", ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
@@ -148,6 +153,7 @@ ABI = [
     ("sph_select_device", ctypes.c_int, [ctypes.c_int]),
     ("sph_sample_box", ctypes.c_longlong, [ctypes.c_double, _dp, _dp, _dp]),
     ("sph_sample_sphere", ctypes.c_longlong, [ctypes.c_double, _dp, ctypes.c_double, _dp]),
+    ("sph_sample_pcisph_box", ctypes.c_longlong, [ctypes.c_double, _dp, _dp, ctypes.c_int, _dp, _dp]),
     ("sph_fluid_block", ctypes.c_longlong, [ctypes.c_double, _dp, _dp, _dp]),
     ("sph_version", ctypes.c_char_p, []),
     ("sph_pool_desc_from_budget", ctypes.c_int, [ctypes.c_ulonglong, ctypes.c_int, ctypes.POINTER(PoolDesc)]),
@@ -226,7 +232,7 @@ _PARAM_MAP = {
     "visc": "viscosity", "bvisc": "boundary_viscosity", "st_method": "surface_tension_method",
     "st": "surface_tension", "adh_method": "adhesion_method", "adh": "adhesion", "has_cube": "has_cube",
     "precision": "precision", "threads_per_particle": "threads_per_particle",
-    "neighbor_list_max": "neighbor_list_max",
+    "neighbor_list_max": "neighbor_list_max", "bh_normal_fct": "bh_normal_fct", "bh_tang_fct": "bh_tangential_fct",
 }
 _VEC = {"gravity", "cube_min", "cube_max", "domain_min", "domain_max"}
 
@@ -296,6 +302,16 @@ class Scene:
                     "sph_ctx_add_boundary_sphere")
         return self
 
+    def add_pcisph_box(self, mn, mx, inverted=True):
+        self._check(lib().sph_ctx_add_pcisph_box(self._h, _d(_v3(mn)), _d(_v3(mx)), int(bool(inverted))),
+                    "sph_ctx_add_pcisph_box")
+        return self
+
+    def add_pcisph_sphere(self, c, radius, inverted=False):
+        self._check(lib().sph_ctx_add_pcisph_sphere(self._h, _d(_v3(c)), float(radius), int(bool(inverted))),
+                    "sph_ctx_add_pcisph_sphere")
+        return self
+
     def add_boundary_points(self, x):
         x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, 3)
         self._check(lib().sph_ctx_add_boundary_points(self._h, _d(x), x.shape[0]), "sph_ctx_add_boundary_points")
@@ -338,7 +354,7 @@ class Scene:
 
     def get(self, field):
         fid, width = FIELDS[field]
-        count = self.nb if field in ("bx", "psi") else self.n
+        count = self.nb if field in ("bx", "psi", "bdens", "bpress") else self.n
         out = np.zeros((count, 3) if width == 3 else count)
         if count:
             self._check(lib().sph_ctx_download(self._h, fid, _d(out)), f"sph_ctx_download({field})")
@@ -347,7 +363,7 @@ class Scene:
     def get_noalloc(self, field):
         """get() through sph_ctx_download_noalloc (fixed device staging array)."""
         fid, width = FIELDS[field]
-        count = self.nb if field in ("bx", "psi") else self.n
+        count = self.nb if field in ("bx", "psi", "bdens", "bpress") else self.n
         out = np.zeros((count, 3) if width == 3 else count)
         if count:
             self._check(lib().sph_ctx_download_noalloc(self._h, fid, _d(out)), f"sph_ctx_download_noalloc({field})")
@@ -415,6 +431,15 @@ def sample_sphere(particle_radius, c, radius):
     out = np.zeros((m, 3))
     L.sph_sample_sphere(particle_radius, _d(_v3(c)), radius, _d(out))
     return out
+
+
+def sample_pcisph_box(h, mn, mx, inverted=True):
+    """PCISPHBoundaryModel::sampleCube as the library samples it: (points, normals)."""
+    L = lib()
+    n = L.sph_sample_pcisph_box(float(h), _d(_v3(mn)), _d(_v3(mx)), int(bool(inverted)), None, None)
+    pts, nrm = np.zeros((n, 3)), np.zeros((n, 3))
+    L.sph_sample_pcisph_box(float(h), _d(_v3(mn)), _d(_v3(mx)), int(bool(inverted)), _d(pts), _d(nrm))
+    return pts, nrm
 
 
 def fluid_block(particle_radius, mn, mx):
@@ -511,7 +536,7 @@ class Pool:
     def get(self, sid, field, out=None):
         fid, width = FIELDS[field]
         nf, nb = self._n[sid]
-        count = nb if field in ("bx", "psi") else nf
+        count = nb if field in ("bx", "psi", "bdens", "bpress") else nf
         shape = (count, 3) if width == 3 else (count,)
         if out is None:
             out = np.zeros(shape)

@@ -44,6 +44,56 @@ long long sample_box(double supportRadius, const double mn[3], const double mx[3
 
 // AkinciBoundaryModel::sampleSphere AkinciBoundayModel.cpp:136-164:
 // equal-area latitude rings, 1.5x the surface / particle-disc count.
+// PCISPHBoundaryModel::sampleCube PCISPHBoundaryModel.cpp:56-184: the box's
+// surface at a spacing of at most 0.45 h per axis; each point carries the
+// normal of its face, or the normalised mean of its two (edge) or three
+// (corner) faces' normals, pointing into the box, negated unless `inverted`
+// (addCube :7-30).
+long long sample_pcisph_box(double supportRadius, const double mn[3], const double mx[3], int inverted, double* out,
+                            double* normals)
+{
+    double len[3], step[3];
+    unsigned cnt[3];
+    for (int a = 0; a < 3; ++a) {
+        len[a] = std::fabs(mn[a] - mx[a]);
+        cnt[a] = (unsigned)std::ceil(len[a] / (0.45 * supportRadius));
+        step[a] = len[a] / cnt[a];
+    }
+    // into-the-box normal of the low / high face of each axis
+    const double lo[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}}, hi[3][3] = {{-1, 0, 0}, {0, -1, 0}, {0, 0, -1}};
+    const double sign = inverted ? 1.0 : -1;
+    long long count = 0;
+    for (unsigned i = 0; i <= cnt[0]; i++)
+        for (unsigned j = 0; j <= cnt[1]; j++)
+            for (unsigned k = 0; k <= cnt[2]; k++) {
+                const unsigned idx[3] = {i, j, k};
+                int faces = 0;
+                const double* f[3];
+                // faces in the order x, z, y: the order the reference adds them in
+                const int order[3] = {0, 2, 1};
+                for (int q = 0; q < 3; ++q) {
+                    const int a = order[q];
+                    if (idx[a] == 0) f[faces++] = lo[a];
+                    else if (idx[a] == cnt[a]) f[faces++] = hi[a];
+                }
+                if (!faces) continue;
+                double n[3] = {f[0][0], f[0][1], f[0][2]};
+                if (faces > 1) {
+                    for (int q = 1; q < faces; ++q)
+                        for (int a = 0; a < 3; ++a) n[a] = n[a] + f[q][a];
+                    for (int a = 0; a < 3; ++a) n[a] = faces == 2 ? n[a] * 0.5 : n[a] / 3.0;
+                    const double inv = 1.0 / std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+                    for (int a = 0; a < 3; ++a) n[a] = n[a] * inv;
+                }
+                if (out) {
+                    for (int a = 0; a < 3; ++a) out[3 * count + a] = idx[a] * step[a] + mn[a];
+                    for (int a = 0; a < 3; ++a) normals[3 * count + a] = sign * n[a];
+                }
+                count++;
+            }
+    return count;
+}
+
 long long sample_sphere(double particleRadius, const double c[3], double radius, double* out)
 {
     const double separation = 1.5;
@@ -140,6 +190,8 @@ int sph_scene_desc_init(sph_scene_desc* d)
     d->cube_max[0] = d->cube_max[1] = d->cube_max[2] = 1.0;
     d->threads_per_particle = 0;
     d->neighbor_list_max = 64;
+    d->bh_normal_fct = 0.0;
+    d->bh_tangential_fct = 1.0;
     return SPH_OK;
 }
 
@@ -205,20 +257,65 @@ int sph_ctx_add_fluid_block(sph_ctx* ctx, const double mn[3], const double mx[3]
     return SPH_OK;
 }
 
-static int add_boundary(sph_ctx* ctx, const double* pts, long long m)
+static int add_boundary(sph_ctx* ctx, const double* pts, long long m, const double* normals = nullptr)
 {
+    const bool pcisph = ctx->scene->d.boundary_method == SPH_BOUNDARY_PCISPH;
+    if (pcisph && !normals)
+        return bad(ctx, "the PCISPH boundary model needs normals: use sph_ctx_add_pcisph_box / _sphere");
     try {
         auto& hb = ctx->scene->hb;
         hb.insert(hb.end(), pts, pts + 3 * m);
+        if (pcisph) ctx->scene->hbn.insert(ctx->scene->hbn.end(), normals, normals + 3 * m);
     } catch (...) {
         return bad(ctx, "out of host memory");
     }
     return SPH_OK;
 }
 
+int sph_ctx_add_pcisph_box(sph_ctx* ctx, const double mn[3], const double mx[3], int inverted)
+{
+    if (!ctx || !mn || !mx) return bad(ctx, "invalid argument");
+    if (ctx->scene->inited) return bad(ctx, "boundary must be added before sph_ctx_init");
+    if (ctx->scene->d.boundary_method != SPH_BOUNDARY_PCISPH) return bad(ctx, "boundary_method is not SPH_BOUNDARY_PCISPH");
+    const double h = 4.0 * ctx->scene->d.particle_radius;
+    const long long m = sph::sample_pcisph_box(h, mn, mx, inverted, nullptr, nullptr);
+    std::vector<double> pts, nrm;
+    try {
+        pts.resize(3 * m + 1);
+        nrm.resize(3 * m + 1);
+    } catch (...) {
+        return bad(ctx, "out of host memory");
+    }
+    sph::sample_pcisph_box(h, mn, mx, inverted, pts.data(), nrm.data());
+    return add_boundary(ctx, pts.data(), m, nrm.data());
+}
+
+int sph_ctx_add_pcisph_sphere(sph_ctx* ctx, const double c[3], double radius, int inverted)
+{
+    if (!ctx || !c || !(radius > 0.0)) return bad(ctx, "invalid argument");
+    if (ctx->scene->inited) return bad(ctx, "boundary must be added before sph_ctx_init");
+    if (ctx->scene->d.boundary_method != SPH_BOUNDARY_PCISPH) return bad(ctx, "boundary_method is not SPH_BOUNDARY_PCISPH");
+    const double r = ctx->scene->d.particle_radius;
+    const long long m = sph::sample_sphere(r, c, radius, nullptr);
+    std::vector<double> pts, nrm;
+    try {
+        pts.resize(3 * m + 1);
+        nrm.resize(3 * m + 1);
+    } catch (...) {
+        return bad(ctx, "out of host memory");
+    }
+    sph::sample_sphere(r, c, radius, pts.data());
+    // PCISPHBoundaryModel::addSphere :32-54: inv * (centre - point), not normalised
+    const double sign = inverted ? 1.0 : -1;
+    for (long long q = 0; q < m; ++q)
+        for (int a = 0; a < 3; ++a) nrm[3 * q + a] = sign * (c[a] - pts[3 * q + a]);
+    return add_boundary(ctx, pts.data(), m, nrm.data());
+}
+
 int sph_ctx_add_boundary_box(sph_ctx* ctx, const double mn[3], const double mx[3])
 {
     if (!ctx || !mn || !mx) return bad(ctx, "invalid argument");
+    if (ctx->scene->d.boundary_method == SPH_BOUNDARY_PCISPH) return sph_ctx_add_pcisph_box(ctx, mn, mx, 1);
     if (ctx->scene->inited) return bad(ctx, "boundary must be added before sph_ctx_init");
     const double h = 4.0 * ctx->scene->d.particle_radius;
     const long long m = sph::sample_box(h, mn, mx, nullptr);
@@ -234,6 +331,7 @@ int sph_ctx_add_boundary_box(sph_ctx* ctx, const double mn[3], const double mx[3
 int sph_ctx_add_boundary_sphere(sph_ctx* ctx, const double c[3], double radius)
 {
     if (!ctx || !c || !(radius > 0.0)) return bad(ctx, "invalid argument");
+    if (ctx->scene->d.boundary_method == SPH_BOUNDARY_PCISPH) return sph_ctx_add_pcisph_sphere(ctx, c, radius, 0);
     if (ctx->scene->inited) return bad(ctx, "boundary must be added before sph_ctx_init");
     const double r = ctx->scene->d.particle_radius;
     const long long m = sph::sample_sphere(r, c, radius, nullptr);
@@ -329,6 +427,13 @@ long long sph_sample_box(double support_radius, const double mn[3], const double
 {
     if (!mn || !mx || !(support_radius > 0.0)) return -1;
     return sph::sample_box(support_radius, mn, mx, out);
+}
+
+long long sph_sample_pcisph_box(double support_radius, const double mn[3], const double mx[3], int inverted,
+                                double* out, double* normals)
+{
+    if (!mn || !mx || !(support_radius > 0.0) || (out && !normals)) return -1;
+    return sph::sample_pcisph_box(support_radius, mn, mx, inverted, out, normals);
 }
 
 long long sph_sample_sphere(double particle_radius, const double c[3], double radius, double* out)

@@ -79,6 +79,8 @@ template <typename R> struct Consts {
     R stiffness, gamma, k_eos;     // k_eos = stiffness * density0 / gamma
     R visc, bvisc, st, adh;
     R cube_min[3], cube_max[3];
+    R bwarm;                       // warm-start boundary factor: 2 (Akinci), 1 (PCISPH model)
+    R bh_nf, bh_tf;                // PCISPH boundary model normal / tangential factors
     int force_flags;
     int has_cube;
 };
@@ -101,7 +103,7 @@ struct DevScalars {
     unsigned long long sumIterations, sumIterationsV;
     unsigned status;               // SPH_STATUS_* bits
     unsigned block_counter;        // last-block-done counter of reductions
-    unsigned pad;
+    unsigned grid_epoch;           // grid builds so far (cell lifetimes, PCISPH boundary model)
 };
 
 enum StatusBits : unsigned {
@@ -149,9 +151,12 @@ __device__ __forceinline__ uint32_t cell_key(const GridView& g, int cx, int cy, 
 // column) is picked by comparing j with the column's two inner cell starts.
 // Columns and z-cells whose box lies farther than h from the particle are
 // skipped: they hold no neighbour, and every smoothing kernel is zero there,
-// so the sums are those of the full 27-cell walk.
+// so the sums are those of the full 27-cell walk.  TRIM = false walks all 27
+// cells: needed where the distance is taken to positions other than the ones
+// the candidates are filed by (PCISPH's predicted positions, filed by their
+// current cells).
 // G > 1 lanes split each cell's range (lane l takes every G-th candidate).
-template <typename R, int G, typename F>
+template <typename R, int G, bool TRIM = true, typename F>
 __device__ __forceinline__ void walk(const GridView& g, const uint32_t* __restrict__ starts, uint32_t pc, V3<R> xi, R h,
                                      int lane, F&& f)
 {
@@ -169,7 +174,7 @@ __device__ __forceinline__ void walk(const GridView& g, const uint32_t* __restri
         const R gxm = ofx > (R)0 ? ofx * ofx : (R)0, gxp = h - ofx > (R)0 ? (h - ofx) * (h - ofx) : (R)0;
         const R gym = ofy > (R)0 ? ofy * ofy : (R)0, gyp = h - ofy > (R)0 ? (h - ofy) * (h - ofy) : (R)0;
         const R gzm = ofz > (R)0 ? ofz * ofz : (R)0, gzp = h - ofz > (R)0 ? (h - ofz) * (h - ofz) : (R)0;
-        const R lim = h * h * (R)(1.0 + 1e-5);
+        const R lim = TRIM ? h * h * (R)(1.0 + 1e-5) : (R)INFINITY;
         uint32_t b[9], m0[9], m1[9], e[9];
 #pragma unroll
         for (int dx = -1; dx <= 1; ++dx) {
@@ -241,6 +246,19 @@ __device__ __forceinline__ void walk(const GridView& g, const uint32_t* __restri
 // ---------------------------------------------------------------------------
 // Smoothing kernels
 // ---------------------------------------------------------------------------
+
+// Poly6::W Poly6.h:30-43 from the squared distance (the length is formed and
+// squared again, as the reference does).
+template <typename R> __device__ __forceinline__ R poly6_W(const Consts<R>& c, R r2)
+{
+    const R mod_r = sqrt(r2);
+    const R mod_r2 = mod_r * mod_r;
+    if (mod_r2 <= c.p6_h2) {
+        const R diff = c.p6_h2 - mod_r2;
+        return c.p6_value * diff * diff * diff;
+    }
+    return (R)0;
+}
 
 // CubicSpline::W CubicSpline.h:28-46, from the distance r.
 template <typename R> __device__ __forceinline__ R cubic_W(const Consts<R>& c, R r)

@@ -36,11 +36,15 @@ template <typename R> struct Fluid {
 };
 
 template <typename R> struct Boundary {
-    P4<R>* pos;      // xyz: position (frame as fluid); w: density0 * psi
+    P4<R>* pos;      // xyz: position (frame as fluid); w: solver weight (density0 * psi or the model's mass)
     R* psi;
     uint32_t* cell;
     uint32_t* id;
     uint32_t n;
+    // PCISPH boundary model (two-way): normals, densities, pressures and
+    // p / rho^2 for the pressure walks (null for the Akinci model)
+    P4<R>* nrm;
+    R *dens, *press, *dp;
 };
 
 constexpr unsigned kBlock = 128;
@@ -149,10 +153,11 @@ __global__ void k_download(uint32_t n, const P4<R>* __restrict__ v4, const R* __
 // Moves particles (MOVE: x += v dt, DFSPHSolver::updatePositions
 // DFSPHSolver.cpp:216-236), recomputes their cells (HashTable.h:81) and
 // counts them per cell key.
-template <typename R, bool MOVE>
+template <typename R, bool MOVE, bool KEY = true>
 __global__ void k_cell_update(uint32_t n, P4<R>* __restrict__ pos, const P4<R>* __restrict__ vel, uint32_t* __restrict__ cell,
                               uint32_t* __restrict__ key, uint32_t* __restrict__ slot, uint32_t* __restrict__ count,
-                              GridView g, R h, double hd, DevScalars* sc)
+                              GridView g, R h, double hd, DevScalars* sc, uint32_t* __restrict__ cell_epoch = nullptr,
+                              P4<R>* __restrict__ carry = nullptr)
 {
     const uint32_t i = gtid();
     if (i >= n) return;
@@ -171,6 +176,11 @@ __global__ void k_cell_update(uint32_t n, P4<R>* __restrict__ pos, const P4<R>* 
         const int ccx = min(max(cx, 0), g.nx - 1), ccy = min(max(cy, 0), g.ny - 1), ccz = min(max(cz, 0), g.nz - 1);
         if (ccx != cx || ccy != cy || ccz != cz) atomicOr(&sc->status, (unsigned)ST_OUT_OF_GRID);
         p.x -= (R)(ccx - x0) * h; p.y -= (R)(ccy - y0) * h; p.z -= (R)(ccz - z0) * h;
+        if (carry) {  // a second point stored in the particle's frame (PCISPH predicted position)
+            P4<R> q = carry[i];
+            q.x -= (R)(ccx - x0) * h; q.y -= (R)(ccy - y0) * h; q.z -= (R)(ccz - z0) * h;
+            carry[i] = q;
+        }
         // keep in-grid offsets inside [0, h) so the 27-cell walk covers the support
         if (ccx == cx) p.x = fminf(fmaxf(p.x, 0.f), __int_as_float(__float_as_int(h) - 1));
         if (ccy == cy) p.y = fminf(fmaxf(p.y, 0.f), __int_as_float(__float_as_int(h) - 1));
@@ -186,7 +196,9 @@ __global__ void k_cell_update(uint32_t n, P4<R>* __restrict__ pos, const P4<R>* 
     }
     pos[i] = p;
     cell[i] = pack_cell(cx, cy, cz);
+    if (!KEY) return;  // positions and cells only (the PCISPH boundary corrections follow)
     const uint32_t k = cell_key(g, cx, cy, cz);
+    if (cell_epoch) atomicMin(cell_epoch + k, sc->grid_epoch);  // the cell exists from this build on
     key[i] = k;
     slot[i] = atomicAdd(count + k, 1u);
 }
@@ -368,6 +380,9 @@ __global__ void k_gather_fluid(uint32_t n, const uint32_t* __restrict__ tmp, con
     dst.pred[d] = src.pred[i];
     dst.cell[d] = src.cell[i];
     dst.id[d] = src.id[i];
+    // PCISPH boundary model: a particle's normal from its last collision is
+    // read by the next step's velocity correction (double-buffered then)
+    if (src.normal != dst.normal) dst.normal[d] = src.normal[i];
 }
 
 template <typename R>
@@ -381,6 +396,7 @@ __global__ void k_gather_boundary(uint32_t n, const uint32_t* __restrict__ tmp, 
     dst.pos[d] = src.pos[i];
     dst.cell[d] = src.cell[i];
     dst.id[d] = src.id[i];
+    if (src.nrm) dst.nrm[d] = src.nrm[i];
 }
 
 // ===========================================================================
@@ -482,7 +498,7 @@ __global__ void __launch_bounds__(kBlock) k_density(Fluid<R> f, const P4<R>* __r
 template <typename R, int G>
 __global__ void __launch_bounds__(kBlock) k_wcsph_pressure_force(Fluid<R> f, const P4<R>* __restrict__ bpos, GridView g,
                                                                  const uint32_t* __restrict__ cs, const uint32_t* __restrict__ bs,
-                                                                 Consts<R> c, int akinci)
+                                                                 Consts<R> c, int akinci, const R* __restrict__ bdp)
 {
     const uint32_t t = gtid();
     const uint32_t i = t / G;
@@ -505,7 +521,10 @@ __global__ void __launch_bounds__(kBlock) k_wcsph_pressure_force(Fluid<R> f, con
                 const P4<R> pb = ldg4(bpos + j);
                 const V3<R> r = s - xyz(pb);
                 const R r2 = dot3(r, r);
-                if (r2 <= c.cull2) sum = sum - (pb.w * (dpi * (R)1)) * cubic_gradW(c, r, r2);
+                // Akinci: rho0 psi_b (p_i / rho_i^2); PCISPH model: m_b (p_i / rho_i^2 + p_b / rho_b^2)
+                // (WCSPHSolver.cpp:162-186)
+                const R q = bdp ? dpi + bdp[j] : dpi * (R)1;
+                if (r2 <= c.cull2) sum = sum - (pb.w * q) * cubic_gradW(c, r, r2);
             });
     }
     if (G > 1) sum = group_sum3<G>(sum);
@@ -733,7 +752,7 @@ __global__ void __launch_bounds__(kBlock) k_dfsph_correct(Fluid<R> f, const P4<R
             const R r2 = dot3(r, r);
             if (r2 <= c.cull2) sum = sum + (c.mass * kSum) * cubic_gradW(c, r, r2);
         });
-        const R kb = MODE == 0 ? (R)2 * ki : ki;
+        const R kb = MODE == 0 ? c.bwarm * ki : ki;
         if (akinci && fabs(kb) > c.eps)
             walk<R, G>(g, bs, pc, xi, c.h, lane, [&](uint32_t j, V3<R> s) {
                 const P4<R> pb = ldg4(bpos + j);
@@ -1028,7 +1047,7 @@ __global__ void __launch_bounds__(kBlock) k_pcisph_density_pressure(Fluid<R> f, 
     if (valid) {
         const V3<R> xi = xyz(f.predR[i]);
         const uint32_t pc = f.cell[i];
-        walk<R, G>(g, cs, pc, xi, c.h, lane, [&](uint32_t j, V3<R> s) {
+        walk<R, G, false>(g, cs, pc, xi, c.h, lane, [&](uint32_t j, V3<R> s) {
             const V3<R> r = s - xyz(ldg4(f.predR + j));
             const R r2 = dot3(r, r);
             if (r2 <= c.cull2) density += c.mass * cubic_W(c, sqrt(r2));
@@ -1068,7 +1087,8 @@ __global__ void __launch_bounds__(kBlock) k_pcisph_density_pressure(Fluid<R> f, 
 template <typename R, int G>
 __global__ void __launch_bounds__(kBlock) k_pcisph_pressure_acc(Fluid<R> f, const P4<R>* __restrict__ bpos, GridView g,
                                                                 const uint32_t* __restrict__ cs, const uint32_t* __restrict__ bs,
-                                                                Consts<R> c, int akinci, const DevScalars* __restrict__ sc)
+                                                                Consts<R> c, int akinci, const DevScalars* __restrict__ sc,
+                                                                const R* __restrict__ bdp)
 {
     if (!sc->active) return;
     const uint32_t t = gtid();
@@ -1092,12 +1112,185 @@ __global__ void __launch_bounds__(kBlock) k_pcisph_pressure_acc(Fluid<R> f, cons
                 const P4<R> pb = ldg4(bpos + j);
                 const V3<R> r = s - xyz(pb);
                 const R r2 = dot3(r, r);
-                if (r2 <= c.cull2) pacc = pacc - (pb.w * dpi) * spiky_gradW(c, r, r2);
+                // PCISPHSolver.cpp:332-356, as the WCSPH force
+                const R q = bdp ? dpi + bdp[j] : dpi;
+                if (r2 <= c.cull2) pacc = pacc - (pb.w * q) * spiky_gradW(c, r, r2);
             });
     }
     if (G > 1) pacc = group_sum3<G>(pacc);
     if (!valid || lane != 0) return;
     f.pacc[i] = P4<R>{pacc.x, pacc.y, pacc.z, 0};
+}
+
+// ===========================================================================
+// PCISPH boundary model (PCISPHBoundaryModel.cpp): boundary particles with
+// the fluid's mass, normals, and their own densities and pressures.
+// ===========================================================================
+
+// SPHSolver::computeBoundaryDensities SPHSolver.cpp:94-127 (cubic spline,
+// current positions; MODE 0), followed by WCSPHSolver::computeBoundaryPressures
+// WCSPHSolver.cpp:97-114 (MODE 1); or PCISPHSolver::predictBoundaryDensities
+// PCISPHSolver.cpp:214-247 (Poly6, predicted fluid positions) followed by the
+// boundary part of updatePressure :276-293 (MODE 2, inside the loop).
+// MODE 1 and 2 also store p / rho^2 for the pressure walks.
+template <typename R, int MODE>
+__global__ void k_bh_boundary(Boundary<R> b, Fluid<R> f, GridView g, const uint32_t* __restrict__ cs,
+                              const uint32_t* __restrict__ bs, Consts<R> c, const DevScalars* __restrict__ sc)
+{
+    if (MODE == 2 && !sc->active) return;
+    const uint32_t i = gtid();
+    if (i >= b.n) return;
+    const V3<R> xi = xyz(b.pos[i]);
+    const uint32_t pc = b.cell[i];
+    const P4<R>* fx = MODE == 2 ? f.predR : f.pos;
+    R density = 0;
+    // the fluid candidates' predicted positions (MODE 2) may lie outside the
+    // cells they are filed by: no trimming then
+    auto fluid_term = [&](uint32_t j, V3<R> s) {
+        const V3<R> r = s - xyz(ldg4(fx + j));
+        const R r2 = dot3(r, r);
+        if (r2 <= c.cull2) density += c.mass * (MODE == 2 ? poly6_W(c, r2) : cubic_W(c, sqrt(r2)));
+    };
+    if (MODE == 2) walk<R, 1, false>(g, cs, pc, xi, c.h, 0, fluid_term);
+    else walk<R, 1>(g, cs, pc, xi, c.h, 0, fluid_term);
+    walk<R, 1>(g, bs, pc, xi, c.h, 0, [&](uint32_t j, V3<R> s) {
+        const V3<R> r = s - xyz(ldg4(b.pos + j));
+        const R r2 = dot3(r, r);
+        if (r2 <= c.cull2) density += c.mass * (MODE == 2 ? poly6_W(c, r2) : cubic_W(c, sqrt(r2)));
+    });
+    b.dens[i] = density;
+    if (MODE == 0) return;
+    R p;
+    if (MODE == 1) {
+        p = fmax((R)0, c.k_eos * (pow(density / c.density0, c.gamma) - (R)1));
+    } else {
+        const R e = density - c.density0 > (R)0 ? density - c.density0 : (R)0;
+        p = b.press[i] + (R)sc->scaling * e;
+    }
+    b.press[i] = p;
+    b.dp[i] = p / (density * density);
+}
+
+// One more grid build (cell lifetimes of the PCISPH boundary model).
+static __global__ void k_bh_epoch(DevScalars* sc) { sc->grid_epoch += 1; }
+
+// Cells holding boundary points exist from the first build on.
+static __global__ void k_bh_mark_cells(uint32_t n, const uint32_t* __restrict__ key, uint32_t* __restrict__ cell_epoch)
+{
+    const uint32_t i = gtid();
+    if (i < n) atomicMin(cell_epoch + key[i], 1u);
+}
+
+// PCISPHSolver::initPressure PCISPHSolver.cpp:105-119: boundary pressures 0.
+template <typename R>
+__global__ void k_bh_zero_pressure(Boundary<R> b)
+{
+    const uint32_t i = gtid();
+    if (i >= b.n) return;
+    b.press[i] = 0;
+    b.dp[i] = 0;
+}
+
+// PCISPHBoundaryModel::correctPositions :219-316 (MODE 0: weights from the
+// current positions, WCSPH / DFSPH; MODE 1: from the predicted positions,
+// PCISPH) and ::correctPredPositions :394-448 (MODE 2: corrects the
+// predicted positions).  Boundary points closer than h/2 to the particle
+// (current positions) push it back along the weighted mean of their normals;
+// the particle's normal is always rewritten (normalised mean, NaN when no
+// point is that close, as glm::normalize of a zero vector gives).  Cells
+// must be current for the positions tested (positions rebased first).
+template <typename R, int MODE>
+__global__ void k_bh_collide(Fluid<R> f, Boundary<R> b, GridView g, const uint32_t* __restrict__ bs, Consts<R> c,
+                             const DevScalars* __restrict__ sc, uint32_t* __restrict__ cell_epoch)
+{
+    if (MODE == 2 && !sc->active) return;
+    const uint32_t i = gtid();
+    if (i >= f.n) return;
+    const V3<R> xi = xyz(f.pos[i]);
+    const uint32_t pc = f.cell[i];
+    // The reference looks the candidates up in a hash table whose cells come
+    // into existence when a point is inserted or a lookup creates them
+    // (unordered_map::operator[]), and get candidate lists at the next
+    // neighbour search: a particle in a cell that did not exist at the last
+    // search (one that left the region ever occupied, or the grid box) has
+    // no candidates, and the lookup creates the cell for the next search.
+    bool has_cands = true;
+    {
+        bool out = false;
+        if constexpr (sizeof(R) == 4) {
+            out = !(xi.x >= (R)0 && xi.x < c.h && xi.y >= (R)0 && xi.y < c.h && xi.z >= (R)0 && xi.z < c.h);
+        } else {
+            out = (int)floor((double)xi.x / c.h) - g.ox != cell_x(pc) || (int)floor((double)xi.y / c.h) - g.oy != cell_y(pc) ||
+                  (int)floor((double)xi.z / c.h) - g.oz != cell_z(pc);
+        }
+        if (out) {
+            has_cands = false;
+        } else if (cell_epoch) {
+            const uint32_t k = cell_key(g, cell_x(pc), cell_y(pc), cell_z(pc));
+            const unsigned E = sc->grid_epoch;
+            if (cell_epoch[k] > E) {
+                has_cands = false;
+                atomicMin(cell_epoch + k, E + 1);
+            }
+        }
+    }
+    const V3<R> wi = MODE == 0 ? xi : xyz(f.predR[i]);
+    const R rest = (R)0.5 * c.h;
+    V3<R> avg = {0, 0, 0};
+    R wsum = 0, w2sum = 0;
+    if (has_cands) walk<R, 1>(g, bs, pc, xi, c.h, 0, [&](uint32_t j, V3<R> s) {
+        const P4<R> pb = ldg4(b.pos + j);
+        const V3<R> rib = s - xyz(pb);
+        if (!(sqrt(dot3(rib, rib)) < rest)) return;
+        V3<R> prib;
+        if (MODE == 0) prib = rib;
+        else if constexpr (sizeof(R) == 8) prib = wi - xyz(pb);
+        else prib = rib + (wi - xi);  // the predicted position in the candidate's frame
+        const R lp = sqrt(dot3(prib, prib));
+        const R w = fmax((R)0, (rest - lp) / rest);
+        wsum += w;
+        w2sum += w * (rest - lp);
+        avg = avg + w * xyz(ldg4(b.nrm + j));
+    });
+    const V3<R> ni = avg * ((R)1 / sqrt(dot3(avg, avg)));
+    f.normal[i] = P4<R>{ni.x, ni.y, ni.z, 0};
+    if (wsum > (R)0) {
+        const V3<R> d = ((R)1 / wsum * w2sum) * ni;
+        P4<R>* tgt = MODE == 2 ? f.predR : f.pos;
+        P4<R> p = tgt[i];
+        p.x = p.x + d.x; p.y = p.y + d.y; p.z = p.z + d.z;
+        tgt[i] = p;
+    }
+}
+
+// PCISPHBoundaryModel::correctVelocities :318-392: for particles with a valid
+// normal, v = tangentialFct * v_t - normalFct * v_n of the velocity (PRED:
+// of the last predicted velocity, PCISPH).
+template <typename R, bool PRED>
+__global__ void k_bh_correct_velocities(Fluid<R> f, Consts<R> c)
+{
+    const uint32_t i = gtid();
+    if (i >= f.n) return;
+    const V3<R> ni = xyz(f.normal[i]);
+    if (!(sqrt(dot3(ni, ni)) > (R)0)) return;
+    const V3<R> u = xyz(PRED ? f.predV[i] : f.vel[i]);
+    const V3<R> nVel = dot3(u, ni) * ni;
+    const V3<R> tVel = u - nVel;
+    const V3<R> v = c.bh_tf * tVel - c.bh_nf * nVel;
+    P4<R> o = f.vel[i];
+    o.x = v.x; o.y = v.y; o.z = v.z;
+    f.vel[i] = o;
+}
+
+// Boundary normals from the host (FP64 xyz) and the model's mass as the
+// walks' boundary weight.
+template <typename R>
+__global__ void k_bh_upload(const double* __restrict__ nrm, uint32_t n, Boundary<R> b, R mass)
+{
+    const uint32_t i = gtid();
+    if (i >= n) return;
+    b.nrm[i] = P4<R>{(R)nrm[3 * i], (R)nrm[3 * i + 1], (R)nrm[3 * i + 2], 0};
+    b.pos[i].w = mass;
 }
 
 // End of one PCISPH iteration: PCISPHSolver.cpp:383 (++iterations) and the

@@ -205,7 +205,7 @@ __device__ __noinline__ V3<R> correct_sum_cells(const Fluid<R>& f, const P4<R>* 
         const R r2 = dot3(r, r);
         if (r2 <= c.cull2) sum = sum + (c.mass * kSum) * cubic_gradW(c, r, r2);
     });
-    const R kb = MODE == 0 ? (R)2 * ki : ki;
+    const R kb = MODE == 0 ? c.bwarm * ki : ki;
     if (akinci && fabs(kb) > c.eps)
         walk<R, 1>(g, bs, pc, xi, c.h, 0, [&](uint32_t j, V3<R> s) {
             const P4<R> pb = ldg4(bpos + j);
@@ -272,7 +272,7 @@ __device__ __forceinline__ V3<R> correct_sum_one(uint32_t i, const Fluid<R>& f, 
             const R kSum = ki + __ldg(kb_ + as_idx(q.w));
             if (fabs(kSum) > c.eps) sum = sum + kSum * xyz(q);
         }
-        const R kb = MODE == 0 ? (R)2 * ki : ki;
+        const R kb = MODE == 0 ? c.bwarm * ki : ki;
         if (akinci && fabs(kb) > c.eps) sum = sum + kb * xyz(L.bgrad[i]);
     } else {
         sum = correct_sum_cells<R, MODE>(f, bpos, g, cs, bs, c, akinci, i, ki, kb_);

@@ -71,6 +71,10 @@ void scene_constants(const sph_scene_desc& d, Consts<R>* out_c, LoopLimits* out_
     c.adh = (R)d.adhesion;
     for (int k = 0; k < 3; ++k) { c.cube_min[k] = (R)d.cube_min[k]; c.cube_max[k] = (R)d.cube_max[k]; }
     c.has_cube = (d.boundary_method == SPH_BOUNDARY_CUBE && d.has_cube) ? 1 : 0;
+    // warm start: Akinci boundaries take 2 k_i, the PCISPH model k_i (DFSPHSolver.cpp:646-672)
+    c.bwarm = (R)(d.boundary_method == SPH_BOUNDARY_PCISPH ? 1.0 : 2.0);
+    c.bh_nf = (R)d.bh_normal_fct;
+    c.bh_tf = (R)d.bh_tangential_fct;
     int fl = 0;
     if (d.viscosity_method > -1 && d.viscosity != 0.0) {
         if (d.viscosity_method == SPH_VISCOSITY_STANDARD) fl |= F_STD_VISC;
@@ -216,9 +220,14 @@ public:
         SPH_CUDA(cudaMallocHost((void**)&h_sc_, sizeof(DevScalars)));
         n_ = (unsigned)(hx.size() / 3);
         akinci_ = d.boundary_method == SPH_BOUNDARY_AKINCI ? 1 : 0;
-        nb_ = akinci_ ? (unsigned)(hb.size() / 3) : 0u;
+        bh_ = d.boundary_method == SPH_BOUNDARY_PCISPH ? 1 : 0;
+        hasb_ = akinci_ || bh_;
+        nb_ = hasb_ ? (unsigned)(hb.size() / 3) : 0u;
         if (n_ == 0) { fail("no fluid particles"); return SPH_ERR_INVALID; }
-        if (d.boundary_method == SPH_BOUNDARY_PCISPH) { fail("PCISPH boundary particles are not implemented"); return SPH_ERR_UNSUPPORTED; }
+        if (bh_ && hbn.size() != hb.size()) {
+            fail("the PCISPH boundary model needs a normal per boundary point (sph_ctx_add_pcisph_box / _sphere)");
+            return SPH_ERR_INVALID;
+        }
         setup_constants();
         int rc = setup_grid();
         if (rc) return rc;
@@ -248,13 +257,23 @@ public:
             SPH_CUDA(cudaMemcpyAsync(tb.p, hb.data(), hb.size() * 8, cudaMemcpyHostToDevice, st_));
             k_upload_boundary<R><<<blocks(nb_, 256), 256, 0, st_>>>(tb.p, nb_, B(0), gv_, hd_, sc_.p);
             SPH_CUDA(cudaGetLastError());
+            DevBuf<double> tn;
+            if (bh_) {
+                // PCISPH boundary model: normals, and the model's mass (the fluid's,
+                // Simulation.cpp:464-468) as the walks' boundary weight
+                SPH_CUDA(tn.alloc(hbn.size()));
+                SPH_CUDA(cudaMemcpyAsync(tn.p, hbn.data(), hbn.size() * 8, cudaMemcpyHostToDevice, st_));
+                k_bh_upload<R><<<blocks(nb_, 256), 256, 0, st_>>>(tn.p, nb_, B(0), c_.mass);
+                SPH_CUDA(cudaGetLastError());
+            }
             k_cell_count<<<blocks(nb_, 256), 256, 0, st_>>>(nb_, B(0).cell, key_.p, slot_.p, count_.p, gv_);
+            if (bh_) k_bh_mark_cells<<<blocks(nb_, 256), 256, 0, st_>>>(nb_, key_.p, cell_epoch_.p);
             rc = scan(bstarts_.p);
             if (rc) return rc;
             k_scatter<<<blocks(nb_, 256), 256, 0, st_>>>(nb_, key_.p, slot_.p, bstarts_.p, tmp_.p);
             k_gather_boundary<R><<<blocks(nb_, 256), 256, 0, st_>>>(nb_, tmp_.p, key_.p, bstarts_.p, B(0), B(1));
             SPH_CUDA(cudaGetLastError());
-            k_boundary_psi<R><<<blocks(nb_, 128), 128, 0, st_>>>(B(1), gv_, bstarts_.p, c_);
+            if (akinci_) k_boundary_psi<R><<<blocks(nb_, 128), 128, 0, st_>>>(B(1), gv_, bstarts_.p, c_);
             SPH_CUDA(cudaGetLastError());
             SPH_CUDA(cudaStreamSynchronize(st_));
         } else {
@@ -266,6 +285,7 @@ public:
             // DFSPHSolver::init DFSPHSolver.cpp:24-36
             rc = lists_ ? launch_build_lists() : launch_density(true, false);
             if (rc) return rc;
+            launch_bh_boundary(0);
         }
         SPH_CUDA(cudaStreamSynchronize(st_));
         inited = true;
@@ -394,7 +414,16 @@ public:
     int download(int field, double* out) override
     {
         if (!inited) { fail("not initialised"); return SPH_ERR_INVALID; }
-        const bool bnd = field == SPH_FIELD_BOUNDARY_POSITION || field == SPH_FIELD_BOUNDARY_VOLUME;
+        const bool bnd = field == SPH_FIELD_BOUNDARY_POSITION || field == SPH_FIELD_BOUNDARY_VOLUME ||
+                         field == SPH_FIELD_BOUNDARY_DENSITY || field == SPH_FIELD_BOUNDARY_PRESSURE;
+        if ((field == SPH_FIELD_BOUNDARY_DENSITY || field == SPH_FIELD_BOUNDARY_PRESSURE) && !bh_) {
+            fail("boundary densities and pressures exist for the PCISPH boundary model only");
+            return SPH_ERR_INVALID;
+        }
+        if ((field == SPH_FIELD_PRESSURE_ACC && pacc_.n < n_) || (field == SPH_FIELD_NORMAL && normal_.n < n_)) {
+            fail("this solver configuration keeps no such field");
+            return SPH_ERR_INVALID;
+        }
         const unsigned n = bnd ? nb_ : n_;
         const bool vec = field == SPH_FIELD_POSITION || field == SPH_FIELD_VELOCITY || field == SPH_FIELD_ACCELERATION ||
                          field == SPH_FIELD_PRESSURE_ACC || field == SPH_FIELD_NORMAL ||
@@ -423,6 +452,8 @@ public:
             case SPH_FIELD_KAPPA_V: s = f.kappav; kind = 2; break;
             case SPH_FIELD_BOUNDARY_POSITION: v4 = b.pos; kind = 1; break;
             case SPH_FIELD_BOUNDARY_VOLUME: s = b.psi; kind = 2; break;
+            case SPH_FIELD_BOUNDARY_DENSITY: s = b.dens; kind = 2; break;
+            case SPH_FIELD_BOUNDARY_PRESSURE: s = b.press; kind = 2; break;
             default: fail("unknown field"); return SPH_ERR_INVALID;
         }
         k_download<R><<<blocks(n, 256), 256, 0, st_>>>(n, v4, s, bnd ? b.id : f.id, bnd ? b.cell : f.cell, gv_, hd_, kind,
@@ -436,7 +467,16 @@ public:
     int field_view(int field, FieldView* v) override
     {
         if (!inited) { fail("not initialised"); return SPH_ERR_INVALID; }
-        const bool bnd = field == SPH_FIELD_BOUNDARY_POSITION || field == SPH_FIELD_BOUNDARY_VOLUME;
+        const bool bnd = field == SPH_FIELD_BOUNDARY_POSITION || field == SPH_FIELD_BOUNDARY_VOLUME ||
+                         field == SPH_FIELD_BOUNDARY_DENSITY || field == SPH_FIELD_BOUNDARY_PRESSURE;
+        if ((field == SPH_FIELD_BOUNDARY_DENSITY || field == SPH_FIELD_BOUNDARY_PRESSURE) && !bh_) {
+            fail("boundary densities and pressures exist for the PCISPH boundary model only");
+            return SPH_ERR_INVALID;
+        }
+        if ((field == SPH_FIELD_PRESSURE_ACC && pacc_.n < n_) || (field == SPH_FIELD_NORMAL && normal_.n < n_)) {
+            fail("this solver configuration keeps no such field");
+            return SPH_ERR_INVALID;
+        }
         Fluid<R> f = F();
         Boundary<R> b = B(1);
         FieldView o;
@@ -458,6 +498,8 @@ public:
             case SPH_FIELD_KAPPA_V: o.s = f.kappav; o.kind = 2; break;
             case SPH_FIELD_BOUNDARY_POSITION: o.v4 = b.pos; o.kind = 1; break;
             case SPH_FIELD_BOUNDARY_VOLUME: o.s = b.psi; o.kind = 2; break;
+            case SPH_FIELD_BOUNDARY_DENSITY: o.s = b.dens; o.kind = 2; break;
+            case SPH_FIELD_BOUNDARY_PRESSURE: o.s = b.press; o.kind = 2; break;
             default: fail("unknown field"); return SPH_ERR_INVALID;
         }
         o.count = (size_t)o.n * (o.kind == 2 ? 1 : 3);
@@ -602,7 +644,7 @@ private:
     int setup_grid()
     {
         GridPlan p;
-        const int rc = grid_plan(d, hx, hb, akinci_ != 0, hd_, &p, &err);
+        const int rc = grid_plan(d, hx, hb, hasb_ != 0, hd_, &p, &err);
         if (rc) return rc;
         nkeys_ = (uint32_t)p.nkeys;
         SPH_CUDA(mortx_.alloc(p.nn[0]));
@@ -632,7 +674,18 @@ private:
         const bool pci = d.simulation_method == SPH_PCISPH;
         const bool st = (c_.force_flags & F_SURFACE_TENSION) != 0;
         SPH_CUDA(predR_.alloc(pci ? n : 1)); SPH_CUDA(predV_.alloc(pci ? n : 1)); SPH_CUDA(pacc_.alloc(pci ? n : 1));
-        SPH_CUDA(normal_.alloc(st ? n : 1));
+        const bool bh = d.boundary_method == SPH_BOUNDARY_PCISPH;
+        SPH_CUDA(normal_.alloc(st || bh ? n : 1));
+        SPH_CUDA(normal2_.alloc(bh ? n : 1));
+        for (int k = 0; k < 2; ++k) SPH_CUDA(bnrm_[k].alloc(bh ? nb : 1));
+        SPH_CUDA(bdens_.alloc(bh ? nb : 1)); SPH_CUDA(bpress_.alloc(bh ? nb : 1)); SPH_CUDA(bdp_.alloc(bh ? nb : 1));
+        SPH_CUDA(cell_epoch_.alloc(bh ? nkeys_ : 1));
+        SPH_CUDA(cudaMemsetAsync(cell_epoch_.p, 0xFF, cell_epoch_.n * sizeof(uint32_t), st_));  // no cell exists yet
+        if (bh) {
+            SPH_CUDA(cudaMemsetAsync(bdens_.p, 0, nb * sizeof(R), st_));
+            SPH_CUDA(cudaMemsetAsync(bpress_.p, 0, nb * sizeof(R), st_));
+            SPH_CUDA(cudaMemsetAsync(bdp_.p, 0, nb * sizeof(R), st_));
+        }
         lists_ = d.simulation_method == SPH_DFSPH && d.neighbor_list_max > 0;
         kmax_ = lists_ ? (uint32_t)d.neighbor_list_max : 0u;
         SPH_CUDA(pairs_.alloc(lists_ ? (size_t)kmax_ * n : 1));
@@ -651,6 +704,7 @@ private:
         SPH_CUDA(sc_.alloc(1));
         SPH_CUDA(cudaMemsetAsync(sc_.p, 0, sizeof(DevScalars), st_));
         SPH_CUDA(cudaMemsetAsync(normal_.p, 0, normal_.n * sizeof(P4<R>), st_));
+        SPH_CUDA(cudaMemsetAsync(normal2_.p, 0, normal2_.n * sizeof(P4<R>), st_));
         SPH_CUDA(cudaMemsetAsync(pacc_.p, 0, pacc_.n * sizeof(P4<R>), st_));
         SPH_CUDA(cudaMemsetAsync(alpha_.p, 0, n * sizeof(R), st_));
         SPH_CUDA(cudaMemsetAsync(div_.p, 0, n * sizeof(R), st_));
@@ -659,11 +713,16 @@ private:
             Fluid<R>& f = fl_[k];
             f.pos = pos_[k].p; f.vel = vel_[k].p; f.kappa = kappa_[k].p; f.kappav = kappav_[k].p;
             f.cell = cell_[k].p; f.id = id_[k].p; f.pred = pred_[k].p;
-            f.acc = acc_.p; f.xk = xk_.p; f.predR = predR_.p; f.predV = predV_.p; f.pacc = pacc_.p; f.normal = normal_.p;
+            f.acc = acc_.p; f.xk = xk_.p; f.predR = predR_.p; f.predV = predV_.p; f.pacc = pacc_.p;
+            f.normal = (bh && k == 1) ? normal2_.p : normal_.p;
             f.rho = rho_.p; f.alpha = alpha_.p; f.div = div_.p; f.press = press_.p;
             f.n = (uint32_t)n_;
             Boundary<R>& b = bd_[k];
             b.pos = bpos_[k].p; b.cell = bcell_[k].p; b.id = bid_[k].p; b.psi = bpsi_.p; b.n = nb_;
+            b.nrm = bh ? bnrm_[k].p : nullptr;
+            b.dens = bh ? bdens_.p : nullptr;
+            b.press = bh ? bpress_.p : nullptr;
+            b.dp = bh ? bdp_.p : nullptr;
         }
         cur_ = 0;
         return SPH_OK;
@@ -686,12 +745,14 @@ private:
     int build_grid(bool move)
     {
         Fluid<R> a = F();
+        uint32_t* ce = bh_ ? cell_epoch_.p : nullptr;
+        if (bh_) run("k_bh_epoch", [&] { k_bh_epoch<<<1, 1, 0, ls_>>>(sc_.p); });
         if (move)
             run("k_cell_update", [&] { k_cell_update<R, true><<<blocks(n_, 256), 256, 0, ls_>>>(n_, a.pos, a.vel, a.cell, key_.p, slot_.p, count_.p, gv_,
-                                                                     c_.h, hd_, sc_.p); });
+                                                                     c_.h, hd_, sc_.p, ce); });
         else
             run("k_cell_update", [&] { k_cell_update<R, false><<<blocks(n_, 256), 256, 0, ls_>>>(n_, a.pos, a.vel, a.cell, key_.p, slot_.p, count_.p,
-                                                                      gv_, c_.h, hd_, sc_.p); });
+                                                                      gv_, c_.h, hd_, sc_.p, ce); });
         SPH_CUDA(cudaGetLastError());
         int rc = scan(starts_.p);
         if (rc) return rc;
@@ -724,11 +785,11 @@ private:
         withG([&](auto gt) {
             constexpr int G = decltype(gt)::value;
             if (alpha)
-                run("k_density", [&] { k_density<R, G, true, false><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_); });
+                run("k_density", [&] { k_density<R, G, true, false><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, hasb_); });
             else if (eos)
-                run("k_density", [&] { k_density<R, G, false, true><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_); });
+                run("k_density", [&] { k_density<R, G, false, true><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, hasb_); });
             else
-                run("k_density", [&] { k_density<R, G, false, false><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_); });
+                run("k_density", [&] { k_density<R, G, false, false><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, hasb_); });
         });
         SPH_CUDA(cudaGetLastError());
         return SPH_OK;
@@ -740,10 +801,53 @@ private:
         Fluid<R> f = F();
         const P4<R>* bp = bd_[1].pos;
         Lists<R> L = LS();
-        run("k_build_lists", [&] { k_build_lists<R><<<blocks(n_, kBlock), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_, L); });
+        run("k_build_lists", [&] { k_build_lists<R><<<blocks(n_, kBlock), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, hasb_, L); });
         SPH_CUDA(cudaGetLastError());
         return SPH_OK;
     }
+
+    // ---- PCISPH boundary model passes (no-ops for other boundary models) ----
+    // Boundary densities (MODE 0), + WCSPH pressures (1), or the PCISPH
+    // predicted densities and pressure update inside the loop (2).
+    void launch_bh_boundary(int mode)
+    {
+        if (!bh_ || !nb_) return;
+        Fluid<R> f = F();
+        Boundary<R> b = B(1);
+        const unsigned nbk = blocks(nb_, 128);
+        if (mode == 0) run("k_bh_boundary", [&] { k_bh_boundary<R, 0><<<nbk, 128, 0, ls_>>>(b, f, gv_, starts_.p, bstarts_.p, c_, sc_.p); });
+        else if (mode == 1) run("k_bh_boundary", [&] { k_bh_boundary<R, 1><<<nbk, 128, 0, ls_>>>(b, f, gv_, starts_.p, bstarts_.p, c_, sc_.p); });
+        else run("k_bh_boundary", [&] { k_bh_boundary<R, 2><<<nbk, 128, 0, ls_>>>(b, f, gv_, starts_.p, bstarts_.p, c_, sc_.p); });
+    }
+    // Positions and cells after the integration (and MOVE: after the DFSPH
+    // position update), then PCISPHBoundaryModel::correctPositions (MODE 0 /
+    // 1) and, when VEL, ::correctVelocities (PRED for PCISPH).
+    template <bool MOVE, int MODE, bool VEL, bool PRED> void launch_bh_after_move()
+    {
+        Fluid<R> f = F();
+        // PCISPH: the predicted positions move into the new cell frames too
+        P4<R>* carry = MODE == 1 ? f.predR : nullptr;
+        run("k_cell_update", [&] { k_cell_update<R, MOVE, false><<<blocks(n_, 256), 256, 0, ls_>>>(n_, f.pos, f.vel, f.cell, key_.p, slot_.p,
+                                                                                             count_.p, gv_, c_.h, hd_, sc_.p, nullptr,
+                                                                                             carry); });
+        run("k_bh_collide", [&] { k_bh_collide<R, MODE><<<blocks(n_, 128), 128, 0, ls_>>>(f, B(1), gv_, bstarts_.p, c_, sc_.p,
+                                                                                          cell_epoch_.p); });
+        if (VEL) run("k_bh_correct_velocities", [&] { k_bh_correct_velocities<R, PRED><<<blocks(n_, 256), 256, 0, ls_>>>(f, c_); });
+    }
+    // DFSPHSolver::step :51-57: correctVelocities after predictVelocities.
+    void launch_bh_velocities()
+    {
+        if (bh_) run("k_bh_correct_velocities", [&] { k_bh_correct_velocities<R, false><<<blocks(n_, 256), 256, 0, ls_>>>(F(), c_); });
+    }
+    // updatePositions, then (PCISPH boundary model) correctPositions
+    // DFSPHSolver.cpp:65-75, then the grid build.
+    int dfsph_move_and_build()
+    {
+        if (!bh_) return build_grid(true);
+        launch_bh_after_move<true, 0, false, false>();
+        return build_grid(false);
+    }
+    const R* bdp() const { return bh_ ? bdp_.p : nullptr; }
 
     // DFSPHSolver::step DFSPHSolver.cpp:38-112 over the pair lists.
     int dfsph_step_lists()
@@ -757,26 +861,28 @@ private:
             Lists<R> L = LS();
             run("k_dfsph_cfl", [&] { k_dfsph_cfl<R><<<blocks(n_, 256), 256, 0, ls_>>>(f, c_, sc_.p, lim_, partials_.p); });
             run("k_dfsph_predict_v_warm", [&] { k_dfsph_predict_v_warm_list<R><<<blocks(n_, 256), 256, 0, ls_>>>(f, c_, sc_.p, L.kbuf); });
-            run("k_dfsph_correct_list", [&] { k_dfsph_correct_list<R, 0><<<nb, kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_, sc_.p, L); });
+            launch_bh_velocities();
+            run("k_dfsph_correct_list", [&] { k_dfsph_correct_list<R, 0><<<nb, kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, hasb_, sc_.p, L); });
             SPH_CUDA(cudaGetLastError());
             // correctDensityError DFSPHSolver.cpp:311-406
             rc = solve_loop(1,
                 [&](cudaGraphConditionalHandle h) {
                     run("k_dfsph_predict_density_list", [&] { k_dfsph_predict_density_list<R, true><<<nb, kBlock, 0, ls_>>>(
-                        f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_, sc_.p, lim_, partials_.p, h, L); });
+                        f, bp, gv_, starts_.p, bstarts_.p, c_, hasb_, sc_.p, lim_, partials_.p, h, L); });
                 },
                 [&](cudaGraphConditionalHandle h) {
-                    run("k_dfsph_correct_list", [&] { k_dfsph_correct_list<R, 1><<<nb, kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_, sc_.p, L); });
+                    run("k_dfsph_correct_list", [&] { k_dfsph_correct_list<R, 1><<<nb, kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, hasb_, sc_.p, L); });
                     run("k_dfsph_predict_density_list", [&] { k_dfsph_predict_density_list<R, false><<<nb, kBlock, 0, ls_>>>(
-                        f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_, sc_.p, lim_, partials_.p, h, L); });
+                        f, bp, gv_, starts_.p, bstarts_.p, c_, hasb_, sc_.p, lim_, partials_.p, h, L); });
                 },
                 lim_.minIt, lim_.maxIt);
             if (rc) return rc;
         }
-        rc = build_grid(true);  // updatePositions + fill grid + neighbour search
+        rc = dfsph_move_and_build();  // updatePositions + fill grid + neighbour search
         if (rc) return rc;
         rc = launch_build_lists();  // computeDensities + computeAlpha + pair lists
         if (rc) return rc;
+        launch_bh_boundary(0);
         {
             Fluid<R> f = F();
             const P4<R>* bp = bd_[1].pos;
@@ -785,12 +891,12 @@ private:
             rc = solve_loop(2,
                 [&](cudaGraphConditionalHandle h) {
                     run("k_dfsph_divergence_list", [&] { k_dfsph_divergence_list<R, true><<<nb, kBlock, 0, ls_>>>(
-                        f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_, sc_.p, lim_, partials_.p, h, L); });
+                        f, bp, gv_, starts_.p, bstarts_.p, c_, hasb_, sc_.p, lim_, partials_.p, h, L); });
                 },
                 [&](cudaGraphConditionalHandle h) {
-                    run("k_dfsph_correct_list", [&] { k_dfsph_correct_list<R, 2><<<nb, kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_, sc_.p, L); });
+                    run("k_dfsph_correct_list", [&] { k_dfsph_correct_list<R, 2><<<nb, kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, hasb_, sc_.p, L); });
                     run("k_dfsph_divergence_list", [&] { k_dfsph_divergence_list<R, false><<<nb, kBlock, 0, ls_>>>(
-                        f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_, sc_.p, lim_, partials_.p, h, L); });
+                        f, bp, gv_, starts_.p, bstarts_.p, c_, hasb_, sc_.p, lim_, partials_.p, h, L); });
                 },
                 lim_.minItV, lim_.maxIt);
             if (rc) return rc;
@@ -903,10 +1009,11 @@ private:
             run("k_dfsph_cfl", [&] { k_dfsph_cfl<R><<<blocks(n_, 256), 256, 0, ls_>>>(f, c_, sc_.p, lim_, partials_.p); });
             run("k_dfsph_predict_v_warm", [&] { k_dfsph_predict_v_warm<R><<<blocks(n_, 256), 256, 0, ls_>>>(f, c_, sc_.p); });
             SPH_CUDA(cudaGetLastError());
+            launch_bh_velocities();
             const P4<R>* bp = bd_[1].pos;
             withG([&](auto gt) {
                 constexpr int G = decltype(gt)::value;
-                run("k_dfsph_correct", [&] { k_dfsph_correct<R, G, 0><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_, sc_.p); });
+                run("k_dfsph_correct", [&] { k_dfsph_correct<R, G, 0><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, hasb_, sc_.p); });
             });
             SPH_CUDA(cudaGetLastError());
             // correctDensityError DFSPHSolver.cpp:311-406
@@ -915,25 +1022,26 @@ private:
                     withG([&](auto gt) {
                         constexpr int G = decltype(gt)::value;
                         run("k_dfsph_predict_density", [&] { k_dfsph_predict_density<R, G, true><<<wblocks(), kBlock, 0, ls_>>>(
-                            f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_, sc_.p, lim_, partials_.p, h); });
+                            f, bp, gv_, starts_.p, bstarts_.p, c_, hasb_, sc_.p, lim_, partials_.p, h); });
                     });
                 },
                 [&](cudaGraphConditionalHandle h) {
                     withG([&](auto gt) {
                         constexpr int G = decltype(gt)::value;
-                        run("k_dfsph_correct", [&] { k_dfsph_correct<R, G, 1><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_,
+                        run("k_dfsph_correct", [&] { k_dfsph_correct<R, G, 1><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, hasb_,
                                                                                  sc_.p); });
                         run("k_dfsph_predict_density", [&] { k_dfsph_predict_density<R, G, false><<<wblocks(), kBlock, 0, ls_>>>(
-                            f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_, sc_.p, lim_, partials_.p, h); });
+                            f, bp, gv_, starts_.p, bstarts_.p, c_, hasb_, sc_.p, lim_, partials_.p, h); });
                     });
                 },
                 lim_.minIt, lim_.maxIt);
             if (rc) return rc;
         }
-        rc = build_grid(true);  // updatePositions + fill grid + neighbour search
+        rc = dfsph_move_and_build();  // updatePositions + fill grid + neighbour search
         if (rc) return rc;
         rc = launch_density(true, false);  // computeDensities + computeAlpha
         if (rc) return rc;
+        launch_bh_boundary(0);
         {
             Fluid<R> f = F();
             const P4<R>* bp = bd_[1].pos;
@@ -943,16 +1051,16 @@ private:
                     withG([&](auto gt) {
                         constexpr int G = decltype(gt)::value;
                         run("k_dfsph_divergence", [&] { k_dfsph_divergence<R, G, true><<<wblocks(), kBlock, 0, ls_>>>(
-                            f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_, sc_.p, lim_, partials_.p, h); });
+                            f, bp, gv_, starts_.p, bstarts_.p, c_, hasb_, sc_.p, lim_, partials_.p, h); });
                     });
                 },
                 [&](cudaGraphConditionalHandle h) {
                     withG([&](auto gt) {
                         constexpr int G = decltype(gt)::value;
-                        run("k_dfsph_correct", [&] { k_dfsph_correct<R, G, 2><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_,
+                        run("k_dfsph_correct", [&] { k_dfsph_correct<R, G, 2><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, hasb_,
                                                                                  sc_.p); });
                         run("k_dfsph_divergence", [&] { k_dfsph_divergence<R, G, false><<<wblocks(), kBlock, 0, ls_>>>(
-                            f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_, sc_.p, lim_, partials_.p, h); });
+                            f, bp, gv_, starts_.p, bstarts_.p, c_, hasb_, sc_.p, lim_, partials_.p, h); });
                     });
                 },
                 lim_.minItV, lim_.maxIt);
@@ -971,16 +1079,19 @@ private:
         if (rc) return rc;
         rc = launch_density(false, true);
         if (rc) return rc;
+        launch_bh_boundary(1);
         Fluid<R> f = F();
         const P4<R>* bp = bd_[1].pos;
+        const R* dp = bdp();
         withG([&](auto gt) {
             constexpr int G = decltype(gt)::value;
-            run("k_wcsph_pressure_force", [&] { k_wcsph_pressure_force<R, G><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_); });
+            run("k_wcsph_pressure_force", [&] { k_wcsph_pressure_force<R, G><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, hasb_, dp); });
         });
         SPH_CUDA(cudaGetLastError());
         rc = launch_npforces();
         if (rc) return rc;
         run("k_integrate", [&] { k_integrate<R, false><<<blocks(n_, 256), 256, 0, ls_>>>(f, gv_, hd_, c_, sc_.p); });
+        if (bh_) launch_bh_after_move<false, 0, true, false>();  // WCSPHSolver.cpp:62-72
         run("k_finish_step", [&] { k_finish_step<<<1, 1, 0, ls_>>>(sc_.p); });
         SPH_CUDA(cudaGetLastError());
         return SPH_OK;
@@ -993,27 +1104,35 @@ private:
         if (rc) return rc;
         rc = launch_density(false, false);
         if (rc) return rc;
+        launch_bh_boundary(0);
         rc = launch_npforces();
         if (rc) return rc;
         Fluid<R> f = F();
         const P4<R>* bp = bd_[1].pos;
+        const R* dp = bdp();
         run("k_pcisph_init", [&] { k_pcisph_init<R><<<blocks(n_, 256), 256, 0, ls_>>>(f); });
+        if (bh_ && nb_) run("k_bh_zero_pressure", [&] { k_bh_zero_pressure<R><<<blocks(nb_, 256), 256, 0, ls_>>>(B(1)); });
         rc = solve_loop(1,
             [&](cudaGraphConditionalHandle h) { run("k_pcisph_loop_begin", [&] { k_pcisph_loop_begin<<<1, 1, 0, ls_>>>(sc_.p, lim_, h); }); },
             [&](cudaGraphConditionalHandle h) {
                 run("k_pcisph_predict", [&] { k_pcisph_predict<R><<<blocks(n_, 256), 256, 0, ls_>>>(f, c_, sc_.p); });
+                if (bh_)  // correctPredPositions PCISPHSolver.cpp:367-377
+                    run("k_bh_collide", [&] { k_bh_collide<R, 2><<<blocks(n_, 128), 128, 0, ls_>>>(f, B(1), gv_, bstarts_.p, c_, sc_.p,
+                                                                                              cell_epoch_.p); });
                 withG([&](auto gt) {
                     constexpr int G = decltype(gt)::value;
                     run("k_pcisph_density_pressure", [&] { k_pcisph_density_pressure<R, G><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_,
-                                                                                   akinci_, sc_.p, lim_, partials_.p); });
-                    run("k_pcisph_pressure_acc", [&] { k_pcisph_pressure_acc<R, G><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, akinci_,
-                                                                               sc_.p); });
+                                                                                   hasb_, sc_.p, lim_, partials_.p); });
+                    launch_bh_boundary(2);
+                    run("k_pcisph_pressure_acc", [&] { k_pcisph_pressure_acc<R, G><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, hasb_,
+                                                                               sc_.p, dp); });
                 });
                 run("k_pcisph_loop_next", [&] { k_pcisph_loop_next<<<1, 1, 0, ls_>>>(sc_.p, lim_, h); });
             },
             lim_.minIt, lim_.maxIt);
         if (rc) return rc;
         run("k_integrate", [&] { k_integrate<R, true><<<blocks(n_, 256), 256, 0, ls_>>>(f, gv_, hd_, c_, sc_.p); });
+        if (bh_) launch_bh_after_move<false, 1, true, true>();  // PCISPHSolver.cpp:65-75
         run("k_finish_step", [&] { k_finish_step<<<1, 1, 0, ls_>>>(sc_.p); });
         SPH_CUDA(cudaGetLastError());
         return SPH_OK;
@@ -1061,7 +1180,9 @@ private:
     GridView gv_{};
     double hd_ = 0, mass_ = 0;
     unsigned n_ = 0, nb_ = 0;
-    int akinci_ = 0;
+    int akinci_ = 0;   // Akinci boundary model: boundary terms in the forces too
+    int bh_ = 0;       // PCISPH boundary model
+    int hasb_ = 0;     // boundary particles take part in the solver sums
     int device_ = 0;
     int G_ = 1;
     uint32_t nkeys_ = 0;
@@ -1083,8 +1204,11 @@ private:
     DevBuf<P4<R>> pos_[2], vel_[2], bpos_[2];
     DevBuf<R> kappa_[2], kappav_[2], pred_[2];
     DevBuf<uint32_t> cell_[2], id_[2], bcell_[2], bid_[2];
-    DevBuf<P4<R>> acc_, xk_, predR_, predV_, pacc_, normal_;
+    DevBuf<P4<R>> acc_, xk_, predR_, predV_, pacc_, normal_, normal2_;
     DevBuf<R> rho_, alpha_, div_, press_, bpsi_;
+    DevBuf<P4<R>> bnrm_[2];
+    DevBuf<R> bdens_, bpress_, bdp_;
+    DevBuf<uint32_t> cell_epoch_;  // PCISPH boundary model: first grid build at which each cell exists
     DevBuf<uint32_t> mortx_, morty_, key_, slot_, tmp_, count_, starts_, bstarts_, tile_sums_;
     DevBuf<double> partials_;
     DevBuf<P4<R>> pairs_, bgrad_;

@@ -24,6 +24,8 @@ namespace sph {
 // Host restatements of the scene-construction helpers (sph_api.cu).
 long long sample_box(double support_radius, const double mn[3], const double mx[3], double* out);
 long long sample_sphere(double particle_radius, const double c[3], double radius, double* out);
+long long sample_pcisph_box(double support_radius, const double mn[3], const double mx[3], int inverted, double* out,
+                            double* normals);
 long long fluid_block(double r, const double mn[3], const double mx[3], double* out);
 
 // Where a downloadable field lives on the device (sorted order), for
@@ -47,6 +49,7 @@ struct SceneBase {
     sph_scene_desc d{};
     std::string err;
     std::vector<double> hx, hv, hb;   // staged points before init
+    std::vector<double> hbn;          // PCISPH boundary model: a normal per boundary point
     bool inited = false;
     virtual ~SceneBase() {}
     void fail(const std::string& m) { err = m; }

@@ -23,7 +23,7 @@ def L():
 def header_functions():
     src = open(os.path.join(ROOT, "include", "sph_gb300.h")).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    return sorted(set(re.findall(r"^\s*(?:const\s+)?[a-z_ ]+\**\s*\**(sph_[a-z0-9_]+)\s*\(", src, flags=re.M)))
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?[a-z_ ]+?[\s*]+(sph_[a-z0-9_]+)\s*\(", src, flags=re.M)))
 
 
 def test_header_symbols_exported(L):
@@ -71,3 +71,15 @@ def test_fluid_block_matches_oracle(L):
     a = sph_gb300.fluid_block(0.01, (0, 0, 0), (0.5, 0.5, 0.5))
     assert a.shape == (15625, 3)
     assert np.array_equal(a, oracle.fluid_block(0.01, (0, 0, 0), (0.5, 0.5, 0.5)))
+
+
+def test_pcisph_model_sampler_matches_oracle():
+    """The library's PCISPHBoundaryModel::sampleCube (points and normals, both
+    orientations) equals the oracle's bit for bit."""
+    import oracle
+
+    for mn, mx in [((0, 0, 0), (0.6, 0.6, 0.6)), ((-0.1, 0.2, 0.05), (0.7, 0.55, 0.33))]:
+        for inv in (True, False):
+            a, an = sph_gb300.sample_pcisph_box(0.08, mn, mx, inv)
+            b, bn = oracle.sample_bh_box(0.08, mn, mx, inv)
+            assert np.array_equal(a, b) and np.array_equal(an, bn)

@@ -15,23 +15,40 @@ import pytest
 
 import oracle
 import sph_gb300
-from scenes import SCENES, jitter, scene
+from scenes import SCENES, jitter, scene, scene_extra
 from util import golden, relerr
 
 pytestmark = pytest.mark.gpu
 
 DFSPH_SCENES = [n for n in SCENES if SCENES[n]["params"]["method"] == 2]
 STEP_FIELDS = ("x", "v", "rho", "p", "alpha", "div", "pred", "k", "kv", "pacc")
+# PCISPH boundary model: fluid normals (NaN where no boundary point was within
+# h/2), boundary densities and pressures
+BH_FIELDS = ("normal", "bdens", "bpress")
+
+
+def nan_relerr(a, b):
+    """relerr over the entries finite in both; inf when NaN patterns differ."""
+    a, b = np.ravel(a), np.ravel(b)
+    if not np.array_equal(np.isnan(a), np.isnan(b)):
+        return np.inf
+    m = ~np.isnan(b)
+    return relerr(a[m], b[m]) if m.any() else 0.0
 
 
 def gpu_scene(name, precision="f64", G=0, graph=False, lists=64):
     params, x, boxes, spheres = scene(name)
+    v, bh_boxes, bh_spheres = scene_extra(name, x)
     s = sph_gb300.Scene(precision=precision, threads_per_particle=G, neighbor_list_max=lists, **params)
-    s.set_fluid(x)
+    s.set_fluid(x, v)
     for mn, mx in boxes:
         s.add_boundary_box(mn, mx)
     for c, r in spheres:
         s.add_boundary_sphere(c, r)
+    for mn, mx, inv in bh_boxes:
+        s.add_pcisph_box(mn, mx, inv)
+    for c, r, inv in bh_spheres:
+        s.add_pcisph_sphere(c, r, inv)
     s.init()
     if graph:
         s.set_graph(True)
@@ -42,6 +59,8 @@ def gpu_scene(name, precision="f64", G=0, graph=False, lists=64):
 def test_f64_init_matches_reference(gpu_lib, name):
     g = golden(name)
     s = gpu_scene(name)
+    if SCENES[name]["params"]["boundary"] == 1:
+        assert np.array_equal(s.get("bx").ravel(), g["b.x"])
     if "b.psi" in g:
         assert np.array_equal(s.get("bx").ravel(), g["b.x"])
         assert relerr(s.get("psi"), g["b.psi"]) <= 1e-10
@@ -58,7 +77,7 @@ def test_neighbour_sets_bit_exact(gpu_lib, name):
     assert np.array_equal(nb["cell_rank"], g["init.cell_rank"])
     assert np.array_equal(nb["nbr_off"], g["init.nbr_off"])
     assert np.array_equal(nb["nbr"], g["init.nbr"])
-    if SCENES[name]["params"]["boundary"] == 2:
+    if SCENES[name]["params"]["boundary"] in (1, 2):
         # (the reference's cube model also files its two corner points as
         # boundary points in the grid; no walk ever reads them)
         assert np.array_equal(nb["bnbr_off"], g["init.bnbr_off"])
@@ -77,6 +96,11 @@ def test_f64_steps_match_reference(gpu_lib, name, lists):
             key = f"s{step}.{f}"
             if key in g:
                 e = relerr(s.get(f), g[key])
+                assert e <= 1e-5, (name, key, e)
+        for f in BH_FIELDS:
+            key = f"s{step}.{f}"
+            if key in g:
+                e = nan_relerr(s.get(f), g[key])
                 assert e <= 1e-5, (name, key, e)
         st = s.stats()
         assert abs(st["dt"] - g[f"s{step}.dt"][0]) <= 1e-12 * g[f"s{step}.dt"][0]
@@ -194,3 +218,22 @@ def test_pair_list_overflow_falls_back_to_cell_walk(gpu_lib, precision):
         assert relerr(b.get(f), a.get(f)) <= tol, f
     assert b.stats()["list_overflow"] > 0 and a.stats()["list_overflow"] == 0
     assert a.stats()["list_pairs"] > 20 * a.n
+
+
+@pytest.mark.parametrize("name", ["wcsph_bh", "pcisph_bh", "dfsph_bh"])
+def test_pcisph_boundary_model_twelve_steps_match_oracle(gpu_lib, name):
+    """PCISPH boundary model, FP64, 12 steps with particles colliding every
+    step: positions, velocities, densities, normals (NaN where no boundary
+    point was within h/2) and boundary densities / pressures against the
+    oracle within 1e-5 relative, identical iteration counts."""
+    params, x, boxes, spheres = scene(name)
+    v, bh_boxes, bh_spheres = scene_extra(name, x)
+    o = oracle.OracleScene(params, x, v, bh_boxes=bh_boxes, bh_spheres=bh_spheres)
+    s = gpu_scene(name)
+    for step in range(12):
+        o.step(1)
+        s.step(1)
+        for f in ("x", "v", "rho", "normal", "bdens", "bpress"):
+            e = nan_relerr(s.get(f), o.get(f))
+            assert e <= 1e-5, (name, step, f, e)
+        assert s.stats()["iterations"] == o.scalar("iterations"), (name, step)
