@@ -104,6 +104,11 @@ def lib():
         L.orc_sample_bh_box.argtypes = [ctypes.c_double, dp, dp, ctypes.c_int, dp, dp]
         L.orc_sample_bh_box.restype = ctypes.c_longlong
         L.orc_perturb.argtypes = [vp, ctypes.c_double, ctypes.c_double, ctypes.c_ulonglong]
+        L.orc_add_emitter.argtypes = [vp, ctypes.c_int, ctypes.c_uint, dp, ctypes.c_double, dp, ctypes.c_double,
+                                      ctypes.c_double, ctypes.c_double, ctypes.c_double]
+        L.orc_pause_emitters.argtypes = [vp, ctypes.c_int]
+        L.orc_emitter_group.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, dp]
+        L.orc_emitter_group.restype = ctypes.c_longlong
         L.orc_init.argtypes = [vp]
         L.orc_step.argtypes = [vp, ctypes.c_int]
         L.orc_num_fluid.argtypes = [vp]
@@ -161,6 +166,27 @@ def sample_bh_box(h, mn, mx, inverted=True):
     return pts, nrm
 
 
+def emitter_group(type, particle_radius, width, height=0.0):
+    """Emitter::buildSquareGroup (type 0) / buildCircleGroup (type 1)."""
+    L = lib()
+    n = L.orc_emitter_group(int(type), float(particle_radius), float(width), float(height), None)
+    out = np.zeros((n, 3))
+    if n:
+        L.orc_emitter_group(int(type), float(particle_radius), float(width), float(height), _dptr(out))
+    return out
+
+
+EMITTER_KEYS = ("type", "num", "position", "velocity", "rotation", "start", "width", "height", "spacing")
+
+
+def _emitter_args(e):
+    """An emitter dict (EMITTER_KEYS; rotation (w, x, y, z)) as flat values."""
+    rot = e.get("rotation", (1.0, 0.0, 0.0, 0.0))
+    return (int(e["type"]), int(e["num"]), [float(t) for t in e["position"]], float(e["velocity"]),
+            [float(t) for t in rot], float(e.get("start", 0.0)), float(e.get("width", 0.0)),
+            float(e.get("height", 0.0)), float(e.get("spacing", 1.0)))
+
+
 def fluid_block(radius, mn, mx):
     """Lattice of Simulation::buildFluidBlock (spacing 2r from min + r)."""
     L = lib()
@@ -192,7 +218,8 @@ def sample_sphere(particle_radius, c, radius):
 class OracleScene:
     """One scene of the C restatement (one fluid model, one boundary model)."""
 
-    def __init__(self, params: dict, x, v=None, boxes=(), spheres=(), points=None, bh_boxes=(), bh_spheres=()):
+    def __init__(self, params: dict, x, v=None, boxes=(), spheres=(), points=None, bh_boxes=(), bh_spheres=(),
+                 emitters=()):
         L = lib()
         self.params = dict(params)
         self._p = make_params(**params)
@@ -203,6 +230,11 @@ class OracleScene:
         v = np.zeros_like(x) if v is None else np.ascontiguousarray(v, dtype=np.float64).reshape(-1, 3)
         if L.orc_set_fluid(self.h, _dptr(x), _dptr(v), x.shape[0]) != 0:
             raise RuntimeError("orc_set_fluid failed")
+        for e in emitters:
+            t, num, pos, vel, rot, start, w, hgt, sp = _emitter_args(e)
+            rot = np.array(rot)
+            if L.orc_add_emitter(self.h, t, num, _dptr(_vec3(pos)), vel, _dptr(rot), start, w, hgt, sp) != 0:
+                raise RuntimeError("orc_add_emitter failed")
         for mn, mx in boxes:
             L.orc_add_box(self.h, _dptr(_vec3(mn)), _dptr(_vec3(mx)))
         for c, r in spheres:
@@ -244,6 +276,10 @@ class OracleScene:
         if rc != 0:
             raise KeyError(field)
         return out
+
+    def pause_emitters(self, pause=True):
+        if lib().orc_pause_emitters(self.h, int(bool(pause))) != 0:
+            raise RuntimeError("orc_pause_emitters failed")
 
     def perturb(self, dx, dv, seed):
         """Test instrument: add U(-dx, dx) to positions, U(-dv, dv) to velocities."""
@@ -306,7 +342,7 @@ def read_dump(path):
 
 
 def run_reference(params: dict, x, v=None, boxes=(), spheres=(), steps=1, dump_neighbors=False,
-                  dump_every=1, timed=False, threads=1, workdir=None, bh_boxes=(), bh_spheres=()):
+                  dump_every=1, timed=False, threads=1, workdir=None, bh_boxes=(), bh_spheres=(), emitters=()):
     """Run the reference's own solver on the scene and return its dump."""
     exe = REF_TIMED if timed else REF_PARITY
     if not os.path.exists(exe):
@@ -346,6 +382,10 @@ def run_reference(params: dict, x, v=None, boxes=(), spheres=(), steps=1, dump_n
             lines.append("bh_box " + " ".join(repr(float(t)) for t in list(mn) + list(mx)) + f" {int(inv)}")
         for c, r, inv in bh_spheres:
             lines.append("bh_sphere " + " ".join(repr(float(t)) for t in list(c) + [r]) + f" {int(inv)}")
+        for e in emitters:
+            t, num, pos, vel, rot, start, w, hgt, sp = _emitter_args(e)
+            lines.append("emitter " + " ".join([str(t), str(num)] + [repr(float(q)) for q in list(pos) + [vel] + list(rot)
+                                                                     + [start, w, hgt, sp]]))
         scene = os.path.join(td, "scene.txt")
         with open(scene, "w") as f:
             f.write("\n".join(lines) + "\n")

@@ -103,6 +103,8 @@ struct Spec {
     double cube[6] = {0, 0, 0, 1, 1, 1};
     std::vector<std::vector<double>> boxes, spheres;
     std::vector<std::vector<double>> bh_boxes, bh_spheres;  // + inverted flag
+    // type num rx ry rz v qw qx qy qz start width height spacing
+    std::vector<std::vector<double>> emitters;
     double bh_normal_fct = 0, bh_tang_fct = 1;
     std::string fluid, out;
     int steps = 1;
@@ -150,6 +152,7 @@ static Spec read_spec(const char* path)
         else if (k == "sphere") { std::vector<double> b(4); for (double& c : b) is >> c; s.spheres.push_back(b); }
         else if (k == "bh_box") { std::vector<double> b(7); for (double& c : b) is >> c; s.bh_boxes.push_back(b); }
         else if (k == "bh_sphere") { std::vector<double> b(5); for (double& c : b) is >> c; s.bh_spheres.push_back(b); }
+        else if (k == "emitter") { std::vector<double> b(14); for (double& c : b) is >> c; s.emitters.push_back(b); }
         else if (k == "bh_normal_fct") is >> s.bh_normal_fct;
         else if (k == "bh_tang_fct") is >> s.bh_tang_fct;
         else if (k == "fluid") is >> s.fluid;
@@ -323,6 +326,11 @@ int main(int argc, char** argv)
     sim->setAdhesionMethod(s.adh_method);
 
     FluidModel* fm = sim->addFluidModel(pos, vel);
+    // emitters as importScene adds them, before the fluid's forces
+    // (src/Simulation.cpp:403-418, SceneLoader.cpp:123-139)
+    for (auto& e : s.emitters)
+        fm->addEmitter((unsigned)e[0], (unsigned)e[1], Vector3r(e[2], e[3], e[4]), e[5], Quat4r(e[6], e[7], e[8], e[9]),
+                       e[10], e[11], e[12], e[13]);
     fm->setRefDensity(s.density0);
     if (s.visc_method > -1 && s.visc != 0.0) fm->setViscosityForce(s.visc, s.bvisc);
     if (s.st_method > -1 && s.st != 0.0) fm->setSurfaceTensionForce(s.st);

@@ -290,6 +290,20 @@ struct orc_scene {
     double maxVel;
     grid g;
     int inited;
+    /* emitters (FluidModel.h:28, Emitter.h:9-40): n is numActiveParticles,
+     * cap is numParticles (initial fluid plus every emitter's reservation) */
+    unsigned cap;
+    unsigned nem;
+    struct orc_emitter {
+        int type;
+        unsigned numParticles;
+        v3 r;
+        double v, rot[4];            /* rot: w, x, y, z */
+        double nextTimeEmit, spacing;
+        int pause;
+        v3* group;
+        unsigned ng;
+    } em[64];
 };
 
 static void* xcalloc(size_t n, size_t sz) { return calloc(n ? n : 1, sz); }
@@ -993,6 +1007,56 @@ static void dfsph_update_time_step(orc_scene* s)
     s->ts = newTs;
 }
 
+/* ------------------------------------------------------------------------ */
+/* Emitters (src/Emitter.cpp)                                                */
+/* ------------------------------------------------------------------------ */
+
+/* GLM's quat * vec3 for a unit quaternion (w, u): v + ((u x v) w + u x (u x v)) 2 */
+static v3 vcross(v3 a, v3 b) { return V(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y); }
+static v3 quat_rotate(const double q[4], v3 v)
+{
+    const v3 u = V(q[1], q[2], q[3]);
+    const v3 uv = vcross(u, v);
+    const v3 uuv = vcross(u, uv);
+    return vadd(v, vmul(vadd(vmul(uv, q[0]), uuv), 2.0));
+}
+
+/* Emitter::emitSquare / emitCircle Emitter.cpp:99-161 (identical bodies) */
+static void emitter_emit(orc_scene* s, struct orc_emitter* e, double timeOffset)
+{
+    const double dist = 2.0 * s->prm.radius;
+    const unsigned numActiveParticles = s->n;
+    unsigned id = numActiveParticles;
+    if (numActiveParticles + e->ng <= numActiveParticles + e->numParticles) {
+        for (unsigned i = 0; i < e->ng; ++i) {
+            v3 velocity = V(0, 0, e->v);
+            const v3 g = V(s->prm.gravity[0], s->prm.gravity[1], s->prm.gravity[2]);
+            v3 position = vadd(e->group[i], smul(timeOffset, vadd(velocity, vmul(g, timeOffset))));
+            position = quat_rotate(e->rot, position);
+            velocity = quat_rotate(e->rot, velocity);
+            position = vadd(position, e->r);
+            s->x[id] = position;
+            s->v[id] = velocity;
+            ++id;
+        }
+        s->n = numActiveParticles + e->ng;   /* FluidModel::setNumActiveParticles */
+        e->numParticles -= e->ng;
+        e->nextTimeEmit += e->spacing * 1.105 * dist / e->v;
+    }
+}
+
+/* Simulation::emitParticles -> FluidModel::emitParticles -> Emitter::
+ * emitParticles (Simulation.cpp:325-329, FluidModel.cpp:145-149,
+ * Emitter.cpp:85-97) */
+static void emit_particles(orc_scene* s)
+{
+    const double time = s->time;
+    for (unsigned k = 0; k < s->nem; ++k) {
+        struct orc_emitter* e = &s->em[k];
+        if (time >= e->nextTimeEmit && !e->pause) emitter_emit(s, e, time - e->nextTimeEmit);
+    }
+}
+
 /* DFSPHSolver::step DFSPHSolver.cpp:38-112 */
 static void dfsph_step(orc_scene* s)
 {
@@ -1004,6 +1068,7 @@ static void dfsph_step(orc_scene* s)
     dfsph_correct_density_error(s);
     dfsph_update_positions(s);
     if (bh(s)) bh_correct_positions(s, 0);       /* :65-75 */
+    emit_particles(s);                           /* :77 */
     grid_build(s);
     compute_densities(s);
     if (bh(s)) bh_boundary_densities(s);         /* SPHSolver::computeDensities :129-139 */
@@ -1082,6 +1147,7 @@ static void wcsph_step(orc_scene* s)
         bh_correct_positions(s, 0);
         bh_correct_velocities(s, 0);
     }
+    emit_particles(s);                           /* :75 */
     s->time = s->time + s->ts;
 }
 
@@ -1261,6 +1327,7 @@ static void pcisph_step(orc_scene* s)
         bh_correct_positions(s, 1);
         bh_correct_velocities(s, 1);
     }
+    emit_particles(s);                           /* :78 */
     s->time = s->time + s->ts;
 }
 
@@ -1321,20 +1388,38 @@ void orc_destroy(orc_scene* s)
     free(s->alpha); free(s->div); free(s->pred); free(s->k); free(s->kv);
     free(s->predR); free(s->predV); free(s->pacc); free(s->normal);
     free(s->bx); free(s->psi); free(s->bw); free(s->bn); free(s->bdens); free(s->bpress);
+    for (unsigned k = 0; k < s->nem; ++k) free(s->em[k].group);
     grid_free(&s->g);
     free(s);
 }
 
+/* FluidModel::resizeFluid + solver resizeData (FluidModel.cpp:51-60,
+ * DFSPHSolver.cpp:802-823, PCISPHSolver.cpp:423-441): per-particle arrays
+ * of `cap` entries, new entries zero (std::vector::resize). */
+static void* grow(void* p, size_t old, size_t nw, size_t sz)
+{
+    char* q = (char*)realloc(p, (nw ? nw : 1) * sz);
+    if (q && nw > old) memset(q + old * sz, 0, (nw - old) * sz);
+    return q;
+}
+static void fluid_resize(orc_scene* s, unsigned cap)
+{
+    const unsigned o = s->cap;
+    s->x = (v3*)grow(s->x, o, cap, sizeof(v3)); s->v = (v3*)grow(s->v, o, cap, sizeof(v3));
+    s->a = (v3*)grow(s->a, o, cap, sizeof(v3));
+    s->rho = (double*)grow(s->rho, o, cap, 8); s->p = (double*)grow(s->p, o, cap, 8);
+    s->alpha = (double*)grow(s->alpha, o, cap, 8); s->div = (double*)grow(s->div, o, cap, 8);
+    s->pred = (double*)grow(s->pred, o, cap, 8); s->k = (double*)grow(s->k, o, cap, 8); s->kv = (double*)grow(s->kv, o, cap, 8);
+    s->predR = (v3*)grow(s->predR, o, cap, sizeof(v3)); s->predV = (v3*)grow(s->predV, o, cap, sizeof(v3));
+    s->pacc = (v3*)grow(s->pacc, o, cap, sizeof(v3)); s->normal = (v3*)grow(s->normal, o, cap, sizeof(v3));
+    s->cap = cap;
+}
+
 int orc_set_fluid(orc_scene* s, const double* x, const double* v, unsigned n)
 {
-    if (!s || s->inited) return -1;
+    if (!s || s->inited || s->n || s->nem) return -1;
+    fluid_resize(s, n);
     s->n = n;
-    s->x = (v3*)xcalloc(n, sizeof(v3)); s->v = (v3*)xcalloc(n, sizeof(v3)); s->a = (v3*)xcalloc(n, sizeof(v3));
-    s->rho = (double*)xcalloc(n, 8); s->p = (double*)xcalloc(n, 8);
-    s->alpha = (double*)xcalloc(n, 8); s->div = (double*)xcalloc(n, 8); s->pred = (double*)xcalloc(n, 8);
-    s->k = (double*)xcalloc(n, 8); s->kv = (double*)xcalloc(n, 8);
-    s->predR = (v3*)xcalloc(n, sizeof(v3)); s->predV = (v3*)xcalloc(n, sizeof(v3)); s->pacc = (v3*)xcalloc(n, sizeof(v3));
-    s->normal = (v3*)xcalloc(n, sizeof(v3));
     for (unsigned i = 0; i < n; ++i) {
         s->x[i] = V(x[3 * i], x[3 * i + 1], x[3 * i + 2]);
         s->v[i] = v ? V(v[3 * i], v[3 * i + 1], v[3 * i + 2]) : V(0, 0, 0);
@@ -1556,6 +1641,80 @@ int orc_add_bh_sphere(orc_scene* s, const double c[3], double radius, int invert
     boundary_append_n(s, pts, nrm, m);
     free(pts);
     free(nrm);
+    return 0;
+}
+
+/* Emitter::buildCircleGroup / buildSquareGroup Emitter.cpp:31-79 (a
+ * negative level count, converted to unsigned unchecked by the reference,
+ * is taken as zero) */
+long long orc_emitter_group(int type, double particleRadius, double width, double height, double* out)
+{
+    long long count = 0;
+#define PUT(px, py) do { if (out) { out[3 * count] = (px); out[3 * count + 1] = (py); out[3 * count + 2] = 0.0; } ++count; } while (0)
+    if (type == 1) {
+        const double dist = 2.0 * particleRadius;
+        const double lv = floor((width - 0.5 * dist) / dist);
+        const unsigned numLevels = lv > 0.0 ? (unsigned)lv : 0u;
+        PUT(0.0, 0.0);
+        for (unsigned i = 0; i < numLevels; ++i) {
+            const double radius = (i + 1) * dist;
+            const double l = 2.0 * M_PI * radius;
+            const unsigned nParts = (unsigned)floor(l / dist);
+            const double inc = 2 * M_PI / nParts;
+            for (unsigned j = 0; j < nParts; ++j) {
+                const double angle = j * inc;
+                PUT(radius * sin(angle), radius * cos(angle));
+            }
+        }
+    } else {
+        const double dist = particleRadius * 2.0;
+        const double fx = floor(width / dist), fy = floor(height / dist);
+        const unsigned numX = fx > 0.0 ? (unsigned)fx : 0u, numY = fy > 0.0 ? (unsigned)fy : 0u;
+        const double realWidth = (numX - 1) * dist;
+        const double realHeight = (numY - 1) * dist;
+        for (unsigned i = 0; i < numX; ++i)
+            for (unsigned j = 0; j < numY; ++j) PUT(realWidth * 0.5 - i * dist, realHeight * 0.5 - j * dist);
+    }
+#undef PUT
+    return count;
+}
+
+/* FluidModel::addEmitter FluidModel.cpp:124-143 and the Emitter
+ * constructor Emitter.cpp:10-29 */
+int orc_add_emitter(orc_scene* s, int type, unsigned numParticles, const double r[3], double v, const double rot[4],
+                    double startTime, double w, double h, double spacing)
+{
+    if (!s || s->inited || s->nem >= 64 || (type != 0 && type != 1)) return -1;
+    struct orc_emitter* e = &s->em[s->nem];
+    memset(e, 0, sizeof *e);
+    e->type = type;
+    e->numParticles = numParticles;
+    e->r = V(r[0], r[1], r[2]);
+    e->v = v;
+    for (int k = 0; k < 4; ++k) e->rot[k] = rot[k];
+    e->nextTimeEmit = startTime;
+    e->spacing = spacing;
+    const long long m = orc_emitter_group(type, s->prm.radius, w, h, NULL);
+    double* buf = (double*)xcalloc((size_t)m * 3, 8);
+    orc_emitter_group(type, s->prm.radius, w, h, buf);
+    e->group = (v3*)xcalloc((size_t)m, sizeof(v3));
+    for (long long i = 0; i < m; ++i) e->group[i] = V(buf[3 * i], buf[3 * i + 1], buf[3 * i + 2]);
+    free(buf);
+    e->ng = (unsigned)m;
+    s->nem++;
+    fluid_resize(s, s->cap + numParticles);
+    return 0;
+}
+
+/* Simulation::setEmittersPause -> Emitter::setPause (Simulation.h:316,
+ * Emitter.cpp:80-84) */
+int orc_pause_emitters(orc_scene* s, int pause)
+{
+    if (!s) return -1;
+    for (unsigned k = 0; k < s->nem; ++k) {
+        s->em[k].pause = pause != 0;
+        s->em[k].nextTimeEmit = s->time;
+    }
     return 0;
 }
 

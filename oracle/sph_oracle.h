@@ -50,6 +50,12 @@ int orc_add_bh_box(orc_scene* s, const double mn[3], const double mx[3], int inv
 int orc_add_bh_sphere(orc_scene* s, const double c[3], double radius, int inverted);
 long long orc_sample_bh_box(double supportRadius, const double mn[3], const double mx[3], int inverted, double* pts,
                             double* normals);
+/* emitters: type 0 square, 1 circle; rot = (w, x, y, z).  After
+ * orc_set_fluid (which may pass n = 0). */
+int orc_add_emitter(orc_scene* s, int type, unsigned numParticles, const double r[3], double v, const double rot[4],
+                    double startTime, double w, double h, double spacing);
+int orc_pause_emitters(orc_scene* s, int pause);
+long long orc_emitter_group(int type, double particleRadius, double width, double height, double* out);
 int orc_init(orc_scene* s);
 int orc_step(orc_scene* s, int nsteps);
 /* test instrument: uniform noise on positions and velocities */

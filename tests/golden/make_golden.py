@@ -20,7 +20,7 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "tests"))
 
 import oracle  # noqa: E402
-from scenes import SCENES, scene, scene_extra  # noqa: E402
+from scenes import EMIT_DUMP_EVERY, EMIT_SCENES, EMIT_STEPS, SCENES, emit_scene, scene, scene_extra  # noqa: E402
 
 STEPS = 3
 KEEP = ("x", "v", "a", "rho", "p", "alpha", "div", "pred", "k", "kv", "pacc", "time", "dt", "iterations",
@@ -46,6 +46,18 @@ def main(ref_tree="/root/reference"):
                 out[k] = v
         np.savez_compressed(os.path.join(here, f"{name}.npz"), **out)
         print(name, x.shape[0], "fluid,", len(dump.get("b.x", [])) // 3, "boundary")
+    # emitter scenes: EMIT_STEPS steps, the state of every EMIT_DUMP_EVERY-th
+    for name in EMIT_SCENES:
+        params, x, boxes, spheres, emitters = emit_scene(name)
+        dump = oracle.run_reference(params, x, None, boxes=boxes, spheres=spheres, steps=EMIT_STEPS,
+                                    dump_every=EMIT_DUMP_EVERY, emitters=emitters)
+        out = {"input.x": x}
+        for k, v in dump.items():
+            tag, _, field = k.partition(".")
+            if k in ("b.x", "b.psi", "h", "mass") or k.startswith("init.") or field in KEEP:
+                out[k] = v
+        np.savez_compressed(os.path.join(here, f"{name}.npz"), **out)
+        print(name, x.shape[0], "fluid at start,", len(dump[f"s{EMIT_STEPS}.rho"]), "after", EMIT_STEPS, "steps")
 
 
 if __name__ == "__main__":

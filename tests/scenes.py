@@ -141,3 +141,47 @@ def scene_extra(name, x):
     s = SCENES[name]
     v = s["velocity"](x) if "velocity" in s else None
     return v, s.get("bh_boxes", []), s.get("bh_spheres", [])
+
+
+# Emitters (Emitter.cpp, FluidModel::addEmitter): a tilted circular emitter
+# firing from t = 0 and a square one firing downwards from t = 3 ms, each
+# budgeted for a few groups (the circle's budget is not a whole number of
+# groups, so its last partial group is never emitted), over a jittered pool.
+# 30 steps, state kept every third step.  DFSPH and PCISPH with Akinci walls,
+# WCSPH with the cube boundary, and a DFSPH scene whose fluid comes only from
+# an emitter.
+def _unit(q):
+    q = np.asarray(q, dtype=np.float64)
+    return tuple(float(t) for t in q / np.linalg.norm(q))
+
+
+_EMIT_CIRCLE = dict(type=1, num=19 * 3 + 5, position=(0.4, 0.55, 0.4), velocity=2.0, rotation=_unit((0.9, 0.3, 0.2, 0.1)),
+                    start=0.0, width=0.1, height=0.0, spacing=1.0)
+_EMIT_SQUARE = dict(type=0, num=24 * 2, position=(0.25, 0.5, 0.3), velocity=1.5,
+                    rotation=(0.7071067811865476, 0.7071067811865476, 0.0, 0.0), start=0.003, width=0.24, height=0.16,
+                    spacing=1.2)
+_BOX08 = [((0.0, 0.0, 0.0), (0.8, 0.8, 0.8))]
+
+
+def _emit_pool():
+    return jitter(lattice(0.02, (0.04, 0.04, 0.04), (0.3, 0.2, 0.3)), 0.02, 5)
+
+
+EMIT_SCENES = {
+    "dfsph_emit": dict(params=dict(method=2, boundary=2, radius=0.02, dt=2e-3, eta=0.001, eta_v=0.001),
+                       fluid=_emit_pool, boxes=_BOX08, spheres=[], emitters=[_EMIT_CIRCLE, _EMIT_SQUARE]),
+    "wcsph_emit": dict(params=dict(method=0, boundary=0, radius=0.02, dt=5e-4, stiffness=1000.0, gamma=7.0, has_cube=1,
+                                   cube_min=(0.0, 0.0, 0.0), cube_max=(0.8, 0.8, 0.8)),
+                       fluid=_emit_pool, boxes=[], spheres=[], emitters=[_EMIT_CIRCLE, _EMIT_SQUARE]),
+    "pcisph_emit": dict(params=dict(method=1, boundary=2, radius=0.02, dt=1e-3, eta=0.01, min_it=3, max_it=20),
+                        fluid=_emit_pool, boxes=_BOX08, spheres=[], emitters=[_EMIT_CIRCLE, _EMIT_SQUARE]),
+    "dfsph_emit_only": dict(params=dict(method=2, boundary=2, radius=0.02, dt=2e-3),
+                            fluid=lambda: np.zeros((0, 3)), boxes=_BOX08, spheres=[], emitters=[_EMIT_CIRCLE]),
+}
+EMIT_STEPS, EMIT_DUMP_EVERY = 30, 3
+
+
+def emit_scene(name):
+    """(params, x, boxes, spheres, emitters) of an emitter scene."""
+    s = EMIT_SCENES[name]
+    return s["params"], s["fluid"](), s["boxes"], s["spheres"], s["emitters"]

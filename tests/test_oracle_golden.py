@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 import oracle
-from scenes import SCENES, scene, scene_extra
+from scenes import EMIT_DUMP_EVERY, EMIT_SCENES, EMIT_STEPS, SCENES, emit_scene, scene, scene_extra
 from util import golden
 
 FIELDS = ("x", "v", "rho", "p", "alpha", "div", "pred", "k", "kv", "pacc", "normal", "bdens", "bpress")
@@ -49,6 +49,54 @@ def test_oracle_reproduces_reference_bit_exact(name):
         assert o.scalar("iterations") == g[f"s{step}.iterations"][0]
         step += 1
     assert step > 1
+
+
+@pytest.mark.parametrize("name", list(EMIT_SCENES))
+def test_oracle_reproduces_reference_with_emitters(name):
+    """Emitter scenes: identical bits and identical active-particle counts at
+    every stored step (every third of 30), with groups emitted on the way."""
+    params, x, boxes, spheres, emitters = emit_scene(name)
+    g = golden(name)
+    assert np.array_equal(g["input.x"], x), "scene inputs changed; regenerate the fixtures"
+    o = oracle.OracleScene(params, x, boxes=boxes, spheres=spheres, emitters=emitters)
+    checked = 0
+    for step in range(1, EMIT_STEPS + 1):
+        o.step(1)
+        if f"s{step}.x" not in g:
+            continue
+        assert o.n == g[f"s{step}.rho"].size, (name, step)
+        for f in FIELDS:
+            key = f"s{step}.{f}"
+            if key in g:
+                assert same(o.get(f).ravel(), g[key]), (name, key)
+        assert o.scalar("dt") == g[f"s{step}.dt"][0]
+        assert o.scalar("iterations") == g[f"s{step}.iterations"][0]
+        checked += 1
+    assert checked == EMIT_STEPS // EMIT_DUMP_EVERY
+    assert o.n >= x.shape[0] + 2 * 19
+
+
+def test_oracle_emitter_pause_restarts_the_clock():
+    """Emitter::setPause: no group while paused; on resume the next group
+    leaves at once with a zero time offset (nextTimeEmit = current time)."""
+    params, x, boxes, spheres, emitters = emit_scene("dfsph_emit_only")
+    o = oracle.OracleScene(params, x, boxes=boxes, spheres=spheres, emitters=emitters)
+    o.step(1)
+    assert o.n == 19
+    o.pause_emitters(True)
+    o.step(20)
+    assert o.n == 19
+    o.pause_emitters(False)
+    o.step(1)
+    assert o.n == 38
+    # the resumed group sits exactly at the emitter's rotated group points
+    e = emitters[0]
+    grp = oracle.emitter_group(1, params["radius"], e["width"])
+    w, qx, qy, qz = e["rotation"]
+    u = np.array([qx, qy, qz])
+    uv = np.cross(u, grp)
+    rot = grp + 2.0 * (w * uv + np.cross(u, uv)) + np.array(e["position"])
+    assert np.allclose(o.get("x")[19:38], rot, atol=1e-3)
 
 
 def test_pcisph_model_cube_sampler():
