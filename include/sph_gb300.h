@@ -125,6 +125,8 @@ typedef struct sph_stats {
     unsigned num_fluid, num_boundary;
     unsigned long long list_pairs; /* DFSPH pair lists: stored pairs (0 without lists) */
     unsigned list_overflow;       /* particles whose neighbours exceed neighbor_list_max */
+    unsigned num_fluid_total;     /* FluidModel::getNumParticles: active + slots reserved by emitters;
+                                     num_fluid is getNumActiveParticles */
 } sph_stats;
 
 /* Defaults of the reference (SPHSolver.cpp:12-19, DFSPHSolver.cpp:10-22,
@@ -154,6 +156,25 @@ int sph_ctx_add_boundary_points(sph_ctx* ctx, const double* x, unsigned n);
  * normals (sph_ctx_add_boundary_points) are rejected for this model. */
 int sph_ctx_add_pcisph_box(sph_ctx* ctx, const double mn[3], const double mx[3], int inverted);
 int sph_ctx_add_pcisph_sphere(sph_ctx* ctx, const double c[3], double radius, int inverted);
+
+/* FluidModel::addEmitter (FluidModel.cpp:124-143, Emitter.cpp:10-29), before
+ * sph_ctx_init: an emitter of num_particles particles, square (type
+ * SPH_EMITTER_SQUARE, width x height) or circular (SPH_EMITTER_CIRCLE, radius
+ * width), at position, rotated by the unit quaternion rotation = (w, x, y, z)
+ * (the scene file's "rotation" array, SceneLoader.cpp:128-131), emitting along
+ * its local z at speed velocity from start_time on, one group every
+ * spacing * 1.105 * 2r / velocity seconds (Emitter.cpp:85-161).  Emitted
+ * particles take the next original indices; sph_ctx_num_particles and the
+ * downloads cover the active ones.  At most 64 emitters per scene; the
+ * fluid set by sph_ctx_set_fluid may be empty when a scene has emitters. */
+#define SPH_EMITTER_SQUARE 0
+#define SPH_EMITTER_CIRCLE 1
+int sph_ctx_add_emitter(sph_ctx* ctx, int type, unsigned num_particles, const double position[3], double velocity,
+                        const double rotation[4], double start_time, double width, double height, double spacing);
+/* Simulation::setEmittersPause (Simulation.h:316, Emitter.cpp:80-84): pause
+ * (1) or resume (0) every emitter; both restart its clock at the current
+ * time.  After sph_ctx_init. */
+int sph_ctx_pause_emitters(sph_ctx* ctx, int pause);
 
 /* Simulation::init -> solver->init (Simulation.cpp:102-110,
  * SPHSolver.cpp:22-39, DFSPHSolver.cpp:24-36, PCISPHSolver.cpp:12-19):
@@ -307,6 +328,9 @@ long long sph_sample_pcisph_box(double support_radius, const double mn[3], const
                                 double* out, double* normals);
 long long sph_sample_sphere(double particle_radius, const double center[3], double radius, double* out);
 long long sph_fluid_block(double particle_radius, const double min[3], const double max[3], double* out);
+/* Emitter::buildSquareGroup / buildCircleGroup (Emitter.cpp:31-79): the
+ * group an emitter emits each time, in its local frame (out may be NULL). */
+long long sph_emitter_group(int type, double particle_radius, double width, double height, double* out);
 
 /* Build identification string. */
 const char* sph_version(void);

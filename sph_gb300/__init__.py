@@ -96,6 +96,7 @@ class Stats(ctypes.Structure):
         ("num_boundary", ctypes.c_uint),
         ("list_pairs", ctypes.c_ulonglong),
         ("list_overflow", ctypes.c_uint),
+        ("num_fluid_total", ctypes.c_uint),
     ]
 
 
@@ -136,6 +137,9 @@ ABI = [
     ("sph_ctx_add_boundary_points", ctypes.c_int, [_vp, _dp, ctypes.c_uint]),
     ("sph_ctx_add_pcisph_box", ctypes.c_int, [_vp, _dp, _dp, ctypes.c_int]),
     ("sph_ctx_add_pcisph_sphere", ctypes.c_int, [_vp, _dp, ctypes.c_double, ctypes.c_int]),
+    ("sph_ctx_add_emitter", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_uint, _dp, ctypes.c_double, _dp, ctypes.c_double,
+                                           ctypes.c_double, ctypes.c_double, ctypes.c_double]),
+    ("sph_ctx_pause_emitters", ctypes.c_int, [_vp, ctypes.c_int]),
     ("sph_ctx_init", ctypes.c_int, [_vp]),
     ("sph_ctx_step", ctypes.c_int, [_vp, ctypes.c_int]),
     ("sph_ctx_step_timed", ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
@@ -155,6 +159,7 @@ ABI = [
     ("sph_sample_sphere", ctypes.c_longlong, [ctypes.c_double, _dp, ctypes.c_double, _dp]),
     ("sph_sample_pcisph_box", ctypes.c_longlong, [ctypes.c_double, _dp, _dp, ctypes.c_int, _dp, _dp]),
     ("sph_fluid_block", ctypes.c_longlong, [ctypes.c_double, _dp, _dp, _dp]),
+    ("sph_emitter_group", ctypes.c_longlong, [ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, _dp]),
     ("sph_version", ctypes.c_char_p, []),
     ("sph_pool_desc_from_budget", ctypes.c_int, [ctypes.c_ulonglong, ctypes.c_int, ctypes.POINTER(PoolDesc)]),
     ("sph_pool_create", ctypes.c_int, [ctypes.POINTER(PoolDesc), ctypes.POINTER(_vp)]),
@@ -312,6 +317,20 @@ class Scene:
                     "sph_ctx_add_pcisph_sphere")
         return self
 
+    def add_emitter(self, type, num_particles, position, velocity, rotation=(1.0, 0.0, 0.0, 0.0), start_time=0.0,
+                    width=0.0, height=0.0, spacing=1.0):
+        """FluidModel::addEmitter: type EMITTER_SQUARE (0) or EMITTER_CIRCLE (1);
+        rotation is the unit quaternion (w, x, y, z)."""
+        q = np.ascontiguousarray(np.asarray(rotation, dtype=np.float64).reshape(4))
+        self._check(lib().sph_ctx_add_emitter(self._h, int(type), int(num_particles), _d(_v3(position)), float(velocity),
+                                              _d(q), float(start_time), float(width), float(height), float(spacing)),
+                    "sph_ctx_add_emitter")
+        return self
+
+    def pause_emitters(self, pause=True):
+        """Simulation::setEmittersPause: pause or resume every emitter (both restart its clock now)."""
+        self._check(lib().sph_ctx_pause_emitters(self._h, int(bool(pause))), "sph_ctx_pause_emitters")
+
     def add_boundary_points(self, x):
         x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, 3)
         self._check(lib().sph_ctx_add_boundary_points(self._h, _d(x), x.shape[0]), "sph_ctx_add_boundary_points")
@@ -440,6 +459,21 @@ def sample_pcisph_box(h, mn, mx, inverted=True):
     pts, nrm = np.zeros((n, 3)), np.zeros((n, 3))
     L.sph_sample_pcisph_box(float(h), _d(_v3(mn)), _d(_v3(mx)), int(bool(inverted)), _d(pts), _d(nrm))
     return pts, nrm
+
+
+EMITTER_SQUARE, EMITTER_CIRCLE = 0, 1
+
+
+def emitter_group(type, particle_radius, width, height=0.0):
+    """Emitter::buildSquareGroup / buildCircleGroup: the group emitted each time, emitter frame."""
+    L = lib()
+    m = L.sph_emitter_group(int(type), float(particle_radius), float(width), float(height), None)
+    if m < 0:
+        raise SPHError("invalid emitter group arguments")
+    out = np.zeros((m, 3))
+    if m:
+        L.sph_emitter_group(int(type), float(particle_radius), float(width), float(height), _d(out))
+    return out
 
 
 def fluid_block(particle_radius, mn, mx):

@@ -145,6 +145,52 @@ long long fluid_block(double r, const double mn[3], const double mx[3], double* 
     return count;
 }
 
+// Emitter::buildCircleGroup / buildSquareGroup Emitter.cpp:31-79: the
+// group of points emitted each time, in the emitter's frame (z = 0).
+// Circle: the centre and rings of radius (i + 1) 2r, i < floor((width - r) /
+// 2r), each with floor(2 pi radius / 2r) points at equal angles from the +y
+// axis (x = R sin a, y = R cos a).  Square: a floor(width / 2r) x
+// floor(height / 2r) lattice at spacing 2r centred on the origin, x outer.
+// (A negative level count, which the reference converts to unsigned
+// unchecked, is taken as zero.)
+long long emitter_group(int type, double particleRadius, double width, double height, double* out)
+{
+    long long count = 0;
+    auto put = [&](double x, double y) {
+        if (out) {
+            out[3 * count] = x;
+            out[3 * count + 1] = y;
+            out[3 * count + 2] = 0.0;
+        }
+        ++count;
+    };
+    if (type == SPH_EMITTER_CIRCLE) {
+        const double dist = 2.0 * particleRadius;
+        const double lv = std::floor((width - 0.5 * dist) / dist);
+        const unsigned numLevels = lv > 0.0 ? (unsigned)lv : 0u;
+        put(0.0, 0.0);
+        for (unsigned i = 0; i < numLevels; ++i) {
+            const double radius = (i + 1) * dist;
+            const double l = 2.0 * M_PI * radius;
+            const unsigned nParts = (unsigned)std::floor(l / dist);
+            const double inc = 2 * M_PI / nParts;
+            for (unsigned k = 0; k < nParts; ++k) {
+                const double angle = k * inc;
+                put(radius * std::sin(angle), radius * std::cos(angle));
+            }
+        }
+    } else {
+        const double dist = particleRadius * 2.0;
+        const double fx = std::floor(width / dist), fy = std::floor(height / dist);
+        const unsigned numX = fx > 0.0 ? (unsigned)fx : 0u, numY = fy > 0.0 ? (unsigned)fy : 0u;
+        const double realWidth = (numX - 1) * dist;
+        const double realHeight = (numY - 1) * dist;
+        for (unsigned i = 0; i < numX; ++i)
+            for (unsigned j = 0; j < numY; ++j) put(realWidth * 0.5 - i * dist, realHeight * 0.5 - j * dist);
+    }
+    return count;
+}
+
 }  // namespace sph
 
 static int bad(sph_ctx* ctx, const char* m)
@@ -350,6 +396,47 @@ int sph_ctx_add_boundary_points(sph_ctx* ctx, const double* x, unsigned n)
     return add_boundary(ctx, x, n);
 }
 
+int sph_ctx_add_emitter(sph_ctx* ctx, int type, unsigned num_particles, const double position[3], double velocity,
+                        const double rotation[4], double start_time, double width, double height, double spacing)
+{
+    if (!ctx || !position || !rotation) return bad(ctx, "invalid argument");
+    if (ctx->scene->inited) return bad(ctx, "emitters must be added before sph_ctx_init");
+    if (type != SPH_EMITTER_SQUARE && type != SPH_EMITTER_CIRCLE)
+        return bad(ctx, "emitter type must be SPH_EMITTER_SQUARE (0) or SPH_EMITTER_CIRCLE (1)");
+    if (ctx->scene->hem.size() >= 64) return bad(ctx, "at most 64 emitters per scene");
+    const double vals[] = {position[0], position[1], position[2], velocity, rotation[0], rotation[1], rotation[2],
+                           rotation[3], start_time, width, height, spacing};
+    for (double x : vals)
+        if (!std::isfinite(x)) return bad(ctx, "emitter parameters must be finite");
+    try {
+        sph::EmitterSpec e;
+        e.type = type;
+        e.num = num_particles;
+        for (int k = 0; k < 3; ++k) e.r[k] = position[k];
+        for (int k = 0; k < 4; ++k) e.q[k] = rotation[k];
+        e.v = velocity;
+        e.start = start_time;
+        e.width = width;
+        e.height = height;
+        e.spacing = spacing;
+        const double r = ctx->scene->d.particle_radius;
+        const long long m = sph::emitter_group(type, r, width, height, nullptr);
+        if (m > (1ll << 24)) return bad(ctx, "emitter group larger than 2^24 particles");
+        e.group.resize(3 * (size_t)m);
+        sph::emitter_group(type, r, width, height, e.group.data());
+        ctx->scene->hem.push_back(std::move(e));
+    } catch (...) {
+        return bad(ctx, "out of host memory");
+    }
+    return SPH_OK;
+}
+
+int sph_ctx_pause_emitters(sph_ctx* ctx, int pause)
+{
+    if (!ctx) return SPH_ERR_INVALID;
+    return relay(ctx, ctx->scene->pause_emitters(pause));
+}
+
 int sph_ctx_init(sph_ctx* ctx)
 {
     if (!ctx) return SPH_ERR_INVALID;
@@ -440,6 +527,14 @@ long long sph_sample_sphere(double particle_radius, const double c[3], double ra
 {
     if (!c || !(particle_radius > 0.0) || !(radius > 0.0)) return -1;
     return sph::sample_sphere(particle_radius, c, radius, out);
+}
+
+long long sph_emitter_group(int type, double particle_radius, double width, double height, double* out)
+{
+    if ((type != SPH_EMITTER_SQUARE && type != SPH_EMITTER_CIRCLE) || !(particle_radius > 0.0) || !std::isfinite(width) ||
+        !std::isfinite(height))
+        return -1;
+    return sph::emitter_group(type, particle_radius, width, height, out);
 }
 
 long long sph_fluid_block(double particle_radius, const double mn[3], const double mx[3], double* out)

@@ -104,6 +104,7 @@ struct DevScalars {
     unsigned status;               // SPH_STATUS_* bits
     unsigned block_counter;        // last-block-done counter of reductions
     unsigned grid_epoch;           // grid builds so far (cell lifetimes, PCISPH boundary model)
+    unsigned n_active;             // active fluid particles (grows when emitters emit)
 };
 
 enum StatusBits : unsigned {

@@ -32,7 +32,11 @@ template <typename R> struct Fluid {
     R* kappav;       // DFSPH divergence accumulator (kv)
     uint32_t* cell;  // packed cell coordinates
     uint32_t* id;    // original particle index
-    uint32_t n;
+    uint32_t n;      // particle slots: launch bound and pair-list stride
+    // Scenes with emitters: the active particle count on the device (slots
+    // [0, *na) hold particles; emission appends).  nullptr: all n slots.
+    const uint32_t* na;
+    __device__ __forceinline__ uint32_t count() const { return na ? *na : n; }
 };
 
 template <typename R> struct Boundary {
@@ -66,15 +70,13 @@ template <int G, typename R> __device__ __forceinline__ V3<R> group_sum3(V3<R> v
 // Upload / download
 // ===========================================================================
 
-// Host positions (FP64, xyz per particle) into the device layout.
+// One particle from FP64 host-layout position and velocity into slot i of
+// the device layout (FP32: offset from the clamped cell's corner), with the
+// per-particle solver state zeroed.
 template <typename R>
-__global__ void k_upload_fluid(const double* __restrict__ x, const double* __restrict__ v, uint32_t n,
-                               uint32_t first, Fluid<R> f, GridView g, double h, DevScalars* sc)
+__device__ __forceinline__ void store_particle(const Fluid<R>& f, uint32_t i, double px, double py, double pz, double vx,
+                                               double vy, double vz, const GridView& g, double h, DevScalars* sc)
 {
-    const uint32_t t = gtid();
-    if (t >= n) return;
-    const uint32_t i = first + t;
-    const double px = x[3 * t], py = x[3 * t + 1], pz = x[3 * t + 2];
     int cx = (int)floor(px / h) - g.ox, cy = (int)floor(py / h) - g.oy, cz = (int)floor(pz / h) - g.oz;
     const int ccx = min(max(cx, 0), g.nx - 1), ccy = min(max(cy, 0), g.ny - 1), ccz = min(max(cz, 0), g.nz - 1);
     if (ccx != cx || ccy != cy || ccz != cz) atomicOr(&sc->status, (unsigned)ST_OUT_OF_GRID);
@@ -85,13 +87,23 @@ __global__ void k_upload_fluid(const double* __restrict__ x, const double* __res
         p = {(R)px, (R)py, (R)pz, 0};
     }
     f.pos[i] = p;
-    f.vel[i] = P4<R>{(R)v[3 * t], (R)v[3 * t + 1], (R)v[3 * t + 2], 0};
+    f.vel[i] = P4<R>{(R)vx, (R)vy, (R)vz, 0};
     f.acc[i] = P4<R>{0, 0, 0, 0};
     f.kappa[i] = 0;
     f.kappav[i] = 0;
     f.press[i] = 0;
     f.cell[i] = pack_cell(ccx, ccy, ccz);
     f.id[i] = i;
+}
+
+// Host positions (FP64, xyz per particle) into the device layout.
+template <typename R>
+__global__ void k_upload_fluid(const double* __restrict__ x, const double* __restrict__ v, uint32_t n,
+                               uint32_t first, Fluid<R> f, GridView g, double h, DevScalars* sc)
+{
+    const uint32_t t = gtid();
+    if (t >= n) return;
+    store_particle(f, first + t, x[3 * t], x[3 * t + 1], x[3 * t + 2], v[3 * t], v[3 * t + 1], v[3 * t + 2], g, h, sc);
 }
 
 template <typename R>
@@ -157,10 +169,10 @@ template <typename R, bool MOVE, bool KEY = true>
 __global__ void k_cell_update(uint32_t n, P4<R>* __restrict__ pos, const P4<R>* __restrict__ vel, uint32_t* __restrict__ cell,
                               uint32_t* __restrict__ key, uint32_t* __restrict__ slot, uint32_t* __restrict__ count,
                               GridView g, R h, double hd, DevScalars* sc, uint32_t* __restrict__ cell_epoch = nullptr,
-                              P4<R>* __restrict__ carry = nullptr)
+                              P4<R>* __restrict__ carry = nullptr, const uint32_t* __restrict__ na = nullptr)
 {
     const uint32_t i = gtid();
-    if (i >= n) return;
+    if (i >= (na ? *na : n)) return;
     P4<R> p = pos[i];
     if (MOVE) {
         const R dt = (R)sc->dt;
@@ -340,10 +352,10 @@ static __global__ void __launch_bounds__(kScanThreads) k_scan_add(uint32_t nkeys
 }
 
 static __global__ void k_scatter(uint32_t n, const uint32_t* __restrict__ key, const uint32_t* __restrict__ slot,
-                          const uint32_t* __restrict__ starts, uint32_t* __restrict__ tmp)
+                          const uint32_t* __restrict__ starts, uint32_t* __restrict__ tmp, const uint32_t* __restrict__ na = nullptr)
 {
     const uint32_t i = gtid();
-    if (i >= n) return;
+    if (i >= (na ? *na : n)) return;
     tmp[starts[key[i]] + slot[i]] = i;
 }
 
@@ -370,7 +382,7 @@ __global__ void k_gather_fluid(uint32_t n, const uint32_t* __restrict__ tmp, con
                                const uint32_t* __restrict__ starts, Fluid<R> src, Fluid<R> dst)
 {
     const uint32_t p = gtid();
-    if (p >= n) return;
+    if (p >= src.count()) return;
     uint32_t i;
     const uint32_t d = final_slot(p, tmp, key, src.id, starts, &i);
     dst.pos[d] = src.pos[i];
@@ -434,7 +446,7 @@ __global__ void __launch_bounds__(kBlock) k_density(Fluid<R> f, const P4<R>* __r
     const uint32_t t = gtid();
     const uint32_t i = t / G;
     const int lane = (int)(t % G);
-    const bool valid = i < f.n;
+    const bool valid = i < f.count();
     R density = 0, sumSq = 0;
     V3<R> sumGrad = {0, 0, 0};
     V3<R> xi = {0, 0, 0};
@@ -503,7 +515,7 @@ __global__ void __launch_bounds__(kBlock) k_wcsph_pressure_force(Fluid<R> f, con
     const uint32_t t = gtid();
     const uint32_t i = t / G;
     const int lane = (int)(t % G);
-    const bool valid = i < f.n;
+    const bool valid = i < f.count();
     V3<R> sum = {0, 0, 0};
     if (valid) {
         const P4<R> pi = f.xk[i];
@@ -541,7 +553,7 @@ __global__ void __launch_bounds__(kBlock) k_st_normals(Fluid<R> f, GridView g, c
     const uint32_t t = gtid();
     const uint32_t i = t / G;
     const int lane = (int)(t % G);
-    const bool valid = i < f.n;
+    const bool valid = i < f.count();
     V3<R> ni = {0, 0, 0};
     if (valid) {
         const V3<R> xi = xyz(f.pos[i]);
@@ -576,7 +588,7 @@ __global__ void __launch_bounds__(kBlock) k_npforce(Fluid<R> f, const P4<R>* __r
     const uint32_t t = gtid();
     const uint32_t i = t / G;
     const int lane = (int)(t % G);
-    const bool valid = i < f.n;
+    const bool valid = i < f.count();
     const int fl = c.force_flags;
     V3<R> av = {0, 0, 0}, avb = {0, 0, 0}, ast = {0, 0, 0}, aad = {0, 0, 0};
     if (valid) {
@@ -676,7 +688,7 @@ __global__ void __launch_bounds__(256) k_dfsph_cfl(Fluid<R> f, Consts<R> c, DevS
     const uint32_t i = gtid();
     const R dt = (R)sc->dt;
     double m = 0.1;
-    if (i < f.n) {
+    if (i < f.count()) {
         const P4<R> v = f.vel[i], a = f.acc[i];
         const V3<R> cur = {v.x + (a.x + c.gx) * dt, v.y + (a.y + c.gy) * dt, v.z + (a.z + c.gz) * dt};
         m = fmax(m, (double)sqrt(sqrt(dot3(cur, cur))));
@@ -705,7 +717,7 @@ template <typename R>
 __global__ void k_dfsph_predict_v_warm(Fluid<R> f, Consts<R> c, const DevScalars* __restrict__ sc)
 {
     const uint32_t i = gtid();
-    if (i >= f.n) return;
+    if (i >= f.count()) return;
     const R dt = (R)sc->dt;
     P4<R> v = f.vel[i];
     const P4<R> a = f.acc[i];
@@ -736,7 +748,7 @@ __global__ void __launch_bounds__(kBlock) k_dfsph_correct(Fluid<R> f, const P4<R
     const uint32_t t = gtid();
     const uint32_t i = t / G;
     const int lane = (int)(t % G);
-    const bool valid = i < f.n;
+    const bool valid = i < f.count();
     V3<R> sum = {0, 0, 0};
     R ki = 0;
     if (valid) {
@@ -786,7 +798,7 @@ __global__ void __launch_bounds__(kBlock) k_dfsph_predict_density(Fluid<R> f, co
     const uint32_t t = gtid();
     const uint32_t i = t / G;
     const int lane = (int)(t % G);
-    const bool valid = i < f.n;
+    const bool valid = i < f.count();
     R dc = 0;
     V3<R> xi = {0, 0, 0};
     if (valid) {
@@ -820,7 +832,7 @@ __global__ void __launch_bounds__(kBlock) k_dfsph_predict_density(Fluid<R> f, co
     }
     double total;
     if (finish_reduction<false>(err, partials, &sc->block_counter, sh, &total) && threadIdx.x == 0) {
-        const double avg = f.n ? total / (double)f.n : 0.0;
+        const double avg = f.count() ? total / (double)f.count() : 0.0;
         if (!(avg == avg)) sc->status |= ST_NONFINITE;
         if (INITIAL) {
             sc->iterations = 0;
@@ -855,7 +867,7 @@ __global__ void __launch_bounds__(kBlock) k_dfsph_divergence(Fluid<R> f, const P
     const uint32_t t = gtid();
     const uint32_t i = t / G;
     const int lane = (int)(t % G);
-    const bool valid = i < f.n;
+    const bool valid = i < f.count();
     R dv = 0;
     unsigned nn = 0;
     V3<R> xi = {0, 0, 0};
@@ -892,7 +904,7 @@ __global__ void __launch_bounds__(kBlock) k_dfsph_divergence(Fluid<R> f, const P
     }
     double total;
     if (finish_reduction<false>(err, partials, &sc->block_counter, sh, &total) && threadIdx.x == 0) {
-        const double avg = total / (double)f.n;
+        const double avg = total / (double)f.count();
         const double lim_v = lim.maxErrorV / sc->dt;
         if (!(avg == avg)) sc->status |= ST_NONFINITE;
         if (INITIAL) {
@@ -958,7 +970,7 @@ template <typename R>
 __global__ void k_dfsph_cube(Fluid<R> f, GridView g, double h, Consts<R> c)
 {
     const uint32_t i = gtid();
-    if (i >= f.n) return;
+    if (i >= f.count()) return;
     P4<R> p = f.pos[i], v = f.vel[i];
     cube_clamp(p, v, f.cell[i], g, h, c);
     f.pos[i] = p;
@@ -972,7 +984,7 @@ template <typename R, bool PCI>
 __global__ void k_integrate(Fluid<R> f, GridView g, double h, Consts<R> c, const DevScalars* __restrict__ sc)
 {
     const uint32_t i = gtid();
-    if (i >= f.n) return;
+    if (i >= f.count()) return;
     const R dt = (R)sc->dt;
     P4<R> a = f.acc[i], v = f.vel[i], p = f.pos[i];
     if (PCI) {
@@ -998,7 +1010,7 @@ template <typename R>
 __global__ void k_pcisph_init(Fluid<R> f)
 {
     const uint32_t i = gtid();
-    if (i >= f.n) return;
+    if (i >= f.count()) return;
     f.press[i] = 0;
     f.pacc[i] = P4<R>{0, 0, 0, 0};
 }
@@ -1018,7 +1030,7 @@ __global__ void k_pcisph_predict(Fluid<R> f, Consts<R> c, const DevScalars* __re
 {
     if (!sc->active) return;
     const uint32_t i = gtid();
-    if (i >= f.n) return;
+    if (i >= f.count()) return;
     const R dt = (R)sc->dt;
     const P4<R> a = f.acc[i], pa = f.pacc[i], v = f.vel[i], x = f.pos[i];
     const V3<R> acc = {(a.x + pa.x) + c.gx, (a.y + pa.y) + c.gy, (a.z + pa.z) + c.gz};
@@ -1042,7 +1054,7 @@ __global__ void __launch_bounds__(kBlock) k_pcisph_density_pressure(Fluid<R> f, 
     const uint32_t t = gtid();
     const uint32_t i = t / G;
     const int lane = (int)(t % G);
-    const bool valid = i < f.n;
+    const bool valid = i < f.count();
     R density = 0;
     if (valid) {
         const V3<R> xi = xyz(f.predR[i]);
@@ -1094,7 +1106,7 @@ __global__ void __launch_bounds__(kBlock) k_pcisph_pressure_acc(Fluid<R> f, cons
     const uint32_t t = gtid();
     const uint32_t i = t / G;
     const int lane = (int)(t % G);
-    const bool valid = i < f.n;
+    const bool valid = i < f.count();
     V3<R> pacc = {0, 0, 0};
     if (valid) {
         const P4<R> pi = f.xk[i];
@@ -1205,7 +1217,7 @@ __global__ void k_bh_collide(Fluid<R> f, Boundary<R> b, GridView g, const uint32
 {
     if (MODE == 2 && !sc->active) return;
     const uint32_t i = gtid();
-    if (i >= f.n) return;
+    if (i >= f.count()) return;
     const V3<R> xi = xyz(f.pos[i]);
     const uint32_t pc = f.cell[i];
     // The reference looks the candidates up in a hash table whose cells come
@@ -1270,7 +1282,7 @@ template <typename R, bool PRED>
 __global__ void k_bh_correct_velocities(Fluid<R> f, Consts<R> c)
 {
     const uint32_t i = gtid();
-    if (i >= f.n) return;
+    if (i >= f.count()) return;
     const V3<R> ni = xyz(f.normal[i]);
     if (!(sqrt(dot3(ni, ni)) > (R)0)) return;
     const V3<R> u = xyz(PRED ? f.predV[i] : f.vel[i]);
@@ -1318,6 +1330,121 @@ static __global__ void k_list_stats(uint32_t n, const uint32_t* __restrict__ cou
     if (c > kmax) atomicAdd(out + 1, 1ull);
 }
 
+// ===========================================================================
+// Emitters (Emitter.cpp:85-161, FluidModel::emitParticles FluidModel.cpp:
+// 145-149): particle groups appended at the end of the active slots.
+// ===========================================================================
+constexpr int kMaxEmitters = 64;
+
+struct EmitterDev {
+    double r[3];           // emitter position
+    double v;              // emission speed along the emitter's local z
+    double q[4];           // rotation quaternion (w, x, y, z)
+    double next;           // nextTimeEmit
+    double period;         // spacing * 1.105 * 2r / v, added after each emission
+    uint32_t remaining;    // particles left to emit
+    uint32_t first, count; // the group's points in the group table
+    uint32_t pause;
+};
+
+// a x b, component order and operand order of GLM's cross().
+__device__ __forceinline__ void cross_rn(const double a[3], const double b[3], double o[3])
+{
+    o[0] = __dsub_rn(__dmul_rn(a[1], b[2]), __dmul_rn(b[1], a[2]));
+    o[1] = __dsub_rn(__dmul_rn(a[2], b[0]), __dmul_rn(b[2], a[0]));
+    o[2] = __dsub_rn(__dmul_rn(a[0], b[1]), __dmul_rn(b[0], a[1]));
+}
+
+// Rotation of v by the unit quaternion q = (w, u): v + 2 (w (u x v) + u x (u x v)),
+// GLM's quat * vec3, each operation rounded on its own.
+__device__ __forceinline__ void quat_rotate_rn(const double q[4], const double v[3], double o[3])
+{
+    const double u[3] = {q[1], q[2], q[3]};
+    double uv[3], uuv[3];
+    cross_rn(u, v, uv);
+    cross_rn(u, uv, uuv);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) o[k] = __dadd_rn(v[k], __dmul_rn(__dadd_rn(__dmul_rn(uv[k], q[0]), uuv[k]), 2.0));
+}
+
+enum EmitFlags : unsigned { EMIT_PCISPH = 1u, EMIT_NORMALS = 2u };
+
+// Simulation::emitParticles at the current time: thread 0 decides, in
+// emitter order, which emitters fire (time >= nextTimeEmit, not paused, a
+// whole group left: Emitter.cpp:85-97,105) and reserves their slots; then
+// every particle of a firing group gets
+//   x = R (g_i + t_off (v_e + gravity t_off)) + r,  v = R v_e,  v_e = (0, 0, v),
+// t_off = time - nextTimeEmit (Emitter.cpp:107-124), in FP64.  One block.
+template <typename R>
+__global__ void __launch_bounds__(256) k_emit(Fluid<R> f, EmitterDev* __restrict__ em, int nem, const double* __restrict__ group,
+                                              GridView g, double h, double gx, double gy, double gz, DevScalars* sc,
+                                              uint32_t* __restrict__ na, unsigned flags)
+{
+    __shared__ uint32_t base[kMaxEmitters];
+    __shared__ double toff[kMaxEmitters];
+    __shared__ int any;
+    if (threadIdx.x == 0) {
+        uint32_t n = *na;
+        const double t = sc->time;
+        any = 0;
+        for (int e = 0; e < nem; ++e) {
+            EmitterDev& E = em[e];
+            base[e] = 0xffffffffu;
+            if (t >= E.next && !E.pause && E.count <= E.remaining) {
+                base[e] = n;
+                toff[e] = __dsub_rn(t, E.next);
+                n += E.count;
+                E.remaining -= E.count;
+                E.next = __dadd_rn(E.next, E.period);
+                any = 1;
+            }
+        }
+        *na = n;
+    }
+    __syncthreads();
+    if (!any) return;
+    for (int e = 0; e < nem; ++e) {
+        if (base[e] == 0xffffffffu) continue;
+        const double to = toff[e];
+        const EmitterDev& E = em[e];
+        const double s[3] = {__dadd_rn(0.0, __dmul_rn(gx, to)), __dadd_rn(0.0, __dmul_rn(gy, to)), __dadd_rn(E.v, __dmul_rn(gz, to))};
+        const double v0[3] = {0.0, 0.0, E.v};
+        double vr[3];
+        quat_rotate_rn(E.q, v0, vr);
+        for (uint32_t k = threadIdx.x; k < E.count; k += blockDim.x) {
+            const double* gp = group + 3 * (size_t)(E.first + k);
+            const double p[3] = {__dadd_rn(gp[0], __dmul_rn(to, s[0])), __dadd_rn(gp[1], __dmul_rn(to, s[1])),
+                                 __dadd_rn(gp[2], __dmul_rn(to, s[2]))};
+            double pr[3];
+            quat_rotate_rn(E.q, p, pr);
+            const uint32_t i = base[e] + k;
+            store_particle(f, i, __dadd_rn(pr[0], E.r[0]), __dadd_rn(pr[1], E.r[1]), __dadd_rn(pr[2], E.r[2]), vr[0], vr[1],
+                           vr[2], g, h, sc);
+            f.rho[i] = 0;
+            f.alpha[i] = 0;
+            f.div[i] = 0;
+            f.pred[i] = 0;
+            if (flags & EMIT_PCISPH) {
+                f.predR[i] = P4<R>{0, 0, 0, 0};
+                f.predV[i] = P4<R>{0, 0, 0, 0};
+                f.pacc[i] = P4<R>{0, 0, 0, 0};
+            }
+            if (flags & EMIT_NORMALS) f.normal[i] = P4<R>{0, 0, 0, 0};
+        }
+    }
+}
+
+// Emitter::setPause (Emitter.cpp:80-84) on every emitter: the flag, and the
+// next emission at the current time.
+static __global__ void k_emit_pause(EmitterDev* __restrict__ em, int nem, uint32_t pause, const DevScalars* __restrict__ sc)
+{
+    const int e = (int)threadIdx.x;
+    if (e < nem) {
+        em[e].pause = pause;
+        em[e].next = sc->time;
+    }
+}
+
 // Simulation::step bookkeeping: time += dt, steps++ (DFSPHSolver.cpp:111).
 static __global__ void k_finish_step(DevScalars* sc)
 {
@@ -1339,7 +1466,7 @@ __global__ void k_neighbors(Fluid<R> f, const P4<R>* __restrict__ bpos, const ui
                             int* __restrict__ rank)
 {
     const uint32_t i = gtid();
-    if (i >= f.n) return;
+    if (i >= f.count()) return;
     const uint32_t me = f.id[i];
     const uint32_t pc = f.cell[i];
     double xi[3];

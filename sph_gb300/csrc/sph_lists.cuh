@@ -184,7 +184,7 @@ __global__ void __launch_bounds__(kBlock, 7) k_build_lists(Fluid<R> f, const P4<
 {
     __shared__ uint32_t q[kQueue * kBlock];
     const uint32_t i = gtid();
-    if (i >= f.n) return;
+    if (i >= f.count()) return;
     build_lists_one(i, f, bpos, g, cs, bs, c, akinci, L, q);
 }
 
@@ -302,7 +302,7 @@ __global__ void __launch_bounds__(kBlock, 8) k_dfsph_correct_list(Fluid<R> f, co
 {
     if (MODE != 0 && !sc->active) return;
     const uint32_t i = gtid();
-    if (i >= f.n) return;
+    if (i >= f.count()) return;
     const V3<R> sum = correct_sum_one<R, MODE>(i, f, bpos, g, cs, bs, c, akinci, L);
     correct_apply<R, MODE>(i, f, c, (R)sc->dt, sum);
 }
@@ -355,7 +355,7 @@ __global__ void __launch_bounds__(kBlock, 8) k_dfsph_predict_density_list(Fluid<
     if (!INITIAL && !sc->active) return;
     const uint32_t i = gtid();
     double err = 0.0;
-    if (i < f.n) {
+    if (i < f.count()) {
         const V3<R> vi = xyz(f.vel[i]);
         uint32_t nn;
         const R dc = velocity_div_one(i, f, bpos, g, cs, bs, c, akinci, L, vi, &nn);
@@ -369,7 +369,7 @@ __global__ void __launch_bounds__(kBlock, 8) k_dfsph_predict_density_list(Fluid<
     }
     double total;
     if (finish_reduction<false>(err, partials, &sc->block_counter, sh, &total) && threadIdx.x == 0) {
-        const double avg = f.n ? total / (double)f.n : 0.0;
+        const double avg = f.count() ? total / (double)f.count() : 0.0;
         if (!(avg == avg)) sc->status |= ST_NONFINITE;
         if (INITIAL) {
             sc->iterations = 0;
@@ -402,7 +402,7 @@ __global__ void __launch_bounds__(kBlock, 8) k_dfsph_divergence_list(Fluid<R> f,
     if (!INITIAL && !sc->active) return;
     const uint32_t i = gtid();
     double err = 0.0;
-    if (i < f.n) {
+    if (i < f.count()) {
         const V3<R> vi = xyz(f.vel[i]);
         uint32_t nn;
         R dv = velocity_div_one(i, f, bpos, g, cs, bs, c, akinci, L, vi, &nn);
@@ -414,7 +414,7 @@ __global__ void __launch_bounds__(kBlock, 8) k_dfsph_divergence_list(Fluid<R> f,
     }
     double total;
     if (finish_reduction<false>(err, partials, &sc->block_counter, sh, &total) && threadIdx.x == 0) {
-        const double avg = total / (double)f.n;
+        const double avg = total / (double)f.count();
         const double lim_v = lim.maxErrorV / sc->dt;
         if (!(avg == avg)) sc->status |= ST_NONFINITE;
         if (INITIAL) {
@@ -442,7 +442,7 @@ template <typename R>
 __global__ void k_dfsph_predict_v_warm_list(Fluid<R> f, Consts<R> c, const DevScalars* __restrict__ sc, R* __restrict__ kbuf)
 {
     const uint32_t i = gtid();
-    if (i >= f.n) return;
+    if (i >= f.count()) return;
     const R dt = (R)sc->dt;
     P4<R> v = f.vel[i];
     const P4<R> a = f.acc[i];

@@ -573,7 +573,7 @@ public:
         }
         double hh, mass;
         scene_constants<float>(d, &e.t.c, &e.t.lim, &hh, &mass);
-        int rc = grid_plan(d, e.x, e.b, true, hh, &e.plan, &err);
+        int rc = grid_plan(d, e.x, e.b, true, std::vector<double>(), hh, &e.plan, &err);
         if (rc) return rc;
         // capacity check against everything resident or pending
         uint64_t P = 0, B = 0, K = 0;

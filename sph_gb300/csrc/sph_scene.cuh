@@ -115,7 +115,7 @@ struct GridPlan {
 };
 
 inline int grid_plan(const sph_scene_desc& d, const std::vector<double>& hx, const std::vector<double>& hb, bool akinci,
-                     double h, GridPlan* out, std::string* err)
+                     const std::vector<double>& he, double h, GridPlan* out, std::string* err)
 {
     double lo[3], hi[3];
     bool given = false;
@@ -129,6 +129,7 @@ inline int grid_plan(const sph_scene_desc& d, const std::vector<double>& hx, con
                 for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], v[i + k]); hi[k] = std::max(hi[k], v[i + k]); }
         };
         acc(hx);
+        acc(he);
         if (akinci) acc(hb);
         if (d.boundary_method == SPH_BOUNDARY_CUBE && d.has_cube)
             for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], d.cube_min[k]); hi[k] = std::max(hi[k], d.cube_max[k]); }
@@ -203,7 +204,7 @@ public:
         for (auto e : tev_) if (e) cudaEventDestroy(e);
     }
 
-    unsigned nfluid() const override { return inited ? n_ : (unsigned)(hx.size() / 3); }
+    unsigned nfluid() const override { return inited ? active() : (unsigned)(hx.size() / 3); }
     unsigned nboundary() const override { return inited ? nb_ : (unsigned)(hb.size() / 3); }
 
     // ------------------------------------------------------------------
@@ -218,11 +219,20 @@ public:
         SPH_CUDA(cudaStreamCreateWithFlags(&st2_, cudaStreamNonBlocking));
         ls_ = st_;
         SPH_CUDA(cudaMallocHost((void**)&h_sc_, sizeof(DevScalars)));
-        n_ = (unsigned)(hx.size() / 3);
+        n0_ = (unsigned)(hx.size() / 3);
         akinci_ = d.boundary_method == SPH_BOUNDARY_AKINCI ? 1 : 0;
         bh_ = d.boundary_method == SPH_BOUNDARY_PCISPH ? 1 : 0;
         hasb_ = akinci_ || bh_;
         nb_ = hasb_ ? (unsigned)(hb.size() / 3) : 0u;
+        // FluidModel::addEmitter FluidModel.cpp:124-143: every emitter's
+        // particles get slots up front; emission only activates them
+        nem_ = (int)hem.size();
+        {
+            unsigned long long cap = n0_;
+            for (const EmitterSpec& e : hem) cap += e.num;
+            if (cap > (1ull << 31)) { fail("fluid plus emitter particles exceed 2^31"); return SPH_ERR_CAPACITY; }
+            n_ = (unsigned)cap;
+        }
         if (n_ == 0) { fail("no fluid particles"); return SPH_ERR_INVALID; }
         if (bh_ && hbn.size() != hb.size()) {
             fail("the PCISPH boundary model needs a normal per boundary point (sph_ctx_add_pcisph_box / _sphere)");
@@ -237,6 +247,7 @@ public:
         DevScalars s{};
         s.dt = d.time_step;
         s.scaling = pcisph_scaling();
+        s.n_active = n0_;
         SPH_CUDA(cudaMemcpyAsync(sc_.p, &s, sizeof s, cudaMemcpyHostToDevice, st_));
         // fluid upload
         {
@@ -244,10 +255,14 @@ public:
             SPH_CUDA(tx.alloc(hx.size()));
             SPH_CUDA(tv.alloc(hx.size()));
             if (hv.size() != hx.size()) hv.assign(hx.size(), 0.0);
-            SPH_CUDA(cudaMemcpyAsync(tx.p, hx.data(), hx.size() * 8, cudaMemcpyHostToDevice, st_));
-            SPH_CUDA(cudaMemcpyAsync(tv.p, hv.data(), hv.size() * 8, cudaMemcpyHostToDevice, st_));
-            k_upload_fluid<R><<<blocks(n_, 256), 256, 0, st_>>>(tx.p, tv.p, n_, 0, F(), gv_, hd_, sc_.p);
-            SPH_CUDA(cudaGetLastError());
+            if (n0_) {
+                SPH_CUDA(cudaMemcpyAsync(tx.p, hx.data(), hx.size() * 8, cudaMemcpyHostToDevice, st_));
+                SPH_CUDA(cudaMemcpyAsync(tv.p, hv.data(), hv.size() * 8, cudaMemcpyHostToDevice, st_));
+                k_upload_fluid<R><<<blocks(n0_, 256), 256, 0, st_>>>(tx.p, tv.p, n0_, 0, F(), gv_, hd_, sc_.p);
+                SPH_CUDA(cudaGetLastError());
+            }
+            rc = upload_emitters();
+            if (rc) return rc;
             SPH_CUDA(cudaStreamSynchronize(st_));
         }
         // boundary upload, sort, volumes (SPHSolver::init SPHSolver.cpp:22-39)
@@ -363,6 +378,16 @@ public:
         return k;
     }
 
+    int pause_emitters(int pause) override
+    {
+        if (!inited) { fail("not initialised"); return SPH_ERR_INVALID; }
+        if (!nem_) return SPH_OK;
+        k_emit_pause<<<1, kMaxEmitters, 0, st_>>>(em_.p, nem_, pause ? 1u : 0u, sc_.p);
+        SPH_CUDA(cudaGetLastError());
+        SPH_CUDA(cudaStreamSynchronize(st_));
+        return SPH_OK;
+    }
+
     int launch_count(unsigned long long* out) override
     {
         if (!inited) { *out = 0; return SPH_OK; }
@@ -424,7 +449,7 @@ public:
             fail("this solver configuration keeps no such field");
             return SPH_ERR_INVALID;
         }
-        const unsigned n = bnd ? nb_ : n_;
+        const unsigned n = bnd ? nb_ : active();
         const bool vec = field == SPH_FIELD_POSITION || field == SPH_FIELD_VELOCITY || field == SPH_FIELD_ACCELERATION ||
                          field == SPH_FIELD_PRESSURE_ACC || field == SPH_FIELD_NORMAL ||
                          field == SPH_FIELD_BOUNDARY_POSITION;
@@ -480,7 +505,7 @@ public:
         Fluid<R> f = F();
         Boundary<R> b = B(1);
         FieldView o;
-        o.n = bnd ? nb_ : n_;
+        o.n = bnd ? nb_ : active();
         o.id = bnd ? b.id : f.id;
         o.cell = bnd ? b.cell : f.cell;
         switch (field) {
@@ -518,7 +543,8 @@ public:
         unsigned long long ls[2] = {0, 0};
         if (lists_) {
             SPH_CUDA(cudaMemsetAsync(lstat_.p, 0, 2 * sizeof(unsigned long long), st_));
-            k_list_stats<<<blocks(n_, 256), 256, 0, st_>>>(n_, lcount_.p, kmax_, lstat_.p);
+            const unsigned na = active();
+            k_list_stats<<<blocks(na, 256), 256, 0, st_>>>(na, lcount_.p, kmax_, lstat_.p);
             SPH_CUDA(cudaGetLastError());
             SPH_CUDA(cudaMemcpyAsync(ls, lstat_.p, sizeof ls, cudaMemcpyDeviceToHost, st_));
         }
@@ -540,7 +566,8 @@ public:
         out->status = s.status;
         out->sum_iterations = s.sumIterations;
         out->sum_iterations_v = s.sumIterationsV;
-        out->num_fluid = n_;
+        out->num_fluid = nem_ ? s.n_active : n_;
+        out->num_fluid_total = n_;
         out->num_boundary = nb_;
         return SPH_OK;
     }
@@ -548,40 +575,41 @@ public:
     int neighbors(int* cells, int* rank, int* off, int* nbr, int* boff, int* bnbr, long long* totals) override
     {
         if (!inited) { fail("not initialised"); return SPH_ERR_INVALID; }
+        const unsigned na = active();
         DevBuf<int> cnt, bcnt, dcells, drank;
-        SPH_CUDA(cnt.alloc(n_));
-        SPH_CUDA(bcnt.alloc(n_));
-        SPH_CUDA(dcells.alloc(3 * (size_t)n_));
-        SPH_CUDA(drank.alloc(n_));
+        SPH_CUDA(cnt.alloc(na));
+        SPH_CUDA(bcnt.alloc(na));
+        SPH_CUDA(dcells.alloc(3 * (size_t)na));
+        SPH_CUDA(drank.alloc(na));
         Fluid<R> f = F();
         Boundary<R> b = B(1);
         k_neighbors<R><<<blocks(n_, 128), 128, 0, st_>>>(f, b.pos, b.id, b.cell, gv_, starts_.p, bstarts_.p, c_, hd_, nullptr,
                                                          nullptr, cnt.p, bcnt.p, nullptr, nullptr, dcells.p, drank.p);
         SPH_CUDA(cudaGetLastError());
-        std::vector<int> hc(n_), hbc(n_);
-        SPH_CUDA(cudaMemcpyAsync(hc.data(), cnt.p, n_ * 4, cudaMemcpyDeviceToHost, st_));
-        SPH_CUDA(cudaMemcpyAsync(hbc.data(), bcnt.p, n_ * 4, cudaMemcpyDeviceToHost, st_));
-        if (cells) SPH_CUDA(cudaMemcpyAsync(cells, dcells.p, 3 * (size_t)n_ * 4, cudaMemcpyDeviceToHost, st_));
-        if (rank) SPH_CUDA(cudaMemcpyAsync(rank, drank.p, (size_t)n_ * 4, cudaMemcpyDeviceToHost, st_));
+        std::vector<int> hc(na), hbc(na);
+        SPH_CUDA(cudaMemcpyAsync(hc.data(), cnt.p, na * 4, cudaMemcpyDeviceToHost, st_));
+        SPH_CUDA(cudaMemcpyAsync(hbc.data(), bcnt.p, na * 4, cudaMemcpyDeviceToHost, st_));
+        if (cells) SPH_CUDA(cudaMemcpyAsync(cells, dcells.p, 3 * (size_t)na * 4, cudaMemcpyDeviceToHost, st_));
+        if (rank) SPH_CUDA(cudaMemcpyAsync(rank, drank.p, (size_t)na * 4, cudaMemcpyDeviceToHost, st_));
         SPH_CUDA(cudaStreamSynchronize(st_));
-        std::vector<int> ho(n_ + 1), hbo(n_ + 1);
+        std::vector<int> ho(na + 1), hbo(na + 1);
         long long a = 0, bt = 0;
-        for (unsigned i = 0; i < n_; ++i) {
+        for (unsigned i = 0; i < na; ++i) {
             ho[i] = (int)a; hbo[i] = (int)bt;
             a += hc[i]; bt += hbc[i];
         }
-        ho[n_] = (int)a; hbo[n_] = (int)bt;
+        ho[na] = (int)a; hbo[na] = (int)bt;
         if (totals) { totals[0] = a; totals[1] = bt; }
-        if (off) std::memcpy(off, ho.data(), (n_ + 1) * 4);
-        if (boff) std::memcpy(boff, hbo.data(), (n_ + 1) * 4);
+        if (off) std::memcpy(off, ho.data(), (na + 1) * 4);
+        if (boff) std::memcpy(boff, hbo.data(), (na + 1) * 4);
         if (nbr || bnbr) {
             DevBuf<int> doff, dboff, dn, dbn;
-            SPH_CUDA(doff.alloc(n_ + 1));
-            SPH_CUDA(dboff.alloc(n_ + 1));
+            SPH_CUDA(doff.alloc(na + 1));
+            SPH_CUDA(dboff.alloc(na + 1));
             SPH_CUDA(dn.alloc((size_t)std::max<long long>(a, 1)));
             SPH_CUDA(dbn.alloc((size_t)std::max<long long>(bt, 1)));
-            SPH_CUDA(cudaMemcpyAsync(doff.p, ho.data(), (n_ + 1) * 4, cudaMemcpyHostToDevice, st_));
-            SPH_CUDA(cudaMemcpyAsync(dboff.p, hbo.data(), (n_ + 1) * 4, cudaMemcpyHostToDevice, st_));
+            SPH_CUDA(cudaMemcpyAsync(doff.p, ho.data(), (na + 1) * 4, cudaMemcpyHostToDevice, st_));
+            SPH_CUDA(cudaMemcpyAsync(dboff.p, hbo.data(), (na + 1) * 4, cudaMemcpyHostToDevice, st_));
             k_neighbors<R><<<blocks(n_, 128), 128, 0, st_>>>(f, b.pos, b.id, b.cell, gv_, starts_.p, bstarts_.p, c_, hd_,
                                                              doff.p, dboff.p, nullptr, nullptr, dn.p, dbn.p, nullptr,
                                                              nullptr);
@@ -644,7 +672,17 @@ private:
     int setup_grid()
     {
         GridPlan p;
-        const int rc = grid_plan(d, hx, hb, hasb_ != 0, hd_, &p, &err);
+        // emitters' groups where they are placed (rotated, translated)
+        std::vector<double> he;
+        for (const EmitterSpec& e : hem)
+            for (size_t k = 0; k + 2 < e.group.size(); k += 3) {
+                const double v[3] = {e.group[k], e.group[k + 1], e.group[k + 2]};
+                const double* q = e.q;
+                const double uv[3] = {q[2] * v[2] - v[1] * q[3], q[3] * v[0] - v[2] * q[1], q[1] * v[1] - v[0] * q[2]};
+                const double uuv[3] = {q[2] * uv[2] - uv[1] * q[3], q[3] * uv[0] - uv[2] * q[1], q[1] * uv[1] - uv[0] * q[2]};
+                for (int c = 0; c < 3; ++c) he.push_back(v[c] + (uv[c] * q[0] + uuv[c]) * 2.0 + e.r[c]);
+            }
+        const int rc = grid_plan(d, hx, hb, hasb_ != 0, he, hd_, &p, &err);
         if (rc) return rc;
         nkeys_ = (uint32_t)p.nkeys;
         SPH_CUDA(mortx_.alloc(p.nn[0]));
@@ -717,6 +755,7 @@ private:
             f.normal = (bh && k == 1) ? normal2_.p : normal_.p;
             f.rho = rho_.p; f.alpha = alpha_.p; f.div = div_.p; f.press = press_.p;
             f.n = (uint32_t)n_;
+            f.na = nem_ ? &sc_.p->n_active : nullptr;
             Boundary<R>& b = bd_[k];
             b.pos = bpos_[k].p; b.cell = bcell_[k].p; b.id = bid_[k].p; b.psi = bpsi_.p; b.n = nb_;
             b.nrm = bh ? bnrm_[k].p : nullptr;
@@ -749,14 +788,14 @@ private:
         if (bh_) run("k_bh_epoch", [&] { k_bh_epoch<<<1, 1, 0, ls_>>>(sc_.p); });
         if (move)
             run("k_cell_update", [&] { k_cell_update<R, true><<<blocks(n_, 256), 256, 0, ls_>>>(n_, a.pos, a.vel, a.cell, key_.p, slot_.p, count_.p, gv_,
-                                                                     c_.h, hd_, sc_.p, ce); });
+                                                                     c_.h, hd_, sc_.p, ce, nullptr, a.na); });
         else
             run("k_cell_update", [&] { k_cell_update<R, false><<<blocks(n_, 256), 256, 0, ls_>>>(n_, a.pos, a.vel, a.cell, key_.p, slot_.p, count_.p,
-                                                                      gv_, c_.h, hd_, sc_.p, ce); });
+                                                                      gv_, c_.h, hd_, sc_.p, ce, nullptr, a.na); });
         SPH_CUDA(cudaGetLastError());
         int rc = scan(starts_.p);
         if (rc) return rc;
-        run("k_scatter", [&] { k_scatter<<<blocks(n_, 256), 256, 0, ls_>>>(n_, key_.p, slot_.p, starts_.p, tmp_.p); });
+        run("k_scatter", [&] { k_scatter<<<blocks(n_, 256), 256, 0, ls_>>>(n_, key_.p, slot_.p, starts_.p, tmp_.p, a.na); });
         run("k_gather_fluid", [&] { k_gather_fluid<R><<<blocks(n_, 256), 256, 0, ls_>>>(n_, tmp_.p, key_.p, starts_.p, fl_[cur_], fl_[1 - cur_]); });
         SPH_CUDA(cudaGetLastError());
         cur_ = 1 - cur_;
@@ -829,7 +868,7 @@ private:
         P4<R>* carry = MODE == 1 ? f.predR : nullptr;
         run("k_cell_update", [&] { k_cell_update<R, MOVE, false><<<blocks(n_, 256), 256, 0, ls_>>>(n_, f.pos, f.vel, f.cell, key_.p, slot_.p,
                                                                                              count_.p, gv_, c_.h, hd_, sc_.p, nullptr,
-                                                                                             carry); });
+                                                                                             carry, f.na); });
         run("k_bh_collide", [&] { k_bh_collide<R, MODE><<<blocks(n_, 128), 128, 0, ls_>>>(f, B(1), gv_, bstarts_.p, c_, sc_.p,
                                                                                           cell_epoch_.p); });
         if (VEL) run("k_bh_correct_velocities", [&] { k_bh_correct_velocities<R, PRED><<<blocks(n_, 256), 256, 0, ls_>>>(f, c_); });
@@ -843,9 +882,69 @@ private:
     // DFSPHSolver.cpp:65-75, then the grid build.
     int dfsph_move_and_build()
     {
-        if (!bh_) return build_grid(true);
-        launch_bh_after_move<true, 0, false, false>();
+        if (!bh_ && !nem_) return build_grid(true);
+        if (bh_) {
+            launch_bh_after_move<true, 0, false, false>();
+        } else {
+            Fluid<R> f = F();
+            run("k_cell_update", [&] { k_cell_update<R, true, false><<<blocks(n_, 256), 256, 0, ls_>>>(n_, f.pos, f.vel, f.cell, key_.p, slot_.p,
+                                                                                              count_.p, gv_, c_.h, hd_, sc_.p, nullptr,
+                                                                                              nullptr, f.na); });
+        }
+        launch_emit();  // Simulation::emitParticles DFSPHSolver.cpp:77, before the grid fill
         return build_grid(false);
+    }
+
+    // Simulation::emitParticles (Simulation.cpp:325-329) at the current time.
+    void launch_emit()
+    {
+        if (!nem_) return;
+        const unsigned flags = (d.simulation_method == SPH_PCISPH ? EMIT_PCISPH : 0u) | (normal_.n >= n_ ? EMIT_NORMALS : 0u);
+        Fluid<R> f = F();
+        run("k_emit", [&] { k_emit<R><<<1, 256, 0, ls_>>>(f, em_.p, nem_, egroup_.p, gv_, hd_, d.gravity[0], d.gravity[1],
+                                                          d.gravity[2], sc_.p, &sc_.p->n_active, flags); });
+    }
+
+    // Emitter state and the group table on the device.
+    int upload_emitters()
+    {
+        if (!nem_) return SPH_OK;
+        if (nem_ > kMaxEmitters) { fail("at most 64 emitters per scene"); return SPH_ERR_INVALID; }
+        std::vector<EmitterDev> he(nem_);
+        std::vector<double> tab;
+        for (int e = 0; e < nem_; ++e) {
+            const EmitterSpec& s = hem[e];
+            EmitterDev& o = he[e];
+            for (int k = 0; k < 3; ++k) o.r[k] = s.r[k];
+            for (int k = 0; k < 4; ++k) o.q[k] = s.q[k];
+            o.v = s.v;
+            o.next = s.start;
+            // Emitter::emitSquare / emitCircle Emitter.cpp:127,159
+            const double dist = 2.0 * d.particle_radius;
+            o.period = s.spacing * 1.105 * dist / s.v;
+            o.remaining = s.num;
+            o.first = (uint32_t)(tab.size() / 3);
+            o.count = (uint32_t)(s.group.size() / 3);
+            o.pause = 0;
+            tab.insert(tab.end(), s.group.begin(), s.group.end());
+        }
+        SPH_CUDA(em_.alloc(nem_));
+        SPH_CUDA(egroup_.alloc(tab.size()));
+        SPH_CUDA(cudaMemcpyAsync(em_.p, he.data(), nem_ * sizeof(EmitterDev), cudaMemcpyHostToDevice, st_));
+        if (!tab.empty()) SPH_CUDA(cudaMemcpyAsync(egroup_.p, tab.data(), tab.size() * 8, cudaMemcpyHostToDevice, st_));
+        SPH_CUDA(cudaStreamSynchronize(st_));  // the host tables are freed on return
+        return SPH_OK;
+    }
+
+    // getNumActiveParticles: the device count for scenes with emitters.
+    unsigned active() const
+    {
+        if (!inited) return n0_;
+        if (!nem_) return n_;
+        unsigned v = 0;
+        if (cudaStreamSynchronize(st_) != cudaSuccess) return 0;
+        if (cudaMemcpy(&v, &sc_.p->n_active, sizeof v, cudaMemcpyDeviceToHost) != cudaSuccess) return 0;
+        return v;
     }
     const R* bdp() const { return bh_ ? bdp_.p : nullptr; }
 
@@ -1092,6 +1191,7 @@ private:
         if (rc) return rc;
         run("k_integrate", [&] { k_integrate<R, false><<<blocks(n_, 256), 256, 0, ls_>>>(f, gv_, hd_, c_, sc_.p); });
         if (bh_) launch_bh_after_move<false, 0, true, false>();  // WCSPHSolver.cpp:62-72
+        launch_emit();  // WCSPHSolver.cpp:75
         run("k_finish_step", [&] { k_finish_step<<<1, 1, 0, ls_>>>(sc_.p); });
         SPH_CUDA(cudaGetLastError());
         return SPH_OK;
@@ -1133,6 +1233,7 @@ private:
         if (rc) return rc;
         run("k_integrate", [&] { k_integrate<R, true><<<blocks(n_, 256), 256, 0, ls_>>>(f, gv_, hd_, c_, sc_.p); });
         if (bh_) launch_bh_after_move<false, 1, true, true>();  // PCISPHSolver.cpp:65-75
+        launch_emit();  // PCISPHSolver.cpp:78
         run("k_finish_step", [&] { k_finish_step<<<1, 1, 0, ls_>>>(sc_.p); });
         SPH_CUDA(cudaGetLastError());
         return SPH_OK;
@@ -1179,7 +1280,11 @@ private:
     LoopLimits lim_{};
     GridView gv_{};
     double hd_ = 0, mass_ = 0;
-    unsigned n_ = 0, nb_ = 0;
+    unsigned n_ = 0, nb_ = 0;   // fluid slots (initial fluid + emitter reservations), boundary points
+    unsigned n0_ = 0;           // fluid particles at init
+    int nem_ = 0;               // emitters
+    DevBuf<EmitterDev> em_;
+    DevBuf<double> egroup_;
     int akinci_ = 0;   // Akinci boundary model: boundary terms in the forces too
     int bh_ = 0;       // PCISPH boundary model
     int hasb_ = 0;     // boundary particles take part in the solver sums

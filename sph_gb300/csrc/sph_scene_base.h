@@ -27,6 +27,19 @@ long long sample_sphere(double particle_radius, const double c[3], double radius
 long long sample_pcisph_box(double support_radius, const double mn[3], const double mx[3], int inverted, double* out,
                             double* normals);
 long long fluid_block(double r, const double mn[3], const double mx[3], double* out);
+long long emitter_group(int type, double particle_radius, double width, double height, double* out);
+
+// An emitter as FluidModel::addEmitter receives it (FluidModel.cpp:124),
+// with its group (Emitter::buildSquareGroup / buildCircleGroup) sampled.
+struct EmitterSpec {
+    int type = 0;
+    unsigned num = 0;
+    double r[3] = {0, 0, 0};
+    double v = 0;
+    double q[4] = {1, 0, 0, 0};   // w, x, y, z
+    double start = 0, width = 0, height = 0, spacing = 0;
+    std::vector<double> group;    // xyz per point, emitter frame
+};
 
 // Where a downloadable field lives on the device (sorted order), for
 // conversion kernels outside the scene's own translation unit.
@@ -50,6 +63,7 @@ struct SceneBase {
     std::string err;
     std::vector<double> hx, hv, hb;   // staged points before init
     std::vector<double> hbn;          // PCISPH boundary model: a normal per boundary point
+    std::vector<EmitterSpec> hem;     // emitters, in the order they were added
     bool inited = false;
     virtual ~SceneBase() {}
     void fail(const std::string& m) { err = m; }
@@ -58,6 +72,7 @@ struct SceneBase {
     virtual int step_timed(int n, float* ms) = 0;
     virtual int sync() = 0;
     virtual int set_graph(int on) = 0;
+    virtual int pause_emitters(int pause) = 0;
     virtual int download(int field, double* out) = 0;
     virtual int stats(sph_stats* s) = 0;
     virtual int neighbors(int* cells, int* rank, int* off, int* nbr, int* boff, int* bnbr, long long* totals) = 0;

@@ -83,3 +83,42 @@ def test_pcisph_model_sampler_matches_oracle():
             a, an = sph_gb300.sample_pcisph_box(0.08, mn, mx, inv)
             b, bn = oracle.sample_bh_box(0.08, mn, mx, inv)
             assert np.array_equal(a, b) and np.array_equal(an, bn)
+
+
+@pytest.mark.parametrize("type_,r,w,h", [(1, 0.02, 0.1, 0.0), (1, 0.005, 0.3, 0.0), (1, 0.02, 0.01, 0.0),
+                                         (0, 0.02, 0.24, 0.16), (0, 0.01, 0.5, 0.05), (0, 0.02, 0.03, 0.5)])
+def test_emitter_group_matches_oracle(L, type_, r, w, h):
+    """Emitter::buildCircleGroup / buildSquareGroup: the library's group
+    equals the oracle's bit for bit (including the degenerate cases: a circle
+    narrower than one ring is its centre, a square narrower than one
+    particle is empty)."""
+    a = sph_gb300.emitter_group(type_, r, w, h)
+    b = oracle.emitter_group(type_, r, w, h)
+    assert a.shape == b.shape and np.array_equal(a, b)
+    if type_ == 1 and w < 3 * r:
+        assert a.shape == (1, 3)
+    if type_ == 0 and w < 2 * r:
+        assert a.shape == (0, 3)
+
+
+def test_circle_group_rings():
+    g = sph_gb300.emitter_group(sph_gb300.EMITTER_CIRCLE, 0.02, 0.1)
+    # centre + floor(2 pi R / 2r) points on rings R = 0.04, 0.08
+    assert g.shape == (1 + 6 + 12, 3)
+    rr = np.sqrt((g[:, :2] ** 2).sum(1))
+    assert np.allclose(sorted(set(np.round(rr, 12))), [0.0, 0.04, 0.08])
+
+
+def test_add_emitter_rejects_bad_arguments(L):
+    s = sph_gb300.Scene(method=2, radius=0.02)
+    with pytest.raises(sph_gb300.SPHError):
+        s.add_emitter(2, 10, (0, 0, 0), 1.0, width=0.1)
+    with pytest.raises(sph_gb300.SPHError):
+        s.add_emitter(1, 10, (0, 0, float("nan")), 1.0, width=0.1)
+    for _ in range(64):
+        s.add_emitter(1, 10, (0, 0, 0), 1.0, width=0.1)
+    with pytest.raises(sph_gb300.SPHError):
+        s.add_emitter(1, 10, (0, 0, 0), 1.0, width=0.1)
+    with pytest.raises(sph_gb300.SPHError):
+        s.pause_emitters(True)  # before init
+    s.close()
