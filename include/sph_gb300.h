@@ -176,6 +176,23 @@ int sph_ctx_add_emitter(sph_ctx* ctx, int type, unsigned num_particles, const do
  * time.  After sph_ctx_init. */
 int sph_ctx_pause_emitters(sph_ctx* ctx, int pause);
 
+/* Scene files (SceneLoader::readConfiguration SceneLoader.cpp:9-198 and
+ * Simulation::importScene Simulation.cpp:331-494).  sph_ctx_load_scene reads
+ * the JSON scene file and creates a context holding its fluid blocks,
+ * emitters and boundary shapes, not yet initialised; sph_ctx_import_scene
+ * also initialises it, as importScene does.  The reference's settings come
+ * from the file; base (may be NULL for the defaults) supplies this
+ * library's own: precision, threads_per_particle, neighbor_list_max and the
+ * grid box.  The scene must have one fluid model and at most one Boundary
+ * entry; mesh boundaries ("geometry") return SPH_ERR_UNSUPPORTED.  As in
+ * importScene, boundaryMethod 0 creates no boundary.  The context steps
+ * only while Configuration.startTime <= time <= endTime and names frame
+ * files after json_path (sph_ctx_set_frame_output).  On failure
+ * sph_scene_load_error() describes the problem. */
+int sph_ctx_load_scene(const char* json_path, const sph_scene_desc* base, sph_ctx** out);
+int sph_ctx_import_scene(const char* json_path, const sph_scene_desc* base, sph_ctx** out);
+const char* sph_scene_load_error(void);
+
 /* Simulation::init -> solver->init (Simulation.cpp:102-110,
  * SPHSolver.cpp:22-39, DFSPHSolver.cpp:24-36, PCISPHSolver.cpp:12-19):
  * uploads, builds the grids, boundary volumes, and DFSPH densities/alpha. */
@@ -195,7 +212,30 @@ int sph_ctx_synchronize(sph_ctx* ctx);
  * (conditional WHILE nodes): no host round trip per iteration.  1 = on. */
 int sph_ctx_set_graph(sph_ctx* ctx, int enable);
 
+/* Simulation::step / run (Simulation.cpp:148-190) and the frame export
+ * (SceneLoader::writeFluid SceneLoader.cpp:200-264, TimeManager::hasToSave
+ * TimeManager.h:101-110).  With a time window set (scene files set it) or
+ * frame output on, sph_ctx_step reads the simulated time around every step:
+ * it steps only while start <= time <= end, and after each step, once
+ * 1/fps has passed since the last frame time, counts a frame and (output
+ * on) writes it to scene_path with "_NNNN" (the frame number, first frame 1)
+ * inserted before its last five characters (".json").  A frame file holds
+ * numActiveParticles, numParticles (active plus emitter slots not yet
+ * used), positions and velocities of every slot (unused ones zero), time
+ * and timeStep.  sph_ctx_run steps until the time leaves the window or
+ * max_steps have run; without frame output it steps in unchecked runs that
+ * provably stay inside the window (the frame count then stands still).
+ * sph_ctx_write_frame writes the current state to any path. */
+int sph_ctx_set_time_window(sph_ctx* ctx, double start_time, double end_time);
+int sph_ctx_set_frame_output(sph_ctx* ctx, const char* scene_path, int active);
+int sph_ctx_get_frame(const sph_ctx* ctx, unsigned* frame);
+int sph_ctx_write_frame(sph_ctx* ctx, const char* path);
+int sph_ctx_run(sph_ctx* ctx, unsigned long long max_steps, unsigned long long* steps_done);
+
 int sph_ctx_num_particles(const sph_ctx* ctx, unsigned* num_fluid, unsigned* num_boundary);
+/* The descriptor the context was created with (for a loaded scene file:
+ * the settings read from it). */
+int sph_ctx_get_desc(const sph_ctx* ctx, sph_scene_desc* out);
 /* Copy a field to host memory in original particle order (FP64). */
 int sph_ctx_download(sph_ctx* ctx, int field, double* out);
 /* Same result as sph_ctx_download, without allocating device memory.  It has

@@ -341,6 +341,52 @@ def read_dump(path):
     return out
 
 
+def read_frames(directory, stem="scene"):
+    """Frame files SceneLoader::writeFluid wrote next to `stem`.json, as
+    arrays: frame{N}.positions / .velocities (flat xyz), .time, .timeStep,
+    .numParticles, .numActiveParticles, and .raw (the file's bytes)."""
+    import glob
+    import json
+
+    out = {}
+    for path in sorted(glob.glob(os.path.join(directory, f"{stem}_*.json"))):
+        num = int(os.path.basename(path)[len(stem) + 1:-5])
+        raw = open(path, "rb").read()
+        st = json.loads(raw)
+        tag = f"frame{num}"
+        for key in ("positions", "velocities"):
+            out[f"{tag}.{key}"] = np.asarray(st.get(key, []), dtype=np.float64).ravel()
+        for key in ("time", "timeStep", "numParticles", "numActiveParticles"):
+            out[f"{tag}.{key}"] = np.array([st[key]], dtype=np.float64)
+        out[f"{tag}.raw"] = np.frombuffer(raw, dtype=np.uint8).copy()
+    return out
+
+
+def run_reference_json(scene: dict, steps=1, dump_every=1, dump_neighbors=False, save=False, workdir=None):
+    """Run the reference's own scene-file path (Simulation::importScene on
+    `scene` written as JSON) and return its dump plus, with save, the frame
+    files SceneLoader::writeFluid wrote (see read_frames)."""
+    import json
+
+    if not os.path.exists(REF_PARITY):
+        raise FileNotFoundError(REF_PARITY)
+    with tempfile.TemporaryDirectory(dir=workdir) as td:
+        path = os.path.join(td, "scene.json")
+        with open(path, "w") as f:
+            json.dump(scene, f)
+        out = os.path.join(td, "out.bin")
+        spec = os.path.join(td, "spec.txt")
+        with open(spec, "w") as f:
+            f.write(f"json {path}\nout {out}\nsteps {steps}\ndump_every {dump_every}\n"
+                    f"dump_neighbors {int(dump_neighbors)}\nsave {int(save)}\n")
+        env = dict(os.environ, OMP_NUM_THREADS="1")
+        with open(os.devnull, "rb") as devnull_in, open(os.devnull, "wb") as devnull_out:
+            subprocess.run([REF_PARITY, spec], stdin=devnull_in, stdout=devnull_out, env=env, check=True, cwd=td)
+        res = read_dump(out)
+        res.update(read_frames(td))
+        return res
+
+
 def run_reference(params: dict, x, v=None, boxes=(), spheres=(), steps=1, dump_neighbors=False,
                   dump_every=1, timed=False, threads=1, workdir=None, bh_boxes=(), bh_spheres=(), emitters=()):
     """Run the reference's own solver on the scene and return its dump."""

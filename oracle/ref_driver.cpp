@@ -107,6 +107,8 @@ struct Spec {
     std::vector<std::vector<double>> emitters;
     double bh_normal_fct = 0, bh_tang_fct = 1;
     std::string fluid, out;
+    std::string json;         // a scene file: Simulation::importScene builds everything
+    int save = 0;             // Simulation::activateSave (frames next to the scene file)
     int steps = 1;
     int dump_neighbors = 0;   // 1: neighbour sets after init and after step 1
     int dump_every = 1;       // dump full state every k steps (0: only the last)
@@ -156,6 +158,8 @@ static Spec read_spec(const char* path)
         else if (k == "bh_normal_fct") is >> s.bh_normal_fct;
         else if (k == "bh_tang_fct") is >> s.bh_tang_fct;
         else if (k == "fluid") is >> s.fluid;
+        else if (k == "json") is >> s.json;
+        else if (k == "save") is >> s.save;
         else if (k == "out") is >> s.out;
         else if (k == "steps") is >> s.steps;
         else if (k == "dump_neighbors") is >> s.dump_neighbors;
@@ -272,98 +276,109 @@ int main(int argc, char** argv)
     if (argc < 2) { std::fprintf(stderr, "usage: ref_driver scene.txt\n"); return 2; }
     Spec s = read_spec(argv[1]);
 
-    std::vector<Vector3r> pos, vel;
-    {
-        FILE* f = std::fopen(s.fluid.c_str(), "rb");
-        if (!f) { std::fprintf(stderr, "cannot open %s\n", s.fluid.c_str()); return 2; }
-        uint64_t n = 0;
-        if (std::fread(&n, 8, 1, f) != 1) return 2;
-        std::vector<double> buf(6 * n);
-        if (std::fread(buf.data(), 8, 6 * n, f) != 6 * n) return 2;
-        std::fclose(f);
-        pos.resize(n); vel.resize(n);
-        for (uint64_t i = 0; i < n; ++i) {
-            pos[i] = Vector3r(buf[3 * i], buf[3 * i + 1], buf[3 * i + 2]);
-            vel[i] = Vector3r(buf[3 * n + 3 * i], buf[3 * n + 3 * i + 1], buf[3 * n + 3 * i + 2]);
-        }
-    }
     g_out = std::fopen(s.out.c_str(), "wb");
     if (!g_out) { std::fprintf(stderr, "cannot open %s\n", s.out.c_str()); return 2; }
 
-    // Same sequence of calls as Simulation::importScene (src/Simulation.cpp:346-487).
     Simulation* sim = Simulation::getCurrent();
-    sim->setTimeStep(s.dt);
-    sim->setFPS(s.fps);
-    sim->setMinTimeStep(s.min_dt);
-    sim->setMaxTimeStep(s.max_dt);
-    sim->setStartTime(0.0);
-    sim->setEndTime(1e30);
-    sim->setSimulationMethod(s.method);
-    sim->setBoundaryMethod(s.boundary);
-    sim->setGravity(Vector3r(s.g[0], s.g[1], s.g[2]));
-    sim->setParticleRadius(s.radius);
-    SPHSolver* solver = sim->getSolver();
-    if (s.method == Simulation::WCSPH_METHOD) {
-        WCSPHSolver* w = static_cast<WCSPHSolver*>(solver);
-        w->setStiffness(s.stiffness);
-        w->setGamma(s.gamma);
-    } else if (s.method == Simulation::PCISPH_METHOD) {
-        solver->setMaxError(s.eta);
-        if (s.min_it >= 0) solver->setMinIterations(s.min_it);
-        if (s.max_it >= 0) solver->setMaxIterations(s.max_it);
+    FluidModel* fm = nullptr;
+    if (!s.json.empty()) {
+        // the reference's own scene-file path (SceneLoader::readConfiguration
+        // + Simulation::importScene, which ends with init())
+        if (!sim->importScene(s.json)) { std::fprintf(stderr, "importScene failed\n"); return 3; }
+        s.method = sim->getSimulationMethod();
+        s.boundary = sim->getBoundaryHandlingMethod();
+        sim->activateSave(s.save != 0);
+        fm = sim->getFluidModel(0);
     } else {
-        DFSPHSolver* d = static_cast<DFSPHSolver*>(solver);
-        d->setMaxError(s.eta);
-        d->setMaxErrorV(s.eta_v);
-        d->setCFLFactor(s.cfl);
-        if (s.min_it >= 0) d->setMinIterations(s.min_it);
-        if (s.max_it >= 0) d->setMaxIterations(s.max_it);
-        if (s.min_it_v >= 0) d->setMinIterationsV(s.min_it_v);
-        if (s.max_it_v >= 0) d->setMaxIterationsV(s.max_it_v);
+        std::vector<Vector3r> pos, vel;
+        {
+            FILE* f = std::fopen(s.fluid.c_str(), "rb");
+            if (!f) { std::fprintf(stderr, "cannot open %s\n", s.fluid.c_str()); return 2; }
+            uint64_t n = 0;
+            if (std::fread(&n, 8, 1, f) != 1) return 2;
+            std::vector<double> buf(6 * n);
+            if (std::fread(buf.data(), 8, 6 * n, f) != 6 * n) return 2;
+            std::fclose(f);
+            pos.resize(n); vel.resize(n);
+            for (uint64_t i = 0; i < n; ++i) {
+                pos[i] = Vector3r(buf[3 * i], buf[3 * i + 1], buf[3 * i + 2]);
+                vel[i] = Vector3r(buf[3 * n + 3 * i], buf[3 * n + 3 * i + 1], buf[3 * n + 3 * i + 2]);
+            }
+        }
+        // Same sequence of calls as Simulation::importScene (src/Simulation.cpp:346-487).
+        sim->setTimeStep(s.dt);
+        sim->setFPS(s.fps);
+        sim->setMinTimeStep(s.min_dt);
+        sim->setMaxTimeStep(s.max_dt);
+        sim->setStartTime(0.0);
+        sim->setEndTime(1e30);
+        sim->setSimulationMethod(s.method);
+        sim->setBoundaryMethod(s.boundary);
+        sim->setGravity(Vector3r(s.g[0], s.g[1], s.g[2]));
+        sim->setParticleRadius(s.radius);
+        SPHSolver* solver = sim->getSolver();
+        if (s.method == Simulation::WCSPH_METHOD) {
+            WCSPHSolver* w = static_cast<WCSPHSolver*>(solver);
+            w->setStiffness(s.stiffness);
+            w->setGamma(s.gamma);
+        } else if (s.method == Simulation::PCISPH_METHOD) {
+            solver->setMaxError(s.eta);
+            if (s.min_it >= 0) solver->setMinIterations(s.min_it);
+            if (s.max_it >= 0) solver->setMaxIterations(s.max_it);
+        } else {
+            DFSPHSolver* d = static_cast<DFSPHSolver*>(solver);
+            d->setMaxError(s.eta);
+            d->setMaxErrorV(s.eta_v);
+            d->setCFLFactor(s.cfl);
+            if (s.min_it >= 0) d->setMinIterations(s.min_it);
+            if (s.max_it >= 0) d->setMaxIterations(s.max_it);
+            if (s.min_it_v >= 0) d->setMinIterationsV(s.min_it_v);
+            if (s.max_it_v >= 0) d->setMaxIterationsV(s.max_it_v);
+        }
+        sim->setViscosityMethod(s.visc_method);
+        sim->setSurfaceTensionMethod(s.st_method);
+        sim->setAdhesionMethod(s.adh_method);
+
+        fm = sim->addFluidModel(pos, vel);
+        // emitters as importScene adds them, before the fluid's forces
+        // (src/Simulation.cpp:403-418, SceneLoader.cpp:123-139)
+        for (auto& e : s.emitters)
+            fm->addEmitter((unsigned)e[0], (unsigned)e[1], Vector3r(e[2], e[3], e[4]), e[5], Quat4r(e[6], e[7], e[8], e[9]),
+                           e[10], e[11], e[12], e[13]);
+        fm->setRefDensity(s.density0);
+        if (s.visc_method > -1 && s.visc != 0.0) fm->setViscosityForce(s.visc, s.bvisc);
+        if (s.st_method > -1 && s.st != 0.0) fm->setSurfaceTensionForce(s.st);
+        if (s.adh_method > -1 && s.adh != 0.0) fm->setAdhesionForce(s.adh);
+
+        if (s.boundary == Simulation::AKINCI_BOUNDARY_METHOD) {
+            AkinciBoundaryModel* bm = new AkinciBoundaryModel();
+            for (auto& b : s.boxes) bm->addCube(Vector3r(b[0], b[1], b[2]), Vector3r(b[3], b[4], b[5]));
+            for (auto& b : s.spheres) bm->addSphere(Vector3r(b[0], b[1], b[2]), b[3]);
+            sim->addBoundaryModel(bm);
+        } else if (s.boundary == Simulation::PCISPH_BOUNDARY_METHOD) {
+            // as Simulation::importScene builds it (src/Simulation.cpp:459-484)
+            PCISPHBoundaryModel* bm = new PCISPHBoundaryModel();
+            Real density0 = fm->getRefDensity();
+            Real particleVolume = pow(2.0 * sim->getParticleRadius(), 3.0);
+            bm->setMass(density0 * particleVolume);
+            bm->setRefDensity(density0);
+            bm->setNormalFct(s.bh_normal_fct);
+            bm->setTangentialFct(s.bh_tang_fct);
+            for (auto& b : s.bh_boxes) bm->addCube(Vector3r(b[0], b[1], b[2]), Vector3r(b[3], b[4], b[5]), b[6] != 0);
+            for (auto& b : s.bh_spheres) bm->addSphere(Vector3r(b[0], b[1], b[2]), b[3], b[4] != 0);
+            sim->addBoundaryModel(bm);
+        } else if (s.boundary == Simulation::CUBE_BOUNDARY_METHOD && s.has_cube) {
+            // importScene never creates a CubeBoundaryModel; it is added the way
+            // CubeBoundaryModel::init expects: two points, min then max.
+            CubeBoundaryModel* cbm = new CubeBoundaryModel();
+            std::vector<Vector3r> pts = {Vector3r(s.cube[0], s.cube[1], s.cube[2]),
+                                         Vector3r(s.cube[3], s.cube[4], s.cube[5])};
+            cbm->init(pts);
+            sim->addBoundaryModel(cbm);
+        }
+
+        sim->init();
     }
-    sim->setViscosityMethod(s.visc_method);
-    sim->setSurfaceTensionMethod(s.st_method);
-    sim->setAdhesionMethod(s.adh_method);
-
-    FluidModel* fm = sim->addFluidModel(pos, vel);
-    // emitters as importScene adds them, before the fluid's forces
-    // (src/Simulation.cpp:403-418, SceneLoader.cpp:123-139)
-    for (auto& e : s.emitters)
-        fm->addEmitter((unsigned)e[0], (unsigned)e[1], Vector3r(e[2], e[3], e[4]), e[5], Quat4r(e[6], e[7], e[8], e[9]),
-                       e[10], e[11], e[12], e[13]);
-    fm->setRefDensity(s.density0);
-    if (s.visc_method > -1 && s.visc != 0.0) fm->setViscosityForce(s.visc, s.bvisc);
-    if (s.st_method > -1 && s.st != 0.0) fm->setSurfaceTensionForce(s.st);
-    if (s.adh_method > -1 && s.adh != 0.0) fm->setAdhesionForce(s.adh);
-
-    if (s.boundary == Simulation::AKINCI_BOUNDARY_METHOD) {
-        AkinciBoundaryModel* bm = new AkinciBoundaryModel();
-        for (auto& b : s.boxes) bm->addCube(Vector3r(b[0], b[1], b[2]), Vector3r(b[3], b[4], b[5]));
-        for (auto& b : s.spheres) bm->addSphere(Vector3r(b[0], b[1], b[2]), b[3]);
-        sim->addBoundaryModel(bm);
-    } else if (s.boundary == Simulation::PCISPH_BOUNDARY_METHOD) {
-        // as Simulation::importScene builds it (src/Simulation.cpp:459-484)
-        PCISPHBoundaryModel* bm = new PCISPHBoundaryModel();
-        Real density0 = fm->getRefDensity();
-        Real particleVolume = pow(2.0 * sim->getParticleRadius(), 3.0);
-        bm->setMass(density0 * particleVolume);
-        bm->setRefDensity(density0);
-        bm->setNormalFct(s.bh_normal_fct);
-        bm->setTangentialFct(s.bh_tang_fct);
-        for (auto& b : s.bh_boxes) bm->addCube(Vector3r(b[0], b[1], b[2]), Vector3r(b[3], b[4], b[5]), b[6] != 0);
-        for (auto& b : s.bh_spheres) bm->addSphere(Vector3r(b[0], b[1], b[2]), b[3], b[4] != 0);
-        sim->addBoundaryModel(bm);
-    } else if (s.boundary == Simulation::CUBE_BOUNDARY_METHOD && s.has_cube) {
-        // importScene never creates a CubeBoundaryModel; it is added the way
-        // CubeBoundaryModel::init expects: two points, min then max.
-        CubeBoundaryModel* cbm = new CubeBoundaryModel();
-        std::vector<Vector3r> pts = {Vector3r(s.cube[0], s.cube[1], s.cube[2]),
-                                     Vector3r(s.cube[3], s.cube[4], s.cube[5])};
-        cbm->init(pts);
-        sim->addBoundaryModel(cbm);
-    }
-
-    sim->init();
 
     if (s.boundary == Simulation::AKINCI_BOUNDARY_METHOD && sim->numberBoundaryModels() > 0) {
         AkinciBoundaryModel* bm = static_cast<AkinciBoundaryModel*>(sim->getBoundaryModel(0));

@@ -140,6 +140,15 @@ ABI = [
     ("sph_ctx_add_emitter", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_uint, _dp, ctypes.c_double, _dp, ctypes.c_double,
                                            ctypes.c_double, ctypes.c_double, ctypes.c_double]),
     ("sph_ctx_pause_emitters", ctypes.c_int, [_vp, ctypes.c_int]),
+    ("sph_ctx_load_scene", ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(SceneDesc), ctypes.POINTER(_vp)]),
+    ("sph_ctx_import_scene", ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(SceneDesc), ctypes.POINTER(_vp)]),
+    ("sph_scene_load_error", ctypes.c_char_p, []),
+    ("sph_ctx_get_desc", ctypes.c_int, [_vp, ctypes.POINTER(SceneDesc)]),
+    ("sph_ctx_set_time_window", ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_double]),
+    ("sph_ctx_set_frame_output", ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_int]),
+    ("sph_ctx_get_frame", ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_uint)]),
+    ("sph_ctx_write_frame", ctypes.c_int, [_vp, ctypes.c_char_p]),
+    ("sph_ctx_run", ctypes.c_int, [_vp, ctypes.c_ulonglong, ctypes.POINTER(ctypes.c_ulonglong)]),
     ("sph_ctx_init", ctypes.c_int, [_vp]),
     ("sph_ctx_step", ctypes.c_int, [_vp, ctypes.c_int]),
     ("sph_ctx_step_timed", ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
@@ -269,6 +278,59 @@ class Scene:
         if rc != 0:
             raise SPHError(f"sph_ctx_create failed ({rc})")
         self._inited = False
+
+    @classmethod
+    def load(cls, path, init=True, **params):
+        """A scene file (Simulation::importScene): the reference's settings,
+        fluid blocks, emitters and boundary shapes from the JSON file at
+        `path`; `params` set this library's own (precision,
+        threads_per_particle, neighbor_list_max, domain_min/max).  With
+        init=False the scene is returned before sph_ctx_init."""
+        L = lib()
+        self = cls.__new__(cls)
+        self._desc = make_desc(**params)
+        self._h = ctypes.c_void_p()
+        fn = L.sph_ctx_import_scene if init else L.sph_ctx_load_scene
+        rc = fn(os.fsencode(path), ctypes.byref(self._desc), ctypes.byref(self._h))
+        if rc != 0:
+            msg = L.sph_scene_load_error()
+            raise SPHError(f"loading {path} failed ({rc}): {msg.decode() if msg else ''}")
+        L.sph_ctx_get_desc(self._h, ctypes.byref(self._desc))
+        self._inited = bool(init)
+        return self
+
+    def desc(self) -> dict:
+        d = SceneDesc()
+        self._check(lib().sph_ctx_get_desc(self._h, ctypes.byref(d)), "sph_ctx_get_desc")
+        out = {}
+        for name, _ in SceneDesc._fields_:
+            v = getattr(d, name)
+            out[name] = list(v) if hasattr(v, "__len__") else v
+        return out
+
+    def set_time_window(self, start, end):
+        self._check(lib().sph_ctx_set_time_window(self._h, float(start), float(end)), "sph_ctx_set_time_window")
+
+    def set_frame_output(self, scene_path=None, active=True):
+        """Simulation::activateSave: write frame files named after scene_path."""
+        p = None if scene_path is None else os.fsencode(scene_path)
+        self._check(lib().sph_ctx_set_frame_output(self._h, p, int(bool(active))), "sph_ctx_set_frame_output")
+
+    @property
+    def frame(self):
+        f = ctypes.c_uint()
+        self._check(lib().sph_ctx_get_frame(self._h, ctypes.byref(f)), "sph_ctx_get_frame")
+        return f.value
+
+    def write_frame(self, path):
+        """SceneLoader::writeFluid to `path`."""
+        self._check(lib().sph_ctx_write_frame(self._h, os.fsencode(path)), "sph_ctx_write_frame")
+
+    def run(self, max_steps=2**63):
+        """Simulation::run: step while the time is inside the window (at most max_steps)."""
+        done = ctypes.c_ulonglong()
+        self._check(lib().sph_ctx_run(self._h, int(max_steps), ctypes.byref(done)), "sph_ctx_run")
+        return done.value
 
     def close(self):
         if getattr(self, "_h", None) and self._h.value:

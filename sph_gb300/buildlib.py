@@ -1,6 +1,6 @@
 """Build recipe of the sph_gb300 shared library (sm_103a, nvcc, no cmake).
 
-The three translation units compile in parallel and link into
+The translation units compile in parallel and link into
 ``sph_gb300/lib/libsph_gb300.so``, which the Python host layer and any C/C++
 caller load.  The FP64 parity form is compiled without FMA contraction so its
 sums round as the reference's own (non-fast-math) build does; host code is
@@ -29,8 +29,9 @@ UNITS = {
     "sph_scene_f64.cu": ["-fmad=false"],
     "sph_noalloc.cu": [],
     "sph_pool.cu": [],
+    "sph_scene_io.cpp": [],
 }
-HEADERS = ["sph_device.cuh", "sph_kernels.cuh", "sph_lists.cuh", "sph_scene.cuh", "sph_scene_base.h"]
+HEADERS = ["sph_device.cuh", "sph_kernels.cuh", "sph_lists.cuh", "sph_scene.cuh", "sph_scene_base.h", "sph_ctx.h"]
 
 
 def nvcc() -> str:
@@ -55,7 +56,7 @@ def build(verbose: bool = False, force: bool = False, extra: list[str] | None = 
     jobs = []
     for unit, flags in UNITS.items():
         src = os.path.join(CSRC, unit)
-        obj = os.path.join(OBJDIR, unit.replace(".cu", ".o"))
+        obj = os.path.join(OBJDIR, os.path.splitext(unit)[0] + ".o")
         if force or _stale(obj, src):
             jobs.append([cc, *COMMON, *flags, *(extra or []), "-c", src, "-o", obj])
 
@@ -69,7 +70,7 @@ def build(verbose: bool = False, force: bool = False, extra: list[str] | None = 
 
     with cf.ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
         list(ex.map(run, jobs))
-    objs = [os.path.join(OBJDIR, u.replace(".cu", ".o")) for u in UNITS]
+    objs = [os.path.join(OBJDIR, os.path.splitext(u)[0] + ".o") for u in UNITS]
     if jobs or not os.path.exists(LIB):
         run([cc, ARCH, "-shared", "-o", LIB, *objs, "-lcudart"])
     return LIB

@@ -6,14 +6,10 @@
 #include <string>
 
 #include "../../include/sph_gb300.h"
+#include "sph_ctx.h"
 #include "sph_scene_base.h"
 
 #include <cuda_runtime.h>
-
-struct sph_ctx {
-    sph::SceneBase* scene = nullptr;
-    std::string err;
-};
 
 namespace sph {
 
@@ -446,7 +442,12 @@ int sph_ctx_init(sph_ctx* ctx)
 int sph_ctx_step(sph_ctx* ctx, int nsteps)
 {
     if (!ctx || nsteps < 0) return bad(ctx, "invalid argument");
-    return relay(ctx, ctx->scene->step(nsteps));
+    if (!ctx->track) return relay(ctx, ctx->scene->step(nsteps));
+    for (int k = 0; k < nsteps; ++k) {
+        const int rc = sph::tracked_step(ctx);
+        if (rc != SPH_OK) return rc;
+    }
+    return SPH_OK;
 }
 
 int sph_ctx_step_timed(sph_ctx* ctx, int nsteps, float* elapsed_ms)
@@ -466,6 +467,13 @@ int sph_ctx_set_graph(sph_ctx* ctx, int enable)
 {
     if (!ctx) return SPH_ERR_INVALID;
     return relay(ctx, ctx->scene->set_graph(enable));
+}
+
+int sph_ctx_get_desc(const sph_ctx* ctx, sph_scene_desc* out)
+{
+    if (!ctx || !out) return SPH_ERR_INVALID;
+    *out = ctx->scene->d;
+    return SPH_OK;
 }
 
 int sph_ctx_num_particles(const sph_ctx* ctx, unsigned* nf, unsigned* nb)

@@ -23,6 +23,9 @@ import oracle  # noqa: E402
 from scenes import EMIT_DUMP_EVERY, EMIT_SCENES, EMIT_STEPS, SCENES, emit_scene, scene, scene_extra  # noqa: E402
 
 STEPS = 3
+SCENE_FILE_STEPS = 12
+# read before the reference first sets them (uninitialised solver members)
+UNSET_AT_INIT = ("init.iterationsV", "init.avgDensError", "init.avgDivError")
 KEEP = ("x", "v", "a", "rho", "p", "alpha", "div", "pred", "k", "kv", "pacc", "time", "dt", "iterations",
         "iterationsV", "avgDensError", "avgDivError", "maxDensityError", "scaling", "normal", "bdens", "bpress")
 
@@ -42,6 +45,8 @@ def main(ref_tree="/root/reference"):
             out["input.v"] = v
         for k, v in dump.items():
             tag, _, field = k.partition(".")
+            if k in UNSET_AT_INIT:
+                continue
             if k in ("b.x", "b.psi", "h", "mass") or k.startswith("init.") or field in KEEP:
                 out[k] = v
         np.savez_compressed(os.path.join(here, f"{name}.npz"), **out)
@@ -54,10 +59,33 @@ def main(ref_tree="/root/reference"):
         out = {"input.x": x}
         for k, v in dump.items():
             tag, _, field = k.partition(".")
+            if k in UNSET_AT_INIT:
+                continue
             if k in ("b.x", "b.psi", "h", "mass") or k.startswith("init.") or field in KEEP:
                 out[k] = v
         np.savez_compressed(os.path.join(here, f"{name}.npz"), **out)
         print(name, x.shape[0], "fluid at start,", len(dump[f"s{EMIT_STEPS}.rho"]), "after", EMIT_STEPS, "steps")
+    # scene files (scenes/*.json) through the reference's own loader
+    # (Simulation::importScene) with frame output on: state every third of
+    # SCENE_FILE_STEPS steps and every frame file SceneLoader::writeFluid wrote
+    import json
+
+    for fn in sorted(os.listdir(os.path.join(here, "scenes"))):
+        if not fn.endswith(".json"):
+            continue
+        with open(os.path.join(here, "scenes", fn)) as f:
+            sc = json.load(f)
+        dump = oracle.run_reference_json(sc, steps=SCENE_FILE_STEPS, dump_every=3, save=True,
+                                         dump_neighbors=sc["Configuration"]["simulationMethod"] == 2)
+        out = {}
+        for k, v in dump.items():
+            tag, _, field = k.partition(".")
+            if k in UNSET_AT_INIT:
+                continue
+            if k in ("b.x", "b.psi", "h", "mass") or k.startswith("init.") or k.startswith("frame") or field in KEEP:
+                out[k] = v
+        np.savez_compressed(os.path.join(here, "file_" + fn[:-5] + ".npz"), **out)
+        print("file", fn, len(dump["init.rho"]), "fluid at init,", sum(1 for k in dump if k.endswith(".raw")), "frames")
 
 
 if __name__ == "__main__":
