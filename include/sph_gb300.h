@@ -156,6 +156,13 @@ int sph_ctx_add_boundary_points(sph_ctx* ctx, const double* x, unsigned n);
  * normals (sph_ctx_add_boundary_points) are rejected for this model. */
 int sph_ctx_add_pcisph_box(sph_ctx* ctx, const double mn[3], const double mx[3], int inverted);
 int sph_ctx_add_pcisph_sphere(sph_ctx* ctx, const double c[3], double radius, int inverted);
+/* AkinciBoundaryModel::addGeometry (AkinciBoundayModel.cpp:78-98,166-221):
+ * the surface of a triangulated OBJ mesh sampled at most max_distance apart
+ * (vertices, edges, then lines across each face; the scene file's
+ * "geometry" entry passes spacing * 2r), rotated by pi/2 about x as the
+ * reference places every mesh: (x, y, z) -> (x, -z, y).  Akinci boundary
+ * model only. */
+int sph_ctx_add_boundary_mesh(sph_ctx* ctx, const char* obj_path, double max_distance);
 
 /* FluidModel::addEmitter (FluidModel.cpp:124-143, Emitter.cpp:10-29), before
  * sph_ctx_init: an emitter of num_particles particles, square (type
@@ -184,8 +191,10 @@ int sph_ctx_pause_emitters(sph_ctx* ctx, int pause);
  * from the file; base (may be NULL for the defaults) supplies this
  * library's own: precision, threads_per_particle, neighbor_list_max and the
  * grid box.  The scene must have one fluid model and at most one Boundary
- * entry; mesh boundaries ("geometry") return SPH_ERR_UNSUPPORTED.  As in
- * importScene, boundaryMethod 0 creates no boundary.  The context steps
+ * entry.  Mesh files ("geometry") are read relative to the working
+ * directory, as the reference reads them, and sampled for the Akinci model
+ * only; as in importScene, boundaryMethod 0 creates no boundary and the
+ * PCISPH boundary model takes boxes and spheres only.  The context steps
  * only while Configuration.startTime <= time <= endTime and names frame
  * files after json_path (sph_ctx_set_frame_output).  On failure
  * sph_scene_load_error() describes the problem. */
@@ -371,6 +380,9 @@ long long sph_fluid_block(double particle_radius, const double min[3], const dou
 /* Emitter::buildSquareGroup / buildCircleGroup (Emitter.cpp:31-79): the
  * group an emitter emits each time, in its local frame (out may be NULL). */
 long long sph_emitter_group(int type, double particle_radius, double width, double height, double* out);
+/* The points sph_ctx_add_boundary_mesh adds (out may be NULL to count; -1
+ * when the file cannot be read or is malformed). */
+long long sph_sample_mesh(const char* obj_path, double max_distance, double* out);
 
 /* Build identification string. */
 const char* sph_version(void);

@@ -388,7 +388,8 @@ def run_reference_json(scene: dict, steps=1, dump_every=1, dump_neighbors=False,
 
 
 def run_reference(params: dict, x, v=None, boxes=(), spheres=(), steps=1, dump_neighbors=False,
-                  dump_every=1, timed=False, threads=1, workdir=None, bh_boxes=(), bh_spheres=(), emitters=()):
+                  dump_every=1, timed=False, threads=1, workdir=None, bh_boxes=(), bh_spheres=(), emitters=(),
+                  geometries=()):
     """Run the reference's own solver on the scene and return its dump."""
     exe = REF_TIMED if timed else REF_PARITY
     if not os.path.exists(exe):
@@ -428,6 +429,8 @@ def run_reference(params: dict, x, v=None, boxes=(), spheres=(), steps=1, dump_n
             lines.append("bh_box " + " ".join(repr(float(t)) for t in list(mn) + list(mx)) + f" {int(inv)}")
         for c, r, inv in bh_spheres:
             lines.append("bh_sphere " + " ".join(repr(float(t)) for t in list(c) + [r]) + f" {int(inv)}")
+        for path, spacing in geometries:
+            lines.append(f"geometry {os.path.abspath(path)} {float(spacing)!r}")
         for e in emitters:
             t, num, pos, vel, rot, start, w, hgt, sp = _emitter_args(e)
             lines.append("emitter " + " ".join([str(t), str(num)] + [repr(float(q)) for q in list(pos) + [vel] + list(rot)

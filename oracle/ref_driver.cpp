@@ -27,7 +27,6 @@
 #include "PCISPHBoundaryModel.h"
 #include "CubicSpline.h"
 #include "HashTable.h"
-#include "../extern/RegularTriangleSampling.h"
 
 #include <omp.h>
 #include <cstdio>
@@ -39,16 +38,6 @@
 #include <string>
 #include <vector>
 
-// Mesh sampling is not on the simulated path and needs Eigen; this stub makes
-// the link succeed and refuses to run.
-namespace SPH {
-void RegularTriangleSampling::sampleMesh(const unsigned int, const Vector3r*, const unsigned int,
-                                         const unsigned int*, const Real, std::vector<Vector3r>&)
-{
-    std::fprintf(stderr, "ref_driver: mesh sampling is not available in the oracle build\n");
-    std::abort();
-}
-}  // namespace SPH
 
 // Read access to protected solver state through member pointers (legal C++:
 // a member pointer formed in a derived class's scope applies to the base).
@@ -103,6 +92,7 @@ struct Spec {
     double cube[6] = {0, 0, 0, 1, 1, 1};
     std::vector<std::vector<double>> boxes, spheres;
     std::vector<std::vector<double>> bh_boxes, bh_spheres;  // + inverted flag
+    std::vector<std::pair<std::string, double>> geometries;  // OBJ path, spacing (in 2r)
     // type num rx ry rz v qw qx qy qz start width height spacing
     std::vector<std::vector<double>> emitters;
     double bh_normal_fct = 0, bh_tang_fct = 1;
@@ -154,6 +144,7 @@ static Spec read_spec(const char* path)
         else if (k == "sphere") { std::vector<double> b(4); for (double& c : b) is >> c; s.spheres.push_back(b); }
         else if (k == "bh_box") { std::vector<double> b(7); for (double& c : b) is >> c; s.bh_boxes.push_back(b); }
         else if (k == "bh_sphere") { std::vector<double> b(5); for (double& c : b) is >> c; s.bh_spheres.push_back(b); }
+        else if (k == "geometry") { std::string p; double sp; is >> p >> sp; s.geometries.emplace_back(p, sp); }
         else if (k == "emitter") { std::vector<double> b(14); for (double& c : b) is >> c; s.emitters.push_back(b); }
         else if (k == "bh_normal_fct") is >> s.bh_normal_fct;
         else if (k == "bh_tang_fct") is >> s.bh_tang_fct;
@@ -354,6 +345,8 @@ int main(int argc, char** argv)
             AkinciBoundaryModel* bm = new AkinciBoundaryModel();
             for (auto& b : s.boxes) bm->addCube(Vector3r(b[0], b[1], b[2]), Vector3r(b[3], b[4], b[5]));
             for (auto& b : s.spheres) bm->addSphere(Vector3r(b[0], b[1], b[2]), b[3]);
+            // as importScene (src/Simulation.cpp:441-442): maximum sample distance spacing * 2r
+            for (auto& gm : s.geometries) bm->addGeometry(gm.first, gm.second * s.radius * 2.0);
             sim->addBoundaryModel(bm);
         } else if (s.boundary == Simulation::PCISPH_BOUNDARY_METHOD) {
             // as Simulation::importScene builds it (src/Simulation.cpp:459-484)

@@ -151,12 +151,13 @@ struct tmat4 {
     const tvec4<T>& operator[](int c) const { return m[c]; }
 };
 
+// m * v as GLM evaluates it: (m[0] v.x + m[1] v.y) + (m[2] v.z + m[3] v.w)
 template <typename T>
 tvec4<T> operator*(const tmat4<T>& a, const tvec4<T>& v)
 {
     tvec4<T> r;
     for (int row = 0; row < 4; ++row)
-        r[row] = a[0][row] * v.x + a[1][row] * v.y + a[2][row] * v.z + a[3][row] * v.w;
+        r[row] = (a[0][row] * v.x + a[1][row] * v.y) + (a[2][row] * v.z + a[3][row] * v.w);
     return r;
 }
 

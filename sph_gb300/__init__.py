@@ -140,6 +140,8 @@ ABI = [
     ("sph_ctx_add_emitter", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_uint, _dp, ctypes.c_double, _dp, ctypes.c_double,
                                            ctypes.c_double, ctypes.c_double, ctypes.c_double]),
     ("sph_ctx_pause_emitters", ctypes.c_int, [_vp, ctypes.c_int]),
+    ("sph_ctx_add_boundary_mesh", ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_double]),
+    ("sph_sample_mesh", ctypes.c_longlong, [ctypes.c_char_p, ctypes.c_double, _dp]),
     ("sph_ctx_load_scene", ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(SceneDesc), ctypes.POINTER(_vp)]),
     ("sph_ctx_import_scene", ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(SceneDesc), ctypes.POINTER(_vp)]),
     ("sph_scene_load_error", ctypes.c_char_p, []),
@@ -379,6 +381,12 @@ class Scene:
                     "sph_ctx_add_pcisph_sphere")
         return self
 
+    def add_boundary_mesh(self, obj_path, max_distance):
+        """AkinciBoundaryModel::addGeometry: an OBJ mesh's surface samples as boundary points."""
+        self._check(lib().sph_ctx_add_boundary_mesh(self._h, os.fsencode(obj_path), float(max_distance)),
+                    "sph_ctx_add_boundary_mesh")
+        return self
+
     def add_emitter(self, type, num_particles, position, velocity, rotation=(1.0, 0.0, 0.0, 0.0), start_time=0.0,
                     width=0.0, height=0.0, spacing=1.0):
         """FluidModel::addEmitter: type EMITTER_SQUARE (0) or EMITTER_CIRCLE (1);
@@ -524,6 +532,18 @@ def sample_pcisph_box(h, mn, mx, inverted=True):
 
 
 EMITTER_SQUARE, EMITTER_CIRCLE = 0, 1
+
+
+def sample_mesh(obj_path, max_distance):
+    """The boundary points AkinciBoundaryModel::addGeometry makes of an OBJ mesh."""
+    L = lib()
+    m = L.sph_sample_mesh(os.fsencode(obj_path), float(max_distance), None)
+    if m < 0:
+        raise SPHError(f"cannot sample {obj_path}")
+    out = np.zeros((m, 3))
+    if m:
+        L.sph_sample_mesh(os.fsencode(obj_path), float(max_distance), _d(out))
+    return out
 
 
 def emitter_group(type, particle_radius, width, height=0.0):

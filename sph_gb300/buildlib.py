@@ -30,6 +30,7 @@ UNITS = {
     "sph_noalloc.cu": [],
     "sph_pool.cu": [],
     "sph_scene_io.cpp": [],
+    "sph_mesh.cpp": [],
 }
 HEADERS = ["sph_device.cuh", "sph_kernels.cuh", "sph_lists.cuh", "sph_scene.cuh", "sph_scene_base.h", "sph_ctx.h"]
 

@@ -385,6 +385,28 @@ int sph_ctx_add_boundary_sphere(sph_ctx* ctx, const double c[3], double radius)
     return rc;
 }
 
+int sph_ctx_add_boundary_mesh(sph_ctx* ctx, const char* obj_path, double max_distance)
+{
+    if (!ctx || !obj_path) return bad(ctx, "invalid argument");
+    if (ctx->scene->inited) return bad(ctx, "boundary must be added before sph_ctx_init");
+    if (ctx->scene->d.boundary_method != SPH_BOUNDARY_AKINCI)
+        return bad(ctx, "mesh boundaries belong to the Akinci boundary model (AkinciBoundaryModel::addGeometry)");
+    std::vector<double> pts;
+    std::string err;
+    long long m;
+    try {
+        m = sph::sample_mesh(obj_path, max_distance, &pts, &err);
+    } catch (...) {
+        return bad(ctx, "out of host memory");
+    }
+    if (m < 0) {
+        ctx->err = err;
+        return SPH_ERR_INVALID;
+    }
+    if (m > 0xffffffffll) return bad(ctx, "too many mesh samples");
+    return add_boundary(ctx, pts.data(), (unsigned)m);
+}
+
 int sph_ctx_add_boundary_points(sph_ctx* ctx, const double* x, unsigned n)
 {
     if (!ctx || (!x && n)) return bad(ctx, "invalid argument");
@@ -535,6 +557,21 @@ long long sph_sample_sphere(double particle_radius, const double c[3], double ra
 {
     if (!c || !(particle_radius > 0.0) || !(radius > 0.0)) return -1;
     return sph::sample_sphere(particle_radius, c, radius, out);
+}
+
+long long sph_sample_mesh(const char* obj_path, double max_distance, double* out)
+{
+    if (!obj_path) return -1;
+    std::vector<double> pts;
+    std::string err;
+    long long m;
+    try {
+        m = sph::sample_mesh(obj_path, max_distance, &pts, &err);
+    } catch (...) {
+        return -1;
+    }
+    if (m > 0 && out) std::memcpy(out, pts.data(), pts.size() * sizeof(double));
+    return m;
 }
 
 long long sph_emitter_group(int type, double particle_radius, double width, double height, double* out)

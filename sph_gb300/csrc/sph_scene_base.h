@@ -28,6 +28,9 @@ long long sample_pcisph_box(double support_radius, const double mn[3], const dou
                             double* normals);
 long long fluid_block(double r, const double mn[3], const double mx[3], double* out);
 long long emitter_group(int type, double particle_radius, double width, double height, double* out);
+// sph_mesh.cpp: AkinciBoundaryModel::addGeometry's surface samples of an OBJ
+// file (xyz per point); -1 and *err on failure.
+long long sample_mesh(const char* path, double max_distance, std::vector<double>* out, std::string* err);
 
 // An emitter as FluidModel::addEmitter receives it (FluidModel.cpp:124),
 // with its group (Emitter::buildSquareGroup / buildCircleGroup) sampled.

@@ -392,6 +392,7 @@ int load_scene(const char* path, const sph_scene_desc* base, sph_ctx** out, std:
     // SceneLoader::readBoundaryInfo SceneLoader.cpp:143-198
     struct Shape { double a[3], b[3]; double radius; int inverted; };
     std::vector<Shape> boxes, spheres;
+    std::vector<std::pair<std::string, double>> meshes;  // OBJ path, spacing in particle diameters
     const JVal* bnd = A.list(&root, "Boundary");
     if (bnd && bnd->arr.size() > 1) {
         // the reference builds one model per entry, and AkinciBoundaryModel::
@@ -427,9 +428,12 @@ int load_scene(const char* path, const sph_scene_desc* base, sph_ctx** out, std:
                 spheres.push_back(s);
             }
         if (const JVal* gl = A.list(b, "geometry"))
-            if (!gl->arr.empty()) {
-                *err = "scene file: Boundary[0].geometry (mesh boundaries) is not supported";
-                return SPH_ERR_UNSUPPORTED;
+            for (size_t j = 0; j < gl->arr.size(); ++j) {
+                const std::string W = B + "geometry[" + std::to_string(j) + "].";
+                const JVal* pth = A.need(&gl->arr[j], "path", W);
+                if (pth && pth->k != JVal::Str && A.ok()) A.err = "scene file: " + W + "path is not a string";
+                const double spacing = A.num(&gl->arr[j], "spacing", W);
+                if (A.ok()) meshes.emplace_back(pth->str, spacing);
             }
     }
     if (!A.ok()) { *err = A.err; return SPH_ERR_INVALID; }
@@ -451,6 +455,9 @@ int load_scene(const char* path, const sph_scene_desc* base, sph_ctx** out, std:
             if (check(ctx, sph_ctx_add_boundary_box(ctx, s.a, s.b), "boundary box", err)) return bail(SPH_ERR_INVALID);
         for (const Shape& s : spheres)
             if (check(ctx, sph_ctx_add_boundary_sphere(ctx, s.a, s.radius), "boundary sphere", err)) return bail(SPH_ERR_INVALID);
+        for (const auto& m : meshes)  // addGeometry(path, spacing * particleRadius * 2.0)
+            if (check(ctx, sph_ctx_add_boundary_mesh(ctx, m.first.c_str(), m.second * d.particle_radius * 2.0), "boundary mesh", err))
+                return bail(SPH_ERR_INVALID);
     } else if (d.boundary_method == SPH_BOUNDARY_PCISPH) {  // Simulation.cpp:447-487
         for (const Shape& s : boxes)
             if (check(ctx, sph_ctx_add_pcisph_box(ctx, s.a, s.b, s.inverted), "boundary box", err)) return bail(SPH_ERR_INVALID);

@@ -30,6 +30,19 @@ KEEP = ("x", "v", "a", "rho", "p", "alpha", "div", "pred", "k", "kv", "pacc", "t
         "iterationsV", "avgDensError", "avgDivError", "maxDensityError", "scaling", "normal", "bdens", "bpress")
 
 
+def resolve_mesh_paths(sc, base):
+    """Mesh paths in a scene file are relative to the file; the reference
+    reads them relative to its working directory, so make them absolute."""
+    for b in sc.get("Boundary", []):
+        for g in b.get("geometry", []):
+            g["path"] = os.path.abspath(os.path.join(base, g["path"]))
+
+
+# mesh files and sample spacings (in particle diameters 2r, r = 0.02) whose
+# boundary samples are kept in meshes.npz
+MESH_CASES = (("ramp", 0.5), ("ramp", 1.3), ("tetra_attrs", 1.0), ("tetra_attrs", 0.25))
+
+
 def main(ref_tree="/root/reference"):
     if not oracle.reference_available():
         if not oracle.build_reference(ref_tree):
@@ -75,6 +88,7 @@ def main(ref_tree="/root/reference"):
             continue
         with open(os.path.join(here, "scenes", fn)) as f:
             sc = json.load(f)
+        resolve_mesh_paths(sc, os.path.join(here, "scenes"))
         dump = oracle.run_reference_json(sc, steps=SCENE_FILE_STEPS, dump_every=3, save=True,
                                          dump_neighbors=sc["Configuration"]["simulationMethod"] == 2)
         out = {}
@@ -86,6 +100,22 @@ def main(ref_tree="/root/reference"):
                 out[k] = v
         np.savez_compressed(os.path.join(here, "file_" + fn[:-5] + ".npz"), **out)
         print("file", fn, len(dump["init.rho"]), "fluid at init,", sum(1 for k in dump if k.endswith(".raw")), "frames")
+    mesh_fixture(here)
+
+
+def mesh_fixture(here):
+    """AkinciBoundaryModel::addGeometry's samples of the test meshes, from
+    the reference build (a box is added first, as a scene file would)."""
+    x = oracle.fluid_block(0.02, (0.2, 0.5, 0.2), (0.3, 0.6, 0.3))
+    nbox = oracle.sample_box(0.08, (0, 0, 0), (0.8, 0.8, 0.8)).shape[0]
+    out = {}
+    for mesh, sp in MESH_CASES:
+        path = os.path.join(here, "meshes", mesh + ".obj")
+        dump = oracle.run_reference(dict(method=2, boundary=2, radius=0.02), x, boxes=[((0, 0, 0), (0.8, 0.8, 0.8))],
+                                    steps=1, geometries=[(path, sp)])
+        out[f"{mesh}/{sp!r}"] = dump["b.x"].reshape(-1, 3)[nbox:]
+    np.savez_compressed(os.path.join(here, "meshes.npz"), **out)
+    print("meshes", {k: v.shape[0] for k, v in out.items()})
 
 
 if __name__ == "__main__":

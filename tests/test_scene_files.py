@@ -18,6 +18,7 @@ import json
 import math
 import os
 import re
+import tempfile
 from decimal import Decimal
 
 import numpy as np
@@ -31,8 +32,26 @@ FILES = sorted(f[:-5] for f in os.listdir(SCENE_DIR) if f.endswith(".json"))
 STEP_FIELDS = ("x", "v", "rho", "p", "alpha", "div", "pred", "k", "kv", "pacc")
 
 
+_RESOLVED = {}
+
+
 def scene_path(name):
-    return os.path.join(SCENE_DIR, name + ".json")
+    """The scene file; a scene with meshes is copied with its mesh paths
+    (relative to the file) made absolute, since they are read relative to
+    the working directory."""
+    path = os.path.join(SCENE_DIR, name + ".json")
+    cfg = json.load(open(path))
+    if not any(b.get("geometry") for b in cfg.get("Boundary", [])):
+        return path
+    if name not in _RESOLVED:
+        for b in cfg["Boundary"]:
+            for g in b.get("geometry", []):
+                g["path"] = os.path.abspath(os.path.join(SCENE_DIR, g["path"]))
+        d = tempfile.mkdtemp(prefix="sph_scene_")
+        _RESOLVED[name] = os.path.join(d, name + ".json")
+        with open(_RESOLVED[name], "w") as f:
+            json.dump(cfg, f)
+    return _RESOLVED[name]
 
 
 def fixture(name):
@@ -121,8 +140,10 @@ def test_scene_file_errors(tmp_path):
     cases = []
     c = json.loads(json.dumps(base)); del c["Configuration"]["fps"]; cases.append((c, "Configuration.fps"))
     c = json.loads(json.dumps(base)); c["Fluid"]["FluidModel"].append(c["Fluid"]["FluidModel"][0]); cases.append((c, "one fluid model"))
-    c = json.loads(json.dumps(base)); c["Boundary"][0]["geometry"] = [{"path": "a.obj", "spacing": 1.0}]
-    cases.append((c, "geometry"))
+    c = json.loads(json.dumps(base)); c["Boundary"][0]["geometry"] = [{"path": "/nonexistent/a.obj", "spacing": 1.0}]
+    cases.append((c, "a.obj"))
+    c = json.loads(json.dumps(base)); c["Boundary"][0]["geometry"] = [{"spacing": 1.0}]
+    cases.append((c, "geometry[0].path"))
     c = json.loads(json.dumps(base)); c["Boundary"].append(c["Boundary"][0]); cases.append((c, "more than one Boundary"))
     c = json.loads(json.dumps(base)); c["Configuration"]["simulationMethod"] = 5; cases.append((c, "simulationMethod"))
     c = json.loads(json.dumps(base)); c["Configuration"]["gravity"] = [0, -9.81]; cases.append((c, "gravity"))
