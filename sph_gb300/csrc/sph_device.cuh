@@ -48,7 +48,12 @@ template <typename R> __device__ __forceinline__ R ldg1(const R* p) { return __l
 // of the same pass re-use from L1.
 __device__ __forceinline__ P4<float> ldcs4(const P4<float>* p)
 {
-    float4 t = __ldcs(reinterpret_cast<const float4*>(p));
+    // read-only and not allocated in L1, which keeps the gathered neighbour
+    // fields
+    float4 t;
+    asm("ld.global.nc.L1::no_allocate.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(t.x), "=f"(t.y), "=f"(t.z), "=f"(t.w)
+                 : "l"(p));
     return P4<float>{t.x, t.y, t.z, t.w};
 }
 __device__ __forceinline__ P4<double> ldcs4(const P4<double>* p)
