@@ -253,6 +253,40 @@ __device__ __forceinline__ void walk(const GridView& g, const uint32_t* __restri
 // Smoothing kernels
 // ---------------------------------------------------------------------------
 
+// W and grad W of one pair from the squared distance, for the pair-list
+// build.  FAST (FP32 pool): 1/|r| from the hardware reciprocal square root
+// (a few ulp) replaces the correctly rounded sqrt and division; the
+// polynomials are those of cubic_W / cubic_gradW.
+template <bool FAST, typename R>
+__device__ __forceinline__ void cubic_W_gradW(const Consts<R>& c, V3<R> r, R r2, R* w, V3<R>* grad)
+{
+    if constexpr (FAST && sizeof(R) == 4) {
+        const float rinv = rsqrtf(r2);
+        const float rl = r2 > 0.f ? r2 * rinv : 0.f;
+        const float q = rl * c.inv_h;
+        float res = 0.f;
+        V3<float> g = {0.f, 0.f, 0.f};
+        if (q <= 1.f) {
+            const V3<float> gradq = r * (rinv * c.inv_h);
+            if (q <= 0.5f) {
+                const float q2 = q * q;
+                res = c.cs_k * (6.f * (q2 * q) - 6.f * q2 + 1.f);
+                g = (c.cs_l * q * (3.f * q - 2.f)) * gradq;
+            } else {
+                const float fq = 1.f - q;
+                res = c.cs_k * (2.f * (fq * fq * fq));
+                g = (c.cs_l * (-fq * fq)) * gradq;
+            }
+            if (!(rl > 1.0e-5f)) g = V3<float>{0.f, 0.f, 0.f};
+        }
+        *w = res;
+        *grad = g;
+    } else {
+        *w = cubic_W(c, sqrt(r2));
+        *grad = cubic_gradW(c, r, r2);
+    }
+}
+
 // Poly6::W Poly6.h:30-43 from the squared distance (the length is formed and
 // squared again, as the reference does).
 template <typename R> __device__ __forceinline__ R poly6_W(const Consts<R>& c, R r2)

@@ -70,7 +70,7 @@ template <typename R> struct BuildSums {
 // Particles whose candidates overflow the shared queue: the whole
 // evaluation inside the walk.  Out of line, so the common path's register
 // allocation does not carry it.
-template <typename R>
+template <typename R, bool FAST>
 __device__ __noinline__ BuildSums<R> build_walk_all(uint32_t i, const Fluid<R>& f, const GridView& g,
                                                     const uint32_t* __restrict__ cs, const Consts<R>& c, const Lists<R>& L,
                                                     V3<R> xi, uint32_t pc)
@@ -81,8 +81,11 @@ __device__ __noinline__ BuildSums<R> build_walk_all(uint32_t i, const Fluid<R>& 
         const V3<R> r = s - xyz(ldg4(f.pos + j));
         const R r2 = dot3(r, r);
         if (!(r2 <= c.cull2)) return;
-        b.density += c.mass * cubic_W(c, sqrt(r2));
-        const V3<R> mg = c.mass * cubic_gradW(c, r, r2);
+        R w;
+        V3<R> gw;
+        cubic_W_gradW<FAST>(c, r, r2, &w, &gw);
+        b.density += c.mass * w;
+        const V3<R> mg = c.mass * gw;
         const R mg2 = dot3(mg, mg);
         if (mg2 > (R)0) {
             b.sumGrad = b.sumGrad + mg;
@@ -99,7 +102,7 @@ __device__ __noinline__ BuildSums<R> build_walk_all(uint32_t i, const Fluid<R>& 
     return b;
 }
 
-template <typename R>
+template <typename R, bool FAST = false>
 __device__ __forceinline__ void build_lists_one(uint32_t i, const Fluid<R>& f, const P4<R>* __restrict__ bpos,
                                                 const GridView& g, const uint32_t* __restrict__ cs,
                                                 const uint32_t* __restrict__ bs, const Consts<R>& c, int akinci,
@@ -114,8 +117,11 @@ __device__ __forceinline__ void build_lists_one(uint32_t i, const Fluid<R>& f, c
     V3<R> sumGrad = {0, 0, 0};
     uint32_t cnt = 0;
     auto accept = [&](uint32_t j, V3<R> r, R r2) {
-        density += c.mass * cubic_W(c, sqrt(r2));
-        const V3<R> mg = c.mass * cubic_gradW(c, r, r2);
+        R w;
+        V3<R> gw;
+        cubic_W_gradW<FAST>(c, r, r2, &w, &gw);
+        density += c.mass * w;
+        const V3<R> mg = c.mass * gw;
         const R mg2 = dot3(mg, mg);
         if (mg2 > (R)0) {
             sumGrad = sumGrad + mg;
@@ -146,7 +152,7 @@ __device__ __forceinline__ void build_lists_one(uint32_t i, const Fluid<R>& f, c
             accept(j, r, dot3(r, r));
         }
     } else {
-        const BuildSums<R> b = build_walk_all(i, f, g, cs, c, L, xi, pc);
+        const BuildSums<R> b = build_walk_all<R, FAST>(i, f, g, cs, c, L, xi, pc);
         density = b.density;
         sumSq = b.sumSq;
         sumGrad = b.sumGrad;
@@ -159,8 +165,11 @@ __device__ __forceinline__ void build_lists_one(uint32_t i, const Fluid<R>& f, c
             const V3<R> r = s - xyz(pb);
             const R r2 = dot3(r, r);
             if (!(r2 <= c.cull2)) return;
-            density += pb.w * cubic_W(c, sqrt(r2));
-            bg = bg + pb.w * cubic_gradW(c, r, r2);
+            R w;
+            V3<R> gw;
+            cubic_W_gradW<FAST>(c, r, r2, &w, &gw);
+            density += pb.w * w;
+            bg = bg + pb.w * gw;
         });
     sumGrad = sumGrad + bg;
     f.rho[i] = density;

@@ -217,7 +217,8 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_pool_build_lists(Fluid<float> f
     if (i >= f.n) return;
     const PoolScene& sd = T[sid[i]];
     if (!sd.running) return;
-    build_lists_one(i, f, bpos, sd.g, cs + sd.key_base, bs + sd.key_base, sd.c, sd.akinci, L, q, (uint32_t)BLOCK, qdepth);
+    build_lists_one<float, true>(i, f, bpos, sd.g, cs + sd.key_base, bs + sd.key_base, sd.c, sd.akinci, L, q, (uint32_t)BLOCK,
+                                 qdepth);
 }
 
 // Non-pressure forces of the scene (XSPH / standard / artificial viscosity;
