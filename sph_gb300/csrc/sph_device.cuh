@@ -162,7 +162,10 @@ __device__ __forceinline__ uint32_t cell_key(const GridView& g, int cx, int cy, 
 // the candidates are filed by (PCISPH's predicted positions, filed by their
 // current cells).
 // G > 1 lanes split each cell's range (lane l takes every G-th candidate).
-template <typename R, int G, bool TRIM = true, typename F>
+// ROLLED (G = 1): the nine columns one after another, each column's range
+// looked up just before it is walked, the visit code emitted once (the
+// same candidates in the same order; smaller code, fewer live registers).
+template <typename R, int G, bool TRIM = true, bool ROLLED = false, typename F>
 __device__ __forceinline__ void walk(const GridView& g, const uint32_t* __restrict__ starts, uint32_t pc, V3<R> xi, R h,
                                      int lane, F&& f)
 {
@@ -170,7 +173,34 @@ __device__ __forceinline__ void walk(const GridView& g, const uint32_t* __restri
     const int cx = cell_x(pc), cy = cell_y(pc), cz = cell_z(pc);
     const int z0 = cz > 0 ? cz - 1 : 0;
     const int z1 = cz + 1 < g.nz ? cz + 1 : g.nz - 1;
-    if constexpr (G == 1) {
+    if constexpr (G == 1 && ROLLED) {
+        const R ofx = REL ? xi.x : xi.x - (R)(cx + g.ox) * h;
+        const R ofy = REL ? xi.y : xi.y - (R)(cy + g.oy) * h;
+        const R ofz = REL ? xi.z : xi.z - (R)(cz + g.oz) * h;
+        const R gxm = ofx > (R)0 ? ofx * ofx : (R)0, gxp = h - ofx > (R)0 ? (h - ofx) * (h - ofx) : (R)0;
+        const R gym = ofy > (R)0 ? ofy * ofy : (R)0, gyp = h - ofy > (R)0 ? (h - ofy) * (h - ofy) : (R)0;
+        const R gzm = ofz > (R)0 ? ofz * ofz : (R)0, gzp = h - ofz > (R)0 ? (h - ofz) * (h - ofz) : (R)0;
+        const R lim = TRIM ? h * h * (R)(1.0 + 1e-5) : (R)INFINITY;
+        const R szm = xi.z + h, sz0 = xi.z, szp = xi.z - h;
+#pragma unroll 1
+        for (int c = 0; c < 9; ++c) {
+            const int dx = c / 3 - 1, dy = c - (c / 3) * 3 - 1;
+            const int x = cx + dx, y = cy + dy;
+            const R gxy = (dx < 0 ? gxm : (dx > 0 ? gxp : (R)0)) + (dy < 0 ? gym : (dy > 0 ? gyp : (R)0));
+            if (x < 0 || x >= g.nx || y < 0 || y >= g.ny || !(gxy <= lim)) continue;
+            const uint32_t base = (__ldg(g.mortx + x) | __ldg(g.morty + y)) * (uint32_t)g.nz;
+            const uint32_t s0 = __ldg(starts + base + z0), sm = __ldg(starts + base + cz);
+            const uint32_t sp = __ldg(starts + base + cz + 1), s1 = __ldg(starts + base + z1 + 1);
+            const uint32_t bb = gxy + gzm <= lim ? s0 : sm;
+            const uint32_t ee = gxy + gzp <= lim ? s1 : sp;
+            V3<R> s = REL ? V3<R>{xi.x - (R)dx * h, xi.y - (R)dy * h, xi.z} : xi;
+#pragma unroll 1
+            for (uint32_t j = bb; j < ee; ++j) {
+                if (REL) s.z = j < sm ? szm : (j < sp ? sz0 : szp);
+                f(j, s);
+            }
+        }
+    } else if constexpr (G == 1) {
         // the particle's offset inside its own cell, and the squared gap from
         // it to each neighbour layer (0 for its own layer): a cell whose box
         // is farther than h from the particle holds no neighbour
@@ -214,7 +244,7 @@ __device__ __forceinline__ void walk(const GridView& g, const uint32_t* __restri
             // absolute form: every candidate is compared with xi itself
             V3<R> s = REL ? V3<R>{xi.x - (R)dx * h, xi.y - (R)dy * h, xi.z} : xi;
             const uint32_t bb = b[c], ee = e[c];
-#pragma unroll 2
+#pragma unroll 1
             for (uint32_t j = bb; j < ee; ++j) {
                 if (REL) s.z = j < m0[c] ? szm : (j < m1[c] ? sz0 : szp);
                 f(j, s);

@@ -137,7 +137,7 @@ __device__ __forceinline__ void build_lists_one(uint32_t i, const Fluid<R>& f, c
     };
     // phase 1: cull
     uint32_t nq = 0;
-    walk<R, 1>(g, cs, pc, xi, c.h, 0, [&](uint32_t j, V3<R> s) {
+    walk<R, 1, true, FAST>(g, cs, pc, xi, c.h, 0, [&](uint32_t j, V3<R> s) {
         const V3<R> r = s - xyz(ldg4(f.pos + j));
         if (dot3(r, r) <= c.cull2) {
             if (nq < qcap) q[nq * qstride + threadIdx.x] = j;
