@@ -234,7 +234,11 @@ int sph_ctx_set_graph(sph_ctx* ctx, int enable);
  * and timeStep.  sph_ctx_run steps until the time leaves the window or
  * max_steps have run; without frame output it steps in unchecked runs that
  * provably stay inside the window (the frame count then stands still).
- * sph_ctx_write_frame writes the current state to any path. */
+ * Frame files are written by a host thread while the next steps run (the
+ * state is captured on the device when the frame is due); they are complete
+ * when sph_ctx_synchronize, sph_ctx_run or sph_ctx_destroy returns, which
+ * also report a failed write.  sph_ctx_write_frame writes the current state
+ * to any path, synchronously. */
 int sph_ctx_set_time_window(sph_ctx* ctx, double start_time, double end_time);
 int sph_ctx_set_frame_output(sph_ctx* ctx, const char* scene_path, int active);
 int sph_ctx_get_frame(const sph_ctx* ctx, unsigned* frame);

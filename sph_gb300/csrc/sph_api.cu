@@ -260,6 +260,7 @@ int sph_ctx_create(const sph_scene_desc* desc, sph_ctx** out)
 int sph_ctx_destroy(sph_ctx* ctx)
 {
     if (!ctx) return SPH_ERR_INVALID;
+    sph::frames_close(ctx);  // queued frame files are written first
     delete ctx->scene;
     delete ctx;
     return SPH_OK;
@@ -482,7 +483,9 @@ int sph_ctx_synchronize(sph_ctx* ctx)
 {
     if (!ctx) return SPH_ERR_INVALID;
     if (!ctx->scene->inited) return SPH_OK;
-    return relay(ctx, ctx->scene->sync());
+    const int rc = relay(ctx, ctx->scene->sync());
+    if (rc != SPH_OK) return rc;
+    return sph::frames_flush(ctx);  // and every queued frame file is on disk
 }
 
 int sph_ctx_set_graph(sph_ctx* ctx, int enable)

@@ -9,6 +9,10 @@
 
 #include "sph_scene_base.h"
 
+namespace sph {
+class FrameWriter;  // sph_scene_io.cpp: frame files written by a host thread
+}
+
 struct sph_ctx {
     sph::SceneBase* scene = nullptr;
     std::string err;
@@ -22,9 +26,15 @@ struct sph_ctx {
     std::string name;         // scene path; frame files are named after it (SceneLoader.cpp:202-212)
     unsigned frame = 1;       // TimeManager::frame, first frame 1 (TimeManager.h:45)
     double last_save = 0.0;   // TimeManager::lastTimeSave
+    sph::FrameWriter* writer = nullptr;  // created with the first frame
 };
 
 namespace sph {
 // Simulation::step for a tracked context (sph_scene_io.cpp).
 int tracked_step(sph_ctx* ctx);
+// Wait until every queued frame file is written; the first write error, if
+// any, is returned (and stored in ctx->err).
+int frames_flush(sph_ctx* ctx);
+// frames_flush, then stop the writer thread (before the scene is freed).
+int frames_close(sph_ctx* ctx);
 }  // namespace sph

@@ -489,6 +489,27 @@ public:
         return SPH_OK;
     }
 
+    int capture_async(double* hx, double* hv, cudaEvent_t done, unsigned* count_out) override
+    {
+        if (!inited) { fail("not initialised"); return SPH_ERR_INVALID; }
+        const unsigned n = active();
+        *count_out = n;
+        if (cap_x_.n < 3 * (size_t)n_) {
+            SPH_CUDA(cap_x_.alloc(3 * (size_t)n_));
+            SPH_CUDA(cap_v_.alloc(3 * (size_t)n_));
+        }
+        if (n) {
+            Fluid<R> f = F();
+            k_download<R><<<blocks(n, 256), 256, 0, st_>>>(n, f.pos, nullptr, f.id, f.cell, gv_, hd_, 1, cap_x_.p);
+            k_download<R><<<blocks(n, 256), 256, 0, st_>>>(n, f.vel, nullptr, f.id, f.cell, gv_, hd_, 0, cap_v_.p);
+            SPH_CUDA(cudaGetLastError());
+            SPH_CUDA(cudaMemcpyAsync(hx, cap_x_.p, 3 * (size_t)n * 8, cudaMemcpyDeviceToHost, st_));
+            SPH_CUDA(cudaMemcpyAsync(hv, cap_v_.p, 3 * (size_t)n * 8, cudaMemcpyDeviceToHost, st_));
+        }
+        SPH_CUDA(cudaEventRecord(done, st_));
+        return SPH_OK;
+    }
+
     int field_view(int field, FieldView* v) override
     {
         if (!inited) { fail("not initialised"); return SPH_ERR_INVALID; }
@@ -1285,6 +1306,7 @@ private:
     int nem_ = 0;               // emitters
     DevBuf<EmitterDev> em_;
     DevBuf<double> egroup_;
+    DevBuf<double> cap_x_, cap_v_;  // staging of asynchronous frame captures
     int akinci_ = 0;   // Akinci boundary model: boundary terms in the forces too
     int bh_ = 0;       // PCISPH boundary model
     int hasb_ = 0;     // boundary particles take part in the solver sums

@@ -77,6 +77,11 @@ struct SceneBase {
     virtual int set_graph(int on) = 0;
     virtual int pause_emitters(int pause) = 0;
     virtual int download(int field, double* out) = 0;
+    // Positions (absolute, FP64) and velocities of the active particles in
+    // original order into host memory x, v (pinned, 3 * active values each),
+    // queued on the scene's stream; `done` is recorded after the copies.
+    // *count_out receives the count copied.  Returns without waiting.
+    virtual int capture_async(double* x, double* v, cudaEvent_t done, unsigned* count_out) = 0;
     virtual int stats(sph_stats* s) = 0;
     virtual int neighbors(int* cells, int* rank, int* off, int* nbr, int* boff, int* bnbr, long long* totals) = 0;
     virtual int field_view(int field, FieldView* v) = 0;

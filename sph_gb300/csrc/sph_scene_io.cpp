@@ -11,6 +11,10 @@
 #include <algorithm>
 #include <charconv>
 #include <cmath>
+#include <condition_variable>
+#include <deque>
+#include <mutex>
+#include <thread>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -20,6 +24,8 @@
 #include <system_error>
 #include <utility>
 #include <vector>
+
+#include <cuda_runtime.h>
 
 #include "../../include/sph_gb300.h"
 #include "sph_ctx.h"
@@ -524,27 +530,16 @@ void put_double(std::string& o, double v)
     }
 }
 
-int write_frame(sph_ctx* ctx, const std::string& path, std::string* err)
+// The frame file's text: keys in sorted order, no whitespace; every slot of
+// the fluid model (slots emitters have not filled yet hold zeros),
+// "positions" and "velocities" absent when there are none
+// (SceneLoader.cpp:214-257).
+void frame_text(std::string& o, unsigned na, unsigned total, const double* x, const double* v, double time, double dt)
 {
-    sph_stats st;
-    int rc = sph_ctx_get_stats(ctx, &st);
-    if (rc != SPH_OK) { *err = sph_ctx_last_error(ctx); return rc; }
-    const unsigned na = st.num_fluid, total = st.num_fluid_total;
-    std::vector<double> x(3 * (size_t)na), v(3 * (size_t)na);
-    if (na) {
-        if ((rc = sph_ctx_download(ctx, SPH_FIELD_POSITION, x.data())) != SPH_OK ||
-            (rc = sph_ctx_download(ctx, SPH_FIELD_VELOCITY, v.data())) != SPH_OK) {
-            *err = sph_ctx_last_error(ctx);
-            return rc;
-        }
-    }
-    // keys in sorted order, no whitespace; every slot of the fluid model
-    // (slots emitters have not filled yet hold zeros), "positions" and
-    // "velocities" absent when there are none (SceneLoader.cpp:214-257)
-    std::string o;
+    o.clear();
     o.reserve(64 + (size_t)total * 120);
     o += "{\"numActiveParticles\":" + std::to_string(na) + ",\"numParticles\":" + std::to_string(total);
-    auto triples = [&](const char* key, const std::vector<double>& a) {
+    auto triples = [&](const char* key, const double* a) {
         o += ",\"";
         o += key;
         o += "\":[";
@@ -561,17 +556,40 @@ int write_frame(sph_ctx* ctx, const std::string& path, std::string* err)
     };
     if (total) triples("positions", x);
     o += ",\"time\":";
-    put_double(o, st.time);
+    put_double(o, time);
     o += ",\"timeStep\":";
-    put_double(o, st.dt);
+    put_double(o, dt);
     if (total) triples("velocities", v);
     o += '}';
+}
+
+int write_text(const std::string& path, const std::string& o, std::string* err)
+{
     FILE* f = std::fopen(path.c_str(), "wb");
     if (!f) { *err = "cannot write " + path; return SPH_ERR_INVALID; }
     const size_t w = std::fwrite(o.data(), 1, o.size(), f);
     const int cl = std::fclose(f);
     if (w != o.size() || cl != 0) { *err = "cannot write " + path; return SPH_ERR_INVALID; }
     return SPH_OK;
+}
+
+int write_frame(sph_ctx* ctx, const std::string& path, std::string* err)
+{
+    sph_stats st;
+    int rc = sph_ctx_get_stats(ctx, &st);
+    if (rc != SPH_OK) { *err = sph_ctx_last_error(ctx); return rc; }
+    const unsigned na = st.num_fluid, total = st.num_fluid_total;
+    std::vector<double> x(3 * (size_t)na), v(3 * (size_t)na);
+    if (na) {
+        if ((rc = sph_ctx_download(ctx, SPH_FIELD_POSITION, x.data())) != SPH_OK ||
+            (rc = sph_ctx_download(ctx, SPH_FIELD_VELOCITY, v.data())) != SPH_OK) {
+            *err = sph_ctx_last_error(ctx);
+            return rc;
+        }
+    }
+    std::string o;
+    frame_text(o, na, total, x.data(), v.data(), st.time, st.dt);
+    return write_text(path, o, err);
 }
 
 // SceneLoader::writeFluid's file name: the frame number zero-padded to four
@@ -593,6 +611,151 @@ double sim_time(sph_ctx* ctx, int* rc)
 
 }  // namespace
 
+// Frame files written off the step loop: a frame is captured into pinned
+// host memory on the scene's stream (positions and velocities in original
+// order), and a host thread waits for the copy, formats the text and writes
+// the file while the next steps run.  Two capture buffers: a third frame
+// waits for the oldest file to be written.
+class FrameWriter {
+public:
+    explicit FrameWriter(int device) : device_(device) { th_ = std::thread([this] { loop(); }); }
+    ~FrameWriter()
+    {
+        {
+            std::lock_guard<std::mutex> lk(m_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        th_.join();
+        for (Slot& s : slots_) {
+            if (s.x) cudaFreeHost(s.x);
+            if (s.v) cudaFreeHost(s.v);
+            if (s.ev) cudaEventDestroy(s.ev);
+        }
+    }
+
+    // Capture the current state and queue its file.
+    int submit(SceneBase* scene, const std::string& path, unsigned total, double time, double dt, std::string* err)
+    {
+        int k = -1;
+        {
+            std::unique_lock<std::mutex> lk(m_);
+            done_cv_.wait(lk, [&] { return !slots_[0].busy || !slots_[1].busy; });
+            if (!err_.empty()) { *err = err_; return SPH_ERR_INVALID; }
+            k = slots_[0].busy ? 1 : 0;
+            slots_[k].busy = true;
+        }
+        Slot& s = slots_[k];
+        const size_t need = 3 * (size_t)std::max(total, 1u);
+        if (s.cap < need) {
+            if (s.x) cudaFreeHost(s.x);
+            if (s.v) cudaFreeHost(s.v);
+            s.x = s.v = nullptr;
+            s.cap = 0;
+            if (cudaMallocHost((void**)&s.x, need * sizeof(double)) != cudaSuccess ||
+                cudaMallocHost((void**)&s.v, need * sizeof(double)) != cudaSuccess) {
+                release(k);
+                *err = "cannot allocate pinned memory for frame capture";
+                return SPH_ERR_CUDA;
+            }
+            s.cap = need;
+        }
+        if (!s.ev && cudaEventCreateWithFlags(&s.ev, cudaEventDisableTiming) != cudaSuccess) {
+            release(k);
+            *err = "cannot create an event for frame capture";
+            return SPH_ERR_CUDA;
+        }
+        unsigned na = 0;
+        const int rc = scene->capture_async(s.x, s.v, s.ev, &na);
+        if (rc != SPH_OK) {
+            release(k);
+            *err = scene->err;
+            return rc;
+        }
+        {
+            std::lock_guard<std::mutex> lk(m_);
+            q_.push_back(Job{path, k, na, total, time, dt});
+        }
+        cv_.notify_all();
+        return SPH_OK;
+    }
+
+    // Wait for every queued file; the first error since the last flush.
+    int flush(std::string* err)
+    {
+        std::unique_lock<std::mutex> lk(m_);
+        done_cv_.wait(lk, [&] { return q_.empty() && !slots_[0].busy && !slots_[1].busy; });
+        if (!err_.empty()) {
+            *err = err_;
+            err_.clear();
+            return SPH_ERR_INVALID;
+        }
+        return SPH_OK;
+    }
+
+private:
+    struct Slot {
+        double* x = nullptr;
+        double* v = nullptr;
+        size_t cap = 0;
+        cudaEvent_t ev = nullptr;
+        bool busy = false;
+    };
+    struct Job {
+        std::string path;
+        int slot;
+        unsigned na, total;
+        double time, dt;
+    };
+
+    void release(int k)
+    {
+        {
+            std::lock_guard<std::mutex> lk(m_);
+            slots_[k].busy = false;
+        }
+        done_cv_.notify_all();
+    }
+
+    void loop()
+    {
+        cudaSetDevice(device_);
+        std::string text;
+        for (;;) {
+            Job j;
+            {
+                std::unique_lock<std::mutex> lk(m_);
+                cv_.wait(lk, [&] { return stop_ || !q_.empty(); });
+                if (q_.empty()) return;  // stop requested and nothing left
+                j = q_.front();
+                q_.pop_front();
+            }
+            Slot& s = slots_[j.slot];
+            std::string e;
+            if (cudaEventSynchronize(s.ev) != cudaSuccess) e = "frame capture failed on the device";
+            if (e.empty()) {
+                frame_text(text, j.na, j.total, s.x, s.v, j.time, j.dt);
+                write_text(j.path, text, &e);
+            }
+            {
+                std::lock_guard<std::mutex> lk(m_);
+                if (!e.empty() && err_.empty()) err_ = e;
+                slots_[j.slot].busy = false;
+            }
+            done_cv_.notify_all();
+        }
+    }
+
+    int device_;
+    std::thread th_;
+    std::mutex m_;
+    std::condition_variable cv_, done_cv_;
+    std::deque<Job> q_;
+    Slot slots_[2];
+    std::string err_;
+    bool stop_ = false;
+};
+
 // Simulation::step Simulation.cpp:148-182: one solver step if the time is
 // inside [startTime, endTime], then TimeManager::hasToSave (frame clock) and,
 // with saving on, SceneLoader::writeFluid.
@@ -604,19 +767,43 @@ int tracked_step(sph_ctx* ctx)
     if (!(t >= ctx->t_start && t <= ctx->t_end)) return SPH_OK;
     rc = ctx->scene->step(1);
     if (rc != SPH_OK) { ctx->err = ctx->scene->err; return rc; }
-    const double now = sim_time(ctx, &rc);
+    sph_stats st;
+    rc = sph_ctx_get_stats(ctx, &st);
     if (rc != SPH_OK) return rc;
     const double fps = ctx->scene->d.fps;
-    if (now - ctx->last_save >= 1.0 / fps) {
+    if (st.time - ctx->last_save >= 1.0 / fps) {
         ctx->last_save = (double)ctx->frame / fps;
         if (ctx->save) {
             std::string err;
-            rc = write_frame(ctx, frame_name(ctx->name, ctx->frame), &err);
+            if (!ctx->writer) {
+                int dev = 0;
+                cudaGetDevice(&dev);
+                ctx->writer = new FrameWriter(dev);
+            }
+            rc = ctx->writer->submit(ctx->scene, frame_name(ctx->name, ctx->frame), st.num_fluid_total, st.time, st.dt,
+                                     &err);
             if (rc != SPH_OK) { ctx->err = err; return rc; }
         }
         ctx->frame += 1;
     }
     return SPH_OK;
+}
+
+int frames_flush(sph_ctx* ctx)
+{
+    if (!ctx->writer) return SPH_OK;
+    std::string err;
+    const int rc = ctx->writer->flush(&err);
+    if (rc != SPH_OK) ctx->err = err;
+    return rc;
+}
+
+int frames_close(sph_ctx* ctx)
+{
+    const int rc = frames_flush(ctx);
+    delete ctx->writer;
+    ctx->writer = nullptr;
+    return rc;
 }
 
 }  // namespace sph
@@ -669,6 +856,7 @@ int sph_ctx_set_frame_output(sph_ctx* ctx, const char* scene_path, int active)
         ctx->err = "no scene path for the frame files";
         return SPH_ERR_INVALID;
     }
+    if (!active && sph::frames_flush(ctx) != SPH_OK) return SPH_ERR_INVALID;
     ctx->save = active != 0;
     ctx->track = true;
     return SPH_OK;
@@ -684,6 +872,7 @@ int sph_ctx_get_frame(const sph_ctx* ctx, unsigned* frame)
 int sph_ctx_write_frame(sph_ctx* ctx, const char* path)
 {
     if (!ctx || !path) return SPH_ERR_INVALID;
+    if (sph::frames_flush(ctx) != SPH_OK) return SPH_ERR_INVALID;
     std::string err;
     const int rc = sph::write_frame(ctx, path, &err);
     if (rc != SPH_OK) ctx->err = err;
@@ -724,7 +913,8 @@ int sph_ctx_run(sph_ctx* ctx, unsigned long long max_steps, unsigned long long* 
         }
     }
     if (steps_done) *steps_done = done;
-    return rc;
+    const int fr = sph::frames_flush(ctx);
+    return rc != SPH_OK ? rc : fr;
 }
 
 }  // extern "C"

@@ -231,6 +231,7 @@ def test_frame_files_match_reference(gpu_lib, name, tmp_path):
     stem = str(tmp_path / "scene.json")
     s.set_frame_output(stem, True)
     s.step(12)
+    s.synchronize()  # frame files are written by a host thread; complete after synchronize
     ref = sorted(int(k[5:-4]) for k in g if k.endswith(".raw"))
     mine = sorted(int(f[6:-5]) for f in os.listdir(tmp_path) if re.fullmatch(r"scene_\d{4}\.json", f))
     assert mine == ref
@@ -263,3 +264,30 @@ def test_run_stops_at_the_end_time(gpu_lib, tmp_path, save):
     assert s.run() == 0
     if save:
         assert sorted(os.listdir(tmp_path)) == ["scene_0001.json", "scene_0002.json"]
+
+
+@pytest.mark.gpu
+def test_frame_files_written_while_stepping_match_synchronous_frames(gpu_lib, tmp_path):
+    """Frames queued to the writer thread during 12 graph steps equal the
+    frames written synchronously (sph_ctx_write_frame) from a second run of
+    the same scene stopped at the same steps, byte for byte."""
+    name = "dfsph_dam_emitter"
+    a = sph_gb300.Scene.load(scene_path(name), precision="f32")
+    a.set_graph(True)
+    a.set_frame_output(str(tmp_path / "a.json"), True)
+    a.step(12)
+    a.close()  # writes what is queued
+    b = sph_gb300.Scene.load(scene_path(name), precision="f32")
+    b.set_graph(True)
+    frames = sorted(f for f in os.listdir(tmp_path) if f.startswith("a_"))
+    assert len(frames) >= 3
+    last_save, frame, fps = 0.0, 1, 200.0
+    for _ in range(12):
+        b.step(1)
+        t = b.stats()["time"]
+        if t - last_save >= 1.0 / fps:
+            last_save = frame / fps
+            b.write_frame(str(tmp_path / f"b_{frame:04d}.json"))
+            frame += 1
+    for f in frames:
+        assert open(tmp_path / f, "rb").read() == open(tmp_path / ("b_" + f[2:]), "rb").read(), f
