@@ -465,18 +465,27 @@ def roofline(prof, n, nb, pairs, workload):
     streamed = stream_launch / (avg_ms / 1000.0) / 1e9 if avg_ms > 0 else 0.0
     peak, peak_kind = load_peaks()
     traffic = None
+    issue = {}
     tp = os.path.join(ROOT, "profiles", f"ncu_{kname}_{workload}.md")
     if os.path.exists(tp):
         for ln in open(tp):
-            if ln.startswith("dram_bytes_per_launch:"):
-                traffic = float(ln.split(":", 1)[1])
+            key, _, val = ln.partition(":")
+            if key == "dram_bytes_per_launch":
+                traffic = float(val)
+            elif key in ("sm_issue_active_pct", "l1_lsu_wavefronts_pct", "fp32_pipe_pct"):
+                issue[key] = float(val)
     total = sum(v[1] for v in prof.values())
-    return {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "peak_kind": f"of {peak_kind}", "traffic": traffic,
-            "algorithmic_bytes_per_launch": bytes_launch, "avg_launch_ms": avg_ms,
-            "kernel_share": kms / total if total else None,
-            "with_pair_lists": {"bytes_per_launch": stream_launch, "achieved": streamed, "frac": streamed / peak,
-                                "note": "field bytes plus the 16-byte pair records the kernel writes or reads"}}
+    out = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
+           "frac": achieved / peak, "peak_kind": f"of {peak_kind}", "traffic": traffic,
+           "algorithmic_bytes_per_launch": bytes_launch, "avg_launch_ms": avg_ms,
+           "kernel_share": kms / total if total else None,
+           "with_pair_lists": {"bytes_per_launch": stream_launch, "achieved": streamed, "frac": streamed / peak,
+                               "note": "field bytes plus the 16-byte pair records the kernel writes or reads"}}
+    if issue:
+        # a neighbour walk is bound by instruction issue and the L1 load pipe,
+        # not by DRAM: the utilisations ncu measured for this kernel
+        out["issue"] = dict(issue, source=os.path.relpath(tp, ROOT))
+    return out
 
 
 def main():

@@ -284,7 +284,7 @@ __device__ __forceinline__ void walk(const GridView& g, const uint32_t* __restri
 // ---------------------------------------------------------------------------
 
 // W and grad W of one pair from the squared distance, for the pair-list
-// build.  FAST (FP32 pool): 1/|r| from the hardware reciprocal square root
+// build.  FAST (FP32 form): 1/|r| from the hardware reciprocal square root
 // (a few ulp) replaces the correctly rounded sqrt and division; the
 // polynomials are those of cubic_W / cubic_gradW.
 template <bool FAST, typename R>

@@ -194,7 +194,7 @@ __global__ void __launch_bounds__(kBlock, 7) k_build_lists(Fluid<R> f, const P4<
     __shared__ uint32_t q[kQueue * kBlock];
     const uint32_t i = gtid();
     if (i >= f.count()) return;
-    build_lists_one(i, f, bpos, g, cs, bs, c, akinci, L, q);
+    build_lists_one<R, sizeof(R) == 4>(i, f, bpos, g, cs, bs, c, akinci, L, q);
 }
 
 // ---- cell-walk fallbacks for particles whose list overflowed -------------
