@@ -299,7 +299,10 @@ int sph_select_device(int device);
  * reference, which holds one scene per process (Simulation singleton,
  * src/Simulation.cpp:84-90); each pooled scene runs the same per-step loop as
  * sph_ctx_step, and its results do not depend on which other scenes share
- * the pool.  Scenes are admitted and removed between steps.
+ * the pool.  Scenes are admitted and removed between steps.  A pool may be
+ * shared by several host threads (a thread submitting scenes while another
+ * steps and polls): calls on one pool are serialised, and each runs on the
+ * device the pool was created on.
  * ------------------------------------------------------------------------ */
 typedef struct sph_pool sph_pool;
 

@@ -31,6 +31,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <list>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -1522,9 +1523,20 @@ private:
 
 }  // namespace sph
 
+// Calls on one pool are serialised (a submitting thread and a stepping
+// thread may share it) and run on the device the pool was created on.
 struct sph_pool {
     sph::Pool pool;
+    std::mutex m;
+    int device = 0;
 };
+
+namespace {
+struct PoolLock {
+    std::lock_guard<std::mutex> lk;
+    explicit PoolLock(sph_pool* p) : lk(p->m) { cudaSetDevice(p->device); }
+};
+}  // namespace
 
 static int pool_bad(sph_pool* p, const char* m)
 {
@@ -1566,6 +1578,7 @@ int sph_pool_create(const sph_pool_desc* desc, sph_pool** out)
     *out = nullptr;
     sph_pool* p = new (std::nothrow) sph_pool();
     if (!p) return SPH_ERR_INVALID;
+    cudaGetDevice(&p->device);
     const int rc = p->pool.create(*desc);
     if (rc) {
         delete p;
@@ -1586,48 +1599,56 @@ int sph_pool_add_scene(sph_pool* p, const sph_scene_desc* d, const double* x, co
                        const double* bx, unsigned nb, unsigned steps, int* scene_id)
 {
     if (!p || !d || !scene_id || (nb && !bx)) return pool_bad(p, "invalid argument");
+    PoolLock lock(p);
     return p->pool.add(*d, x, v, n, bx, nb, steps, scene_id);
 }
 
 int sph_pool_remove_scene(sph_pool* p, int scene_id)
 {
     if (!p) return SPH_ERR_INVALID;
+    PoolLock lock(p);
     return p->pool.remove(scene_id);
 }
 
 int sph_pool_step(sph_pool* p, int nsteps)
 {
     if (!p || nsteps < 0) return pool_bad(p, "invalid argument");
+    PoolLock lock(p);
     return p->pool.step(nsteps);
 }
 
 int sph_pool_set_graph(sph_pool* p, int enable)
 {
     if (!p) return SPH_ERR_INVALID;
+    PoolLock lock(p);
     return p->pool.set_graph(enable);
 }
 
 int sph_pool_synchronize(sph_pool* p)
 {
     if (!p) return SPH_ERR_INVALID;
+    PoolLock lock(p);
     return p->pool.sync();
 }
 
 int sph_pool_query(sph_pool* p, int scene_id, sph_stats* out, int* done)
 {
     if (!p || !out) return pool_bad(p, "invalid argument");
+    PoolLock lock(p);
     return p->pool.query(scene_id, out, done);
 }
 
 int sph_pool_poll(sph_pool* p, int* done_ids, int max_ids, int* num_done)
 {
     if (!p || !num_done) return pool_bad(p, "invalid argument");
+    PoolLock lock(p);
     return p->pool.poll(done_ids, max_ids, num_done);
 }
 
 int sph_pool_download(sph_pool* p, int scene_id, int field, double* out)
 {
     if (!p || !out) return pool_bad(p, "invalid argument");
+    PoolLock lock(p);
     return p->pool.download(scene_id, field, out);
 }
 
@@ -1635,12 +1656,14 @@ int sph_pool_usage(sph_pool* p, unsigned long long* particles, unsigned long lon
                    unsigned* scenes)
 {
     if (!p) return SPH_ERR_INVALID;
+    PoolLock lock(p);
     return p->pool.usage(particles, boundary, keys, scenes);
 }
 
 int sph_pool_get_launch_count(sph_pool* p, unsigned long long* out)
 {
     if (!p || !out) return pool_bad(p, "invalid argument");
+    PoolLock lock(p);
     *out = p->pool.total_launches();
     return SPH_OK;
 }
@@ -1648,30 +1671,35 @@ int sph_pool_get_launch_count(sph_pool* p, unsigned long long* out)
 int sph_pool_step_timed(sph_pool* p, int nsteps, float* elapsed_ms)
 {
     if (!p || nsteps < 0 || !elapsed_ms) return pool_bad(p, "invalid argument");
+    PoolLock lock(p);
     return p->pool.step_timed(nsteps, elapsed_ms);
 }
 
 int sph_pool_set_profiling(sph_pool* p, int enable)
 {
     if (!p) return SPH_ERR_INVALID;
+    PoolLock lock(p);
     return p->pool.set_profiling(enable);
 }
 
 int sph_pool_get_profile(sph_pool* p, char* buf, unsigned long long len)
 {
     if (!p) return SPH_ERR_INVALID;
+    PoolLock lock(p);
     return p->pool.profile(buf, (size_t)len);
 }
 
 int sph_pool_set_autotune(sph_pool* p, int mode)
 {
     if (!p) return SPH_ERR_INVALID;
+    PoolLock lock(p);
     return p->pool.set_autotune(mode);
 }
 
 int sph_pool_get_tuning(sph_pool* p, sph_pool_tuning* out)
 {
     if (!p || !out) return pool_bad(p, "invalid argument");
+    PoolLock lock(p);
     p->pool.get_tuning(out);
     return SPH_OK;
 }
@@ -1679,12 +1707,14 @@ int sph_pool_get_tuning(sph_pool* p, sph_pool_tuning* out)
 int sph_pool_set_tuning(sph_pool* p, const sph_pool_tuning* t)
 {
     if (!p || !t) return pool_bad(p, "invalid argument");
+    PoolLock lock(p);
     return p->pool.set_tuning(*t);
 }
 
 int sph_pool_get_tuning_log(sph_pool* p, char* buf, unsigned long long len)
 {
     if (!p) return SPH_ERR_INVALID;
+    PoolLock lock(p);
     const std::string& s = p->pool.tuning_log();
     if (buf && len) {
         std::strncpy(buf, s.c_str(), (size_t)len - 1);
@@ -1696,6 +1726,7 @@ int sph_pool_get_tuning_log(sph_pool* p, char* buf, unsigned long long len)
 int sph_pool_list_pairs(sph_pool* p, unsigned long long* pairs, unsigned* overflow)
 {
     if (!p || !pairs || !overflow) return pool_bad(p, "invalid argument");
+    PoolLock lock(p);
     return p->pool.list_pairs(pairs, overflow);
 }
 

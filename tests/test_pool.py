@@ -186,3 +186,42 @@ def test_autotuned_shapes_do_not_change_results(gpu_lib, tmp_path, monkeypatch):
         Q.set_tuning(build_block=96)
     with pytest.raises(sph_gb300.SPHError):
         Q.set_tuning(solver_occupancy=1000)
+
+
+def test_submitter_thread_and_stepping_thread_share_a_pool(gpu_lib):
+    """One host thread admits scenes while another steps and polls the same
+    pool (calls are serialised by the pool).  Every admitted scene runs its
+    steps, and scene A's results equal A run alone."""
+    import threading
+    import time
+
+    P = sph_gb300.Pool(max_particles=200_000, max_boundary=400_000, max_keys=4_000_000, max_scenes=64)
+    P.set_graph(True)
+    a = P.add_scene(A[0], boundary_points=A[1], steps=30, **A[2])
+    ids, errors = [], []
+
+    def submit():
+        try:
+            for k in range(6):
+                x, b, p = OTHERS[k % len(OTHERS)]
+                ids.append(P.add_scene(x, boundary_points=b, steps=12, **p))
+                time.sleep(0.005)
+        except Exception as e:  # reported below
+            errors.append(e)
+
+    t = threading.Thread(target=submit)
+    t.start()
+    done = set()
+    for _ in range(200):
+        P.step(1)
+        done.update(P.poll())
+        if not t.is_alive() and len(done) == len(ids) + 1:
+            break
+    t.join()
+    assert not errors, errors
+    P.synchronize()
+    done.update(P.poll())
+    assert set(ids) | {a} <= done
+    R, rid = pool_run([A], 30)
+    assert np.array_equal(P.get(a, "x"), R.get(rid[0], "x"))
+    assert np.array_equal(P.get(a, "v"), R.get(rid[0], "v"))
