@@ -12,6 +12,8 @@
 
 #include "sph_device.cuh"
 
+#include <cuda_fp16.h>
+
 namespace sph {
 
 template <typename R> struct Fluid {
@@ -377,15 +379,26 @@ __device__ __forceinline__ uint32_t final_slot(uint32_t p, const uint32_t* __res
 
 // Gather of the state that survives a re-sort (x, v, DFSPH k, kv and the
 // last predicted density; the other fields are recomputed after every build).
+// posh (FP32, optional): also the half-precision copy of the positions the
+// pool's list build culls with (x, y, z, 0 per particle).
 template <typename R>
 __global__ void k_gather_fluid(uint32_t n, const uint32_t* __restrict__ tmp, const uint32_t* __restrict__ key,
-                               const uint32_t* __restrict__ starts, Fluid<R> src, Fluid<R> dst)
+                               const uint32_t* __restrict__ starts, Fluid<R> src, Fluid<R> dst,
+                               uint2* __restrict__ posh = nullptr)
 {
     const uint32_t p = gtid();
     if (p >= src.count()) return;
     uint32_t i;
     const uint32_t d = final_slot(p, tmp, key, src.id, starts, &i);
-    dst.pos[d] = src.pos[i];
+    const P4<R> x = src.pos[i];
+    dst.pos[d] = x;
+    if constexpr (sizeof(R) == 4) {
+        if (posh) {
+            const __half2 xy = __floats2half2_rn(x.x, x.y);
+            const __half2 z0 = __floats2half2_rn(x.z, 0.f);
+            posh[d] = make_uint2(*reinterpret_cast<const uint32_t*>(&xy), *reinterpret_cast<const uint32_t*>(&z0));
+        }
+    }
     dst.vel[d] = src.vel[i];
     dst.kappa[d] = src.kappa[i];
     dst.kappav[d] = src.kappav[i];

@@ -21,6 +21,8 @@
 // terms, which all share the factor of particle i).
 #pragma once
 
+#include <cuda_fp16.h>
+
 #include "sph_kernels.cuh"
 
 namespace sph {
@@ -31,7 +33,72 @@ template <typename R> struct Lists {
     P4<R>* bgrad;       // xyz: sum_b rho0 psi_b gradW_ib
     R* kbuf;            // k (or kv) of the pass in progress
     uint32_t kmax;
+    // FP32 pool: a half-precision copy of the cell-relative positions
+    // (x, y, z, 0 per particle; two particles per 16-byte word) for the
+    // build's cull, or nullptr
+    const uint4* posh;
 };
+
+// Phase 1 of the FP32 list build from the half-precision positions: the
+// nine columns of the 27-cell neighbourhood (trimmed as walk() trims them),
+// two candidates per half2 operation, accepted indices queued in walk order.
+// The test uses r^2 <= 1.02 h^2: half-precision offsets (relative error
+// 2^-11 per value, |offsets| <= 2h) move r^2 by less than 0.6 % of h^2, so
+// every pair the FP32 test accepts is kept; pairs beyond h evaluate to
+// W = 0, grad W = 0 in phase 2 and are dropped there.  Returns the number of
+// accepted candidates (the queue holds the first qcap).
+__device__ __forceinline__ uint32_t cull_half(const GridView& g, const uint32_t* __restrict__ starts, uint32_t pc,
+                                              V3<float> xi, float h, float cull2, const uint4* __restrict__ posh,
+                                              uint32_t* q, uint32_t qstride, uint32_t qcap)
+{
+    const int cx = cell_x(pc), cy = cell_y(pc), cz = cell_z(pc);
+    const int z0 = cz > 0 ? cz - 1 : 0;
+    const int z1 = cz + 1 < g.nz ? cz + 1 : g.nz - 1;
+    const float ofx = xi.x, ofy = xi.y, ofz = xi.z;
+    const float gxm = ofx > 0.f ? ofx * ofx : 0.f, gxp = h - ofx > 0.f ? (h - ofx) * (h - ofx) : 0.f;
+    const float gym = ofy > 0.f ? ofy * ofy : 0.f, gyp = h - ofy > 0.f ? (h - ofy) * (h - ofy) : 0.f;
+    const float gzm = ofz > 0.f ? ofz * ofz : 0.f, gzp = h - ofz > 0.f ? (h - ofz) * (h - ofz) : 0.f;
+    const float lim = h * h * (float)(1.0 + 1e-5);
+    const __half2 thr = __float2half2_rn(cull2 * 1.02f);
+    const __half hzm = __float2half_rn(xi.z + h), hz0 = __float2half_rn(xi.z), hzp = __float2half_rn(xi.z - h);
+    uint32_t nq = 0;
+#pragma unroll 1
+    for (int c = 0; c < 9; ++c) {
+        const int dx = c / 3 - 1, dy = c - (c / 3) * 3 - 1;
+        const int x = cx + dx, y = cy + dy;
+        const float gxy = (dx < 0 ? gxm : (dx > 0 ? gxp : 0.f)) + (dy < 0 ? gym : (dy > 0 ? gyp : 0.f));
+        if (x < 0 || x >= g.nx || y < 0 || y >= g.ny || !(gxy <= lim)) continue;
+        const uint32_t base = (__ldg(g.mortx + x) | __ldg(g.morty + y)) * (uint32_t)g.nz;
+        const uint32_t s0 = __ldg(starts + base + z0), sm = __ldg(starts + base + cz);
+        const uint32_t sp = __ldg(starts + base + cz + 1), s1 = __ldg(starts + base + z1 + 1);
+        const uint32_t bb = gxy + gzm <= lim ? s0 : sm;
+        const uint32_t ee = gxy + gzp <= lim ? s1 : sp;
+        const __half2 sx = __float2half2_rn(xi.x - (float)dx * h), sy = __float2half2_rn(xi.y - (float)dy * h);
+#pragma unroll 1
+        for (uint32_t j = bb & ~1u; j < ee; j += 2) {
+            const uint4 w = __ldg(posh + (j >> 1));
+            const uint32_t px = __byte_perm(w.x, w.z, 0x5410), py = __byte_perm(w.x, w.z, 0x7632);
+            const uint32_t pz = __byte_perm(w.y, w.w, 0x5410);
+            const __half za = j < sm ? hzm : (j < sp ? hz0 : hzp);
+            const __half zb = j + 1 < sm ? hzm : (j + 1 < sp ? hz0 : hzp);
+            const __half2 sz = __halves2half2(za, zb);
+            const __half2 ddx = __hsub2(sx, *reinterpret_cast<const __half2*>(&px));
+            const __half2 ddy = __hsub2(sy, *reinterpret_cast<const __half2*>(&py));
+            const __half2 ddz = __hsub2(sz, *reinterpret_cast<const __half2*>(&pz));
+            const __half2 r2 = __hfma2(ddz, ddz, __hfma2(ddy, ddy, __hmul2(ddx, ddx)));
+            const unsigned m = __hle2_mask(r2, thr);
+            if ((m & 0xFFFFu) && j >= bb) {
+                if (nq < qcap) q[nq * qstride + threadIdx.x] = j;
+                ++nq;
+            }
+            if ((m >> 16) && j + 1 < ee) {
+                if (nq < qcap) q[nq * qstride + threadIdx.x] = j + 1;
+                ++nq;
+            }
+        }
+    }
+    return nq;
+}
 
 __device__ __forceinline__ float idx_as(float, uint32_t j) { return __uint_as_float(j); }
 __device__ __forceinline__ double idx_as(double, uint32_t j) { return __longlong_as_double((long long)j); }
@@ -137,13 +204,17 @@ __device__ __forceinline__ void build_lists_one(uint32_t i, const Fluid<R>& f, c
     };
     // phase 1: cull
     uint32_t nq = 0;
-    walk<R, 1, true, FAST>(g, cs, pc, xi, c.h, 0, [&](uint32_t j, V3<R> s) {
-        const V3<R> r = s - xyz(ldg4(f.pos + j));
-        if (dot3(r, r) <= c.cull2) {
-            if (nq < qcap) q[nq * qstride + threadIdx.x] = j;
-            ++nq;
-        }
-    });
+    if constexpr (FAST && sizeof(R) == 4) {
+        if (L.posh) nq = cull_half(g, cs, pc, xi, c.h, c.cull2, L.posh, q, qstride, qcap);
+    }
+    if (!(FAST && sizeof(R) == 4) || !L.posh)
+        walk<R, 1, true, FAST>(g, cs, pc, xi, c.h, 0, [&](uint32_t j, V3<R> s) {
+            const V3<R> r = s - xyz(ldg4(f.pos + j));
+            if (dot3(r, r) <= c.cull2) {
+                if (nq < qcap) q[nq * qstride + threadIdx.x] = j;
+                ++nq;
+            }
+        });
     if (nq <= qcap) {
         // phase 2: evaluate the queued candidates in walk order
         for (uint32_t k = 0; k < nq; ++k) {

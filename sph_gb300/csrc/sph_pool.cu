@@ -532,6 +532,8 @@ public:
         SPH_CUDA(press_.alloc(P)); SPH_CUDA(kbuf_.alloc(P)); SPH_CUDA(sid_.alloc(P)); SPH_CUDA(bsid_.alloc(B));
         SPH_CUDA(bpsi_.alloc(B)); SPH_CUDA(dummy4_.alloc(1));
         SPH_CUDA(pairs_.alloc(P * kmax_)); SPH_CUDA(lcount_.alloc(P)); SPH_CUDA(bgrad_.alloc(P));
+        SPH_CUDA(posh_.alloc(P + 2));  // whole 16-byte pairs, one past the end
+        SPH_CUDA(cudaMemsetAsync(posh_.p, 0, (P + 2) * sizeof(uint2), st_));
         const size_t M = std::max(P, B);
         SPH_CUDA(key_.alloc(M)); SPH_CUDA(slot_.alloc(M)); SPH_CUDA(tmp_.alloc(M));
         SPH_CUDA(count_.alloc(K)); SPH_CUDA(starts_.alloc(K + 1)); SPH_CUDA(bstarts_.alloc(K + 1));
@@ -1051,7 +1053,10 @@ private:
         return f;
     }
     Boundary<float> B(int k) const { return Boundary<float>{bpos_[k].p, bpsi_.p, bcell_[k].p, bid_[k].p, NB_}; }
-    Lists<float> LS() const { return Lists<float>{pairs_.p, lcount_.p, bgrad_.p, kbuf_.p, kmax_}; }
+    Lists<float> LS() const
+    {
+        return Lists<float>{pairs_.p, lcount_.p, bgrad_.p, kbuf_.p, kmax_, reinterpret_cast<const uint4*>(posh_.p)};
+    }
 
     int scan(uint32_t* out)
     {
@@ -1317,7 +1322,8 @@ private:
         int rc = scan(starts_.p);
         if (rc) return rc;
         run("k_scatter", [&] { k_scatter<<<blocks(N_, 256), 256, 0, ls_>>>(N_, key_.p, slot_.p, starts_.p, tmp_.p); });
-        run("k_gather_fluid", [&] { k_gather_fluid<float><<<blocks(N_, 256), 256, 0, ls_>>>(N_, tmp_.p, key_.p, starts_.p, F(cur_), F(1 - cur_)); });
+        run("k_gather_fluid", [&] { k_gather_fluid<float><<<blocks(N_, 256), 256, 0, ls_>>>(N_, tmp_.p, key_.p, starts_.p, F(cur_), F(1 - cur_),
+                                                                                          posh_.p); });
         SPH_CUDA(cudaGetLastError());
         cur_ = 1 - cur_;
         return SPH_OK;
@@ -1514,6 +1520,7 @@ private:
     DevBuf<float> kappa_[2], kappav_[2], pred_[2];
     DevBuf<uint32_t> cell_[2], id_[2], bcell_[2], bid_[2];
     DevBuf<P4<float>> acc_, dummy4_, pairs_, bgrad_;
+    DevBuf<uint2> posh_;  // half-precision positions for the build's cull
     DevBuf<float> rho_, alpha_, div_, press_, kbuf_, bpsi_;
     DevBuf<uint32_t> sid_, bsid_, lcount_, key_, slot_, tmp_, count_, starts_, bstarts_, tile_sums_, mort_;
     DevBuf<uint32_t> seg_a_, seg_b_, seg_n_;
