@@ -647,7 +647,10 @@ private:
     static unsigned blocks(size_t n, unsigned b) { return (unsigned)std::max<size_t>(1, (n + b - 1) / b); }
 
     Fluid<R> F() const { return fl_[cur_]; }
-    Lists<R> LS() const { return Lists<R>{pairs_.p, lcount_.p, bgrad_.p, kbuf_.p, kmax_}; }
+    Lists<R> LS() const
+    {
+        return Lists<R>{pairs_.p, lcount_.p, bgrad_.p, kbuf_.p, kmax_, reinterpret_cast<const uint4*>(posh_.p)};
+    }
     Boundary<R> B(int k) const { return bd_[k]; }
 
     // Kernel coefficients, evaluated in double as each reference kernel's
@@ -751,6 +754,12 @@ private:
         SPH_CUDA(lcount_.alloc(lists_ ? n : 1));
         SPH_CUDA(bgrad_.alloc(lists_ ? n : 1));
         SPH_CUDA(kbuf_.alloc(n));
+        // FP32 pair lists: half-precision positions for the build's cull
+        // (whole 16-byte pairs, one past the end); written by every gather
+        if (lists_ && sizeof(R) == 4) {
+            SPH_CUDA(posh_.alloc(n + 2));
+            SPH_CUDA(cudaMemsetAsync(posh_.p, 0, (n + 2) * sizeof(uint2), st_));
+        }
         SPH_CUDA(cudaMemsetAsync(lcount_.p, 0, lcount_.n * sizeof(uint32_t), st_));
         SPH_CUDA(cudaMemsetAsync(kbuf_.p, 0, n * sizeof(R), st_));
         SPH_CUDA(lstat_.alloc(2));
@@ -817,7 +826,8 @@ private:
         int rc = scan(starts_.p);
         if (rc) return rc;
         run("k_scatter", [&] { k_scatter<<<blocks(n_, 256), 256, 0, ls_>>>(n_, key_.p, slot_.p, starts_.p, tmp_.p, a.na); });
-        run("k_gather_fluid", [&] { k_gather_fluid<R><<<blocks(n_, 256), 256, 0, ls_>>>(n_, tmp_.p, key_.p, starts_.p, fl_[cur_], fl_[1 - cur_]); });
+        run("k_gather_fluid", [&] { k_gather_fluid<R><<<blocks(n_, 256), 256, 0, ls_>>>(n_, tmp_.p, key_.p, starts_.p, fl_[cur_], fl_[1 - cur_],
+                                                                                  posh_.p); });
         SPH_CUDA(cudaGetLastError());
         cur_ = 1 - cur_;
         return SPH_OK;
@@ -1307,6 +1317,7 @@ private:
     DevBuf<EmitterDev> em_;
     DevBuf<double> egroup_;
     DevBuf<double> cap_x_, cap_v_;  // staging of asynchronous frame captures
+    DevBuf<uint2> posh_;            // FP32 pair lists: half-precision positions (build cull)
     int akinci_ = 0;   // Akinci boundary model: boundary terms in the forces too
     int bh_ = 0;       // PCISPH boundary model
     int hasb_ = 0;     // boundary particles take part in the solver sums
