@@ -577,7 +577,10 @@ public:
         }
         double hh, mass;
         scene_constants<float>(d, &e.t.c, &e.t.lim, &hh, &mass);
-        int rc = grid_plan(d, e.x, e.b, true, std::vector<double>(), hh, &e.plan, &err);
+        // the walls bound a pooled scene: two cells beyond its points, no
+        // proportional margin (a box just over 32 cells wide would double
+        // each Morton axis of its key space)
+        int rc = grid_plan(d, e.x, e.b, true, std::vector<double>(), hh, &e.plan, &err, 0.0);
         if (rc) return rc;
         // capacity check against everything resident or pending
         uint64_t P = 0, B = 0, K = 0;

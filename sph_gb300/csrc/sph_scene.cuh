@@ -106,8 +106,9 @@ void scene_constants(const sph_scene_desc& d, Consts<R>* out_c, LoopLimits* out_
     *out_mass = mass;
 }
 
-// Dense cell box over the domain (given, or the points' bounds + 5 %) with a
-// two-cell margin, and the column-Morton tables of its key space.
+// Dense cell box over the domain (given, or the points' bounds widened by
+// rel_margin of their extent) with a two-cell margin, and the column-Morton
+// tables of its key space.
 struct GridPlan {
     int o[3] = {0, 0, 0}, nn[3] = {0, 0, 0};
     std::vector<uint32_t> mx, my;
@@ -115,7 +116,7 @@ struct GridPlan {
 };
 
 inline int grid_plan(const sph_scene_desc& d, const std::vector<double>& hx, const std::vector<double>& hb, bool akinci,
-                     const std::vector<double>& he, double h, GridPlan* out, std::string* err)
+                     const std::vector<double>& he, double h, GridPlan* out, std::string* err, double rel_margin = 0.05)
 {
     double lo[3], hi[3];
     bool given = false;
@@ -135,8 +136,8 @@ inline int grid_plan(const sph_scene_desc& d, const std::vector<double>& hx, con
             for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], d.cube_min[k]); hi[k] = std::max(hi[k], d.cube_max[k]); }
         for (int k = 0; k < 3; ++k) {
             const double ext = hi[k] - lo[k];
-            lo[k] -= 0.05 * ext;
-            hi[k] += 0.05 * ext;
+            lo[k] -= rel_margin * ext;
+            hi[k] += rel_margin * ext;
         }
     }
     GridPlan p;
