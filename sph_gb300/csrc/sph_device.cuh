@@ -86,9 +86,19 @@ template <typename R> struct Consts {
     R cube_min[3], cube_max[3];
     R bwarm;                       // warm-start boundary factor: 2 (Akinci), 1 (PCISPH model)
     R bh_nf, bh_tf;                // PCISPH boundary model normal / tangential factors
+    double inv_density0;           // 1 / density0 (FP32 form's error reductions)
     int force_flags;
     int has_cube;
 };
+
+// A particle's relative error x / density0 for the solver loops' average:
+// the reference's FP64 division in the parity form, a multiplication by the
+// reciprocal in the FP32 form (FP64 division is slow on this part).
+template <typename R> __device__ __forceinline__ double rel_error(const Consts<R>& c, double x)
+{
+    if constexpr (sizeof(R) == 8) return x / (double)c.density0;
+    else return x * c.inv_density0;
+}
 
 enum ForceFlags : int {
     F_XSPH = 1, F_STD_VISC = 2, F_ART_VISC = 4, F_SURFACE_TENSION = 8, F_ADHESION = 16, F_BVISC = 32,

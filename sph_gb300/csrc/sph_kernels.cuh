@@ -841,7 +841,7 @@ __global__ void __launch_bounds__(kBlock) k_dfsph_predict_density(Fluid<R> f, co
         f.pred[i] = pred;
         const R k = (pred - c.density0) * f.alpha[i] / ((dt * dt) * rho);
         f.xk[i] = P4<R>{xi.x, xi.y, xi.z, k};
-        err = ((double)pred - (double)c.density0) / (double)c.density0;
+        err = rel_error(c, (double)pred - (double)c.density0);
     }
     double total;
     if (finish_reduction<false>(err, partials, &sc->block_counter, sh, &total) && threadIdx.x == 0) {
@@ -913,7 +913,7 @@ __global__ void __launch_bounds__(kBlock) k_dfsph_divergence(Fluid<R> f, const P
         f.div[i] = dv;
         const R kv = dv * f.alpha[i] / (dt * f.rho[i]);
         f.xk[i] = P4<R>{xi.x, xi.y, xi.z, kv};
-        err = (double)dv / (double)c.density0;
+        err = rel_error(c, (double)dv);
     }
     double total;
     if (finish_reduction<false>(err, partials, &sc->block_counter, sh, &total) && threadIdx.x == 0) {

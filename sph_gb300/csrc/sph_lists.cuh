@@ -445,7 +445,7 @@ __global__ void __launch_bounds__(kBlock, 8) k_dfsph_predict_density_list(Fluid<
         pred = pred < c.density0 ? c.density0 : pred;
         f.pred[i] = pred;
         L.kbuf[i] = (pred - c.density0) * f.alpha[i] / ((dt * dt) * rho);
-        err = ((double)pred - (double)c.density0) / (double)c.density0;
+        err = rel_error(c, (double)pred - (double)c.density0);
     }
     double total;
     if (finish_reduction<false>(err, partials, &sc->block_counter, sh, &total) && threadIdx.x == 0) {
@@ -490,7 +490,7 @@ __global__ void __launch_bounds__(kBlock, 8) k_dfsph_divergence_list(Fluid<R> f,
         dv = nn < 20u ? (R)0 : (dv < (R)0 ? (R)0 : dv);
         f.div[i] = dv;
         L.kbuf[i] = dv * f.alpha[i] / (dt * f.rho[i]);
-        err = (double)dv / (double)c.density0;
+        err = rel_error(c, (double)dv);
     }
     double total;
     if (finish_reduction<false>(err, partials, &sc->block_counter, sh, &total) && threadIdx.x == 0) {

@@ -48,6 +48,7 @@ void scene_constants(const sph_scene_desc& d, Consts<R>* out_c, LoopLimits* out_
     c.inv_h = (R)(1.0 / sr);
     c.h2 = (R)(sr * sr);
     c.cull2 = (R)(sr * sr * (sizeof(R) == 8 ? (1.0 + 1e-12) : (1.0 + 1e-6)));
+    c.inv_density0 = 1.0 / (double)(R)d.density0;
     c.cs_k = (R)(8.0 / (pi * h3));
     c.cs_l = (R)(48.0 / (pi * h3));
     c.p6_h2 = (R)(sr * sr);
