@@ -467,6 +467,12 @@ __global__ void k_pool_control(PoolScene* T, uint32_t S, PoolCounters* pc, cudaG
     }
 }
 
+// Each scene's running flag, for a poll that copies S bytes.
+__global__ void k_pool_running(const PoolScene* __restrict__ T, uint32_t S, uint8_t* __restrict__ out)
+{
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < S; k += gridDim.x * blockDim.x) out[k] = T[k].running ? 1 : 0;
+}
+
 __global__ void k_pool_finish(PoolScene* T, uint32_t S)
 {
     for (uint32_t k = threadIdx.x; k < S; k += blockDim.x) {
@@ -509,6 +515,7 @@ public:
         if (st_) cudaStreamDestroy(st_);
         if (st2_) cudaStreamDestroy(st2_);
         if (h_pc_) cudaFreeHost(h_pc_);
+        if (h_run_) cudaFreeHost(h_run_);
     }
 
     void fail(const std::string& m) { err = m; }
@@ -526,6 +533,7 @@ public:
         SPH_CUDA(cudaStreamCreateWithFlags(&st2_, cudaStreamNonBlocking));
         ls_ = st_;
         SPH_CUDA(cudaMallocHost((void**)&h_pc_, sizeof(PoolCounters)));
+        SPH_CUDA(cudaMallocHost((void**)&h_run_, std::max<size_t>(d.max_scenes, 1)));
         const size_t P = d.max_particles, B = std::max<size_t>(d.max_boundary, 1), K = d.max_keys;
         for (int k = 0; k < 2; ++k) {
             SPH_CUDA(pos_[k].alloc(P)); SPH_CUDA(vel_[k].alloc(P)); SPH_CUDA(kappa_[k].alloc(P));
@@ -548,6 +556,7 @@ public:
                                       64 * 256 * (int)sizeof(uint32_t)));
         SPH_CUDA(cudaMemsetAsync(count_.p, 0, K * sizeof(uint32_t), st_));
         SPH_CUDA(table_.alloc(d.max_scenes));
+        SPH_CUDA(run_.alloc(d.max_scenes));
         SPH_CUDA(seg_a_.alloc(d.max_scenes)); SPH_CUDA(seg_b_.alloc(d.max_scenes)); SPH_CUDA(seg_n_.alloc(d.max_scenes));
         SPH_CUDA(pc_.alloc(1));
         SPH_CUDA(cudaMemsetAsync(pc_.p, 0, sizeof(PoolCounters), st_));
@@ -955,12 +964,15 @@ public:
     // Ids of resident scenes whose steps have completed (one table read).
     int poll(int* ids, int max, int* ndone)
     {
-        std::vector<PoolScene> t(S_);
-        if (S_) SPH_CUDA(cudaMemcpyAsync(t.data(), table_.p, S_ * sizeof(PoolScene), cudaMemcpyDeviceToHost, st_));
+        if (S_) {
+            k_pool_running<<<blocks(S_, 256), 256, 0, st_>>>(table_.p, S_, run_.p);
+            SPH_CUDA(cudaGetLastError());
+            SPH_CUDA(cudaMemcpyAsync(h_run_, run_.p, S_, cudaMemcpyDeviceToHost, st_));
+        }
         SPH_CUDA(cudaStreamSynchronize(st_));
         int k = 0;
         for (uint32_t s = 0; s < S_; ++s)
-            if (!t[s].running && !order_[s]->removed) {
+            if (!h_run_[s] && !order_[s]->removed) {
                 if (ids && k < max) ids[k] = order_[s]->id;
                 ++k;
             }
@@ -1528,6 +1540,8 @@ private:
     DevBuf<uint32_t> cell_[2], id_[2], bcell_[2], bid_[2];
     DevBuf<P4<float>> acc_, dummy4_, pairs_, bgrad_;
     DevBuf<uint2> posh_;  // half-precision positions for the build's cull
+    DevBuf<uint8_t> run_;   // per scene: running (poll)
+    uint8_t* h_run_ = nullptr;
     DevBuf<float> rho_, alpha_, div_, press_, kbuf_, bpsi_;
     DevBuf<uint32_t> sid_, bsid_, lcount_, key_, slot_, tmp_, count_, starts_, bstarts_, tile_sums_, mort_;
     DevBuf<uint32_t> seg_a_, seg_b_, seg_n_;
