@@ -33,7 +33,7 @@ template <typename R> struct Lists {
     P4<R>* bgrad;       // xyz: sum_b rho0 psi_b gradW_ib
     R* kbuf;            // k (or kv) of the pass in progress
     uint32_t kmax;
-    // FP32 pool: a half-precision copy of the cell-relative positions
+    // FP32 form: a half-precision copy of the cell-relative positions
     // (x, y, z, 0 per particle; two particles per 16-byte word) for the
     // build's cull, or nullptr
     const uint4* posh;
