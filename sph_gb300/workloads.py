@@ -1,6 +1,9 @@
 """Seeded synthetic scenes for the DFSPH workloads (no dataset is involved).
 
 * ``dam_break``     one 125,000-particle dam break with Akinci walls;
+* ``pcisph_drop``   PCISPH with standard viscosity, Akinci surface tension and
+                    adhesion: a 5-layer pool on the floor of a 1 m Akinci box
+                    and a sphere of fluid (R = 0.2 m) 0.6 m above it, r = 5 mm;
 * ``batched_mix``   independent scenes: per-scene particle counts log-uniform
                     in [2k, 64k], fluid blocks with aspect ratios uniform in
                     [0.5, 2] at the box corner, 0-3 Akinci sphere obstacles of
@@ -70,6 +73,26 @@ def dam_break(r=0.005, n_side=50, box=(1.5, 0.8, 0.8), steps=2000):
     x, _ = _block(r, (2 * r, 2 * r, 2 * r), (n_side, n_side, n_side))
     b = sample_box(4 * r, (0.0, 0.0, 0.0), box)
     return x, b, dict(DFSPH, radius=r), int(steps)
+
+
+def pcisph_drop(r=0.005, steps=1000):
+    """A 5-layer pool (2r off the walls, 48,020 particles at r = 5 mm) and a
+    lattice sphere of R = 0.2 m centred 0.6 m above the pool top (33,401
+    particles) in a 1 m Akinci box; PCISPH, standard viscosity 0.01, Akinci
+    surface tension 0.5 and adhesion 0.1, eta 0.001, 3-100 iterations,
+    dt = 1e-4 s."""
+    d = 2 * r
+    n = int((1.0 - 4 * r) / d)
+    pool, (pmn, pmx) = _block(r, (2 * r, 2 * r, 2 * r), (n, 5, n))
+    c = np.array([0.5, pmx[1] + 0.6, 0.5])
+    R = 0.2
+    cube = fluid_block(r, c - R - r, c + R + r)
+    ball = cube[np.sum((cube - c) ** 2, axis=1) <= R * R]
+    x = np.concatenate([pool, ball])
+    b = sample_box(4 * r, (0.0, 0.0, 0.0), (1.0, 1.0, 1.0))
+    params = dict(method=1, boundary=2, radius=r, eta=0.001, min_it=3, max_it=100, dt=1e-4, visc_method=0,
+                  visc=0.01, st_method=3, st=0.5, adh_method=4, adh=0.1)
+    return x, b, params, int(steps)
 
 
 def big_dam_break(r=0.004, steps=200):
