@@ -42,10 +42,12 @@ template <typename R> struct Lists {
 // Phase 1 of the FP32 list build from the half-precision positions: the
 // nine columns of the 27-cell neighbourhood (trimmed as walk() trims them),
 // two candidates per half2 operation, accepted indices queued in walk order.
-// The test uses r^2 <= 1.02 h^2: half-precision offsets (relative error
-// 2^-11 per value, |offsets| <= 2h) move r^2 by less than 0.6 % of h^2, so
-// every pair the FP32 test accepts is kept; pairs beyond h evaluate to
-// W = 0, grad W = 0 in phase 2 and are dropped there.  Returns the number of
+// The test uses r^2 <= 1.02 h^2: with the particle's offsets inside
+// [-h/2, 3h/2] (the caller's condition), a pair within h has candidate
+// offsets of at most 3.5h, and half-precision values (relative error 2^-11
+// each) move r^2 by less than 1.5 % of h^2, so every pair the FP32 test
+// accepts is kept; pairs beyond h evaluate to W = 0, grad W = 0 in phase 2
+// and are dropped there.  Returns the number of
 // accepted candidates (the queue holds the first qcap).
 __device__ __forceinline__ uint32_t cull_half(const GridView& g, const uint32_t* __restrict__ starts, uint32_t pc,
                                               V3<float> xi, float h, float cull2, const uint4* __restrict__ posh,
@@ -202,12 +204,17 @@ __device__ __forceinline__ void build_lists_one(uint32_t i, const Fluid<R>& f, c
             ++cnt;
         }
     };
-    // phase 1: cull
+    // phase 1: cull.  The half-precision cull's error bound needs the
+    // particle's offsets inside [-h/2, 3h/2]; a particle outside the grid
+    // box (kept in the border cell, offsets unbounded) culls in FP32.
     uint32_t nq = 0;
+    bool half_cull = false;
     if constexpr (FAST && sizeof(R) == 4) {
-        if (L.posh) nq = cull_half(g, cs, pc, xi, c.h, c.cull2, L.posh, q, qstride, qcap);
+        const R hh = (R)0.5 * c.h;
+        half_cull = L.posh && fabsf(xi.x - hh) <= c.h && fabsf(xi.y - hh) <= c.h && fabsf(xi.z - hh) <= c.h;
+        if (half_cull) nq = cull_half(g, cs, pc, xi, c.h, c.cull2, L.posh, q, qstride, qcap);
     }
-    if (!(FAST && sizeof(R) == 4) || !L.posh)
+    if (!half_cull)
         walk<R, 1, true, FAST>(g, cs, pc, xi, c.h, 0, [&](uint32_t j, V3<R> s) {
             const V3<R> r = s - xyz(ldg4(f.pos + j));
             if (dot3(r, r) <= c.cull2) {
