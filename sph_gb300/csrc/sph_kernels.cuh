@@ -164,6 +164,12 @@ __global__ void k_download(uint32_t n, const P4<R>* __restrict__ v4, const R* __
 // Grid build: cell update -> count -> scan -> scatter -> in-cell id order
 // ===========================================================================
 
+// The z offset in the frame of the cell's z index modulo 3, in [0, 3h) for
+// an in-grid particle: the FP32 list build's half-precision cull reads the
+// z distance of a candidate in cells z-1..z+1 from it without the
+// candidate's cell (kept in position.w, which fluid positions leave unused).
+__device__ __forceinline__ float zframe3(float oz, int cz, float h) { return oz + (float)(cz % 3) * h; }
+
 // Moves particles (MOVE: x += v dt, DFSPHSolver::updatePositions
 // DFSPHSolver.cpp:216-236), recomputes their cells (HashTable.h:81) and
 // counts them per cell key.
@@ -199,6 +205,7 @@ __global__ void k_cell_update(uint32_t n, P4<R>* __restrict__ pos, const P4<R>* 
         if (ccx == cx) p.x = fminf(fmaxf(p.x, 0.f), __int_as_float(__float_as_int(h) - 1));
         if (ccy == cy) p.y = fminf(fmaxf(p.y, 0.f), __int_as_float(__float_as_int(h) - 1));
         if (ccz == cz) p.z = fminf(fmaxf(p.z, 0.f), __int_as_float(__float_as_int(h) - 1));
+        p.w = zframe3(p.z, ccz, h);
         cx = ccx; cy = ccy; cz = ccz;
     } else {
         cx = (int)floor((double)p.x / hd) - g.ox;
@@ -380,11 +387,13 @@ __device__ __forceinline__ uint32_t final_slot(uint32_t p, const uint32_t* __res
 // Gather of the state that survives a re-sort (x, v, DFSPH k, kv and the
 // last predicted density; the other fields are recomputed after every build).
 // posh (FP32, optional): also the half-precision copy of the positions the
-// pool's list build culls with (x, y, z, 0 per particle).
+// list build culls with, two particles (2k, 2k+1) per 16-byte word:
+// {x pair, y pair, z pair, unused} as half2, z in the cell's modulo-3 frame
+// (position.w, written by the cell update).
 template <typename R>
 __global__ void k_gather_fluid(uint32_t n, const uint32_t* __restrict__ tmp, const uint32_t* __restrict__ key,
                                const uint32_t* __restrict__ starts, Fluid<R> src, Fluid<R> dst,
-                               uint2* __restrict__ posh = nullptr)
+                               uint4* __restrict__ posh = nullptr)
 {
     const uint32_t p = gtid();
     if (p >= src.count()) return;
@@ -394,9 +403,10 @@ __global__ void k_gather_fluid(uint32_t n, const uint32_t* __restrict__ tmp, con
     dst.pos[d] = x;
     if constexpr (sizeof(R) == 4) {
         if (posh) {
-            const __half2 xy = __floats2half2_rn(x.x, x.y);
-            const __half2 z0 = __floats2half2_rn(x.z, 0.f);
-            posh[d] = make_uint2(*reinterpret_cast<const uint32_t*>(&xy), *reinterpret_cast<const uint32_t*>(&z0));
+            __half* ph = reinterpret_cast<__half*>(posh) + (size_t)(d >> 1) * 8 + (d & 1);
+            ph[0] = __float2half_rn(x.x);
+            ph[2] = __float2half_rn(x.y);
+            ph[4] = __float2half_rn(x.w);
         }
     }
     dst.vel[d] = src.vel[i];

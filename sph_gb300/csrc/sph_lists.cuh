@@ -33,67 +33,72 @@ template <typename R> struct Lists {
     P4<R>* bgrad;       // xyz: sum_b rho0 psi_b gradW_ib
     R* kbuf;            // k (or kv) of the pass in progress
     uint32_t kmax;
-    // FP32 form: a half-precision copy of the cell-relative positions
-    // (x, y, z, 0 per particle; two particles per 16-byte word) for the
-    // build's cull, or nullptr
+    // FP32 form: a half-precision copy of the cell-relative positions for
+    // the build's cull, two particles per 16-byte word ({x, y, z, unused}
+    // half2 pairs, z in the cell's modulo-3 frame), or nullptr
     const uint4* posh;
 };
 
 // Phase 1 of the FP32 list build from the half-precision positions: the
 // nine columns of the 27-cell neighbourhood (trimmed as walk() trims them),
 // two candidates per half2 operation, accepted indices queued in walk order.
-// The test uses r^2 <= 1.02 h^2: with the particle's offsets inside
-// [-h/2, 3h/2] (the caller's condition), a pair within h has candidate
-// offsets of at most 3.5h, and half-precision values (relative error 2^-11
-// each) move r^2 by less than 1.5 % of h^2, so every pair the FP32 test
-// accepts is kept; pairs beyond h evaluate to W = 0, grad W = 0 in phase 2
-// and are dropped there.  Returns the number of
-// accepted candidates (the queue holds the first qcap).
+// The caller guarantees that the particle's cell is at least two cells from
+// every face of the grid box (all 27 cells exist and hold in-grid particles,
+// offsets in [0, h)) and that its own offsets are inside [-h/2, 3h/2].
+//
+// z needs no per-candidate cell: positions carry z in the frame of their
+// cell's z index modulo 3 (in [0, 3h)), so for a candidate in cells
+// z-1..z+1 the difference d of the two frame values is the true z distance
+// plus a multiple of 3h, and min(|d|, 3h - |d|) is the true |dz| whenever
+// |dz| <= 1.5h and above h (so culled) otherwise, up to a sliver of
+// |dz| in [1.97h, 2h) that phase 2 drops.
+//
+// The test uses r^2 <= 1.03 h^2: for a pair within h, half-precision values
+// (relative error 2^-11 each; x, y operands within 2.5h, z within 3h)
+// move r^2 by less than 1.7 % of h^2, so every pair the FP32 test accepts
+// is kept; pairs beyond h evaluate to W = 0, grad W = 0 in phase 2 and are
+// dropped there.  Returns the number of accepted candidates (the queue
+// holds the first qcap).
+__device__ __forceinline__ __half2 as_half2(uint32_t u) { return *reinterpret_cast<const __half2*>(&u); }
+
 __device__ __forceinline__ uint32_t cull_half(const GridView& g, const uint32_t* __restrict__ starts, uint32_t pc,
                                               V3<float> xi, float h, float cull2, const uint4* __restrict__ posh,
                                               uint32_t* q, uint32_t qstride, uint32_t qcap)
 {
     const int cx = cell_x(pc), cy = cell_y(pc), cz = cell_z(pc);
-    const int z0 = cz > 0 ? cz - 1 : 0;
-    const int z1 = cz + 1 < g.nz ? cz + 1 : g.nz - 1;
     const float ofx = xi.x, ofy = xi.y, ofz = xi.z;
     const float gxm = ofx > 0.f ? ofx * ofx : 0.f, gxp = h - ofx > 0.f ? (h - ofx) * (h - ofx) : 0.f;
     const float gym = ofy > 0.f ? ofy * ofy : 0.f, gyp = h - ofy > 0.f ? (h - ofy) * (h - ofy) : 0.f;
     const float gzm = ofz > 0.f ? ofz * ofz : 0.f, gzp = h - ofz > 0.f ? (h - ofz) * (h - ofz) : 0.f;
     const float lim = h * h * (float)(1.0 + 1e-5);
-    const __half2 thr = __float2half2_rn(cull2 * 1.02f);
-    const __half hzm = __float2half_rn(xi.z + h), hz0 = __float2half_rn(xi.z), hzp = __float2half_rn(xi.z - h);
+    const __half2 thr = __float2half2_rn(cull2 * 1.03f);
+    const __half2 zq = __float2half2_rn(zframe3(xi.z, cz, h));
+    const __half2 h3 = __float2half2_rn(3.f * h);
     uint32_t nq = 0;
 #pragma unroll 1
     for (int c = 0; c < 9; ++c) {
         const int dx = c / 3 - 1, dy = c - (c / 3) * 3 - 1;
-        const int x = cx + dx, y = cy + dy;
         const float gxy = (dx < 0 ? gxm : (dx > 0 ? gxp : 0.f)) + (dy < 0 ? gym : (dy > 0 ? gyp : 0.f));
-        if (x < 0 || x >= g.nx || y < 0 || y >= g.ny || !(gxy <= lim)) continue;
-        const uint32_t base = (__ldg(g.mortx + x) | __ldg(g.morty + y)) * (uint32_t)g.nz;
-        const uint32_t s0 = __ldg(starts + base + z0), sm = __ldg(starts + base + cz);
-        const uint32_t sp = __ldg(starts + base + cz + 1), s1 = __ldg(starts + base + z1 + 1);
-        const uint32_t bb = gxy + gzm <= lim ? s0 : sm;
-        const uint32_t ee = gxy + gzp <= lim ? s1 : sp;
+        if (!(gxy <= lim)) continue;
+        const uint32_t base = (__ldg(g.mortx + cx + dx) | __ldg(g.morty + cy + dy)) * (uint32_t)g.nz;
+        const uint32_t bb = __ldg(starts + base + (gxy + gzm <= lim ? cz - 1 : cz));
+        const uint32_t ee = __ldg(starts + base + (gxy + gzp <= lim ? cz + 2 : cz + 1));
         const __half2 sx = __float2half2_rn(xi.x - (float)dx * h), sy = __float2half2_rn(xi.y - (float)dy * h);
 #pragma unroll 1
         for (uint32_t j = bb & ~1u; j < ee; j += 2) {
             const uint4 w = __ldg(posh + (j >> 1));
-            const uint32_t px = __byte_perm(w.x, w.z, 0x5410), py = __byte_perm(w.x, w.z, 0x7632);
-            const uint32_t pz = __byte_perm(w.y, w.w, 0x5410);
-            const __half za = j < sm ? hzm : (j < sp ? hz0 : hzp);
-            const __half zb = j + 1 < sm ? hzm : (j + 1 < sp ? hz0 : hzp);
-            const __half2 sz = __halves2half2(za, zb);
-            const __half2 ddx = __hsub2(sx, *reinterpret_cast<const __half2*>(&px));
-            const __half2 ddy = __hsub2(sy, *reinterpret_cast<const __half2*>(&py));
-            const __half2 ddz = __hsub2(sz, *reinterpret_cast<const __half2*>(&pz));
+            const __half2 ddx = __hsub2(sx, as_half2(w.x));
+            const __half2 ddy = __hsub2(sy, as_half2(w.y));
+            const __half2 dz = __habs2(__hsub2(zq, as_half2(w.z)));
+            const __half2 ddz = __hmin2(dz, __hsub2(h3, dz));
             const __half2 r2 = __hfma2(ddz, ddz, __hfma2(ddy, ddy, __hmul2(ddx, ddx)));
             const unsigned m = __hle2_mask(r2, thr);
-            if ((m & 0xFFFFu) && j >= bb) {
+            // the word's other particle may lie outside the column's range
+            if ((m & 1u) && j >= bb) {
                 if (nq < qcap) q[nq * qstride + threadIdx.x] = j;
                 ++nq;
             }
-            if ((m >> 16) && j + 1 < ee) {
+            if ((m >> 31) && j + 1 < ee) {
                 if (nq < qcap) q[nq * qstride + threadIdx.x] = j + 1;
                 ++nq;
             }
@@ -204,14 +209,17 @@ __device__ __forceinline__ void build_lists_one(uint32_t i, const Fluid<R>& f, c
             ++cnt;
         }
     };
-    // phase 1: cull.  The half-precision cull's error bound needs the
-    // particle's offsets inside [-h/2, 3h/2]; a particle outside the grid
-    // box (kept in the border cell, offsets unbounded) culls in FP32.
+    // phase 1: cull.  The half-precision cull needs all 27 cells inside the
+    // grid box and clear of its border cells (where particles that left the
+    // box are kept, with unbounded offsets), and in-cell offsets; elsewhere
+    // the cull runs in FP32.
     uint32_t nq = 0;
     bool half_cull = false;
     if constexpr (FAST && sizeof(R) == 4) {
         const R hh = (R)0.5 * c.h;
-        half_cull = L.posh && fabsf(xi.x - hh) <= c.h && fabsf(xi.y - hh) <= c.h && fabsf(xi.z - hh) <= c.h;
+        const int cx = cell_x(pc), cy = cell_y(pc), cz = cell_z(pc);
+        half_cull = L.posh && cx >= 2 && cy >= 2 && cz >= 2 && cx <= g.nx - 3 && cy <= g.ny - 3 && cz <= g.nz - 3 &&
+                    fabsf(xi.x - hh) <= c.h && fabsf(xi.y - hh) <= c.h && fabsf(xi.z - hh) <= c.h;
         if (half_cull) nq = cull_half(g, cs, pc, xi, c.h, c.cull2, L.posh, q, qstride, qcap);
     }
     if (!half_cull)

@@ -163,6 +163,7 @@ __global__ void k_pool_cell_update(uint32_t N, Fluid<float> f, const uint32_t* _
     if (ccx == cx) p.x = fminf(fmaxf(p.x, 0.f), __int_as_float(__float_as_int(h) - 1));
     if (ccy == cy) p.y = fminf(fmaxf(p.y, 0.f), __int_as_float(__float_as_int(h) - 1));
     if (ccz == cz) p.z = fminf(fmaxf(p.z, 0.f), __int_as_float(__float_as_int(h) - 1));
+    p.w = zframe3(p.z, ccz, h);
     f.pos[i] = p;
     f.cell[i] = pack_cell(ccx, ccy, ccz);
     const uint32_t k = sd.key_base + cell_key(g, ccx, ccy, ccz);
@@ -544,8 +545,8 @@ public:
         SPH_CUDA(press_.alloc(P)); SPH_CUDA(kbuf_.alloc(P)); SPH_CUDA(sid_.alloc(P)); SPH_CUDA(bsid_.alloc(B));
         SPH_CUDA(bpsi_.alloc(B)); SPH_CUDA(dummy4_.alloc(1));
         SPH_CUDA(pairs_.alloc(P * kmax_)); SPH_CUDA(lcount_.alloc(P)); SPH_CUDA(bgrad_.alloc(P));
-        SPH_CUDA(posh_.alloc(P + 2));  // whole 16-byte pairs, one past the end
-        SPH_CUDA(cudaMemsetAsync(posh_.p, 0, (P + 2) * sizeof(uint2), st_));
+        SPH_CUDA(posh_.alloc(P / 2 + 1));  // particle pairs, the last one whole
+        SPH_CUDA(cudaMemsetAsync(posh_.p, 0, (P / 2 + 1) * sizeof(uint4), st_));
         const size_t M = std::max(P, B);
         SPH_CUDA(key_.alloc(M)); SPH_CUDA(slot_.alloc(M)); SPH_CUDA(tmp_.alloc(M));
         SPH_CUDA(count_.alloc(K)); SPH_CUDA(starts_.alloc(K + 1)); SPH_CUDA(bstarts_.alloc(K + 1));
@@ -1074,7 +1075,7 @@ private:
     Boundary<float> B(int k) const { return Boundary<float>{bpos_[k].p, bpsi_.p, bcell_[k].p, bid_[k].p, NB_}; }
     Lists<float> LS() const
     {
-        return Lists<float>{pairs_.p, lcount_.p, bgrad_.p, kbuf_.p, kmax_, reinterpret_cast<const uint4*>(posh_.p)};
+        return Lists<float>{pairs_.p, lcount_.p, bgrad_.p, kbuf_.p, kmax_, posh_.p};
     }
 
     int scan(uint32_t* out)
@@ -1539,7 +1540,7 @@ private:
     DevBuf<float> kappa_[2], kappav_[2], pred_[2];
     DevBuf<uint32_t> cell_[2], id_[2], bcell_[2], bid_[2];
     DevBuf<P4<float>> acc_, dummy4_, pairs_, bgrad_;
-    DevBuf<uint2> posh_;  // half-precision positions for the build's cull
+    DevBuf<uint4> posh_;  // half-precision positions for the build's cull (particle pairs)
     DevBuf<uint8_t> run_;   // per scene: running (poll)
     uint8_t* h_run_ = nullptr;
     DevBuf<float> rho_, alpha_, div_, press_, kbuf_, bpsi_;

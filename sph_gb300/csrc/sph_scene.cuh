@@ -651,7 +651,7 @@ private:
     Fluid<R> F() const { return fl_[cur_]; }
     Lists<R> LS() const
     {
-        return Lists<R>{pairs_.p, lcount_.p, bgrad_.p, kbuf_.p, kmax_, reinterpret_cast<const uint4*>(posh_.p)};
+        return Lists<R>{pairs_.p, lcount_.p, bgrad_.p, kbuf_.p, kmax_, posh_.p};
     }
     Boundary<R> B(int k) const { return bd_[k]; }
 
@@ -757,10 +757,10 @@ private:
         SPH_CUDA(bgrad_.alloc(lists_ ? n : 1));
         SPH_CUDA(kbuf_.alloc(n));
         // FP32 pair lists: half-precision positions for the build's cull
-        // (whole 16-byte pairs, one past the end); written by every gather
+        // (particle pairs, the last one whole); written by every gather
         if (lists_ && sizeof(R) == 4) {
-            SPH_CUDA(posh_.alloc(n + 2));
-            SPH_CUDA(cudaMemsetAsync(posh_.p, 0, (n + 2) * sizeof(uint2), st_));
+            SPH_CUDA(posh_.alloc(n / 2 + 1));
+            SPH_CUDA(cudaMemsetAsync(posh_.p, 0, (n / 2 + 1) * sizeof(uint4), st_));
         }
         SPH_CUDA(cudaMemsetAsync(lcount_.p, 0, lcount_.n * sizeof(uint32_t), st_));
         SPH_CUDA(cudaMemsetAsync(kbuf_.p, 0, n * sizeof(R), st_));
@@ -1319,7 +1319,7 @@ private:
     DevBuf<EmitterDev> em_;
     DevBuf<double> egroup_;
     DevBuf<double> cap_x_, cap_v_;  // staging of asynchronous frame captures
-    DevBuf<uint2> posh_;            // FP32 pair lists: half-precision positions (build cull)
+    DevBuf<uint4> posh_;            // FP32 pair lists: half-precision positions (build cull, particle pairs)
     int akinci_ = 0;   // Akinci boundary model: boundary terms in the forces too
     int bh_ = 0;       // PCISPH boundary model
     int hasb_ = 0;     // boundary particles take part in the solver sums
