@@ -84,7 +84,7 @@ __device__ __forceinline__ uint32_t cull_half(const GridView& g, const uint32_t*
         const uint32_t bb = __ldg(starts + base + (gxy + gzm <= lim ? cz - 1 : cz));
         const uint32_t ee = __ldg(starts + base + (gxy + gzp <= lim ? cz + 2 : cz + 1));
         const __half2 sx = __float2half2_rn(xi.x - (float)dx * h), sy = __float2half2_rn(xi.y - (float)dy * h);
-#pragma unroll 1
+#pragma unroll 2
         for (uint32_t j = bb & ~1u; j < ee; j += 2) {
             const uint4 w = __ldg(posh + (j >> 1));
             const __half2 ddx = __hsub2(sx, as_half2(w.x));
