@@ -75,14 +75,22 @@ __device__ __forceinline__ uint32_t cull_half(const GridView& g, const uint32_t*
     const __half2 zq = __float2half2_rn(zframe3(xi.z, cz, h));
     const __half2 h3 = __float2half2_rn(3.f * h);
     uint32_t nq = 0;
+    // a column's candidate range (empty when trimmed); loaded one column ahead
+    auto range = [&](int c, uint32_t* b, uint32_t* e) {
+        const int dx = c / 3 - 1, dy = c - (c / 3) * 3 - 1;
+        const float gxy = (dx < 0 ? gxm : (dx > 0 ? gxp : 0.f)) + (dy < 0 ? gym : (dy > 0 ? gyp : 0.f));
+        if (!(gxy <= lim)) { *b = 0u; *e = 0u; return; }
+        const uint32_t base = (__ldg(g.mortx + cx + dx) | __ldg(g.morty + cy + dy)) * (uint32_t)g.nz;
+        *b = __ldg(starts + base + (gxy + gzm <= lim ? cz - 1 : cz));
+        *e = __ldg(starts + base + (gxy + gzp <= lim ? cz + 2 : cz + 1));
+    };
+    uint32_t nb, ne;
+    range(0, &nb, &ne);
 #pragma unroll 1
     for (int c = 0; c < 9; ++c) {
         const int dx = c / 3 - 1, dy = c - (c / 3) * 3 - 1;
-        const float gxy = (dx < 0 ? gxm : (dx > 0 ? gxp : 0.f)) + (dy < 0 ? gym : (dy > 0 ? gyp : 0.f));
-        if (!(gxy <= lim)) continue;
-        const uint32_t base = (__ldg(g.mortx + cx + dx) | __ldg(g.morty + cy + dy)) * (uint32_t)g.nz;
-        const uint32_t bb = __ldg(starts + base + (gxy + gzm <= lim ? cz - 1 : cz));
-        const uint32_t ee = __ldg(starts + base + (gxy + gzp <= lim ? cz + 2 : cz + 1));
+        const uint32_t bb = nb, ee = ne;
+        if (c < 8) range(c + 1, &nb, &ne);
         const __half2 sx = __float2half2_rn(xi.x - (float)dx * h), sy = __float2half2_rn(xi.y - (float)dy * h);
 #pragma unroll 2
         for (uint32_t j = bb & ~1u; j < ee; j += 2) {
