@@ -454,37 +454,86 @@ def run_served(args, rate, seconds, big_every):
     return out
 
 
-def roofline(prof, n, nb, pairs, workload):
-    kern = max(prof.items(), key=lambda kv: kv[1][1]) if prof else ("none", (1, 0.0))
-    kname, (kcount, kms) = kern
-    per_p, touches_b, per_pair = ALGO_BYTES.get(kname, (0, False, 0))
-    bytes_launch = n * per_p + (nb * 16 if touches_b else 0)
-    stream_launch = bytes_launch + pairs * per_pair
-    avg_ms = kms / max(kcount, 1)
-    achieved = bytes_launch / (avg_ms / 1000.0) / 1e9 if avg_ms > 0 else 0.0
-    streamed = stream_launch / (avg_ms / 1000.0) / 1e9 if avg_ms > 0 else 0.0
-    peak, peak_kind = load_peaks()
-    traffic = None
-    issue = {}
-    tp = os.path.join(ROOT, "profiles", f"ncu_{kname}_{workload}.md")
-    if os.path.exists(tp):
-        for ln in open(tp):
+# Instantiations of one __global__ function are one kernel, as the ncu launch
+# list names them: the profile times the error passes under two names.
+KERNEL_OF = {"k_pool_errors_density": "k_pool_errors", "k_pool_errors_div": "k_pool_errors"}
+
+
+def profile_figures(workload):
+    """Per kernel, the ncu figures the summaries under profiles/ record:
+    `dram_bytes_per_launch: V` for the file's own kernel (the name between
+    `ncu_` and the workload), `dram_bytes_per_launch.<kernel>: V` for another
+    kernel of the same capture, and the issue utilisations."""
+    out = {}
+    d = os.path.join(ROOT, "profiles")
+    suffix = f"_{workload}.md"
+    for fn in sorted(os.listdir(d)) if os.path.isdir(d) else []:
+        if not (fn.startswith("ncu_") and fn.endswith(suffix)):
+            continue
+        own = fn[len("ncu_"):-len(suffix)]
+        for ln in open(os.path.join(d, fn)):
             key, _, val = ln.partition(":")
-            if key == "dram_bytes_per_launch":
-                traffic = float(val)
-            elif key in ("sm_issue_active_pct", "l1_lsu_wavefronts_pct", "fp32_pipe_pct"):
-                issue[key] = float(val)
-    total = sum(v[1] for v in prof.values())
-    out = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
-           "frac": achieved / peak, "peak_kind": f"of {peak_kind}", "traffic": traffic,
-           "algorithmic_bytes_per_launch": bytes_launch, "avg_launch_ms": avg_ms,
-           "kernel_share": kms / total if total else None,
-           "with_pair_lists": {"bytes_per_launch": stream_launch, "achieved": streamed, "frac": streamed / peak,
-                               "note": "field bytes plus the 16-byte pair records the kernel writes or reads"}}
-    if issue:
-        # a neighbour walk is bound by instruction issue and the L1 load pipe,
-        # not by DRAM: the utilisations ncu measured for this kernel
-        out["issue"] = dict(issue, source=os.path.relpath(tp, ROOT))
+            key, _, other = key.strip().partition(".")
+            if key not in ("dram_bytes_per_launch", "sm_issue_active_pct", "l1_lsu_wavefronts_pct", "fp32_pipe_pct"):
+                continue
+            try:
+                v = float(val)
+            except ValueError:
+                continue
+            k = other or own
+            out.setdefault(k, {"source": os.path.join("profiles", fn)})[key] = v
+    return out
+
+
+def roofline(prof, n, nb, pairs, workload):
+    """HBM roofline of the kernel with the largest share of the profiled
+    steps (`kernel`), and the same figures for the three largest in
+    `kernels`.  Algorithmic bytes: compulsory field bytes per particle
+    (ALGO_BYTES) x particles, plus 16 B per boundary particle for walks that
+    touch the boundary; `with_pair_lists` adds the 16-byte pair records a
+    list kernel writes or reads."""
+    peak, peak_kind = load_peaks()
+    figs = profile_figures(workload)
+    groups = {}
+    for name, (count, ms) in prof.items():
+        groups.setdefault(KERNEL_OF.get(name, name), []).append((name, count, ms))
+    total = sum(ms for _, ms in prof.values())
+
+    def one(kname, entries):
+        count = sum(c for _, c, _ in entries)
+        ms = sum(m for _, _, m in entries)
+        algo = sum(c * (n * ALGO_BYTES.get(e, (0, False, 0))[0] + (nb * 16 if ALGO_BYTES.get(e, (0, False, 0))[1] else 0))
+                   for e, c, _ in entries)
+        stream = algo + sum(c * pairs * ALGO_BYTES.get(e, (0, False, 0))[2] for e, c, _ in entries)
+        avg_ms = ms / max(count, 1)
+        bytes_launch = algo / max(count, 1)
+        stream_launch = stream / max(count, 1)
+        achieved = bytes_launch / (avg_ms / 1000.0) / 1e9 if avg_ms > 0 else 0.0
+        streamed = stream_launch / (avg_ms / 1000.0) / 1e9 if avg_ms > 0 else 0.0
+        f = figs.get(kname, {})
+        r = {"kernel": kname, "achieved": achieved, "frac": achieved / peak, "traffic": f.get("dram_bytes_per_launch"),
+             "algorithmic_bytes_per_launch": bytes_launch, "avg_launch_ms": avg_ms, "launches": count,
+             "kernel_share": ms / total if total else None,
+             "with_pair_lists": {"bytes_per_launch": stream_launch, "achieved": streamed, "frac": streamed / peak,
+                                 "note": "field bytes plus the 16-byte pair records the kernel writes or reads"}}
+        issue = {k: v for k, v in f.items() if k in ("sm_issue_active_pct", "l1_lsu_wavefronts_pct", "fp32_pipe_pct")}
+        if issue:
+            # a neighbour walk is bound by instruction issue and the L1 load
+            # pipe, not by DRAM: the utilisations ncu measured for this kernel
+            r["issue"] = dict(issue, source=f["source"])
+        if f.get("source"):
+            r["profile"] = f["source"]
+        return r
+
+    ranked = sorted(groups.items(), key=lambda kv: -sum(m for _, _, m in kv[1]))
+    if not ranked:
+        return {"bound": "hbm", "kernel": "none", "achieved": 0.0, "peak": peak, "unit": "GB/s", "frac": 0.0,
+                "peak_kind": f"of {peak_kind}", "traffic": None}
+    top = one(*ranked[0])
+    out = {"bound": "hbm", "kernel": top.pop("kernel"), "achieved": top.pop("achieved"), "peak": peak, "unit": "GB/s",
+           "frac": top.pop("frac"), "peak_kind": f"of {peak_kind}", "traffic": top.pop("traffic")}
+    out.update(top)
+    out["kernels"] = [one(k, e) for k, e in ranked[:3]]
     return out
 
 
