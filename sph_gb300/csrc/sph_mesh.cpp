@@ -111,8 +111,18 @@ bool read_obj(const std::string& path, std::vector<V3f>* x, std::vector<unsigned
     return true;
 }
 
-// RegularTriangleSampling::sampleMesh in FP32.
-void sample_surface(const std::vector<V3f>& vx, const std::vector<unsigned>& faces, float d, std::vector<V3f>* out)
+// Samples an edge or a line of this length gets (ceil(l / d) + 1, ends
+// included), or 0 when that count is beyond what one boundary can hold.
+constexpr float kMaxSamples = 268435456.0f;  // 2^28
+unsigned samples_along(float l, float d)
+{
+    const float n = std::ceil(l / d) + 1.0f;
+    return n < kMaxSamples ? (unsigned)n : 0u;
+}
+
+// RegularTriangleSampling::sampleMesh in FP32.  False when the mesh would
+// need more than 2^28 samples (an edge, a line or the whole surface).
+bool sample_surface(const std::vector<V3f>& vx, const std::vector<unsigned>& faces, float d, std::vector<V3f>* out)
 {
     // vertices
     out->insert(out->end(), vx.begin(), vx.end());
@@ -133,7 +143,8 @@ void sample_surface(const std::vector<V3f>& vx, const std::vector<unsigned>& fac
         const V3f v0 = vx[e.first];
         const V3f dir = vx[e.second] - v0;
         const float l = norm(dir);
-        const unsigned numSamples = (unsigned)std::ceil(l / d) + 1u;
+        const unsigned numSamples = samples_along(l, d);
+        if (numSamples == 0 || out->size() + numSamples > (size_t)kMaxSamples) return false;
         if (numSamples == 1) { out->push_back(v0); continue; }
         for (unsigned i = 1; i < numSamples - 1; i++) out->push_back(v0 + ((float)i / (float)(numSamples - 1)) * dir);
     }
@@ -156,17 +167,20 @@ void sample_surface(const std::vector<V3f>& vx, const std::vector<unsigned>& fac
         const float l = std::sqrt(l2);
         const V3f bn = base / l;
         const float h = norm(toTop - dot(bn, toTop) * bn);
-        const unsigned numLines = (unsigned)std::ceil(h / d) + 1u;
+        const unsigned numLines = samples_along(h, d);
+        if (numLines == 0) return false;
         for (unsigned line = 1; line < numLines - 1; line++) {
             V3f lineStart = v0;
             const float alpha = (float)line / (float)(numLines - 1);
             lineStart = lineStart + alpha * toTop;
             const float lineLength = (1.0f - alpha) * l;
-            const unsigned numSamples = (unsigned)std::ceil(lineLength / d) + 1u;
+            const unsigned numSamples = samples_along(lineLength, d);
+            if (numSamples == 0 || out->size() + numSamples > (size_t)kMaxSamples) return false;
             for (unsigned i = 1; i < numSamples - 1; i++)
                 out->push_back(lineStart + (((float)i * lineLength) / (float)(numSamples - 1)) * bn);
         }
     }
+    return true;
 }
 
 // GLM's rotate(m, angle, axis) and m * v on column-major 4x4 FP64 matrices.
@@ -203,7 +217,10 @@ long long sample_mesh(const char* path, double max_distance, std::vector<double>
     const float d = (float)max_distance;
     if (!(d > 0.0f) || !std::isfinite(d)) { *err = "the maximum sample distance must be positive"; return -1; }
     std::vector<V3f> s;
-    sample_surface(vx, faces, d, &s);
+    if (!sample_surface(vx, faces, d, &s)) {
+        *err = "the mesh needs more than 2^28 samples at this distance";
+        return -1;
+    }
     M4 id;
     for (int i = 0; i < 4; ++i)
         for (int j = 0; j < 4; ++j) id.c[i][j] = i == j ? 1.0 : 0.0;

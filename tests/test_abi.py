@@ -147,6 +147,8 @@ def test_mesh_sampler_rejects_bad_files(L, tmp_path):
     bad.write_text("v 0 0 0\nv 1 0 0\nf 1 2 3\n")
     assert L.sph_sample_mesh(str(bad).encode(), 0.04, None) == -1
     assert L.sph_sample_mesh(os.path.join(MESH_DIR, "ramp.obj").encode(), 0.0, None) == -1
+    # a distance that would need more than 2^28 samples is refused before sampling
+    assert L.sph_sample_mesh(os.path.join(MESH_DIR, "ramp.obj").encode(), 1e-9, None) == -1
     s = sph_gb300.Scene(method=2, boundary=1, radius=0.02)
     with pytest.raises(sph_gb300.SPHError, match="Akinci"):
         s.add_boundary_mesh(os.path.join(MESH_DIR, "ramp.obj"), 0.02)
