@@ -127,6 +127,7 @@ typedef struct sph_stats {
     unsigned list_overflow;       /* particles whose neighbours exceed neighbor_list_max */
     unsigned num_fluid_total;     /* FluidModel::getNumParticles: active + slots reserved by emitters;
                                      num_fluid is getNumActiveParticles */
+    unsigned grid_growths;        /* times the grid box grew to take in particles that left it */
 } sph_stats;
 
 /* Defaults of the reference (SPHSolver.cpp:12-19, DFSPHSolver.cpp:10-22,
@@ -220,6 +221,16 @@ int sph_ctx_synchronize(sph_ctx* ctx);
 /* Run whole steps as one CUDA graph with device-side solver loops
  * (conditional WHILE nodes): no host round trip per iteration.  1 = on. */
 int sph_ctx_set_graph(sph_ctx* ctx, int enable);
+
+/* The reference hashes cells without bounds (src/HashTable.h:79-102); the
+ * dense grid box here grows instead.  Every 16 steps a context reads, without
+ * waiting, whether a step kept a particle in a border cell (SPH_STATUS_OUT_OF_GRID);
+ * if so, before its next step it re-plans the box around every point with a
+ * 25 % margin (results unchanged; sph_stats.grid_growths counts it).  On by
+ * default; 0 keeps the box fixed: particles outside it stay in the border cells,
+ * neighbour sets still exact, walks slower.  The PCISPH boundary model keeps its
+ * box (SPH_ERR_UNSUPPORTED for 1). */
+int sph_ctx_set_grid_growth(sph_ctx* ctx, int enable);
 
 /* Simulation::step / run (Simulation.cpp:148-190) and the frame export
  * (SceneLoader::writeFluid SceneLoader.cpp:200-264, TimeManager::hasToSave

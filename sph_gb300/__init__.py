@@ -97,6 +97,7 @@ class Stats(ctypes.Structure):
         ("list_pairs", ctypes.c_ulonglong),
         ("list_overflow", ctypes.c_uint),
         ("num_fluid_total", ctypes.c_uint),
+        ("grid_growths", ctypes.c_uint),
     ]
 
 
@@ -156,6 +157,7 @@ ABI = [
     ("sph_ctx_step_timed", ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
     ("sph_ctx_synchronize", ctypes.c_int, [_vp]),
     ("sph_ctx_set_graph", ctypes.c_int, [_vp, ctypes.c_int]),
+    ("sph_ctx_set_grid_growth", ctypes.c_int, [_vp, ctypes.c_int]),
     ("sph_ctx_num_particles", ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_uint), ctypes.POINTER(ctypes.c_uint)]),
     ("sph_ctx_download", ctypes.c_int, [_vp, ctypes.c_int, _dp]),
     ("sph_ctx_download_noalloc", ctypes.c_int, [_vp, ctypes.c_int, _dp]),
@@ -426,6 +428,11 @@ class Scene:
 
     def set_graph(self, enable=True):
         self._check(lib().sph_ctx_set_graph(self._h, int(bool(enable))), "sph_ctx_set_graph")
+
+    def set_grid_growth(self, enable=True):
+        """Grow the grid box when particles leave it (the default), or keep it
+        fixed (particles outside stay in its border cells)."""
+        self._check(lib().sph_ctx_set_grid_growth(self._h, int(bool(enable))), "sph_ctx_set_grid_growth")
 
     # -- results ------------------------------------------------------------
     def counts(self):

@@ -494,6 +494,12 @@ int sph_ctx_set_graph(sph_ctx* ctx, int enable)
     return relay(ctx, ctx->scene->set_graph(enable));
 }
 
+int sph_ctx_set_grid_growth(sph_ctx* ctx, int enable)
+{
+    if (!ctx) return SPH_ERR_INVALID;
+    return relay(ctx, ctx->scene->set_grid_growth(enable));
+}
+
 int sph_ctx_get_desc(const sph_ctx* ctx, sph_scene_desc* out)
 {
     if (!ctx || !out) return SPH_ERR_INVALID;

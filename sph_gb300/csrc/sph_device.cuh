@@ -120,6 +120,7 @@ struct DevScalars {
     unsigned block_counter;        // last-block-done counter of reductions
     unsigned grid_epoch;           // grid builds so far (cell lifetimes, PCISPH boundary model)
     unsigned n_active;             // active fluid particles (grows when emitters emit)
+    unsigned escaped;              // a particle was kept in a border cell since the last grid growth
 };
 
 enum StatusBits : unsigned {

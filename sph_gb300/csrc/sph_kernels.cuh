@@ -72,6 +72,14 @@ template <int G, typename R> __device__ __forceinline__ V3<R> group_sum3(V3<R> v
 // Upload / download
 // ===========================================================================
 
+// A particle left the grid box and was kept in a border cell: the sticky
+// status bit, and the flag the host reads to grow the box.
+__device__ __forceinline__ void flag_out_of_grid(DevScalars* sc)
+{
+    atomicOr(&sc->status, (unsigned)ST_OUT_OF_GRID);
+    sc->escaped = 1u;
+}
+
 // One particle from FP64 host-layout position and velocity into slot i of
 // the device layout (FP32: offset from the clamped cell's corner), with the
 // per-particle solver state zeroed.
@@ -81,7 +89,7 @@ __device__ __forceinline__ void store_particle(const Fluid<R>& f, uint32_t i, do
 {
     int cx = (int)floor(px / h) - g.ox, cy = (int)floor(py / h) - g.oy, cz = (int)floor(pz / h) - g.oz;
     const int ccx = min(max(cx, 0), g.nx - 1), ccy = min(max(cy, 0), g.ny - 1), ccz = min(max(cz, 0), g.nz - 1);
-    if (ccx != cx || ccy != cy || ccz != cz) atomicOr(&sc->status, (unsigned)ST_OUT_OF_GRID);
+    if (ccx != cx || ccy != cy || ccz != cz) flag_out_of_grid(sc);
     P4<R> p;
     if constexpr (sizeof(R) == 4) {
         p = {(R)(px - (double)(ccx + g.ox) * h), (R)(py - (double)(ccy + g.oy) * h), (R)(pz - (double)(ccz + g.oz) * h), 0};
@@ -96,6 +104,18 @@ __device__ __forceinline__ void store_particle(const Fluid<R>& f, uint32_t i, do
     f.press[i] = 0;
     f.cell[i] = pack_cell(ccx, ccy, ccz);
     f.id[i] = i;
+}
+
+// Shifts packed cell indices by whole cells (a grid box re-planned around
+// the same cell lattice: cell (x, y, z) of the old box is (x + sx, y + sy,
+// z + sz) of the new one).
+static __global__ void k_shift_cells(uint32_t n, const uint32_t* __restrict__ na, uint32_t* __restrict__ cell, int sx,
+                                     int sy, int sz)
+{
+    const uint32_t i = gtid();
+    if (i >= (na ? *na : n)) return;
+    const uint32_t c = cell[i];
+    cell[i] = pack_cell(cell_x(c) + sx, cell_y(c) + sy, cell_z(c) + sz);
 }
 
 // Host positions (FP64, xyz per particle) into the device layout.
@@ -117,7 +137,7 @@ __global__ void k_upload_boundary(const double* __restrict__ x, uint32_t n, Boun
     const double px = x[3 * i], py = x[3 * i + 1], pz = x[3 * i + 2];
     int cx = (int)floor(px / h) - g.ox, cy = (int)floor(py / h) - g.oy, cz = (int)floor(pz / h) - g.oz;
     const int ccx = min(max(cx, 0), g.nx - 1), ccy = min(max(cy, 0), g.ny - 1), ccz = min(max(cz, 0), g.nz - 1);
-    if (ccx != cx || ccy != cy || ccz != cz) atomicOr(&sc->status, (unsigned)ST_OUT_OF_GRID);
+    if (ccx != cx || ccy != cy || ccz != cz) flag_out_of_grid(sc);
     if constexpr (sizeof(R) == 4)
         b.pos[i] = {(R)(px - (double)(ccx + g.ox) * h), (R)(py - (double)(ccy + g.oy) * h), (R)(pz - (double)(ccz + g.oz) * h), 0};
     else
@@ -194,7 +214,7 @@ __global__ void k_cell_update(uint32_t n, P4<R>* __restrict__ pos, const P4<R>* 
         const int sx = (int)floorf(p.x / h), sy = (int)floorf(p.y / h), sz = (int)floorf(p.z / h);
         cx = x0 + sx; cy = y0 + sy; cz = z0 + sz;
         const int ccx = min(max(cx, 0), g.nx - 1), ccy = min(max(cy, 0), g.ny - 1), ccz = min(max(cz, 0), g.nz - 1);
-        if (ccx != cx || ccy != cy || ccz != cz) atomicOr(&sc->status, (unsigned)ST_OUT_OF_GRID);
+        if (ccx != cx || ccy != cy || ccz != cz) flag_out_of_grid(sc);
         p.x -= (R)(ccx - x0) * h; p.y -= (R)(ccy - y0) * h; p.z -= (R)(ccz - z0) * h;
         if (carry) {  // a second point stored in the particle's frame (PCISPH predicted position)
             P4<R> q = carry[i];
@@ -212,7 +232,7 @@ __global__ void k_cell_update(uint32_t n, P4<R>* __restrict__ pos, const P4<R>* 
         cy = (int)floor((double)p.y / hd) - g.oy;
         cz = (int)floor((double)p.z / hd) - g.oz;
         const int ccx = min(max(cx, 0), g.nx - 1), ccy = min(max(cy, 0), g.ny - 1), ccz = min(max(cz, 0), g.nz - 1);
-        if (ccx != cx || ccy != cy || ccz != cz) atomicOr(&sc->status, (unsigned)ST_OUT_OF_GRID);
+        if (ccx != cx || ccy != cy || ccz != cz) flag_out_of_grid(sc);
         cx = ccx; cy = ccy; cz = ccz;
     }
     pos[i] = p;

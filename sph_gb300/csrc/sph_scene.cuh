@@ -116,20 +116,27 @@ struct GridPlan {
     uint64_t nkeys = 0;
 };
 
+// cover_points: a given domain is widened to hold every point too.
 inline int grid_plan(const sph_scene_desc& d, const std::vector<double>& hx, const std::vector<double>& hb, bool akinci,
-                     const std::vector<double>& he, double h, GridPlan* out, std::string* err, double rel_margin = 0.05)
+                     const std::vector<double>& he, double h, GridPlan* out, std::string* err, double rel_margin = 0.05,
+                     bool cover_points = false)
 {
     double lo[3], hi[3];
     bool given = false;
     for (int k = 0; k < 3; ++k) given |= d.domain_max[k] > d.domain_min[k];
+    auto acc = [&](const std::vector<double>& v) {
+        for (size_t i = 0; i + 2 < v.size(); i += 3)
+            for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], v[i + k]); hi[k] = std::max(hi[k], v[i + k]); }
+    };
     if (given) {
         for (int k = 0; k < 3; ++k) { lo[k] = d.domain_min[k]; hi[k] = d.domain_max[k]; }
+        if (cover_points) {
+            acc(hx);
+            acc(he);
+            if (akinci) acc(hb);
+        }
     } else {
         for (int k = 0; k < 3; ++k) { lo[k] = 1e300; hi[k] = -1e300; }
-        auto acc = [&](const std::vector<double>& v) {
-            for (size_t i = 0; i + 2 < v.size(); i += 3)
-                for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], v[i + k]); hi[k] = std::max(hi[k], v[i + k]); }
-        };
         acc(hx);
         acc(he);
         if (akinci) acc(hb);
@@ -201,6 +208,8 @@ public:
         if (st_) cudaStreamDestroy(st_);
         if (st2_) cudaStreamDestroy(st2_);
         if (h_sc_) cudaFreeHost(h_sc_);
+        if (h_esc_) cudaFreeHost(h_esc_);
+        if (esc_ev_) cudaEventDestroy(esc_ev_);
         for (auto& p : pending_) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
         for (auto e : events_) cudaEventDestroy(e);
         for (auto e : tev_) if (e) cudaEventDestroy(e);
@@ -221,10 +230,14 @@ public:
         SPH_CUDA(cudaStreamCreateWithFlags(&st2_, cudaStreamNonBlocking));
         ls_ = st_;
         SPH_CUDA(cudaMallocHost((void**)&h_sc_, sizeof(DevScalars)));
+        SPH_CUDA(cudaMallocHost((void**)&h_esc_, sizeof(unsigned)));
+        *h_esc_ = 0u;
+        SPH_CUDA(cudaEventCreateWithFlags(&esc_ev_, cudaEventDisableTiming));
         n0_ = (unsigned)(hx.size() / 3);
         akinci_ = d.boundary_method == SPH_BOUNDARY_AKINCI ? 1 : 0;
         bh_ = d.boundary_method == SPH_BOUNDARY_PCISPH ? 1 : 0;
         hasb_ = akinci_ || bh_;
+        if (bh_) grow_ = false;  // cell lifetimes are tied to the key space
         nb_ = hasb_ ? (unsigned)(hb.size() / 3) : 0u;
         // FluidModel::addEmitter FluidModel.cpp:124-143: every emitter's
         // particles get slots up front; emission only activates them
@@ -314,13 +327,111 @@ public:
         if (!inited) { fail("sph_ctx_init has not been called"); return SPH_ERR_INVALID; }
         for (int s = 0; s < nsteps; ++s) {
             int rc;
+            if (grow_ && esc_pending_ && cudaEventQuery(esc_ev_) == cudaSuccess) {
+                esc_pending_ = false;
+                if (*h_esc_) {
+                    rc = grow_grid();
+                    if (rc) return rc;
+                }
+            }
             if (graph_) {
                 rc = graph_step();
             } else {
                 rc = one_step();
             }
             if (rc) return rc;
+            // every kGrowthCheck steps, read the escape flag without waiting
+            if (grow_ && !esc_pending_ && ++since_check_ >= kGrowthCheck) {
+                since_check_ = 0;
+                SPH_CUDA(cudaMemcpyAsync(h_esc_, &sc_.p->escaped, sizeof(unsigned), cudaMemcpyDeviceToHost, st_));
+                SPH_CUDA(cudaEventRecord(esc_ev_, st_));
+                esc_pending_ = true;
+            }
         }
+        return SPH_OK;
+    }
+
+    int set_grid_growth(int on) override
+    {
+        grow_ = on != 0 && !bh_;
+        if (on && bh_) { fail("the grid box of the PCISPH boundary model does not grow"); return SPH_ERR_UNSUPPORTED; }
+        return SPH_OK;
+    }
+
+    // The reference hashes cells without bounds (HashTable.h:79-102); the
+    // dense box here grows instead.  Between steps: the box is re-planned
+    // around every point (fluid where it is now, boundary, emitters) with a
+    // 25 % margin on the same cell lattice, cells are shifted into it (a
+    // particle kept in a border cell is re-binned from its true offset), the
+    // static boundary is re-sorted and its volumes recomputed, the fluid is
+    // re-sorted and the DFSPH densities, alpha factors and lists rebuilt at
+    // the same positions (same values: sums run in the geometric walk order,
+    // which the box does not change), and the step graphs are re-captured.
+    // A box beyond the cell packing's limits stays as it is, and growth stops.
+    int grow_grid()
+    {
+        SPH_CUDA(cudaStreamSynchronize(st_));
+        const unsigned na = active();
+        std::vector<double> xs(3 * (size_t)na);
+        int rc = download(SPH_FIELD_POSITION, xs.data());
+        if (rc) return rc;
+        sph_scene_desc dd = d;
+        for (int k = 0; k < 3; ++k) dd.domain_min[k] = dd.domain_max[k] = 0.0;
+        GridPlan p;
+        std::string perr;
+        if (grid_plan(dd, xs, hb, hasb_ != 0, emitter_points(), hd_, &p, &perr, 0.25) != SPH_OK) {
+            grow_ = false;
+            return SPH_OK;
+        }
+        const int sx = gv_.ox - p.o[0], sy = gv_.oy - p.o[1], sz = gv_.oz - p.o[2];
+        // graph-run kernels so far, before the graphs go
+        SPH_CUDA(cudaMemcpy(h_sc_, sc_.p, sizeof(DevScalars), cudaMemcpyDeviceToHost));
+        if (graph_) graph_launches_ += graph_kernels();
+        snap_it_ = h_sc_->sumIterations;
+        snap_itv_ = h_sc_->sumIterationsV;
+        for (int k = 0; k < 2; ++k) {
+            if (gexec_[k]) cudaGraphExecDestroy(gexec_[k]);
+            gexec_[k] = nullptr;
+            gsteps_[k] = 0;
+            for (int q = 0; q < 3; ++q) gshape_[k][q] = 0;
+        }
+        rc = use_grid(p);
+        if (rc) return rc;
+        SPH_CUDA(count_.alloc(nkeys_)); SPH_CUDA(starts_.alloc(nkeys_ + 1)); SPH_CUDA(bstarts_.alloc(nkeys_ + 1));
+        SPH_CUDA(tile_sums_.alloc(blocks(nkeys_, kScanTile)));
+        SPH_CUDA(cudaMemsetAsync(count_.p, 0, nkeys_ * sizeof(uint32_t), st_));
+        Fluid<R> f = F();
+        k_shift_cells<<<blocks(n_, 256), 256, 0, st_>>>(n_, f.na, f.cell, sx, sy, sz);
+        k_cell_update<R, false, false><<<blocks(n_, 256), 256, 0, st_>>>(n_, f.pos, f.vel, f.cell, key_.p, slot_.p, count_.p,
+                                                                         gv_, c_.h, hd_, sc_.p, nullptr, nullptr, f.na);
+        SPH_CUDA(cudaGetLastError());
+        if (nb_) {
+            // boundary points kept in border cells (outside a given domain)
+            // are re-binned too; the weights in w are rewritten with psi below
+            k_shift_cells<<<blocks(nb_, 256), 256, 0, st_>>>(nb_, nullptr, B(1).cell, sx, sy, sz);
+            k_cell_update<R, false, false><<<blocks(nb_, 256), 256, 0, st_>>>(nb_, B(1).pos, B(1).pos, B(1).cell, key_.p,
+                                                                              slot_.p, count_.p, gv_, c_.h, hd_, sc_.p);
+            k_cell_count<<<blocks(nb_, 256), 256, 0, st_>>>(nb_, B(1).cell, key_.p, slot_.p, count_.p, gv_);
+            SPH_CUDA(cudaGetLastError());
+            rc = scan(bstarts_.p);
+            if (rc) return rc;
+            k_scatter<<<blocks(nb_, 256), 256, 0, st_>>>(nb_, key_.p, slot_.p, bstarts_.p, tmp_.p);
+            k_gather_boundary<R><<<blocks(nb_, 256), 256, 0, st_>>>(nb_, tmp_.p, key_.p, bstarts_.p, B(1), B(0));
+            std::swap(bd_[0], bd_[1]);
+            if (akinci_) k_boundary_psi<R><<<blocks(nb_, 128), 128, 0, st_>>>(B(1), gv_, bstarts_.p, c_);
+            SPH_CUDA(cudaGetLastError());
+        } else {
+            SPH_CUDA(cudaMemsetAsync(bstarts_.p, 0, (nkeys_ + 1) * sizeof(uint32_t), st_));
+        }
+        SPH_CUDA(cudaMemsetAsync(&sc_.p->escaped, 0, sizeof(unsigned), st_));
+        rc = build_grid(false);
+        if (rc) return rc;
+        if (d.simulation_method == SPH_DFSPH) {
+            rc = lists_ ? launch_build_lists() : launch_density(true, false);
+            if (rc) return rc;
+        }
+        SPH_CUDA(cudaStreamSynchronize(st_));
+        ++growths_;
         return SPH_OK;
     }
 
@@ -592,6 +703,7 @@ public:
         out->num_fluid = nem_ ? s.n_active : n_;
         out->num_fluid_total = n_;
         out->num_boundary = nb_;
+        out->grid_growths = growths_;
         return SPH_OK;
     }
 
@@ -695,10 +807,9 @@ private:
     }
 
     // Dense cell box over the domain with a margin; column-Morton key space.
-    int setup_grid()
+    // The emitters' groups where they are placed (rotated, translated).
+    std::vector<double> emitter_points() const
     {
-        GridPlan p;
-        // emitters' groups where they are placed (rotated, translated)
         std::vector<double> he;
         for (const EmitterSpec& e : hem)
             for (size_t k = 0; k + 2 < e.group.size(); k += 3) {
@@ -708,8 +819,21 @@ private:
                 const double uuv[3] = {q[2] * uv[2] - uv[1] * q[3], q[3] * uv[0] - uv[2] * q[1], q[1] * uv[1] - uv[0] * q[2]};
                 for (int c = 0; c < 3; ++c) he.push_back(v[c] + (uv[c] * q[0] + uuv[c]) * 2.0 + e.r[c]);
             }
-        const int rc = grid_plan(d, hx, hb, hasb_ != 0, he, hd_, &p, &err);
+        return he;
+    }
+
+    int setup_grid()
+    {
+        GridPlan p;
+        // a box that grows starts around every point (a given domain widened)
+        const int rc = grid_plan(d, hx, hb, hasb_ != 0, emitter_points(), hd_, &p, &err, 0.05, grow_);
         if (rc) return rc;
+        return use_grid(p);
+    }
+
+    // Installs a planned box: key count, Morton tables, the grid view.
+    int use_grid(const GridPlan& p)
+    {
         nkeys_ = (uint32_t)p.nkeys;
         SPH_CUDA(mortx_.alloc(p.nn[0]));
         SPH_CUDA(morty_.alloc(p.nn[1]));
@@ -1331,6 +1455,11 @@ private:
     cudaGraphExec_t gexec_[2] = {nullptr, nullptr};
     int loop_ctx_ = 0;
     unsigned cap_count_[3] = {0, 0, 0};
+    static constexpr unsigned kGrowthCheck = 16;
+    bool grow_ = true, esc_pending_ = false;
+    unsigned since_check_ = 0, growths_ = 0;
+    unsigned* h_esc_ = nullptr;
+    cudaEvent_t esc_ev_ = nullptr;
     unsigned gshape_[2][3] = {{0, 0, 0}, {0, 0, 0}};
     unsigned long long gsteps_[2] = {0, 0};
     unsigned long long launches_ = 0, graph_launches_ = 0, snap_it_ = 0, snap_itv_ = 0;

@@ -75,6 +75,7 @@ struct SceneBase {
     virtual int step_timed(int n, float* ms) = 0;
     virtual int sync() = 0;
     virtual int set_graph(int on) = 0;
+    virtual int set_grid_growth(int on) = 0;
     virtual int pause_emitters(int pause) = 0;
     virtual int download(int field, double* out) = 0;
     // Positions (absolute, FP64) and velocities of the active particles in

@@ -12,7 +12,8 @@ such a particle in FP32 (the half-precision cull needs in-cell offsets).
 
 Each case starts a jittered block that sticks out of a deliberately small
 grid box on every side and moves down through its floor, with no boundary,
-and compares with the oracle (whose hash grid has no bounds).  FP64: within
+and compares with the oracle (whose hash grid has no bounds), first with the
+box held fixed (sph_ctx_set_grid_growth(0)), then with the box growing.  FP64: within
 1e-5 relative with equal iteration counts.  FP32: leaving the grid box costs
 no accuracy, so the errors against the oracle stay within 1.5x those of the
 same FP32 run in a grid box that holds every particle (measured on GB300,
@@ -52,9 +53,10 @@ def _state():
     return x, v
 
 
-def _scene(params, precision, x, v, domain):
+def _scene(params, precision, x, v, domain, grow=False):
     s = sph_gb300.Scene(precision=precision, **params, **domain)
     s.set_fluid(x, v)
+    s.set_grid_growth(grow)
     s.init()
     return s
 
@@ -95,3 +97,53 @@ def test_particles_outside_the_grid_box_match_oracle(gpu_lib, name, precision):
     # its lowest layer is now more than h below the grid box's floor (0.08 m)
     assert s.get("x")[:, 1].min() < -0.01
     assert s.stats()["status"] & ~OUT_OF_GRID == 0
+    assert s.stats()["grid_growths"] == 0
+
+
+# A box that holds every particle of the growth test for all its steps, and
+# the steps each case needs to fall through the floor of its own starting box
+# (the domain widened to hold the block, plus two cells: y >= -0.16 m).
+BIG = dict(domain_min=(-0.5, -1.0, -0.5), domain_max=(1.3, 0.6, 1.3))
+GROW_STEPS = {"dfsph_open": 48, "wcsph_open": 120}
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+@pytest.mark.parametrize("name", list(CASES))
+def test_grid_box_grows_without_changing_results(gpu_lib, name, precision):
+    """The same open blocks with grid growth on (the default).  The box
+    starts around every point and grows after a periodic check (every 16
+    steps) sees a particle kept in a border cell.  FP64: every step equals
+    the run in a fixed box that holds all particles throughout (same cell
+    lattice, same walk order, absolute positions; only the particles' sorted
+    order differs) to 1e-9, and the oracle to 1e-5, with equal iteration
+    counts.  FP32: a particle kept in a border cell until the check computes
+    its pairs in another cell frame, so the two runs part at rounding level;
+    its errors against the oracle stay within 1.5x those of the fixed big box."""
+    params, _ = CASES[name]
+    x, v = _state()
+    o = oracle.OracleScene(params, x, v=v)
+    s = _scene(params, precision, x, v, DOMAIN, grow=True)
+    ref = _scene(params, precision, x, v, BIG)
+    assert s.stats()["status"] == 0 and ref.stats()["status"] == 0
+    err = np.zeros(3)
+    err_ref = np.zeros(3)
+    for step in range(GROW_STEPS[name]):
+        s.step(1)
+        ref.step(1)
+        o.step(1)
+        if precision == "f64":
+            for f in ("x", "v", "rho"):
+                e = relerr(s.get(f), ref.get(f))
+                assert e <= 1e-9, (name, step, f, e)
+                e = relerr(s.get(f), o.get(f))
+                assert e <= 1e-5, (name, step, f, e)
+            if params["method"] != 0:
+                assert s.stats()["iterations"] == int(o.scalar("iterations")), (name, step)
+        else:
+            err = np.maximum(err, _errors(s, o))
+            err_ref = np.maximum(err_ref, _errors(ref, o))
+    st = s.stats()
+    assert st["grid_growths"] >= 1 and st["status"] == OUT_OF_GRID, st
+    assert ref.stats()["status"] == 0 and ref.stats()["grid_growths"] == 0
+    if precision == "f32":
+        assert np.all(err <= 1.5 * err_ref + np.array([1e-7, 1e-6, 1e-5])), (name, err, err_ref)
