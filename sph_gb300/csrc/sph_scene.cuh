@@ -231,8 +231,7 @@ public:
             const unsigned long long want = (160000ull + n - 1) / n;
             G = want >= 8 ? 8 : want >= 4 ? 4 : want >= 2 ? 2 : 1;
         }
-        if (sizeof(R) == 8) G_ = 1;
-        else G_ = (G == 2 || G == 4 || G == 8) ? G : 1;
+        G_ = (G == 2 || G == 4 || G == 8) ? G : 1;
         SPH_CUDA(cudaGetDevice(&device_));
         SPH_CUDA(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
         SPH_CUDA(cudaStreamCreateWithFlags(&st2_, cudaStreamNonBlocking));
@@ -969,15 +968,11 @@ private:
 
     template <typename Fn> void withG(Fn&& fn)
     {
-        if constexpr (sizeof(R) == 8) {
-            fn(std::integral_constant<int, 1>{});
-        } else {
-            switch (G_) {
-                case 2: fn(std::integral_constant<int, 2>{}); break;
-                case 4: fn(std::integral_constant<int, 4>{}); break;
-                case 8: fn(std::integral_constant<int, 8>{}); break;
-                default: fn(std::integral_constant<int, 1>{}); break;
-            }
+        switch (G_) {
+            case 2: fn(std::integral_constant<int, 2>{}); break;
+            case 4: fn(std::integral_constant<int, 4>{}); break;
+            case 8: fn(std::integral_constant<int, 8>{}); break;
+            default: fn(std::integral_constant<int, 1>{}); break;
         }
     }
     unsigned wblocks() const { return blocks((size_t)n_ * G_, kBlock); }
