@@ -99,6 +99,7 @@ ALGO_BYTES = {
     "k_npforce": (68, True, 0),
     "k_pool_npforce": (68, True, 0),
     "k_st_normals": (36, False, 0),
+    "k_pool_st_normals": (36, False, 0),
 }
 
 

@@ -589,7 +589,25 @@ __global__ void __launch_bounds__(kBlock) k_wcsph_pressure_force(Fluid<R> f, con
     f.acc[i] = a;
 }
 
-// SurfaceTensionAkinci::step, normal pass SurfaceTensionAkinci.h:43-61
+// SurfaceTensionAkinci::step, normal pass SurfaceTensionAkinci.h:43-61: this
+// lane's part of particle i's sum (the caller adds the lanes and scales by h).
+template <typename R, int G>
+__device__ __forceinline__ V3<R> st_normal_sum(uint32_t i, int lane, const Fluid<R>& f, const GridView& g,
+                                               const uint32_t* __restrict__ cs, const Consts<R>& c)
+{
+    V3<R> ni = {0, 0, 0};
+    const V3<R> xi = xyz(f.pos[i]);
+    walk<R, G>(g, cs, f.cell[i], xi, c.h, lane, [&](uint32_t j, V3<R> s) {
+        const V3<R> r = s - xyz(ldg4(f.pos + j));
+        const R r2 = dot3(r, r);
+        if (r2 <= c.cull2) {
+            const R vol = c.mass / ldg4(f.vel + j).w;
+            ni = ni + vol * cubic_gradW(c, r, r2);
+        }
+    });
+    return ni;
+}
+
 template <typename R, int G>
 __global__ void __launch_bounds__(kBlock) k_st_normals(Fluid<R> f, GridView g, const uint32_t* __restrict__ cs, Consts<R> c)
 {
@@ -598,31 +616,118 @@ __global__ void __launch_bounds__(kBlock) k_st_normals(Fluid<R> f, GridView g, c
     const int lane = (int)(t % G);
     const bool valid = i < f.count();
     V3<R> ni = {0, 0, 0};
-    if (valid) {
-        const V3<R> xi = xyz(f.pos[i]);
-        walk<R, G>(g, cs, f.cell[i], xi, c.h, lane, [&](uint32_t j, V3<R> s) {
-            const V3<R> r = s - xyz(ldg4(f.pos + j));
-            const R r2 = dot3(r, r);
-            if (r2 <= c.cull2) {
-                const R vol = c.mass / ldg4(f.vel + j).w;
-                ni = ni + vol * cubic_gradW(c, r, r2);
-            }
-        });
-    }
+    if (valid) ni = st_normal_sum<R, G>(i, lane, f, g, cs, c);
     if (G > 1) ni = group_sum3<G>(ni);
     if (!valid || lane != 0) return;
     ni = ni * ((R)1 * c.h);
     f.normal[i] = P4<R>{ni.x, ni.y, ni.z, 0};
 }
 
-// Non-pressure forces in one walk, each accumulated separately and added in
-// the reference's plugin order (viscosity, surface tension, adhesion;
-// Simulation::computeNonPressureForces Simulation.cpp:313-323):
+// This lane's parts of particle i's non-pressure forces, each accumulated
+// separately (av fluid viscosity, avb boundary viscosity, ast surface
+// tension, aad adhesion) over one fluid and one boundary walk:
 //   XSPHViscosity::step XSPHViscosity.h:32-69
 //   StandardViscosityForce::step StandardViscosityForce.h:29-79
 //   ArtificialViscosity::step ArtificialViscosity.h:31-83
 //   SurfaceTensionAkinci::step (cohesion + curvature) SurfaceTensionAkinci.h:64-97
 //   AdhesionForce::step AdhesionForce.h:30-62
+template <typename R> struct NPForces {
+    V3<R> av, avb, ast, aad;
+};
+
+template <typename R, int G>
+__device__ __forceinline__ NPForces<R> npforce_sums(uint32_t i, int lane, const Fluid<R>& f,
+                                                    const P4<R>* __restrict__ bpos, const GridView& g,
+                                                    const uint32_t* __restrict__ cs, const uint32_t* __restrict__ bs,
+                                                    const Consts<R>& c, int akinci, R dt)
+{
+    const int fl = c.force_flags;
+    V3<R> av = {0, 0, 0}, avb = {0, 0, 0}, ast = {0, 0, 0}, aad = {0, 0, 0};
+    const V3<R> xi = xyz(f.pos[i]);
+    const P4<R> vi4 = f.vel[i];
+    const V3<R> vi = xyz(vi4);
+    const R rho_i = vi4.w;
+    V3<R> ni = {0, 0, 0};
+    if (fl & F_SURFACE_TENSION) ni = xyz(f.normal[i]);
+    const uint32_t pc = f.cell[i];
+    const R h2 = c.h * c.h;
+    if (fl & (F_XSPH | F_STD_VISC | F_ART_VISC | F_SURFACE_TENSION))
+        walk<R, G>(g, cs, pc, xi, c.h, lane, [&](uint32_t j, V3<R> s) {
+            const V3<R> r = s - xyz(ldg4(f.pos + j));
+            const R r2 = dot3(r, r);
+            if (!(r2 <= c.cull2)) return;
+            const P4<R> vj4 = ldg4(f.vel + j);
+            const V3<R> vj = xyz(vj4);
+            const R rho_j = vj4.w;
+            const R rl = sqrt(r2);
+            if (fl & F_XSPH)
+                av = av + (((c.visc * (c.mass / rho_j)) * (vj - vi)) * cubic_W(c, rl)) / dt;
+            if (fl & F_STD_VISC)
+                av = av + ((c.mass * (vj - vi)) / rho_j) * visc_laplW(c, r2);
+            if (fl & F_ART_VISC) {
+                const R dotProd = dot3(vi - vj, r);
+                const R sqDist = rl * rl;
+                const R kij = (R)2 * c.density0 / (rho_i + rho_j);
+                av = av + (kij * (R)10 * (R)0.1 * c.visc * (c.mass / rho_j) * dotProd / (sqDist + (R)0.01 * h2)) *
+                              cubic_gradW(c, r, r2);
+            }
+            if (fl & F_SURFACE_TENSION) {
+                if (rl > (R)0 && rl <= c.h) {
+                    const V3<R> nj = xyz(ldg4(f.normal + j));
+                    const R kij = (R)2 * c.density0 / (rho_i + rho_j);
+                    const V3<R> coh = ((-c.mass * cohesion_W(c, rl)) * r) / rl;
+                    const V3<R> curv = (R)-1 * (ni - nj);
+                    ast = ast + (c.st * kij) * (coh + curv);
+                }
+            }
+        });
+    const bool bvisc = (fl & F_BVISC) && akinci;
+    if ((fl & F_ADHESION) || bvisc)
+        walk<R, G>(g, bs, pc, xi, c.h, lane, [&](uint32_t j, V3<R> s) {
+            const P4<R> pb = ldg4(bpos + j);
+            const V3<R> r = s - xyz(pb);
+            const R r2 = dot3(r, r);
+            if (!(r2 <= c.cull2)) return;
+            const R rl = sqrt(r2);
+            if (bvisc) {
+                if (fl & F_XSPH)
+                    avb = avb + (((c.bvisc * (pb.w / rho_i)) * (-vi)) * cubic_W(c, rl)) / dt;
+                if (fl & F_STD_VISC)
+                    avb = avb + ((pb.w * (-vi)) / rho_i) * visc_laplW(c, r2);
+                if (fl & F_ART_VISC) {
+                    const R dotProd = dot3(vi, r);
+                    const R sqDist = rl * rl;
+                    avb = avb + ((R)10 * (R)0.1 * c.bvisc * (pb.w / rho_i) * dotProd / (sqDist + (R)0.01 * h2)) *
+                                    cubic_gradW(c, r, r2);
+                }
+            }
+            if ((fl & F_ADHESION) && rl > (R)0)
+                aad = aad - ((c.adh * pb.w * adhesion_W(c, rl)) * r) / rl;
+        });
+    return NPForces<R>{av, avb, ast, aad};
+}
+
+// The forces added to particle i's acceleration in the reference's plugin
+// order (viscosity, surface tension, adhesion;
+// Simulation::computeNonPressureForces Simulation.cpp:313-323).
+template <typename R>
+__device__ __forceinline__ void npforce_apply(uint32_t i, const Fluid<R>& f, const Consts<R>& c, NPForces<R> s)
+{
+    if (c.force_flags & F_STD_VISC) {
+        // viscoForce *= visc / density0 (separately for the boundary sum)
+        s.av = s.av * (c.visc / c.density0);
+        s.avb = s.avb * (c.bvisc / c.density0);
+    }
+    P4<R> a = f.acc[i];
+    V3<R> tot = {a.x, a.y, a.z};
+    tot = tot + s.av;
+    tot = tot + s.avb;
+    tot = tot + s.ast;
+    tot = tot + s.aad;
+    f.acc[i] = P4<R>{tot.x, tot.y, tot.z, 0};
+}
+
+// Non-pressure forces in one walk (npforce_sums), lanes added, then applied.
 template <typename R, int G>
 __global__ void __launch_bounds__(kBlock) k_npforce(Fluid<R> f, const P4<R>* __restrict__ bpos, GridView g,
                                                     const uint32_t* __restrict__ cs, const uint32_t* __restrict__ bs,
@@ -632,88 +737,13 @@ __global__ void __launch_bounds__(kBlock) k_npforce(Fluid<R> f, const P4<R>* __r
     const uint32_t i = t / G;
     const int lane = (int)(t % G);
     const bool valid = i < f.count();
-    const int fl = c.force_flags;
-    V3<R> av = {0, 0, 0}, avb = {0, 0, 0}, ast = {0, 0, 0}, aad = {0, 0, 0};
-    if (valid) {
-        const R dt = (R)scr->dt;
-        const V3<R> xi = xyz(f.pos[i]);
-        const P4<R> vi4 = f.vel[i];
-        const V3<R> vi = xyz(vi4);
-        const R rho_i = vi4.w;
-        V3<R> ni = {0, 0, 0};
-        if (fl & F_SURFACE_TENSION) ni = xyz(f.normal[i]);
-        const uint32_t pc = f.cell[i];
-        const R h2 = c.h * c.h;
-        if (fl & (F_XSPH | F_STD_VISC | F_ART_VISC | F_SURFACE_TENSION))
-            walk<R, G>(g, cs, pc, xi, c.h, lane, [&](uint32_t j, V3<R> s) {
-                const V3<R> r = s - xyz(ldg4(f.pos + j));
-                const R r2 = dot3(r, r);
-                if (!(r2 <= c.cull2)) return;
-                const P4<R> vj4 = ldg4(f.vel + j);
-                const V3<R> vj = xyz(vj4);
-                const R rho_j = vj4.w;
-                const R rl = sqrt(r2);
-                if (fl & F_XSPH)
-                    av = av + (((c.visc * (c.mass / rho_j)) * (vj - vi)) * cubic_W(c, rl)) / dt;
-                if (fl & F_STD_VISC)
-                    av = av + ((c.mass * (vj - vi)) / rho_j) * visc_laplW(c, r2);
-                if (fl & F_ART_VISC) {
-                    const R dotProd = dot3(vi - vj, r);
-                    const R sqDist = rl * rl;
-                    const R kij = (R)2 * c.density0 / (rho_i + rho_j);
-                    av = av + (kij * (R)10 * (R)0.1 * c.visc * (c.mass / rho_j) * dotProd / (sqDist + (R)0.01 * h2)) *
-                                  cubic_gradW(c, r, r2);
-                }
-                if (fl & F_SURFACE_TENSION) {
-                    if (rl > (R)0 && rl <= c.h) {
-                        const V3<R> nj = xyz(ldg4(f.normal + j));
-                        const R kij = (R)2 * c.density0 / (rho_i + rho_j);
-                        const V3<R> coh = ((-c.mass * cohesion_W(c, rl)) * r) / rl;
-                        const V3<R> curv = (R)-1 * (ni - nj);
-                        ast = ast + (c.st * kij) * (coh + curv);
-                    }
-                }
-            });
-        const bool bvisc = (fl & F_BVISC) && akinci;
-        if ((fl & F_ADHESION) || bvisc)
-            walk<R, G>(g, bs, pc, xi, c.h, lane, [&](uint32_t j, V3<R> s) {
-                const P4<R> pb = ldg4(bpos + j);
-                const V3<R> r = s - xyz(pb);
-                const R r2 = dot3(r, r);
-                if (!(r2 <= c.cull2)) return;
-                const R rl = sqrt(r2);
-                if (bvisc) {
-                    if (fl & F_XSPH)
-                        avb = avb + (((c.bvisc * (pb.w / rho_i)) * (-vi)) * cubic_W(c, rl)) / dt;
-                    if (fl & F_STD_VISC)
-                        avb = avb + ((pb.w * (-vi)) / rho_i) * visc_laplW(c, r2);
-                    if (fl & F_ART_VISC) {
-                        const R dotProd = dot3(vi, r);
-                        const R sqDist = rl * rl;
-                        avb = avb + ((R)10 * (R)0.1 * c.bvisc * (pb.w / rho_i) * dotProd / (sqDist + (R)0.01 * h2)) *
-                                        cubic_gradW(c, r, r2);
-                    }
-                }
-                if ((fl & F_ADHESION) && rl > (R)0)
-                    aad = aad - ((c.adh * pb.w * adhesion_W(c, rl)) * r) / rl;
-            });
-    }
+    NPForces<R> s = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    if (valid) s = npforce_sums<R, G>(i, lane, f, bpos, g, cs, bs, c, akinci, (R)scr->dt);
     if (G > 1) {
-        av = group_sum3<G>(av); avb = group_sum3<G>(avb); ast = group_sum3<G>(ast); aad = group_sum3<G>(aad);
+        s.av = group_sum3<G>(s.av); s.avb = group_sum3<G>(s.avb); s.ast = group_sum3<G>(s.ast); s.aad = group_sum3<G>(s.aad);
     }
     if (!valid || lane != 0) return;
-    if (fl & F_STD_VISC) {
-        // viscoForce *= visc / density0 (separately for the boundary sum)
-        av = av * (c.visc / c.density0);
-        avb = avb * (c.bvisc / c.density0);
-    }
-    P4<R> a = f.acc[i];
-    V3<R> tot = {a.x, a.y, a.z};
-    tot = tot + av;
-    tot = tot + avb;
-    tot = tot + ast;
-    tot = tot + aad;
-    f.acc[i] = P4<R>{tot.x, tot.y, tot.z, 0};
+    npforce_apply(i, f, c, s);
 }
 
 // ===========================================================================

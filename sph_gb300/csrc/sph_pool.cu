@@ -223,8 +223,24 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_pool_build_lists(Fluid<float> f
                                  qdepth);
 }
 
-// Non-pressure forces of the scene (XSPH / standard / artificial viscosity;
-// k_npforce's arithmetic) over the cell walk.
+constexpr int kPoolForces = F_XSPH | F_STD_VISC | F_ART_VISC | F_SURFACE_TENSION | F_ADHESION;
+
+// Surface normals of the scene's particles (SurfaceTensionAkinci.h:43-61)
+// for the scenes with Akinci surface tension.
+__global__ void __launch_bounds__(kBlock) k_pool_st_normals(Fluid<float> f, const uint32_t* __restrict__ sid,
+                                                            const PoolScene* T, const uint32_t* __restrict__ cs)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= f.n) return;
+    const PoolScene& sd = T[sid[i]];
+    if (!sd.running || !(sd.c.force_flags & F_SURFACE_TENSION)) return;
+    V3<float> ni = st_normal_sum<float, 1>(i, 0, f, sd.g, cs + sd.key_base, sd.c);
+    ni = ni * (1.f * sd.c.h);
+    f.normal[i] = P4<float>{ni.x, ni.y, ni.z, 0};
+}
+
+// Non-pressure forces of the scene (viscosity, surface tension, adhesion:
+// k_npforce's walk and arithmetic, one lane per particle).
 __global__ void __launch_bounds__(kBlock) k_pool_npforce(Fluid<float> f, const P4<float>* __restrict__ bpos,
                                                          const uint32_t* __restrict__ sid, const PoolScene* T,
                                                          const uint32_t* __restrict__ cs, const uint32_t* __restrict__ bs)
@@ -233,50 +249,10 @@ __global__ void __launch_bounds__(kBlock) k_pool_npforce(Fluid<float> f, const P
     if (i >= f.n) return;
     const PoolScene& sd = T[sid[i]];
     const Consts<float>& c = sd.c;
-    const int fl = c.force_flags;
-    if (!sd.running || !(fl & (F_XSPH | F_STD_VISC | F_ART_VISC))) return;
-    const float dt = (float)sd.s.dt;
-    const V3<float> xi = xyz(f.pos[i]);
-    const P4<float> vi4 = f.vel[i];
-    const V3<float> vi = xyz(vi4);
-    const float rho_i = vi4.w;
-    const uint32_t pc = f.cell[i];
-    const float h2 = c.h * c.h;
-    V3<float> av = {0, 0, 0}, avb = {0, 0, 0};
-    walk<float, 1>(sd.g, cs + sd.key_base, pc, xi, c.h, 0, [&](uint32_t j, V3<float> s) {
-        const V3<float> r = s - xyz(ldg4(f.pos + j));
-        const float r2 = dot3(r, r);
-        if (!(r2 <= c.cull2)) return;
-        const P4<float> vj4 = ldg4(f.vel + j);
-        const V3<float> vj = xyz(vj4);
-        const float rho_j = vj4.w;
-        const float rl = sqrtf(r2);
-        if (fl & F_XSPH) av = av + (((c.visc * (c.mass / rho_j)) * (vj - vi)) * cubic_W(c, rl)) / dt;
-        if (fl & F_STD_VISC) av = av + ((c.mass * (vj - vi)) / rho_j) * visc_laplW(c, r2);
-        if (fl & F_ART_VISC) {
-            const float kij = 2.f * c.density0 / (rho_i + rho_j);
-            av = av + (kij * 10.f * 0.1f * c.visc * (c.mass / rho_j) * dot3(vi - vj, r) / (rl * rl + 0.01f * h2)) *
-                          cubic_gradW(c, r, r2);
-        }
-    });
-    if ((fl & F_BVISC) && sd.akinci)
-        walk<float, 1>(sd.g, bs + sd.key_base, pc, xi, c.h, 0, [&](uint32_t j, V3<float> s) {
-            const P4<float> pb = ldg4(bpos + j);
-            const V3<float> r = s - xyz(pb);
-            const float r2 = dot3(r, r);
-            if (!(r2 <= c.cull2)) return;
-            const float rl = sqrtf(r2);
-            if (fl & F_XSPH) avb = avb + (((c.bvisc * (pb.w / rho_i)) * (-vi)) * cubic_W(c, rl)) / dt;
-            if (fl & F_STD_VISC) avb = avb + ((pb.w * (-vi)) / rho_i) * visc_laplW(c, r2);
-            if (fl & F_ART_VISC)
-                avb = avb + (10.f * 0.1f * c.bvisc * (pb.w / rho_i) * dot3(vi, r) / (rl * rl + 0.01f * h2)) *
-                                cubic_gradW(c, r, r2);
-        });
-    if (fl & F_STD_VISC) { av = av * (c.visc / c.density0); avb = avb * (c.bvisc / c.density0); }
-    P4<float> a = f.acc[i];
-    a.x += av.x; a.y += av.y; a.z += av.z;
-    a.x += avb.x; a.y += avb.y; a.z += avb.z;
-    f.acc[i] = a;
+    if (!sd.running || !(c.force_flags & kPoolForces)) return;
+    const NPForces<float> s = npforce_sums<float, 1>(i, 0, f, bpos, sd.g, cs + sd.key_base, bs + sd.key_base, c,
+                                                     sd.akinci, (float)sd.s.dt);
+    npforce_apply(i, f, c, s);
 }
 
 // DFSPHSolver::updateTimeStep per scene: max of sqrt(|v + (a + g) dt|).
@@ -543,7 +519,7 @@ public:
         }
         SPH_CUDA(acc_.alloc(P)); SPH_CUDA(rho_.alloc(P)); SPH_CUDA(alpha_.alloc(P)); SPH_CUDA(div_.alloc(P));
         SPH_CUDA(press_.alloc(P)); SPH_CUDA(kbuf_.alloc(P)); SPH_CUDA(sid_.alloc(P)); SPH_CUDA(bsid_.alloc(B));
-        SPH_CUDA(bpsi_.alloc(B)); SPH_CUDA(dummy4_.alloc(1));
+        SPH_CUDA(bpsi_.alloc(B)); SPH_CUDA(dummy4_.alloc(1)); SPH_CUDA(normal_.alloc(P));
         SPH_CUDA(pairs_.alloc(P * kmax_)); SPH_CUDA(lcount_.alloc(P)); SPH_CUDA(bgrad_.alloc(P));
         SPH_CUDA(posh_.alloc(P / 2 + 1));  // particle pairs, the last one whole
         SPH_CUDA(cudaMemsetAsync(posh_.p, 0, (P / 2 + 1) * sizeof(uint4), st_));
@@ -573,8 +549,6 @@ public:
             fail("the pool runs DFSPH scenes with Akinci boundaries");
             return SPH_ERR_UNSUPPORTED;
         }
-        if (d.surface_tension_method > -1 && d.surface_tension != 0.0) { fail("surface tension is not pooled"); return SPH_ERR_UNSUPPORTED; }
-        if (d.adhesion_method > -1 && d.adhesion != 0.0) { fail("adhesion is not pooled"); return SPH_ERR_UNSUPPORTED; }
         if (n == 0 || !x) { fail("no fluid particles"); return SPH_ERR_INVALID; }
         PoolEntry e;
         e.d = d;
@@ -1068,7 +1042,7 @@ private:
         f.pos = pos_[k].p; f.vel = vel_[k].p; f.kappa = kappa_[k].p; f.kappav = kappav_[k].p; f.pred = pred_[k].p;
         f.cell = cell_[k].p; f.id = id_[k].p;
         f.acc = acc_.p; f.xk = dummy4_.p; f.predR = dummy4_.p; f.predV = dummy4_.p; f.pacc = dummy4_.p;
-        f.normal = dummy4_.p; f.rho = rho_.p; f.alpha = alpha_.p; f.div = div_.p; f.press = press_.p;
+        f.normal = normal_.p; f.rho = rho_.p; f.alpha = alpha_.p; f.div = div_.p; f.press = press_.p;
         f.n = N_;
         return f;
     }
@@ -1287,10 +1261,11 @@ private:
         // drop removed entries; the resident order is the layout order
         entries_.remove_if([](const PoolEntry& e) { return e.removed; });
         order_ = order;
-        any_forces_ = false;
+        any_forces_ = any_st_ = false;
         for (uint32_t s = 0; s < S_; ++s) {
             order_[s]->t = tab[s];
-            any_forces_ |= (tab[s].c.force_flags & (F_XSPH | F_STD_VISC | F_ART_VISC)) != 0;
+            any_forces_ |= (tab[s].c.force_flags & kPoolForces) != 0;
+            any_st_ |= (tab[s].c.force_flags & F_SURFACE_TENSION) != 0;
         }
         // scene ids of fluid and boundary particles
         std::vector<uint32_t> pbv(pb.begin(), pb.end()), bbv(bb.begin(), bb.end());
@@ -1403,6 +1378,8 @@ private:
             Fluid<float> f = F(cur_);
             const P4<float>* bp = bpos_[bcur_].p;
             Lists<float> L = LS();
+            if (any_st_)
+                run("k_pool_st_normals", [&] { k_pool_st_normals<<<nb, kBlock, 0, ls_>>>(f, sid_.p, table_.p, starts_.p); });
             if (any_forces_)
                 run("k_pool_npforce", [&] { k_pool_npforce<<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p); });
             run("k_pool_cfl_accum", [&] { k_pool_cfl_accum<<<nb256, 256, 0, ls_>>>(f, sid_.p, table_.p); });
@@ -1521,7 +1498,7 @@ private:
     unsigned cap_[3] = {0, 0, 0};
     unsigned long long fixed_ = 0, body_d_size_ = 0, body_v_size_ = 0, gsteps_ = 0, snap_d_ = 0, snap_v_ = 0;
     unsigned long long host_launches_ = 0, graph_launches_ = 0, host_body_d_ = 0, host_body_v_ = 0;
-    bool counting_ = true, any_forces_ = false, prof_ = false, tuning_ = false;
+    bool counting_ = true, any_forces_ = false, any_st_ = false, prof_ = false, tuning_ = false;
     Tune tune_;
     int tune_mode_ = 1, tune_source_ = 0, tune_left_ = 0, tune_step_ = 0;
     unsigned long long tune_bucket_ = 0;
@@ -1539,7 +1516,7 @@ private:
     DevBuf<P4<float>> pos_[2], vel_[2], bpos_[2];
     DevBuf<float> kappa_[2], kappav_[2], pred_[2];
     DevBuf<uint32_t> cell_[2], id_[2], bcell_[2], bid_[2];
-    DevBuf<P4<float>> acc_, dummy4_, pairs_, bgrad_;
+    DevBuf<P4<float>> acc_, dummy4_, pairs_, bgrad_, normal_;
     DevBuf<uint4> posh_;  // half-precision positions for the build's cull (particle pairs)
     DevBuf<uint8_t> run_;   // per scene: running (poll)
     uint8_t* h_run_ = nullptr;
@@ -1579,11 +1556,12 @@ int sph_pool_desc_from_budget(unsigned long long hbm_bytes, int neighbor_list_ma
 {
     if (!out || hbm_bytes < (1ull << 20)) return SPH_ERR_INVALID;
     const unsigned long long kmax = neighbor_list_max > 0 ? (unsigned long long)neighbor_list_max : 64ull;
-    // bytes per fluid particle (double-buffered carried state, shared fields,
-    // sort scratch, pair-list slots), per boundary particle and per grid key,
-    // with one boundary particle and sixteen keys budgeted per fluid particle
-    const unsigned long long per_p = 2 * (16 + 16 + 4 + 4 + 4 + 4 + 4) + (16 + 4 + 4 + 4 + 4 + 4 + 4 + 4 + 16) +
-                                     3 * 4 + kmax * 16;
+    // bytes per fluid particle (double-buffered carried state, shared fields
+    // with the half-precision positions and the surface normals, sort
+    // scratch, pair-list slots), per boundary particle and per grid key, with
+    // one boundary particle and sixteen keys budgeted per fluid particle
+    const unsigned long long per_p = 2 * (16 + 16 + 4 + 4 + 4 + 4 + 4) +
+                                     (16 + 4 + 4 + 4 + 4 + 4 + 4 + 4 + 16 + 8 + 16) + 3 * 4 + kmax * 16;
     const unsigned long long per_b = 2 * (16 + 4 + 4) + 4 + 4;
     const unsigned long long per_k = 3 * 4;
     const unsigned long long unit = per_p + per_b + 16 * per_k;
