@@ -153,3 +153,22 @@ def test_mesh_sampler_rejects_bad_files(L, tmp_path):
     with pytest.raises(sph_gb300.SPHError, match="Akinci"):
         s.add_boundary_mesh(os.path.join(MESH_DIR, "ramp.obj"), 0.02)
     s.close()
+
+
+def test_pool_capacity_from_an_hbm_budget(L):
+    """sph_pool_desc_from_budget (host arithmetic only): one boundary particle
+    and sixteen grid keys per fluid particle, about 1.5 KB per fluid particle
+    at 64 pair-list slots, linear in the budget; budgets under 1 MiB are
+    refused."""
+    d = sph_gb300.PoolDesc()
+    assert L.sph_pool_desc_from_budget(80 * 10**9, 64, ctypes.byref(d)) == 0
+    assert d.max_boundary == d.max_particles and d.max_keys == 16 * d.max_particles
+    assert d.neighbor_list_max == 64
+    assert 1400 <= 80 * 10**9 / d.max_particles <= 1600
+    d2 = sph_gb300.PoolDesc()
+    assert L.sph_pool_desc_from_budget(160 * 10**9, 64, ctypes.byref(d2)) == 0
+    assert abs(d2.max_particles - 2 * d.max_particles) <= 1
+    d3 = sph_gb300.PoolDesc()
+    assert L.sph_pool_desc_from_budget(80 * 10**9, 32, ctypes.byref(d3)) == 0
+    assert d3.max_particles > d.max_particles          # fewer slots, more particles
+    assert L.sph_pool_desc_from_budget(1000, 64, ctypes.byref(d3)) == -1
