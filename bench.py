@@ -82,7 +82,8 @@ ALGO_BYTES = {
     "k_gather_fluid": (108, False, 0),
     "k_density": (28, True, 0),
     "k_build_lists": (28, True, 16),
-    "k_pool_build_lists": (28, True, 16),
+    # fused with the divergence solve's first error pass: + v 16, div 4
+    "k_pool_build_lists": (48, True, 16),
     "k_dfsph_cfl": (32, False, 0),
     "k_pool_cfl_accum": (32, False, 0),
     "k_dfsph_predict_v_warm": (76, False, 0),

@@ -184,12 +184,25 @@ __device__ __noinline__ BuildSums<R> build_walk_all(uint32_t i, const Fluid<R>& 
     return b;
 }
 
-template <typename R, bool FAST = false>
+// Forward declarations: the list build's DIV0 form ends with the velocity
+// divergence the first divergence-error pass would compute from the lists.
+template <typename R> struct DivSum;
+template <typename R>
+__device__ __noinline__ DivSum<R> velocity_div_cells(const Fluid<R>& f, const P4<R>* __restrict__ bpos, const GridView& g,
+                                                     const uint32_t* __restrict__ cs, const uint32_t* __restrict__ bs,
+                                                     const Consts<R>& c, int akinci, uint32_t i, V3<R> vi);
+
+// DIV0: also sum m (v_i - v_j) . gradW_ij over the pairs as they are listed,
+// plus v_i . (boundary gradient): the value velocity_div_one would read from
+// the finished lists (same terms, same order), into *div0, with the count of
+// neighbours into *nn0 (a particle whose list or queue overflowed takes the
+// same list or cell walk as velocity_div_one).
+template <typename R, bool FAST = false, bool DIV0 = false>
 __device__ __forceinline__ void build_lists_one(uint32_t i, const Fluid<R>& f, const P4<R>* __restrict__ bpos,
                                                 const GridView& g, const uint32_t* __restrict__ cs,
                                                 const uint32_t* __restrict__ bs, const Consts<R>& c, int akinci,
                                                 const Lists<R>& L, uint32_t* q, uint32_t qstride = kBlock,
-                                                uint32_t qdepth = kQueue)
+                                                uint32_t qdepth = kQueue, R* div0 = nullptr, uint32_t* nn0 = nullptr)
 {
     const uint32_t n = f.n;
     const V3<R> xi = xyz(f.pos[i]);
@@ -198,7 +211,11 @@ __device__ __forceinline__ void build_lists_one(uint32_t i, const Fluid<R>& f, c
     R density = 0, sumSq = 0;
     V3<R> sumGrad = {0, 0, 0};
     uint32_t cnt = 0;
-    auto accept = [&](uint32_t j, V3<R> r, R r2) {
+    V3<R> vi = {0, 0, 0};
+    if constexpr (DIV0) vi = xyz(f.vel[i]);
+    R dv = 0;
+    // vj: the neighbour's velocity (DIV0), loaded beside its position
+    auto accept = [&](uint32_t j, V3<R> r, R r2, V3<R> vj) {
         R w;
         V3<R> gw;
         cubic_W_gradW<FAST>(c, r, r2, &w, &gw);
@@ -215,6 +232,7 @@ __device__ __forceinline__ void build_lists_one(uint32_t i, const Fluid<R>& f, c
             }
             if (cnt < L.kmax) L.pairs[(size_t)cnt * n + i] = P4<R>{mg.x, mg.y, mg.z, idx_as(R(0), j)};
             ++cnt;
+            if constexpr (DIV0) dv += dot3(vi - vj, mg);
         }
     };
     // phase 1: cull.  The half-precision cull needs all 27 cells inside the
@@ -242,8 +260,11 @@ __device__ __forceinline__ void build_lists_one(uint32_t i, const Fluid<R>& f, c
         // phase 2: evaluate the queued candidates in walk order
         for (uint32_t k = 0; k < nq; ++k) {
             const uint32_t j = q[k * qstride + threadIdx.x];
+            // (a plain load for the velocity: other threads write its w here)
+            V3<R> vj = {0, 0, 0};
+            if constexpr (DIV0) vj = xyz(f.vel[j]);
             const V3<R> r = pair_vec(xi, pc, ldg4(f.pos + j), __ldg(f.cell + j), c.h);
-            accept(j, r, dot3(r, r));
+            accept(j, r, dot3(r, r), vj);
         }
     } else {
         const BuildSums<R> b = build_walk_all<R, FAST>(i, f, g, cs, c, L, xi, pc);
@@ -278,6 +299,26 @@ __device__ __forceinline__ void build_lists_one(uint32_t i, const Fluid<R>& f, c
     f.alpha[i] = (fabs(den) > c.eps) ? density / den : (R)0;
     L.count[i] = cnt;
     L.bgrad[i] = P4<R>{bg.x, bg.y, bg.z, 0};
+    if constexpr (DIV0) {
+        if (cnt > L.kmax) {
+            const DivSum<R> d = velocity_div_cells(f, bpos, g, cs, bs, c, akinci, i, vi);
+            *div0 = d.dv;
+            *nn0 = d.nn;
+        } else {
+            if (nq > qcap) {
+                // the list this thread just wrote, re-read as velocity_div_list
+                // reads it (plain loads: it was written in this kernel)
+                dv = 0;
+                for (uint32_t k = 0; k < cnt; ++k) {
+                    const P4<R> pr = L.pairs[(size_t)k * n + i];
+                    dv += dot3(vi - xyz(f.vel[as_idx(pr.w)]), xyz(pr));
+                }
+            }
+            if (akinci) dv += dot3(vi, bg);
+            *div0 = dv;
+            *nn0 = cnt;
+        }
+    }
 }
 
 template <typename R>

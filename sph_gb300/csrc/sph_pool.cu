@@ -207,20 +207,45 @@ __global__ void k_pool_psi(uint32_t N, Boundary<float> b, const uint32_t* __rest
 // queue of qdepth entries per thread (dynamic shared memory, qdepth * BLOCK
 // * 4 bytes) are tuning parameters; the lists do not depend on them (queued
 // and re-walked candidates are accepted in the same walk order).
-template <int BLOCK, int MINB>
+template <int BLOCK, int MINB, bool DIV0>
 __global__ void __launch_bounds__(BLOCK, MINB) k_pool_build_lists(Fluid<float> f, const P4<float>* __restrict__ bpos,
-                                                                         const uint32_t* __restrict__ sid, const PoolScene* T,
+                                                                         const uint32_t* __restrict__ sid, PoolScene* T,
                                                                          const uint32_t* __restrict__ cs,
                                                                          const uint32_t* __restrict__ bs, Lists<float> L,
                                                                          uint32_t qdepth)
 {
     extern __shared__ uint32_t q[];
     const uint32_t i = blockIdx.x * BLOCK + threadIdx.x;
-    if (i >= f.n) return;
-    const PoolScene& sd = T[sid[i]];
-    if (!sd.running) return;
-    build_lists_one<float, true>(i, f, bpos, sd.g, cs + sd.key_base, bs + sd.key_base, sd.c, sd.akinci, L, q, (uint32_t)BLOCK,
-                                 qdepth);
+    uint32_t s = ~0u;
+    unsigned long long contrib = 0ull;
+    if (i < f.n) {
+        const uint32_t k = sid[i];
+        PoolScene& sd = T[k];
+        if (sd.running) {
+            float d = 0.f;
+            uint32_t nn = 0;
+            build_lists_one<float, true, DIV0>(i, f, bpos, sd.g, cs + sd.key_base, bs + sd.key_base, sd.c, sd.akinci, L,
+                                               q, (uint32_t)BLOCK, qdepth, &d, &nn);
+            if constexpr (DIV0) {
+                // the divergence solve's first error pass (k_pool_errors<true,
+                // true>'s arithmetic) from the sum the build just formed
+                const Consts<float>& c = sd.c;
+                const float dt = (float)sd.s.dt;
+                const float inv0 = 1.f / c.density0;
+                d = nn < 20u ? 0.f : (d < 0.f ? 0.f : d);
+                f.div[i] = d;
+                L.kbuf[i] = d * f.alpha[i] / (dt * f.rho[i]);
+                const float e = d * inv0;
+                if (e == e && e < 1e9f) {
+                    contrib = to_fixed((double)e);
+                } else {
+                    atomicOr(&sd.s.status, (unsigned)ST_NONFINITE);
+                }
+                s = k;
+            }
+        }
+    }
+    if constexpr (DIV0) seg_add(s, contrib, T);
 }
 
 constexpr int kPoolForces = F_XSPH | F_STD_VISC | F_ART_VISC | F_SURFACE_TENSION | F_ADHESION;
@@ -527,9 +552,13 @@ public:
         SPH_CUDA(key_.alloc(M)); SPH_CUDA(slot_.alloc(M)); SPH_CUDA(tmp_.alloc(M));
         SPH_CUDA(count_.alloc(K)); SPH_CUDA(starts_.alloc(K + 1)); SPH_CUDA(bstarts_.alloc(K + 1));
         SPH_CUDA(tile_sums_.alloc((K + kScanThreads * 4 - 1) / (kScanThreads * 4) + 1));
-        SPH_CUDA(cudaFuncSetAttribute(k_pool_build_lists<256, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        SPH_CUDA(cudaFuncSetAttribute(k_pool_build_lists<256, 3, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       64 * 256 * (int)sizeof(uint32_t)));
-        SPH_CUDA(cudaFuncSetAttribute(k_pool_build_lists<256, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        SPH_CUDA(cudaFuncSetAttribute(k_pool_build_lists<256, 4, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      64 * 256 * (int)sizeof(uint32_t)));
+        SPH_CUDA(cudaFuncSetAttribute(k_pool_build_lists<256, 3, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      64 * 256 * (int)sizeof(uint32_t)));
+        SPH_CUDA(cudaFuncSetAttribute(k_pool_build_lists<256, 4, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       64 * 256 * (int)sizeof(uint32_t)));
         SPH_CUDA(cudaMemsetAsync(count_.p, 0, K * sizeof(uint32_t), st_));
         SPH_CUDA(table_.alloc(d.max_scenes));
@@ -1073,13 +1102,14 @@ private:
 
     // ---- tuned launches ---------------------------------------------------
     // Shapes: (threads per block, threads per SM the register budget allows).
-    void launch_build(Fluid<float> f, const P4<float>* bp, Lists<float> L)
+    // DIV0: the build also forms the divergence solve's first error pass.
+    template <bool DIV0 = false> void launch_build(Fluid<float> f, const P4<float>* bp, Lists<float> L)
     {
         const int bb = tune_.build_block, bo = tune_.build_occ;
         const uint32_t qd = (uint32_t)tune_.queue;
         const size_t smem = (size_t)qd * (size_t)bb * sizeof(uint32_t);
 #define SPH_BUILD(BL, MB) \
-    k_pool_build_lists<BL, MB><<<blocks(N_, BL), BL, smem, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L, qd)
+    k_pool_build_lists<BL, MB, DIV0><<<blocks(N_, BL), BL, smem, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p, L, qd)
         if (bb == 128 && bo == 896) SPH_BUILD(128, 7);
         else if (bb == 128) SPH_BUILD(128, 8);
         else if (bo == 1024) SPH_BUILD(256, 4);
@@ -1406,12 +1436,12 @@ private:
             Fluid<float> f = F(cur_);
             const P4<float>* bp = bpos_[bcur_].p;
             Lists<float> L = LS();
-            run("k_pool_build_lists", [&] { launch_build(f, bp, L); });
+            // the build also forms the divergence solve's first error pass
+            run("k_pool_build_lists", [&] { launch_build<true>(f, bp, L); });
             SPH_CUDA(cudaGetLastError());
             rc = solve_loop(
                 2,
                 [&](cudaGraphConditionalHandle h) {
-                    run("k_pool_errors_div", [&] { launch_errors<true, true>(f, bp, L); });
                     run("k_pool_control", [&] { k_pool_control<2><<<1, 256, 0, ls_>>>(table_.p, S_, pc_.p, h); });
                 },
                 [&](cudaGraphConditionalHandle h) {
