@@ -8,7 +8,8 @@ Two oracles live here:
 
 * ``liboracle.so`` (``sph_oracle.c``): the project's C restatement of the
   reference's solvers, FP64, in the reference's own evaluation order.  It
-  builds on any host (``make -C oracle oracle``) and travels to the GPU machine.
+  builds on any host (``make -C oracle oracle``), with or without the
+  reference tree.
 * ``_ref/ref_parity`` / ``_ref/ref_timed``: the reference simulator's own
   sources compiled headless against the project's GLM shim, driven by
   ``ref_driver.cpp`` (``make -C oracle ref``).  It needs the reference tree,
