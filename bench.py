@@ -313,6 +313,7 @@ def run_batched(scenes, args, world, local):
     itsv = sum(b[1] - a[1] for a, b in zip(s0, s1)) / (len(ids) * K)
     sim = sum(b[2] - a[2] for a, b in zip(s0, s1)) / len(ids)
     pairs, overflow = pool.list_pairs()
+    work = pool.count_work()  # the list build's candidates and pairs (not timed)
 
     # per-kernel CUDA-event timing over P host-driven steps of the same pool
     pool.set_graph(False)
@@ -324,7 +325,7 @@ def run_batched(scenes, args, world, local):
     pool.close()
     return dict(ms=ms, n=n, nb=nb, launches=l1 - l0, clocks=clocks.summary(), its=its, itsv=itsv,
                 sim_s_per_scene=sim, pairs=pairs, overflow=overflow, prof=prof, finished_early=finished_early,
-                tuning=tuning)
+                tuning=tuning, work=work)
 
 
 def run_plain(scenes, args):
@@ -487,7 +488,45 @@ def profile_figures(workload):
     return out
 
 
-def roofline(prof, n, nb, pairs, workload):
+def fp32_peak_tflops():
+    """FP32 (non-tensor) throughput of this GPU, measured: an 8192^3 FP32
+    matrix product with TF32 off (cuBLAS SGEMM on the FMA pipe), best of 5,
+    CUDA events."""
+    import torch
+
+    prev = torch.get_float32_matmul_precision()
+    torch.set_float32_matmul_precision("highest")
+    try:
+        n = 8192
+        a = torch.randn(n, n, device="cuda")
+        b = torch.randn(n, n, device="cuda")
+        c = torch.empty_like(a)
+        for _ in range(2):
+            torch.matmul(a, b, out=c)
+        best = float("inf")
+        for _ in range(5):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            torch.matmul(a, b, out=c)
+            e1.record()
+            e1.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        del a, b, c
+        return 2.0 * n ** 3 / (best / 1000.0) / 1e12
+    finally:
+        torch.set_float32_matmul_precision(prev)
+
+
+# FP32 work of one list-build launch: 8 flop per candidate for the distance
+# test (3 subtractions, r^2 by 3 multiply-adds, the compare), 12 for W plus 22
+# for grad W and the accumulations per pair within h (fluid and boundary), and
+# 6 for the fused divergence term per fluid pair (3 subtractions, 3 multiply-adds).
+def build_flops(work):
+    return (8 * (work["fluid_candidates"] + work["boundary_candidates"])
+            + 34 * (work["fluid_pairs"] + work["boundary_pairs"]) + 6 * work["fluid_pairs"])
+
+
+def roofline(prof, n, nb, pairs, workload, work=None, fp32_peak=None):
     """HBM roofline of the kernel with the largest share of the profiled
     steps (`kernel`), and the same figures for the three largest in
     `kernels`.  Algorithmic bytes: compulsory field bytes per particle
@@ -525,6 +564,15 @@ def roofline(prof, n, nb, pairs, workload):
             r["issue"] = dict(issue, source=f["source"])
         if f.get("source"):
             r["profile"] = f["source"]
+        if kname == "k_pool_build_lists" and work and fp32_peak and avg_ms > 0:
+            # the neighbour walks' second bound: FP32 issue
+            flops = build_flops(work)
+            tf = flops / (avg_ms / 1000.0) / 1e12
+            r["fp32"] = {"achieved": tf, "peak": fp32_peak, "unit": "TFLOP/s", "frac": tf / fp32_peak,
+                         "peak_kind": "of measured (FP32 SGEMM, TF32 off)", "flops_per_launch": flops,
+                         "candidates_per_particle": (work["fluid_candidates"] + work["boundary_candidates"]) / max(n, 1),
+                         "pairs_per_particle": (work["fluid_pairs"] + work["boundary_pairs"]) / max(n, 1),
+                         "formula": "8 per candidate + 34 per pair within h + 6 per fluid pair (fused divergence)"}
         return r
 
     ranked = sorted(groups.items(), key=lambda kv: -sum(m for _, _, m in kv[1]))
@@ -583,7 +631,7 @@ def main():
     B = run_batched(scenes, args, world, local)
     t_max = dist_max(B["ms"], world)
     value = world * B["n"] * args.steps / (t_max / 1000.0)
-    roof = roofline(B["prof"], B["n"], B["nb"], B["pairs"], workload)
+    roof = roofline(B["prof"], B["n"], B["nb"], B["pairs"], workload, work=B.get("work"), fp32_peak=fp32_peak_tflops())
     roof["timing"] = f"CUDA events around each launch, {args.profile_steps} host-driven pool steps"
 
     plain = None if args.no_plain else run_plain(scenes, args)

@@ -385,6 +385,10 @@ int sph_pool_set_tuning(sph_pool* pool, const sph_pool_tuning* tuning);
 int sph_pool_get_tuning_log(sph_pool* pool, char* buf, unsigned long long len);
 /* Pair-list occupancy: stored pairs and particles whose neighbours overflow. */
 int sph_pool_list_pairs(sph_pool* pool, unsigned long long* pairs, unsigned* overflow);
+/* The list build's work at the current positions (a diagnostic pass, for its
+ * FP32 roofline): out[0..3] = fluid candidates its walks visit (27 cells,
+ * trimmed), fluid pairs within h, boundary candidates, boundary pairs. */
+int sph_pool_count_work(sph_pool* pool, unsigned long long out[4]);
 const char* sph_pool_last_error(const sph_pool* pool);
 
 /* Sampling helpers with the reference's point sets, usable without a

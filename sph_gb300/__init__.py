@@ -197,6 +197,7 @@ ABI = [
     ("sph_pool_set_tuning", ctypes.c_int, [_vp, ctypes.POINTER(PoolTuning)]),
     ("sph_pool_get_tuning_log", ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_ulonglong]),
     ("sph_pool_list_pairs", ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(ctypes.c_uint)]),
+    ("sph_pool_count_work", ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_ulonglong)]),
     ("sph_pool_last_error", ctypes.c_char_p, [_vp]),
 ]
 
@@ -733,3 +734,10 @@ class Pool:
         p, o = ctypes.c_ulonglong(), ctypes.c_uint()
         self._check(lib().sph_pool_list_pairs(self._h, ctypes.byref(p), ctypes.byref(o)), "sph_pool_list_pairs")
         return p.value, o.value
+
+    def count_work(self):
+        """The list build's work at the current positions: candidates its walks
+        visit and pairs within h, fluid and boundary."""
+        out = (ctypes.c_ulonglong * 4)()
+        self._check(lib().sph_pool_count_work(self._h, out), "sph_pool_count_work")
+        return dict(fluid_candidates=out[0], fluid_pairs=out[1], boundary_candidates=out[2], boundary_pairs=out[3])

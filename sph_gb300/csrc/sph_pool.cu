@@ -280,6 +280,41 @@ __global__ void __launch_bounds__(kBlock) k_pool_npforce(Fluid<float> f, const P
     npforce_apply(i, f, c, s);
 }
 
+// The list build's work at the current positions, for its FP32 roofline:
+// candidates its walks visit (the 27 cells trimmed as the cull trims them;
+// fluid, then boundary) and pairs within h, summed over running scenes into
+// out[0..3] = fluid candidates, fluid pairs, boundary candidates, boundary
+// pairs.  A diagnostic pass, not part of a step.
+__global__ void k_pool_count_work(Fluid<float> f, const P4<float>* __restrict__ bpos, const uint32_t* __restrict__ sid,
+                                  const PoolScene* T, const uint32_t* __restrict__ cs, const uint32_t* __restrict__ bs,
+                                  unsigned long long* out)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long w[4] = {0ull, 0ull, 0ull, 0ull};
+    if (i < f.n) {
+        const PoolScene& sd = T[sid[i]];
+        if (sd.running) {
+            const V3<float> xi = xyz(f.pos[i]);
+            const uint32_t pc = f.cell[i];
+            walk<float, 1, true, true>(sd.g, cs + sd.key_base, pc, xi, sd.c.h, 0, [&](uint32_t j, V3<float> s) {
+                const V3<float> r = s - xyz(ldg4(f.pos + j));
+                ++w[0];
+                if (dot3(r, r) <= sd.c.cull2) ++w[1];
+            });
+            if (sd.akinci)
+                walk<float, 1>(sd.g, bs + sd.key_base, pc, xi, sd.c.h, 0, [&](uint32_t j, V3<float> s) {
+                    const V3<float> r = s - xyz(ldg4(bpos + j));
+                    ++w[2];
+                    if (dot3(r, r) <= sd.c.cull2) ++w[3];
+                });
+        }
+    }
+    for (int q = 0; q < 4; ++q) {
+        const unsigned long long v = warp_sum_u64(w[q]);
+        if ((threadIdx.x & 31) == 0 && v) atomicAdd(out + q, v);
+    }
+}
+
 // DFSPHSolver::updateTimeStep per scene: max of sqrt(|v + (a + g) dt|).
 __global__ void k_pool_cfl_accum(Fluid<float> f, const uint32_t* __restrict__ sid, PoolScene* T)
 {
@@ -931,6 +966,20 @@ public:
         SPH_CUDA(cudaStreamSynchronize(st_));
         *pairs = h[0];
         *overflow = (unsigned)h[1];
+        return SPH_OK;
+    }
+
+    int count_work(unsigned long long out[4])
+    {
+        DevBuf<unsigned long long> o;
+        SPH_CUDA(o.alloc(4));
+        SPH_CUDA(cudaMemsetAsync(o.p, 0, 4 * sizeof(unsigned long long), st_));
+        if (N_)
+            k_pool_count_work<<<blocks(N_, 256), 256, 0, st_>>>(F(cur_), bpos_[bcur_].p, sid_.p, table_.p, starts_.p,
+                                                                 bstarts_.p, o.p);
+        SPH_CUDA(cudaGetLastError());
+        SPH_CUDA(cudaMemcpyAsync(out, o.p, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st_));
+        SPH_CUDA(cudaStreamSynchronize(st_));
         return SPH_OK;
     }
 
@@ -1765,6 +1814,13 @@ int sph_pool_list_pairs(sph_pool* p, unsigned long long* pairs, unsigned* overfl
     if (!p || !pairs || !overflow) return pool_bad(p, "invalid argument");
     PoolLock lock(p);
     return p->pool.list_pairs(pairs, overflow);
+}
+
+int sph_pool_count_work(sph_pool* p, unsigned long long* out)
+{
+    if (!p || !out) return pool_bad(p, "invalid argument");
+    PoolLock lock(p);
+    return p->pool.count_work(out);
 }
 
 const char* sph_pool_last_error(const sph_pool* p)
