@@ -112,6 +112,19 @@ def test_pooled_scene_with_surface_tension_and_adhesion(gpu_lib):
         assert np.array_equal(P.get(i, "v"), P0.get(j, "v"))
 
 
+def test_build_work_counts(gpu_lib):
+    """sph_pool_count_work: every pair within h is a candidate, and the listed
+    pairs (non-zero gradient, self excluded) are among the pairs within h."""
+    P, ids = pool_run([A] + OTHERS, 3)
+    w = P.count_work()
+    pairs, overflow = P.list_pairs()
+    n = sum(P.query(i)[0]["num_fluid"] for i in ids)
+    assert overflow == 0
+    assert w["fluid_candidates"] >= w["fluid_pairs"] >= pairs + n   # + each particle itself
+    assert w["boundary_candidates"] >= w["boundary_pairs"] > 0
+    assert 60 <= w["fluid_candidates"] / n <= 216
+
+
 def test_graph_pool_equals_host_pool(gpu_lib):
     P1, ids1 = pool_run([A] + OTHERS, 6, graph=False)
     P2, ids2 = pool_run([A] + OTHERS, 6, graph=True)
