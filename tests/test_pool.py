@@ -125,6 +125,28 @@ def test_build_work_counts(gpu_lib):
     assert 60 <= w["fluid_candidates"] / n <= 216
 
 
+def test_pool_list_overflow_falls_back_to_cell_walks(gpu_lib):
+    """With 8 list slots every pooled particle overflows its list: the build's
+    first divergence error and every solver pass take the cell walks; results
+    agree with full lists within FP32 rounding, iteration counts equal."""
+    def run(kmax):
+        P = sph_gb300.Pool(max_particles=200_000, max_boundary=400_000, max_keys=4_000_000, max_scenes=64,
+                           neighbor_list_max=kmax)
+        ids = [P.add_scene(x, boundary_points=b, steps=1000, **p) for x, b, p in [A] + OTHERS]
+        P.step(4)
+        P.synchronize()
+        return P, ids
+
+    P64, i64 = run(64)
+    P8, i8 = run(8)
+    assert P8.list_pairs()[1] > 0
+    for a, b in zip(i64, i8):
+        assert relerr(P8.get(b, "x"), P64.get(a, "x")) <= 1e-6
+        assert relerr(P8.get(b, "rho"), P64.get(a, "rho")) <= 1e-5
+        assert np.abs(P8.get(b, "v") - P64.get(a, "v")).max() <= 2.5e-3
+        assert P8.query(b)[0]["sum_iterations"] == P64.query(a)[0]["sum_iterations"]
+
+
 def test_graph_pool_equals_host_pool(gpu_lib):
     P1, ids1 = pool_run([A] + OTHERS, 6, graph=False)
     P2, ids2 = pool_run([A] + OTHERS, 6, graph=True)
