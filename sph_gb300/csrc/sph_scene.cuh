@@ -382,6 +382,16 @@ public:
         std::vector<double> xs(3 * (size_t)na);
         int rc = download(SPH_FIELD_POSITION, xs.data());
         if (rc) return rc;
+        // a particle with non-finite coordinates (a scene that blew up) has no
+        // place in any box: plan around the finite ones
+        size_t keep = 0;
+        for (size_t k = 0; k + 2 < xs.size(); k += 3)
+            if (std::isfinite(xs[k]) && std::isfinite(xs[k + 1]) && std::isfinite(xs[k + 2])) {
+                xs[keep] = xs[k]; xs[keep + 1] = xs[k + 1]; xs[keep + 2] = xs[k + 2];
+                keep += 3;
+            }
+        xs.resize(keep);
+        if (keep == 0) { grow_ = false; return SPH_OK; }
         sph_scene_desc dd = d;
         for (int k = 0; k < 3; ++k) dd.domain_min[k] = dd.domain_max[k] = 0.0;
         GridPlan p;
