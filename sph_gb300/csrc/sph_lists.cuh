@@ -192,6 +192,18 @@ __device__ __noinline__ DivSum<R> velocity_div_cells(const Fluid<R>& f, const P4
                                                      const uint32_t* __restrict__ cs, const uint32_t* __restrict__ bs,
                                                      const Consts<R>& c, int akinci, uint32_t i, V3<R> vi);
 
+template <typename R>
+__device__ __noinline__ R reread_div(const Fluid<R>& f, const Lists<R>& L, uint32_t i, V3<R> vi, uint32_t cnt)
+{
+    const uint32_t n = f.n;
+    R dv = 0;
+    for (uint32_t k = 0; k < cnt; ++k) {
+        const P4<R> pr = L.pairs[(size_t)k * n + i];
+        dv += dot3(vi - xyz(f.vel[as_idx(pr.w)]), xyz(pr));
+    }
+    return dv;
+}
+
 // DIV0: also sum m (v_i - v_j) . gradW_ij over the pairs as they are listed,
 // plus v_i . (boundary gradient): the value velocity_div_one would read from
 // the finished lists (same terms, same order), into *div0, with the count of
@@ -305,15 +317,7 @@ __device__ __forceinline__ void build_lists_one(uint32_t i, const Fluid<R>& f, c
             *div0 = d.dv;
             *nn0 = d.nn;
         } else {
-            if (nq > qcap) {
-                // the list this thread just wrote, re-read as velocity_div_list
-                // reads it (plain loads: it was written in this kernel)
-                dv = 0;
-                for (uint32_t k = 0; k < cnt; ++k) {
-                    const P4<R> pr = L.pairs[(size_t)k * n + i];
-                    dv += dot3(vi - xyz(f.vel[as_idx(pr.w)]), xyz(pr));
-                }
-            }
+            if (nq > qcap) dv = reread_div<R>(f, L, i, vi, cnt);
             if (akinci) dv += dot3(vi, bg);
             *div0 = dv;
             *nn0 = cnt;
