@@ -53,3 +53,28 @@ def test_oracle_matches_live_reference_in_an_open_domain(name, params):
         o.step(1)
         for f in ("x", "v", "rho", "p"):
             assert np.array_equal(o.get(f).ravel(), ref[f"s{s}.{f}"]), (name, s, f)
+
+
+# The full-size configurations of the GPU tests: the restatement equals the
+# reference bit for bit there too, and the workloads' boundary points equal
+# the reference's own sampling of the box.
+FULL = [
+    ("pcisph_drop_81k", "pcisph_drop", ((0.0, 0.0, 0.0), (1.0, 1.0, 1.0))),
+    ("dam_break_125k", "dam_break", ((0.0, 0.0, 0.0), (1.5, 0.8, 0.8))),
+]
+
+
+@pytest.mark.parametrize("name,make,box", FULL, ids=[c[0] for c in FULL])
+def test_oracle_matches_live_reference_at_full_size(name, make, box):
+    from sph_gb300 import workloads
+
+    x, b, params, _ = getattr(workloads, make)()
+    p = {k: v for k, v in params.items() if k != "precision"}
+    ref = oracle.run_reference(p, x, boxes=[box], steps=2)
+    o = oracle.OracleScene(p, x, boxes=[box])
+    o.step(2)
+    for f in ("x", "v", "rho", "p"):
+        assert np.array_equal(o.get(f).ravel(), ref[f"s2.{f}"]), (name, f)
+    o2 = oracle.OracleScene(p, x, points=b)
+    o2.step(2)
+    assert np.array_equal(o2.get("x"), o.get("x"))
