@@ -56,6 +56,16 @@ def test_step_before_init_is_an_error(L):
     s.close()
 
 
+def test_grid_growth_switch(L):
+    """sph_ctx_set_grid_growth is accepted before init (host state only) and
+    refuses a null context."""
+    s = sph_gb300.Scene(method=2, radius=0.02)
+    s.set_grid_growth(False)
+    s.set_grid_growth(True)
+    s.close()
+    assert L.sph_ctx_set_grid_growth(None, 1) == -1
+
+
 @pytest.mark.parametrize("r,mn,mx", [(0.02, (0, 0, 0), (0.6, 0.5, 0.5)), (0.005, (0, 0, 0), (1.5, 0.8, 0.8)),
                                      (0.01, (0.1, 0.2, 0.3), (1.3, 0.7, 0.9))])
 def test_box_sampler_matches_oracle(L, r, mn, mx):
