@@ -114,12 +114,11 @@ def test_f64_steps_match_reference(gpu_lib, name, lists):
 @pytest.mark.parametrize("name", list(SCENES))
 def test_f32_error_against_reference(gpu_lib, name, lists):
     """FP32 production form against the reference's FP64 results, 3 steps.
-    Measured on GB300 with one lane per particle (the default now splits these
-    small scenes' walks over 8 lanes, re-associating sums at rounding level;
-    the bounds hold either way): positions <= 6e-8 rel, densities <= 1e-6 rel,
-    alpha <= 2e-6 rel, WCSPH/PCISPH pressures <= 1e-4 rel, velocities
-    <= 2.5e-4 m/s abs, and identical iteration counts.  Bounds below leave
-    ~10x headroom.  The velocity bound is loose because most of these scenes
+    Measured on GB300 (one lane per particle and the default 8 lanes of these
+    small scenes alike): positions <= 2e-7 rel, densities <= 1.7e-6 rel,
+    alpha <= 3.3e-6 rel, WCSPH/PCISPH pressures <= 1e-4 rel, velocities
+    <= 5.2e-4 m/s abs, and identical iteration counts.  Bounds below leave
+    ~5x headroom.  The velocity bound is loose because most of these scenes
     are exact lattices: neighbours at exactly h make the reference's
     20-neighbour rule and rho* >= rho0 clamp depend on the last bit, so
     single wall-layer particles get or miss a divergence correction; the
