@@ -200,10 +200,10 @@ def dist_barrier(world):
         dist.barrier()
 
 
-def mix(steps):
+def mix(steps, geometry=None):
     from sph_gb300 import workloads
 
-    return workloads.batched_mix(n_scenes=256, seed=42, steps=steps, r=0.01)
+    return workloads.batched_mix(n_scenes=256, seed=42, steps=steps, r=0.01, geometry=geometry)
 
 
 # ---- CPU: the reference's algorithm on a sample of the mix -----------------
@@ -245,7 +245,12 @@ def run_reference_arm(args, world, rank):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    scenes = mix(args.warmup + args.steps)
+    import oracle
+
+    # the same scenes, sampled by the oracle's own lattice and Akinci
+    # samplers (equal point for point to the library's): this arm never
+    # loads the CUDA library
+    scenes = mix(args.warmup + args.steps, geometry=oracle)
     v, desc, done = cpu_mix_sample(scenes, max(1, args.steps), threads, args.ref_budget)
     line = {
         "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
@@ -441,6 +446,25 @@ def stream_mean_work(r=0.01):
     return en * 1100.0
 
 
+def flat_served(plain, served, dam):
+    """The metric's served half and the plain-GPU comparison as scalar config
+    keys (a record that keeps only flat keys still carries them)."""
+    out = {}
+    if plain:
+        out["plain_gpu_pss"] = plain["value"]
+    if served:
+        sat, sub = served["saturated"], served["sub_saturation"]
+        out.update(served_pss_saturated=sat["particle_steps_per_s"], served_p50_s=sat["p50_latency_s"],
+                   served_p99_s=sat["p99_latency_s"], served_completed=sat["completed"],
+                   served_pss_sub=sub["particle_steps_per_s"], served_p50_sub_s=sub["p50_latency_s"],
+                   served_p99_sub_s=sub["p99_latency_s"], served_completed_sub=sub["completed"],
+                   served_rate_sub_per_s=sub["rate_per_s"], served_seconds=sat.get("duration_s"))
+    if dam:
+        out["dam_break_125k_pss"] = dam["value"]
+        out["dam_break_125k_ms_per_step"] = dam["ms_per_step"]
+    return out
+
+
 def run_served(args, rate, seconds, big_every):
     import sph_gb300
     from sph_gb300 import serve, workloads
@@ -451,6 +475,7 @@ def run_served(args, rate, seconds, big_every):
     out = serve.serve(pool, reqs, seconds, epoch_steps=args.epoch_steps)
     out.pop("results", None)
     out["rate_per_s"] = rate
+    out["duration_s"] = seconds
     out["budget_gb"] = args.serve_budget_gb
     out["big_dam_break_every_s"] = big_every
     pool.close()
@@ -681,6 +706,7 @@ def main():
                        "plain_gpu": plain,
                        "batched_over_plain": value / plain["value"] if plain else None,
                        "served": served, "dam_break_125k": dam,
+                       **flat_served(plain, served, dam),
                        "wall_s": time.perf_counter() - wall0},
             "roofline": roof,
             "clocks": B["clocks"],

@@ -276,7 +276,8 @@ int sph_ctx_download(sph_ctx* ctx, int field, double* out);
  *   - The array is held by every GPU that loads the library until exit.
  *   - The first call on a device looks up the array's device address (with
  *     the context's device current); make that first call before any stream
- *     capture.
+ *     capture.  The address is kept until exit: after a cudaDeviceReset of
+ *     a device, do not call this entry point on that device again.
  *   - All calls share the array: calls that overlap on the GPU (contexts used
  *     from several host threads at once) race.  Each call writes every value
  *     it returns, so nothing needs clearing between calls. */

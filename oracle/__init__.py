@@ -318,12 +318,16 @@ def reference_available(timed: bool = False) -> bool:
     return os.path.exists(REF_TIMED if timed else REF_PARITY)
 
 
-def build_reference(ref_tree: str = "/root/reference") -> bool:
-    """Compile the reference headless into _ref/ (this container only)."""
-    if not os.path.isdir(os.path.join(ref_tree, "src")):
-        return False
-    subprocess.run(["make", "-C", HERE, "ref", f"REF={ref_tree}", "-j8"], check=True, capture_output=True)
-    return True
+def build_reference(ref_tree: str | None = None) -> bool:
+    """Compile the reference headless into _ref/ with the Makefile's `ref`
+    recipe.  The tree is `ref_tree`, else the environment's
+    SPH_REFERENCE_TREE, else the recipe's default; where none holds the
+    reference's sources nothing is built.  Returns whether the build exists."""
+    cmd = ["make", "-C", HERE, "ref", "-j8"]
+    if ref_tree:
+        cmd.append(f"REF={ref_tree}")
+    subprocess.run(cmd, check=True, capture_output=True)
+    return reference_available()
 
 
 def read_dump(path):

@@ -14,7 +14,10 @@
 // In host code its name is only a host-side stand-in, never a device address:
 // its device address is looked up with cudaGetSymbolAddress once per device
 // (with that device current), on the first call made on that device, and
-// that pointer is what the kernel receives.
+// that pointer is what the kernel receives.  The address is kept for the
+// life of the process: a cudaDeviceReset on a device ends every context
+// there, and a process that resets a device must not call this entry point
+// on that device again.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -53,9 +56,9 @@ template <typename R>
 __device__ __forceinline__ void abs_pos_of(const P4<R>& p, uint32_t c, const FieldView& v, double* a)
 {
     if constexpr (sizeof(R) == 4) {
-        a[0] = (double)((int)(c & 2047u) + v.ox) * v.h + (double)p.x;
-        a[1] = (double)((int)((c >> 11) & 2047u) + v.oy) * v.h + (double)p.y;
-        a[2] = (double)((int)(c >> 22) + v.oz) * v.h + (double)p.z;
+        a[0] = (double)(cell_x(c) + v.ox) * v.h + (double)p.x;
+        a[1] = (double)(cell_y(c) + v.oy) * v.h + (double)p.y;
+        a[2] = (double)(cell_z(c) + v.oz) * v.h + (double)p.z;
     } else {
         a[0] = p.x; a[1] = p.y; a[2] = p.z;
     }

@@ -16,36 +16,47 @@
 
 Fluid blocks start 2r off the walls: with its first layer at r from an Akinci
 wall the reference's DFSPH ejects wall-adjacent particles in the first step.
+
+The point sets come from the library's samplers (``sph_gb300.fluid_block``,
+``sample_box``, ``sample_sphere``: the reference's lattice and Akinci
+samplings).  A caller that must not load the library -- a CPU baseline that
+times another implementation of the same scenes -- passes any object with the
+same three functions as ``geometry``.
 """
 from __future__ import annotations
 
 import math
+import types
 
 import numpy as np
 
 from . import fluid_block, sample_box, sample_sphere
 
+LIBRARY_GEOMETRY = types.SimpleNamespace(fluid_block=fluid_block, sample_box=sample_box, sample_sphere=sample_sphere)
+
 DFSPH = dict(method=2, boundary=2, eta=0.001, eta_v=0.001, cfl=1.0, max_it=100, dt=1e-4, min_dt=1e-5, max_dt=5e-3,
              fps=60.0, precision="f32")
 
 
-def _block(r, corner, dims):
+def _block(r, corner, dims, geometry=None):
+    g = geometry or LIBRARY_GEOMETRY
     d = 2.0 * r
     mn = np.asarray(corner, dtype=np.float64)
     mx = mn + np.asarray(dims, dtype=np.float64) * d + 1e-9
-    return fluid_block(r, mn, mx), (mn, mx)
+    return g.fluid_block(r, mn, mx), (mn, mx)
 
 
-def make_scene(rng, n_target, r=0.01, box_side=1.0, steps=500, spheres=True):
+def make_scene(rng, n_target, r=0.01, box_side=1.0, steps=500, spheres=True, geometry=None):
     """One scene of the mix: (x, boundary points, params, steps)."""
+    g = geometry or LIBRARY_GEOMETRY
     d = 2.0 * r
     a_xz = rng.uniform(0.5, 2.0)
     a_y = rng.uniform(0.5, 2.0)
     nmax = int((box_side - 4 * r) / d) - 1
     nx = max(2, int(round((n_target / (a_y * a_xz)) ** (1.0 / 3.0))))
     dims = [min(nx, nmax), min(max(2, int(round(nx * a_y))), nmax), min(max(2, int(round(nx * a_xz))), nmax)]
-    x, (bmn, bmx) = _block(r, (2 * r, 2 * r, 2 * r), dims)
-    pts = [sample_box(4 * r, (0.0, 0.0, 0.0), (box_side, box_side, box_side))]
+    x, (bmn, bmx) = _block(r, (2 * r, 2 * r, 2 * r), dims, g)
+    pts = [g.sample_box(4 * r, (0.0, 0.0, 0.0), (box_side, box_side, box_side))]
     if spheres:
         for _ in range(int(rng.integers(0, 4))):
             for _try in range(50):
@@ -54,18 +65,18 @@ def make_scene(rng, n_target, r=0.01, box_side=1.0, steps=500, spheres=True):
                 # keep clear of the block
                 q = np.clip(c, bmn - 2 * d, bmx + 2 * d)
                 if np.linalg.norm(c - q) > rad + 2 * d:
-                    pts.append(sample_sphere(r, c, rad))
+                    pts.append(g.sample_sphere(r, c, rad))
                     break
     params = dict(DFSPH, radius=r)
     return x, np.concatenate(pts), params, int(steps)
 
 
-def batched_mix(n_scenes=256, seed=42, steps=500, r=0.01):
+def batched_mix(n_scenes=256, seed=42, steps=500, r=0.01, geometry=None):
     rng = np.random.default_rng(seed)
     out = []
     for _ in range(n_scenes):
         n = int(round(math.exp(rng.uniform(math.log(2000), math.log(64000)))))
-        out.append(make_scene(rng, n, r=r, steps=steps))
+        out.append(make_scene(rng, n, r=r, steps=steps, geometry=geometry))
     return out
 
 

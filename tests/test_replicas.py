@@ -67,3 +67,17 @@ def test_reference_arm_under_torchrun_prints_once():
     assert len(lines) == 1
     line = json.loads(lines[0])
     assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
+
+
+def test_reference_arm_never_loads_the_cuda_library():
+    """The reference arm times the CPU algorithm on scenes sampled by the
+    oracle's own samplers: the process maps no library of the CUDA path."""
+    code = ("import runpy, sys; sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', '--warmup', '3', "
+            "'--ref-budget', '1']; runpy.run_path('bench.py', run_name='__main__'); "
+            "maps = open('/proc/self/maps').read(); print('CUDA_LIB_MAPPED', 'libsph_gb300' in maps)")
+    env = dict(os.environ, OMP_NUM_THREADS="2")
+    p = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env, timeout=900, cwd=ROOT)
+    assert p.returncode == 0, p.stderr[-2000:]
+    assert "CUDA_LIB_MAPPED False" in p.stdout
+    line = json.loads([ln for ln in p.stdout.splitlines() if ln.startswith("{")][0])
+    assert line["impl"] == "reference" and line["value"] > 0
