@@ -69,9 +69,13 @@ extern "C" {
 
 /* Device status bits (sph_stats.status). */
 #define SPH_STATUS_OUT_OF_GRID 1u   /* a particle left the grid box; it was kept in the border cell */
-#define SPH_STATUS_NONFINITE 2u     /* a solver reduction produced NaN/Inf */
+#define SPH_STATUS_NONFINITE 2u     /* a position or velocity (checked at every grid build) or a solver
+                                       reduction is NaN/Inf */
 #define SPH_STATUS_ITER_CAP 4u      /* density / pressure solve stopped at maxIterations */
 #define SPH_STATUS_ITER_CAP_V 8u    /* divergence solve stopped at the iteration cap */
+#define SPH_STATUS_DIVERGED 16u     /* pool: a particle's relative solver error exceeded 6e10 / n (n the
+                                       scene's particles; 15,000 at 4M): the scene has blown up, its average
+                                       error reads +Inf and its loop runs to the cap */
 
 typedef struct sph_ctx sph_ctx;
 
@@ -293,6 +297,19 @@ const char* sph_ctx_last_error(const sph_ctx* ctx);
 int sph_ctx_neighbors(sph_ctx* ctx, int* cells, int* cell_rank, int* nbr_off, int* nbr, int* bnbr_off, int* bnbr,
                       long long* totals);
 
+/* Test hook: the DFSPH pair lists (neighbor_list_max > 0) that the solver
+ * passes sum over, as the last grid build stored them: per fluid particle
+ * (original order) every neighbour with a non-zero kernel gradient, in walk
+ * order, as original indices.  These are the neighbourhoods of
+ * HashTable::neighborhoodSearch (src/HashTable.h:136-170) that the
+ * reference's DFSPH sums (DFSPHSolver.cpp:114-590): its candidates j != i
+ * with 1e-5 < |xi - xj| < h.  count[i] is the particle's neighbour count; a
+ * count above neighbor_list_max means the list overflowed and was not stored
+ * (the passes walk that particle's cells instead) and contributes no entries.
+ * Each array may be NULL; off has n + 1 entries (CSR), nbr needs off and
+ * *total entries (the stored pairs, returned in any case). */
+int sph_ctx_pair_lists(sph_ctx* ctx, int* count, int* off, int* nbr, long long* total);
+
 /* Number of kernels of this library the context has launched (graph steps
  * counted from the captured graph and the iterations its loops ran). */
 int sph_ctx_get_launch_count(sph_ctx* ctx, unsigned long long* out);
@@ -339,12 +356,17 @@ int sph_pool_add_scene(sph_pool* pool, const sph_scene_desc* desc, const double*
                        const double* boundary_x, unsigned nb, unsigned steps, int* scene_id);
 /* Release a scene (finished or not) at the next step. */
 int sph_pool_remove_scene(sph_pool* pool, int scene_id);
-/* nsteps steps of every resident scene that still has steps to run. */
+/* nsteps steps of every resident scene that still has steps to run;
+ * nsteps = 0 only applies pending admissions and removals (new scenes
+ * become resident with their initial densities, alpha factors and pair
+ * lists, DFSPHSolver::init). */
 int sph_pool_step(sph_pool* pool, int nsteps);
 /* Whole pool steps as one CUDA graph with device-side solver loops. */
 int sph_pool_set_graph(sph_pool* pool, int enable);
 int sph_pool_synchronize(sph_pool* pool);
-/* Statistics of one scene; *done = 1 once its steps have completed. */
+/* Statistics of one scene; *done = 1 once its steps have completed.  A
+ * scene whose solver reductions turned NaN / Inf (SPH_STATUS_NONFINITE) is
+ * retired after that step: done, with fewer steps than it asked for. */
 int sph_pool_query(sph_pool* pool, int scene_id, sph_stats* out, int* done);
 /* Ids of resident scenes whose steps have completed (up to max_ids). */
 int sph_pool_poll(sph_pool* pool, int* done_ids, int max_ids, int* num_done);
@@ -384,6 +406,9 @@ int sph_pool_get_tuning(sph_pool* pool, sph_pool_tuning* out);
 int sph_pool_set_tuning(sph_pool* pool, const sph_pool_tuning* tuning);
 /* The last measurement, one "candidate: ms" line per candidate. */
 int sph_pool_get_tuning_log(sph_pool* pool, char* buf, unsigned long long len);
+/* A resident scene's pair lists, as sph_ctx_pair_lists (original indices
+ * within the scene). */
+int sph_pool_pair_lists(sph_pool* pool, int scene_id, int* count, int* off, int* nbr, long long* total);
 /* Pair-list occupancy: stored pairs and particles whose neighbours overflow. */
 int sph_pool_list_pairs(sph_pool* pool, unsigned long long* pairs, unsigned* overflow);
 /* The list build's work at the current positions (a diagnostic pass, for its

@@ -35,7 +35,7 @@ FIELDS = {
     "bdens": (14, 1), "bpress": (15, 1),
 }
 
-STATUS_OUT_OF_GRID, STATUS_NONFINITE, STATUS_ITER_CAP, STATUS_ITER_CAP_V = 1, 2, 4, 8
+STATUS_OUT_OF_GRID, STATUS_NONFINITE, STATUS_ITER_CAP, STATUS_ITER_CAP_V, STATUS_DIVERGED = 1, 2, 4, 8, 16
 
 
 class SceneDesc(ctypes.Structure):
@@ -164,6 +164,7 @@ ABI = [
     ("sph_ctx_get_stats", ctypes.c_int, [_vp, ctypes.POINTER(Stats)]),
     ("sph_ctx_last_error", ctypes.c_char_p, [_vp]),
     ("sph_ctx_neighbors", ctypes.c_int, [_vp, _ip, _ip, _ip, _ip, _ip, _ip, ctypes.POINTER(ctypes.c_longlong)]),
+    ("sph_ctx_pair_lists", ctypes.c_int, [_vp, _ip, _ip, _ip, ctypes.POINTER(ctypes.c_longlong)]),
     ("sph_ctx_get_launch_count", ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_ulonglong)]),
     ("sph_ctx_set_profiling", ctypes.c_int, [_vp, ctypes.c_int]),
     ("sph_ctx_get_profile", ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_ulonglong]),
@@ -198,6 +199,7 @@ ABI = [
     ("sph_pool_get_tuning_log", ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_ulonglong]),
     ("sph_pool_list_pairs", ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(ctypes.c_uint)]),
     ("sph_pool_count_work", ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_ulonglong)]),
+    ("sph_pool_pair_lists", ctypes.c_int, [_vp, ctypes.c_int, _ip, _ip, _ip, ctypes.POINTER(ctypes.c_longlong)]),
     ("sph_pool_last_error", ctypes.c_char_p, [_vp]),
 ]
 
@@ -507,6 +509,26 @@ class Scene:
         return dict(cell=cells.reshape(n, 3), cell_rank=rank, nbr_off=off, nbr=nbr[: tot[0]], bnbr_off=boff,
                     bnbr=bnbr[: tot[1]])
 
+    def pair_lists(self):
+        """The DFSPH pair lists the solver passes read: dict(count, off, nbr)
+        by original index (count above the list width: overflowed, not stored)."""
+        def call(c, o, nb, t):
+            self._check(lib().sph_ctx_pair_lists(self._h, c, o, nb, t), "sph_ctx_pair_lists")
+
+        return _pair_lists(call, self.n)
+
+
+def _pair_lists(call, n):
+    """CSR pair lists through a (count, off, nbr, total) dump call: dict of
+    count, off, nbr (original indices)."""
+    tot = ctypes.c_longlong()
+    cnt = np.zeros(max(n, 1), np.int32)
+    off = np.zeros(n + 1, np.int32)
+    call(_i(cnt), _i(off), None, ctypes.byref(tot))
+    nbr = np.zeros(max(tot.value, 1), np.int32)
+    call(_i(cnt), _i(off), _i(nbr), ctypes.byref(tot))
+    return dict(count=cnt[:n], off=off, nbr=nbr[: tot.value])
+
 
 def select_device(device: int):
     rc = lib().sph_select_device(int(device))
@@ -734,6 +756,13 @@ class Pool:
         p, o = ctypes.c_ulonglong(), ctypes.c_uint()
         self._check(lib().sph_pool_list_pairs(self._h, ctypes.byref(p), ctypes.byref(o)), "sph_pool_list_pairs")
         return p.value, o.value
+
+    def pair_lists(self, sid):
+        """A resident scene's pair lists, as Scene.pair_lists."""
+        def call(c, o, nb, t):
+            self._check(lib().sph_pool_pair_lists(self._h, int(sid), c, o, nb, t), "sph_pool_pair_lists")
+
+        return _pair_lists(call, self._n[sid][0])
 
     def count_work(self):
         """The list build's work at the current positions: candidates its walks

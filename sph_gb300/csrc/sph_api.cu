@@ -549,6 +549,13 @@ int sph_ctx_neighbors(sph_ctx* ctx, int* cells, int* cell_rank, int* nbr_off, in
     return relay(ctx, ctx->scene->neighbors(cells, cell_rank, nbr_off, nbr, bnbr_off, bnbr, totals));
 }
 
+int sph_ctx_pair_lists(sph_ctx* ctx, int* count, int* off, int* nbr, long long* total)
+{
+    if (!ctx) return SPH_ERR_INVALID;
+    if (nbr && !off) return bad(ctx, "nbr needs off");
+    return relay(ctx, ctx->scene->pair_lists(count, off, nbr, total));
+}
+
 long long sph_sample_box(double support_radius, const double mn[3], const double mx[3], double* out)
 {
     if (!mn || !mx || !(support_radius > 0.0)) return -1;

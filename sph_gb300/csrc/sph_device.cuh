@@ -124,7 +124,7 @@ struct DevScalars {
 };
 
 enum StatusBits : unsigned {
-    ST_OUT_OF_GRID = 1u, ST_NONFINITE = 2u, ST_ITER_CAP = 4u, ST_ITER_CAP_V = 8u,
+    ST_OUT_OF_GRID = 1u, ST_NONFINITE = 2u, ST_ITER_CAP = 4u, ST_ITER_CAP_V = 8u, ST_DIVERGED = 16u,
 };
 
 // Solver limits used by the device-side loop controls.

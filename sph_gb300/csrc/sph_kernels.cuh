@@ -207,6 +207,9 @@ __global__ void k_cell_update(uint32_t n, P4<R>* __restrict__ pos, const P4<R>* 
         const P4<R> v = vel[i];
         p.x = p.x + v.x * dt; p.y = p.y + v.y * dt; p.z = p.z + v.z * dt;
     }
+    // a NaN / Inf position (or, moved, velocity) never meets a neighbour, so
+    // no solver sum would notice it (as in the reference): flag it here
+    if (!(isfinite(p.x) && isfinite(p.y) && isfinite(p.z))) atomicOr(&sc->status, (unsigned)ST_NONFINITE);
     const uint32_t c0 = cell[i];
     int cx, cy, cz;
     if constexpr (sizeof(R) == 4) {
@@ -906,7 +909,7 @@ __global__ void __launch_bounds__(kBlock) k_dfsph_predict_density(Fluid<R> f, co
     double total;
     if (finish_reduction<false>(err, partials, &sc->block_counter, sh, &total) && threadIdx.x == 0) {
         const double avg = f.count() ? total / (double)f.count() : 0.0;
-        if (!(avg == avg)) sc->status |= ST_NONFINITE;
+        if (!isfinite(avg)) sc->status |= ST_NONFINITE;
         if (INITIAL) {
             sc->iterations = 0;
             sc->avgDensError = avg;
@@ -979,7 +982,7 @@ __global__ void __launch_bounds__(kBlock) k_dfsph_divergence(Fluid<R> f, const P
     if (finish_reduction<false>(err, partials, &sc->block_counter, sh, &total) && threadIdx.x == 0) {
         const double avg = total / (double)f.count();
         const double lim_v = lim.maxErrorV / sc->dt;
-        if (!(avg == avg)) sc->status |= ST_NONFINITE;
+        if (!isfinite(avg)) sc->status |= ST_NONFINITE;
         if (INITIAL) {
             sc->iterationsV = 0;
             sc->avgDivError = avg;
@@ -1161,7 +1164,7 @@ __global__ void __launch_bounds__(kBlock) k_pcisph_density_pressure(Fluid<R> f, 
     if (finish_reduction<true>(err, partials, &sc->block_counter, sh, &mx) && threadIdx.x == 0) {
         mx = fmax(mx, 0.0);
         sc->maxDensityError = mx;
-        if (!(mx == mx)) sc->status |= ST_NONFINITE;
+        if (!isfinite(mx)) sc->status |= ST_NONFINITE;
         const unsigned it = sc->iterations + 1;
         sc->next_active = ((mx > lim.maxError) || (it < lim.minIt)) && (it < lim.maxIt);
     }

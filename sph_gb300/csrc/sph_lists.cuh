@@ -23,6 +23,9 @@
 
 #include <cuda_fp16.h>
 
+#include <cstring>
+#include <vector>
+
 #include "sph_kernels.cuh"
 
 namespace sph {
@@ -92,22 +95,33 @@ __device__ __forceinline__ uint32_t cull_half(const GridView& g, const uint32_t*
         const uint32_t bb = nb, ee = ne;
         if (c < 8) range(c + 1, &nb, &ne);
         const __half2 sx = __float2half2_rn(xi.x - (float)dx * h), sy = __float2half2_rn(xi.y - (float)dy * h);
+        // The column's candidates 32 at a time (16 words): the test's
+        // acceptance bits are gathered into one word, candidate j0 + b at
+        // bit b, and only the accepted candidates (about one in five) are
+        // queued, in walk order.
+        for (uint32_t j0 = bb & ~1u; j0 < ee; j0 += 32) {
+            const uint32_t nw = min(16u, (ee - j0 + 1) >> 1);
+            const uint4* __restrict__ wp = posh + (j0 >> 1);
+            uint32_t bits = 0;
 #pragma unroll 2
-        for (uint32_t j = bb & ~1u; j < ee; j += 2) {
-            const uint4 w = __ldg(posh + (j >> 1));
-            const __half2 ddx = __hsub2(sx, as_half2(w.x));
-            const __half2 ddy = __hsub2(sy, as_half2(w.y));
-            const __half2 dz = __habs2(__hsub2(zq, as_half2(w.z)));
-            const __half2 ddz = __hmin2(dz, __hsub2(h3, dz));
-            const __half2 r2 = __hfma2(ddz, ddz, __hfma2(ddy, ddy, __hmul2(ddx, ddx)));
-            const unsigned m = __hle2_mask(r2, thr);
-            // the word's other particle may lie outside the column's range
-            if ((m & 1u) && j >= bb) {
-                if (nq < qcap) q[nq * qstride + threadIdx.x] = j;
-                ++nq;
+            for (uint32_t k = 0; k < nw; ++k) {
+                const uint4 w = __ldg(wp + k);
+                const __half2 ddx = __hsub2(sx, as_half2(w.x));
+                const __half2 ddy = __hsub2(sy, as_half2(w.y));
+                const __half2 dz = __habs2(__hsub2(zq, as_half2(w.z)));
+                const __half2 ddz = __hmin2(dz, __hsub2(h3, dz));
+                const __half2 r2 = __hfma2(ddz, ddz, __hfma2(ddy, ddy, __hmul2(ddx, ddx)));
+                const unsigned m = __hle2_mask(r2, thr);
+                bits |= ((m & 1u) | ((m >> 30) & 2u)) << (2 * k);
             }
-            if ((m >> 31) && j + 1 < ee) {
-                if (nq < qcap) q[nq * qstride + threadIdx.x] = j + 1;
+            // the first word's low particle may precede the column's range
+            // (bb odd), the last word's high one follow it (ee odd)
+            if (j0 < bb) bits &= ~1u;
+            if (j0 + 2 * nw > ee) bits &= ~(1u << (2 * nw - 1));
+            while (bits) {
+                const uint32_t b = __ffs(bits) - 1;
+                bits &= bits - 1;
+                if (nq < qcap) q[nq * qstride + threadIdx.x] = j0 + b;
                 ++nq;
             }
         }
@@ -518,7 +532,7 @@ __global__ void __launch_bounds__(kBlock, 8) k_dfsph_predict_density_list(Fluid<
     double total;
     if (finish_reduction<false>(err, partials, &sc->block_counter, sh, &total) && threadIdx.x == 0) {
         const double avg = f.count() ? total / (double)f.count() : 0.0;
-        if (!(avg == avg)) sc->status |= ST_NONFINITE;
+        if (!isfinite(avg)) sc->status |= ST_NONFINITE;
         if (INITIAL) {
             sc->iterations = 0;
             sc->avgDensError = avg;
@@ -564,7 +578,7 @@ __global__ void __launch_bounds__(kBlock, 8) k_dfsph_divergence_list(Fluid<R> f,
     if (finish_reduction<false>(err, partials, &sc->block_counter, sh, &total) && threadIdx.x == 0) {
         const double avg = total / (double)f.count();
         const double lim_v = lim.maxErrorV / sc->dt;
-        if (!(avg == avg)) sc->status |= ST_NONFINITE;
+        if (!isfinite(avg)) sc->status |= ST_NONFINITE;
         if (INITIAL) {
             sc->iterationsV = 0;
             sc->avgDivError = avg;
@@ -582,6 +596,75 @@ __global__ void __launch_bounds__(kBlock, 8) k_dfsph_divergence_list(Fluid<R> f,
         }
         if (cond) cudaGraphSetConditional(cond, sc->active);
     }
+}
+
+// The stored lists of the n particles at [base, base + n) of a layout whose
+// list slots are `stride` apart (a pooled scene's segment, or a whole scene
+// with base 0), keyed by original index: cnt[me] = the particle's neighbour
+// count (above kmax when its list overflowed and was not stored) and, with
+// off given, the stored neighbours' original indices in list order at
+// nbr[off[me]...].
+template <typename R>
+__global__ void k_pair_lists(uint32_t n, uint32_t base, uint32_t stride, const uint32_t* __restrict__ id, Lists<R> L,
+                             const int* __restrict__ off, int* __restrict__ cnt, int* __restrict__ nbr)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const uint32_t i = base + t;
+    const uint32_t me = id[i];
+    const uint32_t c = L.count[i];
+    if (cnt) cnt[me] = (int)c;
+    if (off && c <= L.kmax) {
+        int* o = nbr + off[me];
+        for (uint32_t k = 0; k < c; ++k) o[k] = (int)id[as_idx(L.pairs[(size_t)k * stride + i].w)];
+    }
+}
+
+// Host side of a pair-list dump (one-scene context and pool alike):
+// counts, CSR offsets by original index, and the neighbours.  `launch(off,
+// cnt, nbr)` enqueues k_pair_lists on `st`; n = particles.
+template <typename Launch>
+cudaError_t dump_pair_lists(uint32_t n, uint32_t kmax, cudaStream_t st, Launch&& launch, int* count, int* off, int* nbr,
+                            long long* total)
+{
+    int* dc = nullptr;
+    int* doff = nullptr;
+    int* dn = nullptr;
+    std::vector<int> hc(n), ho(n + 1);
+    long long a = 0;
+    cudaError_t e = cudaMalloc((void**)&dc, sizeof(int) * (n ? n : 1));
+    if (e == cudaSuccess && n) {
+        launch((const int*)nullptr, dc, (int*)nullptr);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess && n) e = cudaMemcpyAsync(hc.data(), dc, sizeof(int) * n, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) {
+        for (uint32_t i = 0; i < n; ++i) {
+            ho[i] = (int)a;
+            a += (uint32_t)hc[i] <= kmax ? hc[i] : 0;
+        }
+        ho[n] = (int)a;
+        if (total) *total = a;
+        if (count && n) std::memcpy(count, hc.data(), sizeof(int) * n);
+        if (off) std::memcpy(off, ho.data(), sizeof(int) * (n + 1));
+    }
+    if (e == cudaSuccess && nbr && a) {
+        e = cudaMalloc((void**)&doff, sizeof(int) * (n + 1));
+        if (e == cudaSuccess) e = cudaMalloc((void**)&dn, sizeof(int) * (size_t)a);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(doff, ho.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) {
+            launch((const int*)doff, (int*)nullptr, dn);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaMemcpyAsync(nbr, dn, sizeof(int) * (size_t)a, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    }
+    cudaStreamSynchronize(st);
+    cudaFree(dc);
+    cudaFree(doff);
+    cudaFree(dn);
+    return e;
 }
 
 // Warm-start scaling (as k_dfsph_predict_v_warm) writing k to the list

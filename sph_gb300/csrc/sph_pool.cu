@@ -43,6 +43,12 @@ struct sph_pool;
 namespace sph {
 
 constexpr double kFixScale = 268435456.0;  // 2^28: per-particle error quantum 3.7e-9
+// A scene's fixed-point error sum holds at most 2^64 / 2^28 = 6.9e10: with
+// n particles, a particle error above kErrBudget / n is not added (the sum
+// then cannot wrap) and marks the scene as blown up.  For the largest scenes
+// served (4M particles) that is an error of 15,000 (a density of 15,000 rest
+// densities, or a divergence error of 15,000 / s); for the mix's 64k, 9e5.
+constexpr double kErrBudget = 6.0e10;
 
 struct PoolScene {
     Consts<float> c;
@@ -55,6 +61,8 @@ struct PoolScene {
     uint32_t loop_active;     // this scene's solver loop is still iterating
     uint32_t steps_left;
     uint32_t vmax_bits;       // CFL: max of sqrt(|v|) as float bits
+    uint32_t bad;             // reduction in progress saw: 1 a NaN / Inf error, 2 an error above eclamp
+    float eclamp;             // kErrBudget / n: largest error a particle adds to the fixed-point sum
     int akinci;
 };
 
@@ -85,6 +93,17 @@ __device__ __forceinline__ void seg_add(uint32_t s, unsigned long long v, PoolSc
 }
 
 __device__ __forceinline__ unsigned long long to_fixed(double e) { return (unsigned long long)(e * kFixScale + 0.5); }
+
+// A particle's relative error (>= 0) as its fixed-point contribution to its
+// scene's sum; a NaN / Inf error or one above the scene's clamp is not
+// added, and marks the scene's reduction instead (k_pool_control then reads
+// the scene's average as NaN or +Inf, as an FP64 sum of the same terms would).
+__device__ __forceinline__ unsigned long long error_contribution(float e, PoolScene& sd)
+{
+    if (e <= sd.eclamp) return to_fixed((double)e);
+    atomicOr(&sd.bad, isfinite(e) ? 2u : 1u);
+    return 0ull;
+}
 
 __device__ __forceinline__ uint32_t find_segment(const uint32_t* __restrict__ base, uint32_t S, uint32_t i)
 {
@@ -152,6 +171,9 @@ __global__ void k_pool_cell_update(uint32_t N, Fluid<float> f, const uint32_t* _
         const P4<float> v = f.vel[i];
         p.x = p.x + v.x * dt; p.y = p.y + v.y * dt; p.z = p.z + v.z * dt;
     }
+    // a NaN / Inf position or velocity never meets a neighbour, so no solver
+    // sum would notice it: flag it here (the scene is retired at step end)
+    if (!(isfinite(p.x) && isfinite(p.y) && isfinite(p.z))) atomicOr(&sd.s.status, (unsigned)ST_NONFINITE);
     const GridView& g = sd.g;
     const float h = sd.c.h;
     const uint32_t c0 = f.cell[i];
@@ -235,12 +257,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_pool_build_lists(Fluid<float> f
                 d = nn < 20u ? 0.f : (d < 0.f ? 0.f : d);
                 f.div[i] = d;
                 L.kbuf[i] = d * f.alpha[i] / (dt * f.rho[i]);
-                const float e = d * inv0;
-                if (e == e && e < 1e9f) {
-                    contrib = to_fixed((double)e);
-                } else {
-                    atomicOr(&sd.s.status, (unsigned)ST_NONFINITE);
-                }
+                contrib = error_contribution(d * inv0, sd);
                 s = k;
             }
         }
@@ -435,11 +452,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_pool_errors(Fluid<float> f, con
                 L.kbuf[i] = (pred - c.density0) * f.alpha[i] / ((dt * dt) * rho);
                 e = (pred - c.density0) * inv0;
             }
-            if (e == e && e < 1e9f) {
-                contrib = to_fixed((double)e);
-            } else {
-                atomicOr(&sd.s.status, (unsigned)ST_NONFINITE);
-            }
+            contrib = error_contribution(e, sd);
             s = k;
         }
     }
@@ -456,9 +469,21 @@ __global__ void k_pool_control(PoolScene* T, uint32_t S, PoolCounters* pc, cudaG
     for (uint32_t k = threadIdx.x; k < S; k += blockDim.x) {
         PoolScene& sd = T[k];
         const unsigned long long acc = sd.acc;
+        const uint32_t bad = sd.bad;
         sd.acc = 0ull;
+        sd.bad = 0u;
         if (!sd.running) { sd.loop_active = 0; continue; }
-        const double avg = sd.n ? (double)acc / kFixScale / (double)sd.n : 0.0;
+        double avg = sd.n ? (double)acc / kFixScale / (double)sd.n : 0.0;
+        // a NaN / Inf error makes the average NaN (the loop then stops at its
+        // minimum iterations, as the reference's NaN comparisons do), an
+        // error above the clamp makes it +Inf (the loop runs to its cap)
+        if (bad & 1u) {
+            avg = __longlong_as_double(0x7ff8000000000000ll);
+            sd.s.status |= ST_NONFINITE;
+        } else if (bad & 2u) {
+            avg = __longlong_as_double(0x7ff0000000000000ll);
+            sd.s.status |= ST_DIVERGED;
+        }
         const LoopLimits& lim = sd.lim;
         unsigned act;
         if (PHASE == 0) {
@@ -518,6 +543,9 @@ __global__ void k_pool_finish(PoolScene* T, uint32_t S)
         sd.s.time = sd.s.time + sd.s.dt;
         sd.s.steps += 1;
         sd.steps_left -= 1;
+        // a scene whose state turned NaN / Inf is retired after this step:
+        // polls report it done, its status carries SPH_STATUS_NONFINITE
+        if (sd.s.status & ST_NONFINITE) sd.steps_left = 0;
         sd.running = sd.steps_left > 0;
     }
 }
@@ -666,6 +694,8 @@ public:
 
     int step(int nsteps)
     {
+        // nsteps == 0 applies pending admissions and removals only
+        if (nsteps == 0 && dirty_) return relayout();
         for (int k = 0; k < nsteps; ++k) {
             if (dirty_) {
                 const int rc = relayout();
@@ -1075,6 +1105,29 @@ public:
         return SPH_OK;
     }
 
+    // A resident scene's pair lists by scene-local original index (see
+    // sph_pool_pair_lists).
+    int pair_lists(int id, int* count, int* off, int* nbr, long long* total)
+    {
+        PoolEntry* e = find(id);
+        if (!e || !e->resident) { fail("scene is not resident"); return SPH_ERR_INVALID; }
+        const uint32_t s = slot_of(id);
+        PoolScene t;
+        SPH_CUDA(cudaMemcpyAsync(&t, table_.p + s, sizeof t, cudaMemcpyDeviceToHost, st_));
+        SPH_CUDA(cudaStreamSynchronize(st_));
+        const Lists<float> L = LS();
+        const uint32_t* idp = id_[cur_].p;
+        const uint32_t n = t.n, base = t.pbase, stride = N_;
+        const cudaError_t err = dump_pair_lists(
+            n, kmax_, st_,
+            [&](const int* doff, int* dcnt, int* dn) {
+                k_pair_lists<float><<<blocks(n, 256), 256, 0, st_>>>(n, base, stride, idp, L, doff, dcnt, dn);
+            },
+            count, off, nbr, total);
+        SPH_CUDA(err);
+        return SPH_OK;
+    }
+
     int usage(unsigned long long* p, unsigned long long* b, unsigned long long* k, unsigned* s)
     {
         uint64_t P = 0, B = 0, K = 0;
@@ -1296,6 +1349,7 @@ private:
                 t.running = e->steps > 0;
                 t.loop_active = 0;
                 t.vmax_bits = 0;
+                t.bad = 0;
                 t.akinci = 1;
             }
             t.g.nx = e->plan.nn[0]; t.g.ny = e->plan.nn[1]; t.g.nz = e->plan.nn[2];
@@ -1303,6 +1357,7 @@ private:
             t.g.mortx = mort_.p + mxo[s];
             t.g.morty = mort_.p + myo[s];
             t.key_base = kb[s]; t.n = e->n; t.nb = e->nb; t.pbase = pb[s]; t.bbase = bb[s];
+            t.eclamp = (float)(kErrBudget / (double)std::max(e->n, 1u));
             tab[s] = t;
         }
         S_ = (uint32_t)order.size();
@@ -1736,6 +1791,13 @@ int sph_pool_download(sph_pool* p, int scene_id, int field, double* out)
     if (!p || !out) return pool_bad(p, "invalid argument");
     PoolLock lock(p);
     return p->pool.download(scene_id, field, out);
+}
+
+int sph_pool_pair_lists(sph_pool* p, int scene_id, int* count, int* off, int* nbr, long long* total)
+{
+    if (!p || (nbr && !off)) return pool_bad(p, "invalid argument");
+    PoolLock lock(p);
+    return p->pool.pair_lists(scene_id, count, off, nbr, total);
 }
 
 int sph_pool_usage(sph_pool* p, unsigned long long* particles, unsigned long long* boundary, unsigned long long* keys,

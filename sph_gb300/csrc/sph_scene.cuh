@@ -124,9 +124,13 @@ inline int grid_plan(const sph_scene_desc& d, const std::vector<double>& hx, con
     double lo[3], hi[3];
     bool given = false;
     for (int k = 0; k < 3; ++k) given |= d.domain_max[k] > d.domain_min[k];
+    // non-finite points (a corrupted input) do not shape the box: the upload
+    // keeps them in a border cell and the solver's reductions flag them
     auto acc = [&](const std::vector<double>& v) {
-        for (size_t i = 0; i + 2 < v.size(); i += 3)
+        for (size_t i = 0; i + 2 < v.size(); i += 3) {
+            if (!std::isfinite(v[i]) || !std::isfinite(v[i + 1]) || !std::isfinite(v[i + 2])) continue;
             for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], v[i + k]); hi[k] = std::max(hi[k], v[i + k]); }
+        }
     };
     if (given) {
         for (int k = 0; k < 3; ++k) { lo[k] = d.domain_min[k]; hi[k] = d.domain_max[k]; }
@@ -770,6 +774,26 @@ public:
             if (bnbr && bt) SPH_CUDA(cudaMemcpyAsync(bnbr, dbn.p, bt * 4, cudaMemcpyDeviceToHost, st_));
             SPH_CUDA(cudaStreamSynchronize(st_));
         }
+        return SPH_OK;
+    }
+
+    // The DFSPH pair lists as the last grid build stored them (original
+    // order; see sph_ctx_pair_lists).
+    int pair_lists(int* count, int* off, int* nbr, long long* total) override
+    {
+        if (!inited) { fail("not initialised"); return SPH_ERR_INVALID; }
+        if (!lists_) { fail("the scene keeps no pair lists (DFSPH with neighbor_list_max > 0 only)"); return SPH_ERR_UNSUPPORTED; }
+        const unsigned na = active();
+        const Fluid<R> f = F();
+        const Lists<R> L = LS();
+        const uint32_t stride = n_;
+        const cudaError_t e = dump_pair_lists(
+            na, kmax_, st_,
+            [&](const int* doff, int* dcnt, int* dn) {
+                k_pair_lists<R><<<blocks(na, 256), 256, 0, st_>>>(na, 0u, stride, f.id, L, doff, dcnt, dn);
+            },
+            count, off, nbr, total);
+        SPH_CUDA(e);
         return SPH_OK;
     }
 

@@ -85,6 +85,7 @@ struct SceneBase {
     virtual int capture_async(double* x, double* v, cudaEvent_t done, unsigned* count_out) = 0;
     virtual int stats(sph_stats* s) = 0;
     virtual int neighbors(int* cells, int* rank, int* off, int* nbr, int* boff, int* bnbr, long long* totals) = 0;
+    virtual int pair_lists(int* count, int* off, int* nbr, long long* total) = 0;
     virtual int field_view(int field, FieldView* v) = 0;
     virtual int launch_count(unsigned long long* out) = 0;
     virtual int set_profiling(int on) = 0;
