@@ -162,6 +162,10 @@ int sph_ctx_add_boundary_points(sph_ctx* ctx, const double* x, unsigned n);
  * normals (sph_ctx_add_boundary_points) are rejected for this model. */
 int sph_ctx_add_pcisph_box(sph_ctx* ctx, const double mn[3], const double mx[3], int inverted);
 int sph_ctx_add_pcisph_sphere(sph_ctx* ctx, const double c[3], double radius, int inverted);
+/* PCISPHBoundaryModel points with their normals (xyz each, FP64) as the
+ * model holds them (src/PCISPHBoundaryModel.h:12-16): for a caller that built
+ * the model itself. */
+int sph_ctx_add_pcisph_points(sph_ctx* ctx, const double* x, const double* normals, unsigned n);
 /* AkinciBoundaryModel::addGeometry (AkinciBoundayModel.cpp:78-98,166-221):
  * the surface of a triangulated OBJ mesh sampled at most max_distance apart
  * (vertices, edges, then lines across each face; the scene file's

@@ -323,7 +323,9 @@ def build_reference(ref_tree: str | None = None) -> bool:
     recipe.  The tree is `ref_tree`, else the environment's
     SPH_REFERENCE_TREE, else the recipe's default; where none holds the
     reference's sources nothing is built.  Returns whether the build exists."""
-    cmd = ["make", "-C", HERE, "ref", "-j8"]
+    # the reference's own build, and the GPU drop-in solvers built with it
+    # (they link to sph_gb300/lib/libsph_gb300.so, built first)
+    cmd = ["make", "-C", HERE, "ref", "adapter", "-j8"]
     if ref_tree:
         cmd.append(f"REF={ref_tree}")
     subprocess.run(cmd, check=True, capture_output=True)

@@ -138,6 +138,7 @@ ABI = [
     ("sph_ctx_add_boundary_points", ctypes.c_int, [_vp, _dp, ctypes.c_uint]),
     ("sph_ctx_add_pcisph_box", ctypes.c_int, [_vp, _dp, _dp, ctypes.c_int]),
     ("sph_ctx_add_pcisph_sphere", ctypes.c_int, [_vp, _dp, ctypes.c_double, ctypes.c_int]),
+    ("sph_ctx_add_pcisph_points", ctypes.c_int, [_vp, _dp, _dp, ctypes.c_uint]),
     ("sph_ctx_add_emitter", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_uint, _dp, ctypes.c_double, _dp, ctypes.c_double,
                                            ctypes.c_double, ctypes.c_double, ctypes.c_double]),
     ("sph_ctx_pause_emitters", ctypes.c_int, [_vp, ctypes.c_int]),

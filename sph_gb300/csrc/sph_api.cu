@@ -408,6 +408,14 @@ int sph_ctx_add_boundary_mesh(sph_ctx* ctx, const char* obj_path, double max_dis
     return add_boundary(ctx, pts.data(), (unsigned)m);
 }
 
+int sph_ctx_add_pcisph_points(sph_ctx* ctx, const double* x, const double* normals, unsigned n)
+{
+    if (!ctx || (n && (!x || !normals))) return bad(ctx, "invalid argument");
+    if (ctx->scene->inited) return bad(ctx, "boundary must be added before sph_ctx_init");
+    if (ctx->scene->d.boundary_method != SPH_BOUNDARY_PCISPH) return bad(ctx, "boundary_method is not SPH_BOUNDARY_PCISPH");
+    return add_boundary(ctx, x, n, normals);
+}
+
 int sph_ctx_add_boundary_points(sph_ctx* ctx, const double* x, unsigned n)
 {
     if (!ctx || (!x && n)) return bad(ctx, "invalid argument");
