@@ -473,7 +473,7 @@ def run_served(args, rate, seconds, big_every):
     pool.set_graph(True)
     reqs = workloads.request_stream(rate=rate, duration=seconds, seed=7, big_every=big_every)
     out = serve.serve(pool, reqs, seconds, epoch_steps=args.epoch_steps)
-    out.pop("results", None)
+    out.pop("request_ids", None)
     out["rate_per_s"] = rate
     out["duration_s"] = seconds
     out["budget_gb"] = args.serve_budget_gb

@@ -421,6 +421,58 @@ int sph_pool_list_pairs(sph_pool* pool, unsigned long long* pairs, unsigned* ove
 int sph_pool_count_work(sph_pool* pool, unsigned long long out[4]);
 const char* sph_pool_last_error(const sph_pool* pool);
 
+/* ------------------------------------------------------------------------
+ * Request loop over a pool (no counterpart in the reference): clients submit
+ * scenes from any thread; one driver thread steps the pool in epochs of
+ * epoch_steps, admits queued scenes between epochs as capacity frees up (in
+ * arrival order, trying the first `lookahead`, so a scene that does not fit
+ * does not block smaller ones behind it), and retires completed scenes.
+ * Admission's host work overlaps the epoch running on the device.  While a
+ * server exists, only its driver steps the pool.  Latency is measured from
+ * sph_server_submit to the poll that found the scene complete.
+ * ------------------------------------------------------------------------ */
+typedef struct sph_server sph_server;
+typedef struct sph_server_desc {
+    unsigned epoch_steps;   /* pool steps between admission passes (default 10) */
+    unsigned lookahead;     /* queued requests tried per admission pass (default 8) */
+    int keep_results;       /* keep each completed scene's final positions and velocities (sph_server_fetch) */
+} sph_server_desc;
+#define SPH_REQUEST_QUEUED 0
+#define SPH_REQUEST_RESIDENT 1
+#define SPH_REQUEST_DONE 2
+#define SPH_REQUEST_FAILED 3   /* rejected by the pool (not capacity): sph_pool_last_error */
+typedef struct sph_request_info {
+    long long id;
+    int state;              /* SPH_REQUEST_* */
+    unsigned num_fluid, steps, steps_done, status;  /* status: SPH_STATUS_* bits of the scene */
+    double latency_s;       /* submission to completion (SPH_REQUEST_DONE) */
+} sph_request_info;
+typedef struct sph_server_stats {
+    unsigned long long submitted, admitted, completed, failed, queued, resident, epochs;
+    double wall_s;                    /* since sph_server_create */
+    double particle_steps;            /* completed scenes' plus resident scenes' steps so far, x particles */
+    double particle_steps_per_s;
+    double p50_latency_s, p99_latency_s, mean_latency_s;  /* over completed requests */
+} sph_server_stats;
+int sph_server_desc_init(sph_server_desc* desc);
+int sph_server_create(sph_pool* pool, const sph_server_desc* desc, sph_server** out);
+/* Stops the driver after its current epoch (resident scenes stay in the pool). */
+int sph_server_destroy(sph_server* server);
+/* Queue a scene (the arrays are copied; the call does not wait for the GPU). */
+int sph_server_submit(sph_server* server, const sph_scene_desc* desc, const double* x, const double* v, unsigned n,
+                      const double* boundary_x, unsigned nb, unsigned steps, long long* request_id);
+/* Requests completed (or failed) since the previous call, up to max. */
+int sph_server_completed(sph_server* server, sph_request_info* out, int max, int* num);
+int sph_server_query(sph_server* server, long long request_id, sph_request_info* out);
+/* A completed request's final SPH_FIELD_POSITION or SPH_FIELD_VELOCITY
+ * (keep_results), original particle order, 3 doubles per particle. */
+int sph_server_fetch(sph_server* server, long long request_id, int field, double* out);
+int sph_server_release(sph_server* server, long long request_id);
+/* Wait until nothing is queued or resident, at most timeout_s seconds. */
+int sph_server_drain(sph_server* server, double timeout_s, int* idle);
+int sph_server_get_stats(sph_server* server, sph_server_stats* out);
+const char* sph_server_last_error(const sph_server* server);
+
 /* Sampling helpers with the reference's point sets, usable without a
  * context; out may be NULL to query the count.  Return the point count. */
 long long sph_sample_box(double support_radius, const double min[3], const double max[3], double* out);

@@ -124,6 +124,42 @@ class PoolTuning(ctypes.Structure):
     ]
 
 
+class ServerDesc(ctypes.Structure):
+    _fields_ = [("epoch_steps", ctypes.c_uint), ("lookahead", ctypes.c_uint), ("keep_results", ctypes.c_int)]
+
+
+class RequestInfo(ctypes.Structure):
+    _fields_ = [
+        ("id", ctypes.c_longlong),
+        ("state", ctypes.c_int),
+        ("num_fluid", ctypes.c_uint),
+        ("steps", ctypes.c_uint),
+        ("steps_done", ctypes.c_uint),
+        ("status", ctypes.c_uint),
+        ("latency_s", ctypes.c_double),
+    ]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [
+        ("submitted", ctypes.c_ulonglong),
+        ("admitted", ctypes.c_ulonglong),
+        ("completed", ctypes.c_ulonglong),
+        ("failed", ctypes.c_ulonglong),
+        ("queued", ctypes.c_ulonglong),
+        ("resident", ctypes.c_ulonglong),
+        ("epochs", ctypes.c_ulonglong),
+        ("wall_s", ctypes.c_double),
+        ("particle_steps", ctypes.c_double),
+        ("particle_steps_per_s", ctypes.c_double),
+        ("p50_latency_s", ctypes.c_double),
+        ("p99_latency_s", ctypes.c_double),
+        ("mean_latency_s", ctypes.c_double),
+    ]
+
+
+REQUEST_QUEUED, REQUEST_RESIDENT, REQUEST_DONE, REQUEST_FAILED = 0, 1, 2, 3
+
 # The C ABI, as (name, restype, argtypes); the CPU tests check that the
 # library exports each of these.
 _vp, _dp, _ip = ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)
@@ -202,6 +238,18 @@ ABI = [
     ("sph_pool_count_work", ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_ulonglong)]),
     ("sph_pool_pair_lists", ctypes.c_int, [_vp, ctypes.c_int, _ip, _ip, _ip, ctypes.POINTER(ctypes.c_longlong)]),
     ("sph_pool_last_error", ctypes.c_char_p, [_vp]),
+    ("sph_server_desc_init", ctypes.c_int, [ctypes.POINTER(ServerDesc)]),
+    ("sph_server_create", ctypes.c_int, [_vp, ctypes.POINTER(ServerDesc), ctypes.POINTER(_vp)]),
+    ("sph_server_destroy", ctypes.c_int, [_vp]),
+    ("sph_server_submit", ctypes.c_int, [_vp, ctypes.POINTER(SceneDesc), _dp, _dp, ctypes.c_uint, _dp, ctypes.c_uint,
+                                         ctypes.c_uint, ctypes.POINTER(ctypes.c_longlong)]),
+    ("sph_server_completed", ctypes.c_int, [_vp, ctypes.POINTER(RequestInfo), ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
+    ("sph_server_query", ctypes.c_int, [_vp, ctypes.c_longlong, ctypes.POINTER(RequestInfo)]),
+    ("sph_server_fetch", ctypes.c_int, [_vp, ctypes.c_longlong, ctypes.c_int, _dp]),
+    ("sph_server_release", ctypes.c_int, [_vp, ctypes.c_longlong]),
+    ("sph_server_drain", ctypes.c_int, [_vp, ctypes.c_double, ctypes.POINTER(ctypes.c_int)]),
+    ("sph_server_get_stats", ctypes.c_int, [_vp, ctypes.POINTER(ServerStats)]),
+    ("sph_server_last_error", ctypes.c_char_p, [_vp]),
 ]
 
 _lib = None
@@ -771,3 +819,84 @@ class Pool:
         out = (ctypes.c_ulonglong * 4)()
         self._check(lib().sph_pool_count_work(self._h, out), "sph_pool_count_work")
         return dict(fluid_candidates=out[0], fluid_pairs=out[1], boundary_candidates=out[2], boundary_pairs=out[3])
+
+
+class Server:
+    """The library's request loop over a pool (sph_server_*): submit scenes
+    from any thread; a driver thread in the library steps the pool in epochs,
+    admits queued scenes as capacity frees up and retires completed ones.
+    While it exists, nothing else steps the pool."""
+
+    def __init__(self, pool, epoch_steps=10, lookahead=8, keep_results=False):
+        L = lib()
+        d = ServerDesc()
+        L.sph_server_desc_init(ctypes.byref(d))
+        d.epoch_steps, d.lookahead, d.keep_results = int(epoch_steps), int(lookahead), int(bool(keep_results))
+        self.pool = pool
+        self._h = ctypes.c_void_p()
+        rc = L.sph_server_create(pool._h, ctypes.byref(d), ctypes.byref(self._h))
+        if rc != 0:
+            raise SPHError(f"sph_server_create failed ({rc})")
+        self._n = {}
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            lib().sph_server_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc, what):
+        if rc != 0:
+            msg = lib().sph_server_last_error(self._h)
+            raise SPHError(f"{what} failed ({rc}): {msg.decode() if msg else ''}")
+
+    def submit(self, x, v=None, boundary_points=None, steps=1, **params):
+        x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, 3)
+        vv = None if v is None else np.ascontiguousarray(v, dtype=np.float64).reshape(-1, 3)
+        b = None if boundary_points is None else np.ascontiguousarray(boundary_points, dtype=np.float64).reshape(-1, 3)
+        d = make_desc(**params)
+        rid = ctypes.c_longlong()
+        self._check(lib().sph_server_submit(self._h, ctypes.byref(d), _d(x), None if vv is None else _d(vv), x.shape[0],
+                                            None if b is None else _d(b), 0 if b is None else b.shape[0], int(steps),
+                                            ctypes.byref(rid)), "sph_server_submit")
+        self._n[rid.value] = x.shape[0]
+        return rid.value
+
+    @staticmethod
+    def _info(r):
+        return {name: getattr(r, name) for name, _ in RequestInfo._fields_}
+
+    def completed(self, max_n=4096):
+        buf = (RequestInfo * max_n)()
+        n = ctypes.c_int()
+        self._check(lib().sph_server_completed(self._h, buf, max_n, ctypes.byref(n)), "sph_server_completed")
+        return [self._info(buf[k]) for k in range(n.value)]
+
+    def query(self, rid):
+        r = RequestInfo()
+        self._check(lib().sph_server_query(self._h, int(rid), ctypes.byref(r)), "sph_server_query")
+        return self._info(r)
+
+    def fetch(self, rid, field):
+        fid, _ = FIELDS[field]
+        out = np.zeros((self._n[rid], 3))
+        self._check(lib().sph_server_fetch(self._h, int(rid), fid, _d(out)), f"sph_server_fetch({field})")
+        return out
+
+    def release(self, rid):
+        lib().sph_server_release(self._h, int(rid))
+
+    def drain(self, timeout_s=600.0):
+        idle = ctypes.c_int()
+        self._check(lib().sph_server_drain(self._h, float(timeout_s), ctypes.byref(idle)), "sph_server_drain")
+        return bool(idle.value)
+
+    def stats(self):
+        st = ServerStats()
+        self._check(lib().sph_server_get_stats(self._h, ctypes.byref(st)), "sph_server_get_stats")
+        return {name: getattr(st, name) for name, _ in ServerStats._fields_}

@@ -31,6 +31,7 @@ UNITS = {
     "sph_pool.cu": [],
     "sph_scene_io.cpp": [],
     "sph_mesh.cpp": [],
+    "sph_serve.cpp": [],
 }
 HEADERS = ["sph_device.cuh", "sph_kernels.cuh", "sph_lists.cuh", "sph_scene.cuh", "sph_scene_base.h", "sph_ctx.h"]
 

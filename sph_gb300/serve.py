@@ -1,83 +1,59 @@
-"""Request loop serving DFSPH scenes from one device-resident pool.
+"""Serving a stream of DFSPH scene requests from one device-resident pool.
 
-Scenes arrive over time; the loop admits waiting scenes whenever they fit the
-pool's device-memory budget (first come first served, with a short look-ahead
-so one large scene does not block smaller ones behind it), advances every
-resident scene together in epochs of pool steps (continuous batching: new
-scenes join between steps while others are mid-run), and retires each scene
-when its step count completes.  Reported: completed scenes, per-scene
-latency (arrival to completion) percentiles, and aggregate particle-steps/s.
+The request loop itself is the library's (``sph_server_*``, C++): a driver
+thread steps the pool in epochs, admits waiting scenes as the pool's
+device-memory budget frees up (first come first served, with a look-ahead
+so one large scene does not block smaller ones behind it), overlaps that
+host work with the epoch running on the device, and retires each scene
+when its step count completes (continuous batching).  This module is the
+client side of a benchmark: it submits each request of a stream at its
+arrival time, building the scene just then, and reports completed scenes,
+latency percentiles (submission to completion) and aggregate
+particle-steps/s.
 """
 from __future__ import annotations
 
-import collections
 import time
 
-import numpy as np
-
-from . import Pool, PoolFull
+from . import Server
 
 
-def serve(pool: Pool, requests, duration, epoch_steps=10, lookahead=8, keep_results=False):
-    """Run the request stream [(arrival_s, builder)] for at most `duration`
-    seconds of wall time.  Returns a summary dict."""
+def serve(pool, requests, duration, epoch_steps=10, lookahead=8, keep_results=False):
+    """Submit the stream [(arrival_s, builder)] (builder() -> (x, boundary
+    points, params, steps)) at its arrival times for `duration` seconds of
+    wall time, then stop the server.  Returns a summary dict (with the
+    server when keep_results is set, so completed results can be fetched)."""
+    srv = Server(pool, epoch_steps=epoch_steps, lookahead=lookahead, keep_results=keep_results)
     t0 = time.perf_counter()
-    waiting = collections.deque()
-    resident = {}          # scene id -> (arrival, n, steps)
-    latencies, done_ps, results = [], 0, {}
-    ri = 0
-    admitted = 0
-    while True:
-        now = time.perf_counter() - t0
-        while ri < len(requests) and requests[ri][0] <= now:
-            waiting.append(tuple(requests[ri]))
-            ri += 1
-        # admission by the pool's capacity (device-memory budget)
-        k = 0
-        while waiting and k < min(lookahead, len(waiting)):
-            req = waiting[k]
-            if len(req) == 2:  # build the scene once, on first consideration
-                req = waiting[k] = (req[0], req[1](), 0)
-            arrival, (x, b, params, steps), _ = req
-            try:
-                sid = pool.add_scene(x, boundary_points=b, steps=steps, **params)
-            except PoolFull:
-                k += 1
-                continue
-            del waiting[k]
-            resident[sid] = (arrival, x.shape[0], steps)
-            admitted += 1
-        if not resident:
-            if ri >= len(requests) and not waiting:
-                break
-            if now >= duration:
-                break
-            nxt = requests[ri][0] if ri < len(requests) else now + 0.01
-            time.sleep(max(0.0, min(nxt - now, 0.01)))
-            continue
-        pool.step(epoch_steps)
-        pool.synchronize()
-        tnow = time.perf_counter() - t0
-        for sid in pool.poll():
-            arrival, n, steps = resident.pop(sid)
-            latencies.append(tnow - arrival)
-            done_ps += n * steps
-            if keep_results:
-                results[sid] = pool.get(sid, "x")
-            pool.remove(sid)
-        if tnow >= duration:
+    arrived = 0
+    late = 0.0
+    ids = []
+    for arrival, builder in requests:
+        if arrival > duration:
             break
-    wall = time.perf_counter() - t0
-    partial = 0
-    for sid, (arrival, n, steps) in resident.items():
-        st, _ = pool.query(sid)
-        partial += n * st["steps"]
-    lat = np.asarray(latencies) if latencies else np.zeros(1)
-    return dict(
-        wall_s=wall, arrived=ri, admitted=admitted, completed=len(latencies), waiting=len(waiting),
-        resident=len(resident), particle_steps=done_ps + partial,
-        particle_steps_per_s=(done_ps + partial) / wall if wall > 0 else 0.0,
-        p50_latency_s=float(np.percentile(lat, 50)) if latencies else None,
-        p99_latency_s=float(np.percentile(lat, 99)) if latencies else None,
-        results=results,
+        now = time.perf_counter() - t0
+        if arrival > now:
+            time.sleep(arrival - now)
+        else:
+            late = max(late, now - arrival)
+        x, b, params, steps = builder()
+        ids.append(srv.submit(x, boundary_points=b, steps=steps, **params))
+        arrived += 1
+    rest = duration - (time.perf_counter() - t0)
+    if rest > 0:
+        time.sleep(rest)
+    st = srv.stats()
+    out = dict(
+        wall_s=st["wall_s"], arrived=arrived, admitted=st["admitted"], completed=st["completed"],
+        waiting=st["queued"], resident=st["resident"], failed=st["failed"], epochs=st["epochs"],
+        particle_steps=st["particle_steps"], particle_steps_per_s=st["particle_steps_per_s"],
+        p50_latency_s=st["p50_latency_s"] if st["completed"] else None,
+        p99_latency_s=st["p99_latency_s"] if st["completed"] else None,
+        mean_latency_s=st["mean_latency_s"] if st["completed"] else None,
+        max_submit_lag_s=late, request_ids=ids,
     )
+    if keep_results:
+        out["server"] = srv
+    else:
+        srv.close()
+    return out
