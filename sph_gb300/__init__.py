@@ -688,11 +688,21 @@ class Pool:
             text = f"{what} failed ({rc}): {msg.decode() if msg else ''}"
             raise (PoolFull if rc == -4 else SPHError)(text)
 
+    def _desc(self, params):
+        """The scene descriptor of these parameters (built once per distinct
+        parameter set: a mix of scenes usually shares one)."""
+        key = tuple(sorted((k, tuple(v) if isinstance(v, (list, tuple)) else v) for k, v in params.items()))
+        cache = self.__dict__.setdefault("_descs", {})
+        d = cache.get(key)
+        if d is None:
+            d = cache[key] = make_desc(**params)
+        return d
+
     def add_scene(self, x, v=None, boundary_points=None, steps=1, **params):
         x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, 3)
         vv = None if v is None else np.ascontiguousarray(v, dtype=np.float64).reshape(-1, 3)
         b = None if boundary_points is None else np.ascontiguousarray(boundary_points, dtype=np.float64).reshape(-1, 3)
-        d = make_desc(**params)
+        d = self._desc(params)
         sid = ctypes.c_int()
         rc = lib().sph_pool_add_scene(self._h, ctypes.byref(d), _d(x), None if vv is None else _d(vv), x.shape[0],
                                       None if b is None else _d(b), 0 if b is None else b.shape[0], int(steps),

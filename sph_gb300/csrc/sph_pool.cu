@@ -115,6 +115,39 @@ __device__ __forceinline__ uint32_t find_segment(const uint32_t* __restrict__ ba
     return lo;
 }
 
+// Bounding box of n points (xyz FP64), points with a non-finite coordinate
+// left out (the grid planner's rule): per block {lo xyz, hi xyz} at
+// part[6 * blockIdx.x], reduced over the blocks by the host.
+constexpr int kBoxBlocks = 64;
+__global__ void __launch_bounds__(256) k_point_box(const double* __restrict__ p, uint32_t n, double* __restrict__ part)
+{
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double x = p[3 * (size_t)i], y = p[3 * (size_t)i + 1], z = p[3 * (size_t)i + 2];
+        if (isfinite(x) && isfinite(y) && isfinite(z)) {
+            lo[0] = fmin(lo[0], x); lo[1] = fmin(lo[1], y); lo[2] = fmin(lo[2], z);
+            hi[0] = fmax(hi[0], x); hi[1] = fmax(hi[1], y); hi[2] = fmax(hi[2], z);
+        }
+    }
+    __shared__ double sh[6][8];
+    for (int k = 0; k < 3; ++k) {
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[k] = fmin(lo[k], __shfl_down_sync(0xffffffffu, lo[k], o));
+            hi[k] = fmax(hi[k], __shfl_down_sync(0xffffffffu, hi[k], o));
+        }
+    }
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0)
+        for (int k = 0; k < 3; ++k) { sh[k][w] = lo[k]; sh[3 + k][w] = hi[k]; }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        const int k = threadIdx.x;
+        double v = sh[k][0];
+        for (int j = 1; j < (int)(blockDim.x >> 5); ++j) v = k < 3 ? fmin(v, sh[k][j]) : fmax(v, sh[k][j]);
+        part[6 * blockIdx.x + k] = v;
+    }
+}
+
 // Scene id of every particle of a layout: segments [base[s], base[s] + len[s]).
 __global__ void k_fill_sid(uint32_t N, const uint32_t* __restrict__ base, uint32_t S, uint32_t* __restrict__ sid)
 {
@@ -557,7 +590,8 @@ __global__ void k_pool_finish(PoolScene* T, uint32_t S)
 struct PoolEntry {
     int id = -1;
     sph_scene_desc d{};
-    std::vector<double> x, v, b;  // staged until resident
+    bool staged = false;          // points (x, v, boundary) in the staging arena until resident
+    size_t ox = 0, ov = 0, ob = 0;  // their offsets there
     unsigned n = 0, nb = 0, steps = 0;
     GridPlan plan;
     PoolScene t{};                // last known device entry (layout fields kept by the host)
@@ -579,6 +613,8 @@ public:
         for (auto e : tev_) if (e) cudaEventDestroy(e);
         if (st_) cudaStreamDestroy(st_);
         if (st2_) cudaStreamDestroy(st2_);
+        if (up_) { cudaStreamSynchronize(up_); cudaStreamDestroy(up_); }
+        if (h_box_) cudaFreeHost(h_box_);
         if (h_pc_) cudaFreeHost(h_pc_);
         if (h_run_) cudaFreeHost(h_run_);
     }
@@ -596,6 +632,9 @@ public:
         kmax_ = d.neighbor_list_max > 0 ? (uint32_t)d.neighbor_list_max : 64u;
         SPH_CUDA(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
         SPH_CUDA(cudaStreamCreateWithFlags(&st2_, cudaStreamNonBlocking));
+        SPH_CUDA(cudaStreamCreateWithFlags(&up_, cudaStreamNonBlocking));
+        SPH_CUDA(box_.alloc(12 * kBoxBlocks));
+        SPH_CUDA(cudaMallocHost((void**)&h_box_, 12 * kBoxBlocks * sizeof(double)));
         ls_ = st_;
         SPH_CUDA(cudaMallocHost((void**)&h_pc_, sizeof(PoolCounters)));
         SPH_CUDA(cudaMallocHost((void**)&h_run_, std::max<size_t>(d.max_scenes, 1)));
@@ -647,32 +686,80 @@ public:
         e.n = n;
         e.nb = nb;
         e.steps = steps;
-        try {
-            e.x.assign(x, x + 3 * (size_t)n);
-            if (v) e.v.assign(v, v + 3 * (size_t)n); else e.v.assign(3 * (size_t)n, 0.0);
-            if (nb) e.b.assign(b, b + 3 * (size_t)nb);
-        } catch (...) {
-            fail("out of host memory");
-            return SPH_ERR_INVALID;
-        }
         double hh, mass;
         scene_constants<float>(d, &e.t.c, &e.t.lim, &hh, &mass);
-        // the walls bound a pooled scene: two cells beyond its points, no
-        // proportional margin (a box just over 32 cells wide would double
-        // each Morton axis of its key space)
-        int rc = grid_plan(d, e.x, e.b, true, std::vector<double>(), hh, &e.plan, &err, 0.0);
-        if (rc) return rc;
-        // capacity check against everything resident or pending
+        // capacity check against everything resident or pending (grid keys
+        // once the scene's box is known, below)
         uint64_t P = 0, B = 0, K = 0;
         unsigned S = 0;
         for (auto& q : entries_) {
             if (q.removed) continue;
             P += q.n; B += q.nb; K += q.plan.nkeys; ++S;
         }
-        if (P + n > pd_.max_particles || B + nb > pd_.max_boundary || K + e.plan.nkeys > pd_.max_keys || S + 1 > pd_.max_scenes) {
+        if (P + n > pd_.max_particles || B + nb > pd_.max_boundary || S + 1 > pd_.max_scenes) {
             fail("pool full");
             return SPH_ERR_CAPACITY;
         }
+        // the points go straight from the caller's arrays into the device
+        // staging arena on the upload stream (no host copy; a step running on
+        // the pool's stream meanwhile is not waited for); the copy is complete
+        // when this returns, so the caller may reuse its arrays
+        const size_t nx = 3 * (size_t)n, nbv = 3 * (size_t)nb, need = 2 * nx + nbv;
+        if (arena_used_ + need > arena_.n) {
+            // grow (doubling): the pending scenes' points move to the new arena
+            DevBuf<double> bigger;
+            SPH_CUDA(bigger.alloc(std::max(arena_used_ + need, 2 * arena_.n)));
+            if (arena_used_)
+                SPH_CUDA(cudaMemcpyAsync(bigger.p, arena_.p, arena_used_ * sizeof(double), cudaMemcpyDeviceToDevice, up_));
+            SPH_CUDA(cudaStreamSynchronize(up_));
+            std::swap(arena_.p, bigger.p);
+            std::swap(arena_.n, bigger.n);
+        }
+        e.ox = arena_used_;
+        e.ov = e.ox + nx;
+        e.ob = e.ov + nx;
+        double* a = arena_.p;
+        cudaError_t ce = cudaMemcpyAsync(a + e.ox, x, nx * sizeof(double), cudaMemcpyHostToDevice, up_);
+        if (ce == cudaSuccess)
+            ce = v ? cudaMemcpyAsync(a + e.ov, v, nx * sizeof(double), cudaMemcpyHostToDevice, up_)
+                   : cudaMemsetAsync(a + e.ov, 0, nx * sizeof(double), up_);
+        if (ce == cudaSuccess && nb) ce = cudaMemcpyAsync(a + e.ob, b, nbv * sizeof(double), cudaMemcpyHostToDevice, up_);
+        // the points' bounding box, formed on the device from the staged copy
+        const unsigned gx = std::min<unsigned>(kBoxBlocks, blocks(n, 256));
+        const unsigned gb = nb ? std::min<unsigned>(kBoxBlocks, blocks(nb, 256)) : 0u;
+        if (ce == cudaSuccess) {
+            k_point_box<<<gx, 256, 0, up_>>>(a + e.ox, n, box_.p);
+            if (gb) k_point_box<<<gb, 256, 0, up_>>>(a + e.ob, nb, box_.p + 6 * kBoxBlocks);
+            ce = cudaGetLastError();
+        }
+        if (ce == cudaSuccess) ce = cudaMemcpyAsync(h_box_, box_.p, 12 * kBoxBlocks * sizeof(double), cudaMemcpyDeviceToHost, up_);
+        if (ce == cudaSuccess) ce = cudaStreamSynchronize(up_);
+        if (ce != cudaSuccess) {
+            fail(std::string("staging a scene: ") + cudaGetErrorString(ce));
+            return SPH_ERR_CUDA;
+        }
+        double box[6] = {1e300, 1e300, 1e300, -1e300, -1e300, -1e300};
+        auto merge = [&](const double* part, unsigned nblk) {
+            for (unsigned q = 0; q < nblk; ++q)
+                for (int k = 0; k < 3; ++k) {
+                    box[k] = std::min(box[k], part[6 * q + k]);
+                    box[3 + k] = std::max(box[3 + k], part[6 * q + 3 + k]);
+                }
+        };
+        merge(h_box_, gx);
+        merge(h_box_ + 6 * kBoxBlocks, gb);
+        // the walls bound a pooled scene: two cells beyond its points, no
+        // proportional margin (a box just over 32 cells wide would double
+        // each Morton axis of its key space)
+        int rc = grid_plan(d, PointSpan(x, 3 * (size_t)n), PointSpan(b, 3 * (size_t)nb), true, PointSpan(nullptr, 0), hh,
+                           &e.plan, &err, 0.0, false, box);
+        if (rc) return rc;
+        if (K + e.plan.nkeys > pd_.max_keys) {
+            fail("pool full");
+            return SPH_ERR_CAPACITY;
+        }
+        arena_used_ += need;
+        e.staged = true;
         e.id = next_id_++;
         *id = e.id;
         entries_.push_back(std::move(e));
@@ -1067,10 +1154,8 @@ public:
     {
         PoolEntry* e = find(id);
         if (!e || !e->resident) { fail("scene is not resident"); return SPH_ERR_INVALID; }
-        const uint32_t s = slot_of(id);
-        PoolScene t;
-        SPH_CUDA(cudaMemcpyAsync(&t, table_.p + s, sizeof t, cudaMemcpyDeviceToHost, st_));
-        SPH_CUDA(cudaStreamSynchronize(st_));
+        // the layout fields of the scene's table entry, as the host keeps them
+        const PoolScene& t = e->t;
         const bool bnd = field == SPH_FIELD_BOUNDARY_POSITION || field == SPH_FIELD_BOUNDARY_VOLUME;
         const uint32_t n = bnd ? t.nb : t.n, base = bnd ? t.bbase : t.pbase;
         const bool vec = field == SPH_FIELD_POSITION || field == SPH_FIELD_VELOCITY || field == SPH_FIELD_ACCELERATION ||
@@ -1094,13 +1179,14 @@ public:
         }
         const size_t count = (size_t)n * (vec ? 3 : 1);
         if (!count) return SPH_OK;
-        DevBuf<double> o;
-        SPH_CUDA(o.alloc(count));
+        // a staging buffer kept between downloads (grow-only): no allocation,
+        // and no cudaFree (which waits for the whole device) per call
+        if (dl_.n < count) SPH_CUDA(dl_.alloc(std::max(count, dl_.n + dl_.n / 2)));
         const uint32_t* idp = bnd ? bid_[bcur_].p + base : id_[cur_].p + base;
         const uint32_t* cellp = bnd ? bcell_[bcur_].p + base : cell_[cur_].p + base;
-        k_download<float><<<(n + 255) / 256, 256, 0, st_>>>(n, v4, sc, idp, cellp, t.g, (double)t.c.h, kind, o.p);
+        k_download<float><<<(n + 255) / 256, 256, 0, st_>>>(n, v4, sc, idp, cellp, t.g, (double)t.c.h, kind, dl_.p);
         SPH_CUDA(cudaGetLastError());
-        SPH_CUDA(cudaMemcpyAsync(out, o.p, count * 8, cudaMemcpyDeviceToHost, st_));
+        SPH_CUDA(cudaMemcpyAsync(out, dl_.p, count * 8, cudaMemcpyDeviceToHost, st_));
         SPH_CUDA(cudaStreamSynchronize(st_));
         return SPH_OK;
     }
@@ -1362,34 +1448,29 @@ private:
         }
         S_ = (uint32_t)order.size();
         SPH_CUDA(cudaMemcpyAsync(table_.p, tab.data(), S_ * sizeof(PoolScene), cudaMemcpyHostToDevice, st_));
-        // upload the new scenes into their segments
+        // upload the new scenes into their segments from their staged points
+        // (one wait for all of them); the arena is then free again
         for (size_t s = keep.size(); s < order.size(); ++s) {
             PoolEntry* e = order[s];
-            DevBuf<double> tx, tv, tb;
-            SPH_CUDA(tx.alloc(e->x.size()));
-            SPH_CUDA(tv.alloc(e->v.size()));
-            SPH_CUDA(cudaMemcpyAsync(tx.p, e->x.data(), e->x.size() * 8, cudaMemcpyHostToDevice, st_));
-            SPH_CUDA(cudaMemcpyAsync(tv.p, e->v.data(), e->v.size() * 8, cudaMemcpyHostToDevice, st_));
             Fluid<float> f = F(nc);
             f.pos += pb[s]; f.vel += pb[s]; f.kappa += pb[s]; f.kappav += pb[s]; f.cell += pb[s]; f.id += pb[s];
             f.acc += pb[s]; f.press += pb[s];
             DevScalars* sst = scalars_of(s);
-            k_upload_fluid<float><<<blocks(e->n, 256), 256, 0, st_>>>(tx.p, tv.p, e->n, 0, f, tab[s].g, 4.0 * e->d.particle_radius, sst);
+            k_upload_fluid<float><<<blocks(e->n, 256), 256, 0, st_>>>(arena_.p + e->ox, arena_.p + e->ov, e->n, 0, f,
+                                                                      tab[s].g, 4.0 * e->d.particle_radius, sst);
             SPH_CUDA(cudaMemsetAsync(pred_[nc].p + pb[s], 0, e->n * sizeof(float), st_));
             if (e->nb) {
-                SPH_CUDA(tb.alloc(e->b.size()));
-                SPH_CUDA(cudaMemcpyAsync(tb.p, e->b.data(), e->b.size() * 8, cudaMemcpyHostToDevice, st_));
                 Boundary<float> bo = B(nbc);
                 bo.pos += bb[s]; bo.cell += bb[s]; bo.id += bb[s];
-                k_upload_boundary<float><<<blocks(e->nb, 256), 256, 0, st_>>>(tb.p, e->nb, bo, tab[s].g, 4.0 * e->d.particle_radius, sst);
+                k_upload_boundary<float><<<blocks(e->nb, 256), 256, 0, st_>>>(arena_.p + e->ob, e->nb, bo, tab[s].g,
+                                                                              4.0 * e->d.particle_radius, sst);
             }
             SPH_CUDA(cudaGetLastError());
-            SPH_CUDA(cudaStreamSynchronize(st_));
+            e->staged = false;
             e->resident = true;
-            std::vector<double>().swap(e->x);
-            std::vector<double>().swap(e->v);
-            std::vector<double>().swap(e->b);
         }
+        SPH_CUDA(cudaStreamSynchronize(st_));
+        arena_used_ = 0;
         cur_ = nc;
         bcur_ = nbc;
         // drop removed entries; the resident order is the layout order
@@ -1659,6 +1740,12 @@ private:
     DevBuf<uint32_t> seg_a_, seg_b_, seg_n_;
     DevBuf<PoolScene> table_;
     DevBuf<PoolCounters> pc_;
+    cudaStream_t up_ = nullptr;   // admissions: the new scenes' points to the device
+    DevBuf<double> arena_;        // their staging (grow-only; emptied by each re-layout)
+    size_t arena_used_ = 0;
+    DevBuf<double> box_;          // admissions: per-block bounding boxes of the staged points
+    double* h_box_ = nullptr;
+    DevBuf<double> dl_;           // downloads: original-order FP64 staging (grow-only)
 };
 
 }  // namespace sph

@@ -117,16 +117,29 @@ struct GridPlan {
 };
 
 // cover_points: a given domain is widened to hold every point too.
-inline int grid_plan(const sph_scene_desc& d, const std::vector<double>& hx, const std::vector<double>& hb, bool akinci,
-                     const std::vector<double>& he, double h, GridPlan* out, std::string* err, double rel_margin = 0.05,
-                     bool cover_points = false)
+// A set of points, xyz per point (n doubles).
+struct PointSpan {
+    const double* p;
+    size_t n;
+    PointSpan(const double* ptr, size_t count) : p(ptr), n(count) {}
+    PointSpan(const std::vector<double>& v) : p(v.data()), n(v.size()) {}
+    size_t size() const { return n; }
+    double operator[](size_t i) const { return p[i]; }
+};
+
+// known_box (lo xyz, hi xyz): the points' bounding box, already formed (by
+// the same rule: points with a non-finite coordinate left out); the point
+// spans are then not read.
+inline int grid_plan(const sph_scene_desc& d, PointSpan hx, PointSpan hb, bool akinci, PointSpan he, double h,
+                     GridPlan* out, std::string* err, double rel_margin = 0.05, bool cover_points = false,
+                     const double* known_box = nullptr)
 {
     double lo[3], hi[3];
     bool given = false;
     for (int k = 0; k < 3; ++k) given |= d.domain_max[k] > d.domain_min[k];
     // non-finite points (a corrupted input) do not shape the box: the upload
     // keeps them in a border cell and the solver's reductions flag them
-    auto acc = [&](const std::vector<double>& v) {
+    auto acc = [&](const PointSpan& v) {
         for (size_t i = 0; i + 2 < v.size(); i += 3) {
             if (!std::isfinite(v[i]) || !std::isfinite(v[i + 1]) || !std::isfinite(v[i + 2])) continue;
             for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], v[i + k]); hi[k] = std::max(hi[k], v[i + k]); }
@@ -141,9 +154,13 @@ inline int grid_plan(const sph_scene_desc& d, const std::vector<double>& hx, con
         }
     } else {
         for (int k = 0; k < 3; ++k) { lo[k] = 1e300; hi[k] = -1e300; }
-        acc(hx);
-        acc(he);
-        if (akinci) acc(hb);
+        if (known_box) {
+            for (int k = 0; k < 3; ++k) { lo[k] = known_box[k]; hi[k] = known_box[3 + k]; }
+        } else {
+            acc(hx);
+            acc(he);
+            if (akinci) acc(hb);
+        }
         if (d.boundary_method == SPH_BOUNDARY_CUBE && d.has_cube)
             for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], d.cube_min[k]); hi[k] = std::max(hi[k], d.cube_max[k]); }
         for (int k = 0; k < 3; ++k) {
@@ -151,6 +168,10 @@ inline int grid_plan(const sph_scene_desc& d, const std::vector<double>& hx, con
             lo[k] -= rel_margin * ext;
             hi[k] += rel_margin * ext;
         }
+    }
+    if (!(lo[0] <= hi[0] && lo[1] <= hi[1] && lo[2] <= hi[2])) {
+        *err = "no point with finite coordinates to place the grid box";
+        return SPH_ERR_INVALID;
     }
     GridPlan p;
     for (int k = 0; k < 3; ++k) {
