@@ -410,6 +410,20 @@ int sph_pool_get_tuning(sph_pool* pool, sph_pool_tuning* out);
 int sph_pool_set_tuning(sph_pool* pool, const sph_pool_tuning* tuning);
 /* The last measurement, one "candidate: ms" line per candidate. */
 int sph_pool_get_tuning_log(sph_pool* pool, char* buf, unsigned long long len);
+/* Checkpoint / resume of one pooled scene.  The reference keeps no resumable
+ * state (its frame files, SceneLoader::writeFluid src/SceneLoader.cpp:200-264,
+ * hold positions and velocities only, without the time step, the DFSPH
+ * warm-start k / kv or the iteration history).  A snapshot holds the scene's
+ * device state as stored (cell-relative FP32 positions with their cells,
+ * velocities, k, kv, predicted densities, boundary points), its grid box, its
+ * solver scalars (time, dt, steps, iteration counts and sums, status) and the
+ * steps it has left; a scene restored from it, on this pool or another one of
+ * the same library version, continues bit for bit as if never interrupted.
+ * sph_pool_snapshot with buf NULL returns the size in *size; it waits for the
+ * pool's stream.  sph_pool_restore admits the scene (resident at the next
+ * step) with `steps` more steps to run, 0 for the steps it had left. */
+int sph_pool_snapshot(sph_pool* pool, int scene_id, void* buf, unsigned long long capacity, unsigned long long* size);
+int sph_pool_restore(sph_pool* pool, const void* buf, unsigned long long size, unsigned steps, int* scene_id);
 /* A resident scene's pair lists, as sph_ctx_pair_lists (original indices
  * within the scene). */
 int sph_pool_pair_lists(sph_pool* pool, int scene_id, int* count, int* off, int* nbr, long long* total);

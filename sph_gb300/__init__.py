@@ -237,6 +237,10 @@ ABI = [
     ("sph_pool_list_pairs", ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(ctypes.c_uint)]),
     ("sph_pool_count_work", ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_ulonglong)]),
     ("sph_pool_pair_lists", ctypes.c_int, [_vp, ctypes.c_int, _ip, _ip, _ip, ctypes.POINTER(ctypes.c_longlong)]),
+    ("sph_pool_snapshot", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_void_p, ctypes.c_ulonglong,
+                                         ctypes.POINTER(ctypes.c_ulonglong)]),
+    ("sph_pool_restore", ctypes.c_int, [_vp, ctypes.c_void_p, ctypes.c_ulonglong, ctypes.c_uint,
+                                        ctypes.POINTER(ctypes.c_int)]),
     ("sph_pool_last_error", ctypes.c_char_p, [_vp]),
     ("sph_server_desc_init", ctypes.c_int, [ctypes.POINTER(ServerDesc)]),
     ("sph_server_create", ctypes.c_int, [_vp, ctypes.POINTER(ServerDesc), ctypes.POINTER(_vp)]),
@@ -822,6 +826,27 @@ class Pool:
             self._check(lib().sph_pool_pair_lists(self._h, int(sid), c, o, nb, t), "sph_pool_pair_lists")
 
         return _pair_lists(call, self._n[sid][0])
+
+    def snapshot(self, sid):
+        """A resident scene's snapshot (bytes): everything its future steps
+        depend on, for sph_pool_restore."""
+        size = ctypes.c_ulonglong()
+        self._check(lib().sph_pool_snapshot(self._h, int(sid), None, 0, ctypes.byref(size)), "sph_pool_snapshot")
+        buf = ctypes.create_string_buffer(size.value)
+        self._check(lib().sph_pool_snapshot(self._h, int(sid), buf, size.value, ctypes.byref(size)), "sph_pool_snapshot")
+        return buf.raw
+
+    def restore(self, snap, steps=0):
+        """Admit a scene from a snapshot; `steps` more steps (0: the steps it
+        had left).  Returns its scene id."""
+        buf = ctypes.create_string_buffer(bytes(snap), len(snap))
+        sid = ctypes.c_int()
+        self._check(lib().sph_pool_restore(self._h, buf, len(snap), int(steps), ctypes.byref(sid)), "sph_pool_restore")
+        import struct
+        # header: magic[8], version, desc_size, scalars_size, n, nb, steps_left (uint32)
+        n, nb = struct.unpack_from("<II", bytes(snap), 20)
+        self._n[sid.value] = (n, nb)
+        return sid.value
 
     def count_work(self):
         """The list build's work at the current positions: candidates its walks

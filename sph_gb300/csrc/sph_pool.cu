@@ -592,12 +592,41 @@ struct PoolEntry {
     sph_scene_desc d{};
     bool staged = false;          // points (x, v, boundary) in the staging arena until resident
     size_t ox = 0, ov = 0, ob = 0;  // their offsets there
+    bool restored = false;        // staged from a snapshot: raw device arrays at ox, solver scalars
+    DevScalars snap_s{};
     unsigned n = 0, nb = 0, steps = 0;
     GridPlan plan;
     PoolScene t{};                // last known device entry (layout fields kept by the host)
     bool resident = false;
     bool removed = false;
 };
+
+// A scene snapshot: this header, then the scene's device arrays as stored
+// (sorted order; cell-relative FP32 positions with their packed cells), each
+// starting on a 16-byte boundary.
+struct SnapHeader {
+    char magic[8];          // "SPHPSNP1"
+    uint32_t version, desc_size, scalars_size, n, nb, steps_left;
+    int32_t o[3], nn[3];    // the scene's grid box
+    uint64_t bytes;         // header and arrays
+    sph_scene_desc d;
+    DevScalars s;
+};
+constexpr uint32_t kSnapVersion = 1;
+
+// Byte offsets of the raw arrays after the header: fluid pos, vel (16 B
+// each), kappa, kappav, pred, cell, id (4 B), boundary pos (16 B), cell, id
+// (4 B).  out[10] = total bytes of the arrays.
+inline void snap_layout(size_t n, size_t nb, size_t out[11])
+{
+    const size_t sz[10] = {16 * n, 16 * n, 4 * n, 4 * n, 4 * n, 4 * n, 4 * n, 16 * nb, 4 * nb, 4 * nb};
+    size_t off = 0;
+    for (int k = 0; k < 10; ++k) {
+        out[k] = off;
+        off += (sz[k] + 15) / 16 * 16;
+    }
+    out[10] = off;
+}
 
 class Pool {
 public:
@@ -705,16 +734,7 @@ public:
         // the pool's stream meanwhile is not waited for); the copy is complete
         // when this returns, so the caller may reuse its arrays
         const size_t nx = 3 * (size_t)n, nbv = 3 * (size_t)nb, need = 2 * nx + nbv;
-        if (arena_used_ + need > arena_.n) {
-            // grow (doubling): the pending scenes' points move to the new arena
-            DevBuf<double> bigger;
-            SPH_CUDA(bigger.alloc(std::max(arena_used_ + need, 2 * arena_.n)));
-            if (arena_used_)
-                SPH_CUDA(cudaMemcpyAsync(bigger.p, arena_.p, arena_used_ * sizeof(double), cudaMemcpyDeviceToDevice, up_));
-            SPH_CUDA(cudaStreamSynchronize(up_));
-            std::swap(arena_.p, bigger.p);
-            std::swap(arena_.n, bigger.n);
-        }
+        if (int grc = reserve_arena(need)) return grc;
         e.ox = arena_used_;
         e.ov = e.ox + nx;
         e.ob = e.ov + nx;
@@ -760,6 +780,112 @@ public:
         }
         arena_used_ += need;
         e.staged = true;
+        e.id = next_id_++;
+        *id = e.id;
+        entries_.push_back(std::move(e));
+        dirty_ = true;
+        return SPH_OK;
+    }
+
+    // Room for `need` more doubles in the staging arena (grows by doubling;
+    // the pending scenes' data moves to the new arena).
+    int reserve_arena(size_t need)
+    {
+        if (arena_used_ + need <= arena_.n) return SPH_OK;
+        DevBuf<double> bigger;
+        SPH_CUDA(bigger.alloc(std::max(arena_used_ + need, 2 * arena_.n)));
+        if (arena_used_)
+            SPH_CUDA(cudaMemcpyAsync(bigger.p, arena_.p, arena_used_ * sizeof(double), cudaMemcpyDeviceToDevice, up_));
+        SPH_CUDA(cudaStreamSynchronize(up_));
+        std::swap(arena_.p, bigger.p);
+        std::swap(arena_.n, bigger.n);
+        return SPH_OK;
+    }
+
+    // A resident scene's snapshot (see sph_pool_snapshot).
+    int snapshot(int id, void* buf, unsigned long long cap, unsigned long long* size)
+    {
+        PoolEntry* e = find(id);
+        if (!e || !e->resident) { fail("scene is not resident"); return SPH_ERR_INVALID; }
+        size_t L[11];
+        snap_layout(e->n, e->nb, L);
+        const size_t need = sizeof(SnapHeader) + L[10];
+        *size = need;
+        if (!buf) return SPH_OK;
+        if (cap < need) { fail("snapshot buffer too small"); return SPH_ERR_CAPACITY; }
+        SPH_CUDA(cudaStreamSynchronize(st_));
+        PoolScene t;
+        SPH_CUDA(cudaMemcpy(&t, table_.p + slot_of(id), sizeof t, cudaMemcpyDeviceToHost));
+        SnapHeader h;
+        std::memset(&h, 0, sizeof h);
+        std::memcpy(h.magic, "SPHPSNP1", 8);
+        h.version = kSnapVersion;
+        h.desc_size = sizeof(sph_scene_desc);
+        h.scalars_size = sizeof(DevScalars);
+        h.n = e->n;
+        h.nb = e->nb;
+        h.steps_left = t.steps_left;
+        for (int k = 0; k < 3; ++k) { h.o[k] = e->plan.o[k]; h.nn[k] = e->plan.nn[k]; }
+        h.bytes = need;
+        h.d = e->d;
+        h.s = t.s;
+        char* out = static_cast<char*>(buf);
+        std::memcpy(out, &h, sizeof h);
+        char* a = out + sizeof h;
+        const size_t n = e->n, nb = e->nb, pb = t.pbase, bb = t.bbase;
+        const void* src[10] = {pos_[cur_].p + pb, vel_[cur_].p + pb, kappa_[cur_].p + pb, kappav_[cur_].p + pb,
+                               pred_[cur_].p + pb, cell_[cur_].p + pb, id_[cur_].p + pb, bpos_[bcur_].p + bb,
+                               bcell_[bcur_].p + bb, bid_[bcur_].p + bb};
+        const size_t sz[10] = {16 * n, 16 * n, 4 * n, 4 * n, 4 * n, 4 * n, 4 * n, 16 * nb, 4 * nb, 4 * nb};
+        for (int k = 0; k < 10; ++k)
+            if (sz[k]) SPH_CUDA(cudaMemcpyAsync(a + L[k], src[k], sz[k], cudaMemcpyDeviceToHost, st_));
+        SPH_CUDA(cudaStreamSynchronize(st_));
+        return SPH_OK;
+    }
+
+    // A scene admitted from a snapshot (see sph_pool_restore).
+    int restore(const void* buf, unsigned long long size, unsigned steps, int* id)
+    {
+        SnapHeader h;
+        if (!buf || size < sizeof h) { fail("not a scene snapshot (too short)"); return SPH_ERR_INVALID; }
+        std::memcpy(&h, buf, sizeof h);
+        if (std::memcmp(h.magic, "SPHPSNP1", 8) != 0 || h.version != kSnapVersion || h.desc_size != sizeof(sph_scene_desc) ||
+            h.scalars_size != sizeof(DevScalars)) {
+            fail("not a scene snapshot of this library version");
+            return SPH_ERR_INVALID;
+        }
+        size_t L[11];
+        snap_layout(h.n, h.nb, L);
+        if (h.n == 0 || h.bytes != size || size != sizeof h + L[10]) { fail("scene snapshot of the wrong size"); return SPH_ERR_INVALID; }
+        PoolEntry e;
+        e.d = h.d;
+        e.n = h.n;
+        e.nb = h.nb;
+        e.steps = steps ? steps : h.steps_left;
+        double hh, mass;
+        scene_constants<float>(e.d, &e.t.c, &e.t.lim, &hh, &mass);
+        int rc = grid_plan_box(h.o, h.nn, &e.plan, &err);
+        if (rc) return rc;
+        uint64_t P = 0, B = 0, K = 0;
+        unsigned S = 0;
+        for (auto& q : entries_) {
+            if (q.removed) continue;
+            P += q.n; B += q.nb; K += q.plan.nkeys; ++S;
+        }
+        if (P + e.n > pd_.max_particles || B + e.nb > pd_.max_boundary || K + e.plan.nkeys > pd_.max_keys ||
+            S + 1 > pd_.max_scenes) {
+            fail("pool full");
+            return SPH_ERR_CAPACITY;
+        }
+        const size_t need = (L[10] + 7) / 8;
+        if (int grc = reserve_arena(need)) return grc;
+        e.ox = arena_used_;
+        SPH_CUDA(cudaMemcpyAsync(arena_.p + e.ox, static_cast<const char*>(buf) + sizeof h, L[10], cudaMemcpyHostToDevice, up_));
+        SPH_CUDA(cudaStreamSynchronize(up_));
+        arena_used_ += need;
+        e.staged = true;
+        e.restored = true;
+        e.snap_s = h.s;
         e.id = next_id_++;
         *id = e.id;
         entries_.push_back(std::move(e));
@@ -1427,7 +1553,17 @@ private:
         for (size_t s = 0; s < order.size(); ++s) {
             PoolEntry* e = order[s];
             PoolScene t = e->t;
-            if (!e->resident) {
+            if (!e->resident && e->restored) {
+                t.s = e->snap_s;
+                t.s.block_counter = 0;
+                t.acc = 0;
+                t.steps_left = e->steps;
+                t.running = e->steps > 0;
+                t.loop_active = 0;
+                t.vmax_bits = 0;
+                t.bad = 0;
+                t.akinci = 1;
+            } else if (!e->resident) {
                 t.s = DevScalars{};
                 t.s.dt = e->d.time_step;
                 t.acc = 0;
@@ -1452,6 +1588,25 @@ private:
         // (one wait for all of them); the arena is then free again
         for (size_t s = keep.size(); s < order.size(); ++s) {
             PoolEntry* e = order[s];
+            if (e->restored) {
+                // the snapshot's arrays as they were stored
+                size_t L[11];
+                snap_layout(e->n, e->nb, L);
+                const char* a = reinterpret_cast<const char*>(arena_.p + e->ox);
+                const size_t n = e->n, nb = e->nb;
+                void* dst[10] = {pos_[nc].p + pb[s], vel_[nc].p + pb[s], kappa_[nc].p + pb[s], kappav_[nc].p + pb[s],
+                                 pred_[nc].p + pb[s], cell_[nc].p + pb[s], id_[nc].p + pb[s], bpos_[nbc].p + bb[s],
+                                 bcell_[nbc].p + bb[s], bid_[nbc].p + bb[s]};
+                const size_t sz[10] = {16 * n, 16 * n, 4 * n, 4 * n, 4 * n, 4 * n, 4 * n, 16 * nb, 4 * nb, 4 * nb};
+                for (int k = 0; k < 10; ++k)
+                    if (sz[k]) SPH_CUDA(cudaMemcpyAsync(dst[k], a + L[k], sz[k], cudaMemcpyDeviceToDevice, st_));
+                SPH_CUDA(cudaMemsetAsync(acc_.p + pb[s], 0, n * sizeof(P4<float>), st_));
+                SPH_CUDA(cudaMemsetAsync(press_.p + pb[s], 0, n * sizeof(float), st_));
+                e->staged = false;
+                e->restored = false;
+                e->resident = true;
+                continue;
+            }
             Fluid<float> f = F(nc);
             f.pos += pb[s]; f.vel += pb[s]; f.kappa += pb[s]; f.kappav += pb[s]; f.cell += pb[s]; f.id += pb[s];
             f.acc += pb[s]; f.press += pb[s];
@@ -1885,6 +2040,20 @@ int sph_pool_pair_lists(sph_pool* p, int scene_id, int* count, int* off, int* nb
     if (!p || (nbr && !off)) return pool_bad(p, "invalid argument");
     PoolLock lock(p);
     return p->pool.pair_lists(scene_id, count, off, nbr, total);
+}
+
+int sph_pool_snapshot(sph_pool* p, int scene_id, void* buf, unsigned long long capacity, unsigned long long* size)
+{
+    if (!p || !size) return pool_bad(p, "invalid argument");
+    PoolLock lock(p);
+    return p->pool.snapshot(scene_id, buf, capacity, size);
+}
+
+int sph_pool_restore(sph_pool* p, const void* buf, unsigned long long size, unsigned steps, int* scene_id)
+{
+    if (!p || !buf || !scene_id) return pool_bad(p, "invalid argument");
+    PoolLock lock(p);
+    return p->pool.restore(buf, size, steps, scene_id);
 }
 
 int sph_pool_usage(sph_pool* p, unsigned long long* particles, unsigned long long* boundary, unsigned long long* keys,

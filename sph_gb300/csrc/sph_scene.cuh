@@ -117,6 +117,44 @@ struct GridPlan {
 };
 
 // cover_points: a given domain is widened to hold every point too.
+// The dense cell box with origin cell o and nn cells per axis: its column
+// Morton tables and key count (the part of a plan that follows from the box).
+inline int grid_plan_box(const int o[3], const int nn[3], GridPlan* out, std::string* err)
+{
+    GridPlan p;
+    for (int k = 0; k < 3; ++k) { p.o[k] = o[k]; p.nn[k] = nn[k]; }
+    if (p.nn[0] > 2048 || p.nn[1] > 2048 || p.nn[2] > 1024 || p.nn[0] < 1 || p.nn[1] < 1 || p.nn[2] < 1) {
+        *err = "grid box too large for the cell packing (max 2048 x 2048 x 1024 cells)";
+        return SPH_ERR_CAPACITY;
+    }
+    int bx = 0, by = 0;
+    while ((1 << bx) < p.nn[0]) ++bx;
+    while ((1 << by) < p.nn[1]) ++by;
+    p.mx.assign(p.nn[0], 0u);
+    p.my.assign(p.nn[1], 0u);
+    // interleave bit k of x and y (x first) while both have bits left
+    int pos = 0;
+    std::vector<int> px(bx), py(by);
+    for (int k = 0; k < std::max(bx, by); ++k) {
+        if (k < bx) px[k] = pos++;
+        if (k < by) py[k] = pos++;
+    }
+    for (int v = 0; v < p.nn[0]; ++v) {
+        uint32_t m = 0;
+        for (int k = 0; k < bx; ++k) if (v >> k & 1) m |= 1u << px[k];
+        p.mx[v] = m;
+    }
+    for (int v = 0; v < p.nn[1]; ++v) {
+        uint32_t m = 0;
+        for (int k = 0; k < by; ++k) if (v >> k & 1) m |= 1u << py[k];
+        p.my[v] = m;
+    }
+    p.nkeys = (1ull << (bx + by)) * (uint64_t)p.nn[2];
+    if (p.nkeys > (1ull << 30)) { *err = "grid key space too large"; return SPH_ERR_CAPACITY; }
+    *out = std::move(p);
+    return SPH_OK;
+}
+
 // A set of points, xyz per point (n doubles).
 struct PointSpan {
     const double* p;
@@ -173,41 +211,12 @@ inline int grid_plan(const sph_scene_desc& d, PointSpan hx, PointSpan hb, bool a
         *err = "no point with finite coordinates to place the grid box";
         return SPH_ERR_INVALID;
     }
-    GridPlan p;
+    int o[3], nn[3];
     for (int k = 0; k < 3; ++k) {
-        p.o[k] = (int)std::floor(lo[k] / h) - 2;
-        p.nn[k] = (int)std::floor(hi[k] / h) + 3 - p.o[k];
+        o[k] = (int)std::floor(lo[k] / h) - 2;
+        nn[k] = (int)std::floor(hi[k] / h) + 3 - o[k];
     }
-    if (p.nn[0] > 2048 || p.nn[1] > 2048 || p.nn[2] > 1024 || p.nn[0] < 1 || p.nn[1] < 1 || p.nn[2] < 1) {
-        *err = "grid box too large for the cell packing (max 2048 x 2048 x 1024 cells)";
-        return SPH_ERR_CAPACITY;
-    }
-    int bx = 0, by = 0;
-    while ((1 << bx) < p.nn[0]) ++bx;
-    while ((1 << by) < p.nn[1]) ++by;
-    p.mx.assign(p.nn[0], 0u);
-    p.my.assign(p.nn[1], 0u);
-    // interleave bit k of x and y (x first) while both have bits left
-    int pos = 0;
-    std::vector<int> px(bx), py(by);
-    for (int k = 0; k < std::max(bx, by); ++k) {
-        if (k < bx) px[k] = pos++;
-        if (k < by) py[k] = pos++;
-    }
-    for (int v = 0; v < p.nn[0]; ++v) {
-        uint32_t m = 0;
-        for (int k = 0; k < bx; ++k) if (v >> k & 1) m |= 1u << px[k];
-        p.mx[v] = m;
-    }
-    for (int v = 0; v < p.nn[1]; ++v) {
-        uint32_t m = 0;
-        for (int k = 0; k < by; ++k) if (v >> k & 1) m |= 1u << py[k];
-        p.my[v] = m;
-    }
-    p.nkeys = (1ull << (bx + by)) * (uint64_t)p.nn[2];
-    if (p.nkeys > (1ull << 30)) { *err = "grid key space too large"; return SPH_ERR_CAPACITY; }
-    *out = std::move(p);
-    return SPH_OK;
+    return grid_plan_box(o, nn, out, err);
 }
 
 template <typename T> struct DevBuf {
