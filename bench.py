@@ -392,6 +392,41 @@ def run_dam_break(args):
     return out
 
 
+def run_drop(args, r=0.00275):
+    """The PCISPH drop at r = 2.75 mm (489,771 fluid particles: a 9-layer
+    pool and an R = 0.2 m sphere 0.6 m above it; 198,746 Akinci points),
+    plain solver in graph mode, standard viscosity, Akinci surface tension
+    and adhesion; L2 flushed between timed steps."""
+    import torch
+
+    import sph_gb300
+    from sph_gb300 import workloads
+
+    x, b, params, _ = workloads.pcisph_drop(r)
+    s = sph_gb300.Scene(neighbor_list_max=args.list_max, **dict(params, precision="f32"))
+    s.set_fluid(x)
+    s.add_boundary_points(b)
+    s.init()
+    s.set_graph(True)
+    s.step(max(3, args.warmup))
+    s.synchronize()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
+    st0 = s.stats()
+    ms = 0.0
+    K = args.drop_steps
+    for _ in range(K):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        ms += s.step_timed(1)
+    st1 = s.stats()
+    out = dict(value=s.n * K / (ms / 1000.0), unit="particle-steps/s", ms_per_step=ms / K, steps=K,
+               fluid_particles=s.n, boundary_particles=s.nb, radius=r, dt=params["dt"],
+               mean_pressure_iterations=(st1["sum_iterations"] - st0["sum_iterations"]) / K,
+               status=st1["status"], l2="flushed between timed steps (256 MB write)")
+    s.close()
+    return out
+
+
 def run_e2e(scenes, args):
     """The mix through the pool's C ABI with host buffers, all of it timed:
     pool creation, upload of every scene from pinned host memory, W + K steps
@@ -453,7 +488,7 @@ def stream_mean_work(r=0.01):
     return en * 1100.0
 
 
-def flat_served(plain, served, dam):
+def flat_served(plain, served, dam, drop=None):
     """The metric's served half and the plain-GPU comparison as scalar config
     keys (a record that keeps only flat keys still carries them)."""
     out = {}
@@ -469,6 +504,9 @@ def flat_served(plain, served, dam):
     if dam:
         out["dam_break_125k_pss"] = dam["value"]
         out["dam_break_125k_ms_per_step"] = dam["ms_per_step"]
+    if drop:
+        out["pcisph_drop_490k_pss"] = drop["value"]
+        out["pcisph_drop_490k_ms_per_step"] = drop["ms_per_step"]
     return out
 
 
@@ -632,6 +670,7 @@ def main():
     ap.add_argument("--profile-steps", type=int, default=10, help="host-driven steps timed per kernel")
     ap.add_argument("--plain-steps", type=int, default=0, help="timed steps per scene for the plain arm (0: --steps)")
     ap.add_argument("--dam-steps", type=int, default=500)
+    ap.add_argument("--drop-steps", type=int, default=1000, help="timed steps of the 490k PCISPH drop")
     ap.add_argument("--serve-seconds", type=float, default=30.0)
     ap.add_argument("--serve-budget-gb", type=float, default=80.0)
     ap.add_argument("--epoch-steps", type=int, default=10)
@@ -639,6 +678,7 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-dam", action="store_true")
+    ap.add_argument("--no-drop", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=25.0, help="seconds of CPU baseline work")
     ap.add_argument("--ref-budget", type=float, default=90.0, help="seconds of reference-arm timed work")
@@ -673,6 +713,7 @@ def main():
 
     plain = None if args.no_plain else run_plain(scenes, args)
     dam = None if args.no_dam else run_dam_break(args)
+    drop = None if args.no_drop else run_drop(args)
     e2e = None if args.no_e2e else run_e2e(scenes, args)
     if e2e is not None:
         e2e["value"] = world * e2e["value"] * e2e["wall_s"] / dist_max(e2e["wall_s"], world)
@@ -712,8 +753,8 @@ def main():
                        "list_overflow": B["overflow"], "scenes_finished_early": B["finished_early"],
                        "plain_gpu": plain,
                        "batched_over_plain": value / plain["value"] if plain else None,
-                       "served": served, "dam_break_125k": dam,
-                       **flat_served(plain, served, dam),
+                       "served": served, "dam_break_125k": dam, "pcisph_drop_490k": drop,
+                       **flat_served(plain, served, dam, drop),
                        "wall_s": time.perf_counter() - wall0},
             "roofline": roof,
             "clocks": B["clocks"],

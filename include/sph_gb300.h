@@ -322,6 +322,15 @@ int sph_ctx_get_launch_count(sph_ctx* ctx, unsigned long long* out);
  * launches since the previous call and returns the text length. */
 int sph_ctx_set_profiling(sph_ctx* ctx, int enable);
 int sph_ctx_get_profile(sph_ctx* ctx, char* buf, unsigned long long len);
+/* Step phases under the reference's phase-timer names
+ * (Simulation::startCounting/stopCounting: DFSPHSolver.cpp:43-101,
+ * PCISPHSolver.cpp:26-67, WCSPHSolver.cpp:20-64, "Step computation"
+ * Simulation.cpp:158; fused phases join the names with '+').  Every phase is
+ * an NVTX range; with profiling on, sph_ctx_get_phase_profile writes
+ * "name<TAB>count<TAB>total_ms" lines for the phases timed (CUDA events)
+ * since the previous call and returns the text length.  A graph step is one
+ * "Step computation" phase. */
+int sph_ctx_get_phase_profile(sph_ctx* ctx, char* buf, unsigned long long len);
 
 /* cudaSetDevice for the calling thread; contexts created afterwards live on
  * that device. */
@@ -386,6 +395,8 @@ int sph_pool_step_timed(sph_pool* pool, int nsteps, float* elapsed_ms);
  * "name launches total_ms" lines (as sph_ctx_get_profile). */
 int sph_pool_set_profiling(sph_pool* pool, int enable);
 int sph_pool_get_profile(sph_pool* pool, char* buf, unsigned long long len);
+/* As sph_ctx_get_phase_profile, for the pool's steps (relayouts excluded). */
+int sph_pool_get_phase_profile(sph_pool* pool, char* buf, unsigned long long len);
 /* Launch shapes of the pool's hot kernels.  Results do not depend on them. */
 typedef struct sph_pool_tuning {
     int build_block;      /* pair-list build: threads per block and threads per SM */

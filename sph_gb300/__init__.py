@@ -38,6 +38,19 @@ FIELDS = {
 STATUS_OUT_OF_GRID, STATUS_NONFINITE, STATUS_ITER_CAP, STATUS_ITER_CAP_V, STATUS_DIVERGED = 1, 2, 4, 8, 16
 
 
+def _phases(fn, handle, check, what):
+    """Parse "name<TAB>count<TAB>total_ms" lines of a phase profile."""
+    buf = ctypes.create_string_buffer(1 << 14)
+    n = fn(handle, buf, len(buf))
+    if n < 0:
+        check(n, what)
+    out = {}
+    for line in buf.value.decode().splitlines():
+        name, cnt, ms = line.split("\t")
+        out[name] = (int(cnt), float(ms))
+    return out
+
+
 class SceneDesc(ctypes.Structure):
     _fields_ = [
         ("simulation_method", ctypes.c_int),
@@ -205,6 +218,7 @@ ABI = [
     ("sph_ctx_get_launch_count", ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_ulonglong)]),
     ("sph_ctx_set_profiling", ctypes.c_int, [_vp, ctypes.c_int]),
     ("sph_ctx_get_profile", ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_ulonglong]),
+    ("sph_ctx_get_phase_profile", ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_ulonglong]),
     ("sph_select_device", ctypes.c_int, [ctypes.c_int]),
     ("sph_sample_box", ctypes.c_longlong, [ctypes.c_double, _dp, _dp, _dp]),
     ("sph_sample_sphere", ctypes.c_longlong, [ctypes.c_double, _dp, ctypes.c_double, _dp]),
@@ -230,6 +244,7 @@ ABI = [
     ("sph_pool_step_timed", ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
     ("sph_pool_set_profiling", ctypes.c_int, [_vp, ctypes.c_int]),
     ("sph_pool_get_profile", ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_ulonglong]),
+    ("sph_pool_get_phase_profile", ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_ulonglong]),
     ("sph_pool_set_autotune", ctypes.c_int, [_vp, ctypes.c_int]),
     ("sph_pool_get_tuning", ctypes.c_int, [_vp, ctypes.POINTER(PoolTuning)]),
     ("sph_pool_set_tuning", ctypes.c_int, [_vp, ctypes.POINTER(PoolTuning)]),
@@ -546,6 +561,12 @@ class Scene:
             out[name] = (int(cnt), float(ms))
         return out
 
+    def phase_profile(self):
+        """{phase name: (count, total ms)} since the previous call, under the
+        reference's phase-timer names (profiling on, host-driven steps; a
+        graph step is one "Step computation")."""
+        return _phases(lib().sph_ctx_get_phase_profile, self._h, self._check, "sph_ctx_get_phase_profile")
+
     def neighbors(self):
         L = lib()
         tot = (ctypes.c_longlong * 2)()
@@ -784,6 +805,10 @@ class Pool:
             name, cnt, ms = line.split()
             out[name] = (int(cnt), float(ms))
         return out
+
+    def phase_profile(self):
+        """As Scene.phase_profile, for the pool's steps."""
+        return _phases(lib().sph_pool_get_phase_profile, self._h, self._check, "sph_pool_get_phase_profile")
 
     def set_autotune(self, mode=1):
         """0 off, 1 cached-or-measured after each re-layout (default), 2 measure again."""

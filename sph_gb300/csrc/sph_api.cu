@@ -633,6 +633,15 @@ int sph_ctx_get_profile(sph_ctx* ctx, char* buf, unsigned long long len)
     return n;
 }
 
+int sph_ctx_get_phase_profile(sph_ctx* ctx, char* buf, unsigned long long len)
+{
+    if (!ctx) return SPH_ERR_INVALID;
+    if (!ctx->scene->inited) return bad(ctx, "not initialised");
+    const int n = ctx->scene->phase_profile(buf, (size_t)len);
+    if (n < 0) return relay(ctx, n);
+    return n;
+}
+
 int sph_select_device(int device)
 {
     int count = 0;

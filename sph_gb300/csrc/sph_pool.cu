@@ -915,6 +915,7 @@ public:
                 if (rc) return rc;
             }
             if (S_ == 0) return SPH_OK;
+            Phase ph(phases_, "Step computation", st_, false, prof_ && tune_left_ == 0);
             const int rc = tune_left_ > 0 ? tuning_step() : graph_ ? graph_step() : one_step();
             if (rc) return rc;
         }
@@ -1142,6 +1143,17 @@ public:
         for (auto& e : gexec_) if (e) { cudaGraphExecDestroy(e); e = nullptr; }
     }
     int set_profiling(int on) { prof_ = on != 0; return SPH_OK; }
+
+    // Phase times (CUDA events, profiling on) since the last call.
+    int phase_profile(char* buf, size_t len)
+    {
+        SPH_CUDA(cudaStreamSynchronize(st_));
+        const int n = phases_.report(buf, len);
+        if (n < 0) { fail(cudaGetErrorString((cudaError_t)-n)); return SPH_ERR_CUDA; }
+        return n;
+    }
+    // a named phase of a host-driven step (nothing while capturing or tuning)
+    Phase phase(const char* name) { return Phase(phases_, name, ls_, capturing_, prof_ && counting_ && !tuning_); }
 
     // "name launches total_ms" per kernel for the host-driven steps timed
     // since the previous call.
@@ -1748,13 +1760,17 @@ private:
             Fluid<float> f = F(cur_);
             const P4<float>* bp = bpos_[bcur_].p;
             Lists<float> L = LS();
-            if (any_st_)
-                run("k_pool_st_normals", [&] { k_pool_st_normals<<<nb, kBlock, 0, ls_>>>(f, sid_.p, table_.p, starts_.p); });
-            if (any_forces_)
-                run("k_pool_npforce", [&] { k_pool_npforce<<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p); });
+            if (any_st_ || any_forces_) {
+                auto ph = phase("npForces");
+                if (any_st_)
+                    run("k_pool_st_normals", [&] { k_pool_st_normals<<<nb, kBlock, 0, ls_>>>(f, sid_.p, table_.p, starts_.p); });
+                if (any_forces_)
+                    run("k_pool_npforce", [&] { k_pool_npforce<<<nb, kBlock, 0, ls_>>>(f, bp, sid_.p, table_.p, starts_.p, bstarts_.p); });
+            }
             run("k_pool_cfl_accum", [&] { k_pool_cfl_accum<<<nb256, 256, 0, ls_>>>(f, sid_.p, table_.p); });
             run("k_pool_cfl_control", [&] { k_pool_cfl_control<<<1, 256, 0, ls_>>>(table_.p, S_); });
             run("k_pool_predict_v_warm", [&] { k_pool_predict_v_warm<<<nb256, 256, 0, ls_>>>(f, sid_.p, table_.p, L.kbuf); });
+            auto ph = phase("Density solver");
             run("k_pool_correct", [&] { launch_correct<0>(f, bp, L); });
             SPH_CUDA(cudaGetLastError());
             int rc = solve_loop(
@@ -1770,15 +1786,23 @@ private:
                 });
             if (rc) return rc;
         }
-        int rc = build_grid(true);
+        int rc;
+        {
+            auto ph = phase("Fill grid");  // with the position update fused in
+            rc = build_grid(true);
+        }
         if (rc) return rc;
         {
             Fluid<float> f = F(cur_);
             const P4<float>* bp = bpos_[bcur_].p;
             Lists<float> L = LS();
             // the build also forms the divergence solve's first error pass
-            run("k_pool_build_lists", [&] { launch_build<true>(f, bp, L); });
+            {
+                auto ph = phase("Neigh search+Densities+Alpha factor");
+                run("k_pool_build_lists", [&] { launch_build<true>(f, bp, L); });
+            }
             SPH_CUDA(cudaGetLastError());
+            auto ph = phase("Divergence solver");
             rc = solve_loop(
                 2,
                 [&](cudaGraphConditionalHandle h) {
@@ -1869,6 +1893,7 @@ private:
     unsigned long long fixed_ = 0, body_d_size_ = 0, body_v_size_ = 0, gsteps_ = 0, snap_d_ = 0, snap_v_ = 0;
     unsigned long long host_launches_ = 0, graph_launches_ = 0, host_body_d_ = 0, host_body_v_ = 0;
     bool counting_ = true, any_forces_ = false, any_st_ = false, prof_ = false, tuning_ = false;
+    PhaseLog phases_;
     Tune tune_;
     int tune_mode_ = 1, tune_source_ = 0, tune_left_ = 0, tune_step_ = 0;
     unsigned long long tune_bucket_ = 0;
@@ -2091,6 +2116,13 @@ int sph_pool_get_profile(sph_pool* p, char* buf, unsigned long long len)
     if (!p) return SPH_ERR_INVALID;
     PoolLock lock(p);
     return p->pool.profile(buf, (size_t)len);
+}
+
+int sph_pool_get_phase_profile(sph_pool* p, char* buf, unsigned long long len)
+{
+    if (!p) return SPH_ERR_INVALID;
+    PoolLock lock(p);
+    return p->pool.phase_profile(buf, (size_t)len);
 }
 
 int sph_pool_set_autotune(sph_pool* p, int mode)

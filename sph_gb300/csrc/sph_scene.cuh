@@ -23,6 +23,7 @@
 #include "sph_scene_base.h"
 #include "sph_kernels.cuh"
 #include "sph_lists.cuh"
+#include "sph_phase.cuh"
 
 namespace sph {
 
@@ -375,10 +376,9 @@ public:
                     if (rc) return rc;
                 }
             }
-            if (graph_) {
-                rc = graph_step();
-            } else {
-                rc = one_step();
+            {
+                Phase ph(phases_, "Step computation", ls_, false, prof_);
+                rc = graph_ ? graph_step() : one_step();
             }
             if (rc) return rc;
             // every kGrowthCheck steps, read the escape flag without waiting
@@ -566,6 +566,17 @@ public:
         prof_ = on != 0;
         return SPH_OK;
     }
+
+    // Phase times (CUDA events, profiling on) since the last call.
+    int phase_profile(char* buf, size_t len) override
+    {
+        SPH_CUDA(cudaStreamSynchronize(st_));
+        const int n = phases_.report(buf, len);
+        if (n < 0) { fail(cudaGetErrorString((cudaError_t)-n)); return SPH_ERR_CUDA; }
+        return n;
+    }
+    // a named phase of the host-driven step (nothing while capturing)
+    Phase phase(const char* name) { return Phase(phases_, name, ls_, capturing_, prof_); }
 
     // "name count total_ms" per kernel name, for the launches timed since the
     // last call (host-driven steps with profiling on).
@@ -1106,8 +1117,12 @@ private:
     // DFSPHSolver.cpp:65-75, then the grid build.
     int dfsph_move_and_build()
     {
-        if (!bh_ && !nem_) return build_grid(true);
+        if (!bh_ && !nem_) {
+            auto ph = phase("Fill grid");  // with the position update fused in
+            return build_grid(true);
+        }
         if (bh_) {
+            auto ph = phase("Boundary handling");
             launch_bh_after_move<true, 0, false, false>();
         } else {
             Fluid<R> f = F();
@@ -1116,6 +1131,7 @@ private:
                                                                                               nullptr, f.na); });
         }
         launch_emit();  // Simulation::emitParticles DFSPHSolver.cpp:77, before the grid fill
+        auto ph = phase("Fill grid");
         return build_grid(false);
     }
 
@@ -1175,7 +1191,11 @@ private:
     // DFSPHSolver::step DFSPHSolver.cpp:38-112 over the pair lists.
     int dfsph_step_lists()
     {
-        int rc = launch_npforces();
+        int rc = SPH_OK;
+        if (c_.force_flags) {
+            auto ph = phase("npForces");
+            rc = launch_npforces();
+        }
         if (rc) return rc;
         const unsigned nb = blocks(n_, kBlock);
         {
@@ -1185,6 +1205,7 @@ private:
             run("k_dfsph_cfl", [&] { k_dfsph_cfl<R><<<blocks(n_, 256), 256, 0, ls_>>>(f, c_, sc_.p, lim_, partials_.p); });
             run("k_dfsph_predict_v_warm", [&] { k_dfsph_predict_v_warm_list<R><<<blocks(n_, 256), 256, 0, ls_>>>(f, c_, sc_.p, L.kbuf); });
             launch_bh_velocities();
+            auto ph = phase("Density solver");
             run("k_dfsph_correct_list", [&] { k_dfsph_correct_list<R, 0><<<nb, kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, hasb_, sc_.p, L); });
             SPH_CUDA(cudaGetLastError());
             // correctDensityError DFSPHSolver.cpp:311-406
@@ -1203,14 +1224,18 @@ private:
         }
         rc = dfsph_move_and_build();  // updatePositions + fill grid + neighbour search
         if (rc) return rc;
-        rc = launch_build_lists();  // computeDensities + computeAlpha + pair lists
-        if (rc) return rc;
-        launch_bh_boundary(0);
+        {
+            auto ph = phase("Neigh search+Densities+Alpha factor");
+            rc = launch_build_lists();  // computeDensities + computeAlpha + pair lists
+            if (rc) return rc;
+            launch_bh_boundary(0);
+        }
         {
             Fluid<R> f = F();
             const P4<R>* bp = bd_[1].pos;
             Lists<R> L = LS();
             // correctDivergenceError DFSPHSolver.cpp:494-590
+            auto ph = phase("Divergence solver");
             rc = solve_loop(2,
                 [&](cudaGraphConditionalHandle h) {
                     run("k_dfsph_divergence_list", [&] { k_dfsph_divergence_list<R, true><<<nb, kBlock, 0, ls_>>>(
@@ -1223,7 +1248,11 @@ private:
                 },
                 lim_.minItV, lim_.maxIt);
             if (rc) return rc;
-            if (c_.has_cube) run("k_dfsph_cube", [&] { k_dfsph_cube<R><<<blocks(n_, 256), 256, 0, ls_>>>(f, gv_, hd_, c_); });
+        }
+        if (c_.has_cube) {
+            Fluid<R> f = F();
+            auto ph = phase("Boundary handling");
+            run("k_dfsph_cube", [&] { k_dfsph_cube<R><<<blocks(n_, 256), 256, 0, ls_>>>(f, gv_, hd_, c_); });
         }
         run("k_finish_step", [&] { k_finish_step<<<1, 1, 0, ls_>>>(sc_.p); });
         SPH_CUDA(cudaGetLastError());
@@ -1325,7 +1354,11 @@ private:
     // DFSPHSolver::step DFSPHSolver.cpp:38-112
     int dfsph_step()
     {
-        int rc = launch_npforces();
+        int rc = SPH_OK;
+        if (c_.force_flags) {
+            auto ph = phase("npForces");
+            rc = launch_npforces();
+        }
         if (rc) return rc;
         {
             Fluid<R> f = F();
@@ -1334,6 +1367,7 @@ private:
             SPH_CUDA(cudaGetLastError());
             launch_bh_velocities();
             const P4<R>* bp = bd_[1].pos;
+            auto ph = phase("Density solver");
             withG([&](auto gt) {
                 constexpr int G = decltype(gt)::value;
                 run("k_dfsph_correct", [&] { k_dfsph_correct<R, G, 0><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, hasb_, sc_.p); });
@@ -1362,13 +1396,17 @@ private:
         }
         rc = dfsph_move_and_build();  // updatePositions + fill grid + neighbour search
         if (rc) return rc;
-        rc = launch_density(true, false);  // computeDensities + computeAlpha
-        if (rc) return rc;
-        launch_bh_boundary(0);
+        {
+            auto ph = phase("Densities+Alpha factor");
+            rc = launch_density(true, false);  // computeDensities + computeAlpha
+            if (rc) return rc;
+            launch_bh_boundary(0);
+        }
         {
             Fluid<R> f = F();
             const P4<R>* bp = bd_[1].pos;
             // correctDivergenceError DFSPHSolver.cpp:494-590
+            auto ph = phase("Divergence solver");
             rc = solve_loop(2, 
                 [&](cudaGraphConditionalHandle h) {
                     withG([&](auto gt) {
@@ -1388,7 +1426,11 @@ private:
                 },
                 lim_.minItV, lim_.maxIt);
             if (rc) return rc;
-            if (c_.has_cube) run("k_dfsph_cube", [&] { k_dfsph_cube<R><<<blocks(n_, 256), 256, 0, ls_>>>(f, gv_, hd_, c_); });
+        }
+        if (c_.has_cube) {
+            Fluid<R> f = F();
+            auto ph = phase("Boundary handling");
+            run("k_dfsph_cube", [&] { k_dfsph_cube<R><<<blocks(n_, 256), 256, 0, ls_>>>(f, gv_, hd_, c_); });
         }
         run("k_finish_step", [&] { k_finish_step<<<1, 1, 0, ls_>>>(sc_.p); });
         SPH_CUDA(cudaGetLastError());
@@ -1398,23 +1440,42 @@ private:
     // WCSPHSolver::step WCSPHSolver.cpp:14-78
     int wcsph_step()
     {
-        int rc = build_grid(false);
+        int rc;
+        {
+            auto ph = phase("Fill grid");
+            rc = build_grid(false);
+        }
         if (rc) return rc;
-        rc = launch_density(false, true);
-        if (rc) return rc;
-        launch_bh_boundary(1);
+        {
+            auto ph = phase("Densities+Pressures");  // the equation of state is fused into the density pass
+            rc = launch_density(false, true);
+            if (rc) return rc;
+            launch_bh_boundary(1);
+        }
         Fluid<R> f = F();
         const P4<R>* bp = bd_[1].pos;
         const R* dp = bdp();
-        withG([&](auto gt) {
-            constexpr int G = decltype(gt)::value;
-            run("k_wcsph_pressure_force", [&] { k_wcsph_pressure_force<R, G><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, hasb_, dp); });
-        });
-        SPH_CUDA(cudaGetLastError());
-        rc = launch_npforces();
+        {
+            auto ph = phase("Pressure force");
+            withG([&](auto gt) {
+                constexpr int G = decltype(gt)::value;
+                run("k_wcsph_pressure_force", [&] { k_wcsph_pressure_force<R, G><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, hasb_, dp); });
+            });
+            SPH_CUDA(cudaGetLastError());
+        }
+        {
+            auto ph = phase("NPForces");
+            rc = launch_npforces();
+        }
         if (rc) return rc;
-        run("k_integrate", [&] { k_integrate<R, false><<<blocks(n_, 256), 256, 0, ls_>>>(f, gv_, hd_, c_, sc_.p); });
-        if (bh_) launch_bh_after_move<false, 0, true, false>();  // WCSPHSolver.cpp:62-72
+        {
+            auto ph = phase("Integratio");
+            run("k_integrate", [&] { k_integrate<R, false><<<blocks(n_, 256), 256, 0, ls_>>>(f, gv_, hd_, c_, sc_.p); });
+        }
+        if (bh_) {
+            auto ph = phase("Boundary Handling");
+            launch_bh_after_move<false, 0, true, false>();  // WCSPHSolver.cpp:62-72
+        }
         launch_emit();  // WCSPHSolver.cpp:75
         run("k_finish_step", [&] { k_finish_step<<<1, 1, 0, ls_>>>(sc_.p); });
         SPH_CUDA(cudaGetLastError());
@@ -1424,39 +1485,58 @@ private:
     // PCISPHSolver::step PCISPHSolver.cpp:21-81
     int pcisph_step()
     {
-        int rc = build_grid(false);
+        int rc;
+        {
+            auto ph = phase("Fill grid");
+            rc = build_grid(false);
+        }
         if (rc) return rc;
-        rc = launch_density(false, false);
-        if (rc) return rc;
-        launch_bh_boundary(0);
-        rc = launch_npforces();
+        {
+            auto ph = phase("Densities");
+            rc = launch_density(false, false);
+            if (rc) return rc;
+            launch_bh_boundary(0);
+        }
+        {
+            auto ph = phase("npForces");
+            rc = launch_npforces();
+        }
         if (rc) return rc;
         Fluid<R> f = F();
         const P4<R>* bp = bd_[1].pos;
         const R* dp = bdp();
-        run("k_pcisph_init", [&] { k_pcisph_init<R><<<blocks(n_, 256), 256, 0, ls_>>>(f); });
-        if (bh_ && nb_) run("k_bh_zero_pressure", [&] { k_bh_zero_pressure<R><<<blocks(nb_, 256), 256, 0, ls_>>>(B(1)); });
-        rc = solve_loop(1,
-            [&](cudaGraphConditionalHandle h) { run("k_pcisph_loop_begin", [&] { k_pcisph_loop_begin<<<1, 1, 0, ls_>>>(sc_.p, lim_, h); }); },
-            [&](cudaGraphConditionalHandle h) {
-                run("k_pcisph_predict", [&] { k_pcisph_predict<R><<<blocks(n_, 256), 256, 0, ls_>>>(f, c_, sc_.p); });
-                if (bh_)  // correctPredPositions PCISPHSolver.cpp:367-377
-                    run("k_bh_collide", [&] { k_bh_collide<R, 2><<<blocks(n_, 128), 128, 0, ls_>>>(f, B(1), gv_, bstarts_.p, c_, sc_.p,
-                                                                                              cell_epoch_.p); });
-                withG([&](auto gt) {
-                    constexpr int G = decltype(gt)::value;
-                    run("k_pcisph_density_pressure", [&] { k_pcisph_density_pressure<R, G><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_,
-                                                                                   hasb_, sc_.p, lim_, partials_.p); });
-                    launch_bh_boundary(2);
-                    run("k_pcisph_pressure_acc", [&] { k_pcisph_pressure_acc<R, G><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, hasb_,
-                                                                               sc_.p, dp); });
-                });
-                run("k_pcisph_loop_next", [&] { k_pcisph_loop_next<<<1, 1, 0, ls_>>>(sc_.p, lim_, h); });
-            },
-            lim_.minIt, lim_.maxIt);
+        {
+            auto ph = phase("Pressure solver");
+            run("k_pcisph_init", [&] { k_pcisph_init<R><<<blocks(n_, 256), 256, 0, ls_>>>(f); });
+            if (bh_ && nb_) run("k_bh_zero_pressure", [&] { k_bh_zero_pressure<R><<<blocks(nb_, 256), 256, 0, ls_>>>(B(1)); });
+            rc = solve_loop(1,
+                [&](cudaGraphConditionalHandle h) { run("k_pcisph_loop_begin", [&] { k_pcisph_loop_begin<<<1, 1, 0, ls_>>>(sc_.p, lim_, h); }); },
+                [&](cudaGraphConditionalHandle h) {
+                    run("k_pcisph_predict", [&] { k_pcisph_predict<R><<<blocks(n_, 256), 256, 0, ls_>>>(f, c_, sc_.p); });
+                    if (bh_)  // correctPredPositions PCISPHSolver.cpp:367-377
+                        run("k_bh_collide", [&] { k_bh_collide<R, 2><<<blocks(n_, 128), 128, 0, ls_>>>(f, B(1), gv_, bstarts_.p, c_, sc_.p,
+                                                                                                  cell_epoch_.p); });
+                    withG([&](auto gt) {
+                        constexpr int G = decltype(gt)::value;
+                        run("k_pcisph_density_pressure", [&] { k_pcisph_density_pressure<R, G><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_,
+                                                                                       hasb_, sc_.p, lim_, partials_.p); });
+                        launch_bh_boundary(2);
+                        run("k_pcisph_pressure_acc", [&] { k_pcisph_pressure_acc<R, G><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, hasb_,
+                                                                                   sc_.p, dp); });
+                    });
+                    run("k_pcisph_loop_next", [&] { k_pcisph_loop_next<<<1, 1, 0, ls_>>>(sc_.p, lim_, h); });
+                },
+                lim_.minIt, lim_.maxIt);
+        }
         if (rc) return rc;
-        run("k_integrate", [&] { k_integrate<R, true><<<blocks(n_, 256), 256, 0, ls_>>>(f, gv_, hd_, c_, sc_.p); });
-        if (bh_) launch_bh_after_move<false, 1, true, true>();  // PCISPHSolver.cpp:65-75
+        {
+            auto ph = phase("Integration");
+            run("k_integrate", [&] { k_integrate<R, true><<<blocks(n_, 256), 256, 0, ls_>>>(f, gv_, hd_, c_, sc_.p); });
+        }
+        if (bh_) {
+            auto ph = phase("Boundary handling");
+            launch_bh_after_move<false, 1, true, true>();  // PCISPHSolver.cpp:65-75
+        }
         launch_emit();  // PCISPHSolver.cpp:78
         run("k_finish_step", [&] { k_finish_step<<<1, 1, 0, ls_>>>(sc_.p); });
         SPH_CUDA(cudaGetLastError());
@@ -1531,6 +1611,7 @@ private:
     unsigned long long gsteps_[2] = {0, 0};
     unsigned long long launches_ = 0, graph_launches_ = 0, snap_it_ = 0, snap_itv_ = 0;
     bool prof_ = false;
+    PhaseLog phases_;
     cudaEvent_t tev_[2] = {nullptr, nullptr};
     struct Timed { const char* name; cudaEvent_t a, b; };
     std::vector<Timed> pending_;

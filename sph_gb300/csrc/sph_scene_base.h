@@ -90,6 +90,7 @@ struct SceneBase {
     virtual int launch_count(unsigned long long* out) = 0;
     virtual int set_profiling(int on) = 0;
     virtual int profile(char* buf, size_t len) = 0;
+    virtual int phase_profile(char* buf, size_t len) = 0;
     virtual unsigned nfluid() const = 0;
     virtual unsigned nboundary() const = 0;
 };

@@ -87,14 +87,16 @@ def dam_break(r=0.005, n_side=50, box=(1.5, 0.8, 0.8), steps=2000):
 
 
 def pcisph_drop(r=0.005, steps=1000):
-    """A 5-layer pool (2r off the walls, 48,020 particles at r = 5 mm) and a
-    lattice sphere of R = 0.2 m centred 0.6 m above the pool top (33,401
-    particles) in a 1 m Akinci box; PCISPH, standard viscosity 0.01, Akinci
-    surface tension 0.5 and adhesion 0.1, eta 0.001, 3-100 iterations,
-    dt = 1e-4 s."""
+    """A 0.05 m-deep pool (round(0.05 / 2r) layers, 2r off the walls) and a
+    lattice sphere of R = 0.2 m centred 0.6 m above the pool top in a 1 m
+    Akinci box; PCISPH, standard viscosity 0.01, Akinci surface tension 0.5
+    and adhesion 0.1, eta 0.001, 3-100 iterations, dt = 1e-4 s.  At r = 5 mm:
+    5 layers, 48,020 + 33,401 = 81,421 particles; at r = 2.75 mm: 9 layers,
+    291,600 + 198,171 = 489,771 particles (the 500k drop)."""
     d = 2 * r
     n = int((1.0 - 4 * r) / d)
-    pool, (pmn, pmx) = _block(r, (2 * r, 2 * r, 2 * r), (n, 5, n))
+    layers = max(1, int(round(0.05 / d)))
+    pool, (pmn, pmx) = _block(r, (2 * r, 2 * r, 2 * r), (n, layers, n))
     c = np.array([0.5, pmx[1] + 0.6, 0.5])
     R = 0.2
     cube = fluid_block(r, c - R - r, c + R + r)
