@@ -102,18 +102,29 @@ __device__ __forceinline__ uint32_t cull_half(const GridView& g, const uint32_t*
         for (uint32_t j0 = bb & ~1u; j0 < ee; j0 += 32) {
             const uint32_t nw = min(16u, (ee - j0 + 1) >> 1);
             const uint4* __restrict__ wp = posh + (j0 >> 1);
-            uint32_t bits = 0;
-#pragma unroll 2
-            for (uint32_t k = 0; k < nw; ++k) {
-                const uint4 w = __ldg(wp + k);
+            // acceptance mask of one word: 0xffff per accepted half
+            auto test = [&](const uint4 w) {
                 const __half2 ddx = __hsub2(sx, as_half2(w.x));
                 const __half2 ddy = __hsub2(sy, as_half2(w.y));
                 const __half2 dz = __habs2(__hsub2(zq, as_half2(w.z)));
                 const __half2 ddz = __hmin2(dz, __hsub2(h3, dz));
                 const __half2 r2 = __hfma2(ddz, ddz, __hfma2(ddy, ddy, __hmul2(ddx, ddx)));
-                const unsigned m = __hle2_mask(r2, thr);
-                bits |= ((m & 1u) | ((m >> 30) & 2u)) << (2 * k);
+                return __hle2_mask(r2, thr);
+            };
+            // Two words (four candidates) per iteration: bytes 0 and 2 of
+            // each mask (one per half) gathered into one word, then bit 8k+k
+            // of that word's byte k moved to bit 24+k by one multiply (the
+            // shifted copies land on distinct bits, so nothing carries).  An
+            // odd word count reads one word past the range (the buffer holds
+            // a spare word); its bits are cleared below.
+            uint32_t bits = 0;
+#pragma unroll 1
+            for (uint32_t k = 0; k < nw; k += 2) {
+                const unsigned m0 = test(__ldg(wp + k)), m1 = test(__ldg(wp + k + 1));
+                const uint32_t u = __byte_perm(m0, m1, 0x6420u) & 0x08040201u;
+                bits |= ((u * 0x01010101u) >> 24) << (2 * k);
             }
+            if (nw < 16u) bits &= (1u << (2 * nw)) - 1u;
             // the first word's low particle may precede the column's range
             // (bb odd), the last word's high one follow it (ee odd)
             if (j0 < bb) bits &= ~1u;

@@ -677,8 +677,8 @@ public:
         SPH_CUDA(press_.alloc(P)); SPH_CUDA(kbuf_.alloc(P)); SPH_CUDA(sid_.alloc(P)); SPH_CUDA(bsid_.alloc(B));
         SPH_CUDA(bpsi_.alloc(B)); SPH_CUDA(dummy4_.alloc(1)); SPH_CUDA(normal_.alloc(P));
         SPH_CUDA(pairs_.alloc(P * kmax_)); SPH_CUDA(lcount_.alloc(P)); SPH_CUDA(bgrad_.alloc(P));
-        SPH_CUDA(posh_.alloc(P / 2 + 1));  // particle pairs, the last one whole
-        SPH_CUDA(cudaMemsetAsync(posh_.p, 0, (P / 2 + 1) * sizeof(uint4), st_));
+        SPH_CUDA(posh_.alloc(P / 2 + 2));  // particle pairs, the last one whole, and a spare word for the cull
+        SPH_CUDA(cudaMemsetAsync(posh_.p, 0, (P / 2 + 2) * sizeof(uint4), st_));
         const size_t M = std::max(P, B);
         SPH_CUDA(key_.alloc(M)); SPH_CUDA(slot_.alloc(M)); SPH_CUDA(tmp_.alloc(M));
         SPH_CUDA(count_.alloc(K)); SPH_CUDA(starts_.alloc(K + 1)); SPH_CUDA(bstarts_.alloc(K + 1));

@@ -965,8 +965,8 @@ private:
         // FP32 pair lists: half-precision positions for the build's cull
         // (particle pairs, the last one whole); written by every gather
         if (lists_ && sizeof(R) == 4) {
-            SPH_CUDA(posh_.alloc(n / 2 + 1));
-            SPH_CUDA(cudaMemsetAsync(posh_.p, 0, (n / 2 + 1) * sizeof(uint4), st_));
+            SPH_CUDA(posh_.alloc(n / 2 + 2));  // a spare word past the last pair for the cull
+            SPH_CUDA(cudaMemsetAsync(posh_.p, 0, (n / 2 + 2) * sizeof(uint4), st_));
         }
         SPH_CUDA(cudaMemsetAsync(lcount_.p, 0, lcount_.n * sizeof(uint32_t), st_));
         SPH_CUDA(cudaMemsetAsync(kbuf_.p, 0, n * sizeof(R), st_));
