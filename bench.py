@@ -495,12 +495,15 @@ def flat_served(plain, served, dam, drop=None):
     if plain:
         out["plain_gpu_pss"] = plain["value"]
     if served:
-        sat, sub = served["saturated"], served["sub_saturation"]
+        sat = served["saturated"]
         out.update(served_pss_saturated=sat["particle_steps_per_s"], served_p50_s=sat["p50_latency_s"],
                    served_p99_s=sat["p99_latency_s"], served_completed=sat["completed"],
-                   served_pss_sub=sub["particle_steps_per_s"], served_p50_sub_s=sub["p50_latency_s"],
-                   served_p99_sub_s=sub["p99_latency_s"], served_completed_sub=sub["completed"],
-                   served_rate_sub_per_s=sub["rate_per_s"], served_seconds=sat.get("duration_s"))
+                   served_rejected=sat.get("rejected"), served_seconds=sat.get("duration_s"))
+        sub = served.get("sub_saturation")
+        if sub:
+            out.update(served_pss_sub=sub["particle_steps_per_s"], served_p50_sub_s=sub["p50_latency_s"],
+                       served_p99_sub_s=sub["p99_latency_s"], served_completed_sub=sub["completed"],
+                       served_rate_sub_per_s=sub["rate_per_s"])
     if dam:
         out["dam_break_125k_pss"] = dam["value"]
         out["dam_break_125k_ms_per_step"] = dam["ms_per_step"]
@@ -517,11 +520,13 @@ def run_served(args, rate, seconds, big_every):
     pool = sph_gb300.Pool(budget_bytes=int(args.serve_budget_gb * 1e9), neighbor_list_max=args.list_max)
     pool.set_graph(True)
     reqs = workloads.request_stream(rate=rate, duration=seconds, seed=7, big_every=big_every)
-    out = serve.serve(pool, reqs, seconds, epoch_steps=args.epoch_steps)
+    out = serve.serve(pool, reqs, seconds, epoch_steps=args.epoch_steps,
+                      max_queued_bytes=int(args.serve_queue_gb * 1e9))
     out.pop("request_ids", None)
     out["rate_per_s"] = rate
     out["duration_s"] = seconds
     out["budget_gb"] = args.serve_budget_gb
+    out["max_queued_gb"] = args.serve_queue_gb
     out["big_dam_break_every_s"] = big_every
     pool.close()
     return out
@@ -673,8 +678,11 @@ def main():
     ap.add_argument("--drop-steps", type=int, default=1000, help="timed steps of the 490k PCISPH drop")
     ap.add_argument("--serve-seconds", type=float, default=30.0)
     ap.add_argument("--serve-budget-gb", type=float, default=80.0)
+    ap.add_argument("--serve-queue-gb", type=float, default=16.0,
+                    help="host bytes of queued requests beyond which submissions are refused")
     ap.add_argument("--epoch-steps", type=int, default=10)
     ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--no-sub-saturation", action="store_true", help="served: only the 200 scenes/s stream")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-dam", action="store_true")
@@ -722,11 +730,10 @@ def main():
     if not args.no_served and world == 1:
         big_load = 4_000_000 * 200 / 10.0
         sub_rate = max(0.5, (0.5 * value - big_load) / stream_mean_work())
-        served = {
-            "saturated": run_served(args, 200.0, args.serve_seconds, 10.0),
-            "sub_saturation": run_served(args, round(sub_rate, 2), args.serve_seconds, 10.0),
-            "sub_saturation_rate_rule": "offered load = half the batched value, 4M dam break included",
-        }
+        served = {"saturated": run_served(args, 200.0, args.serve_seconds, 10.0)}
+        if not args.no_sub_saturation:
+            served["sub_saturation"] = run_served(args, round(sub_rate, 2), args.serve_seconds, 10.0)
+            served["sub_saturation_rate_rule"] = "offered load = half the batched value, 4M dam break included"
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

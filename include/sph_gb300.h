@@ -461,6 +461,8 @@ typedef struct sph_server_desc {
     unsigned epoch_steps;   /* pool steps between admission passes (default 10) */
     unsigned lookahead;     /* queued requests tried per admission pass (default 8) */
     int keep_results;       /* keep each completed scene's final positions and velocities (sph_server_fetch) */
+    unsigned long long max_queued_bytes;  /* host bytes of queued (not yet admitted) requests; a submission
+                                           * beyond it is rejected with SPH_ERR_CAPACITY (0: no bound) */
 } sph_server_desc;
 #define SPH_REQUEST_QUEUED 0
 #define SPH_REQUEST_RESIDENT 1
@@ -478,12 +480,16 @@ typedef struct sph_server_stats {
     double particle_steps;            /* completed scenes' plus resident scenes' steps so far, x particles */
     double particle_steps_per_s;
     double p50_latency_s, p99_latency_s, mean_latency_s;  /* over completed requests */
+    unsigned long long rejected;      /* submissions refused by max_queued_bytes */
+    unsigned long long queued_bytes;  /* host bytes held by queued requests */
 } sph_server_stats;
 int sph_server_desc_init(sph_server_desc* desc);
 int sph_server_create(sph_pool* pool, const sph_server_desc* desc, sph_server** out);
 /* Stops the driver after its current epoch (resident scenes stay in the pool). */
 int sph_server_destroy(sph_server* server);
-/* Queue a scene (the arrays are copied; the call does not wait for the GPU). */
+/* Queue a scene (the arrays are copied; the call does not wait for the GPU).
+ * SPH_ERR_CAPACITY: the queue holds max_queued_bytes already (nothing
+ * queued, no request id). */
 int sph_server_submit(sph_server* server, const sph_scene_desc* desc, const double* x, const double* v, unsigned n,
                       const double* boundary_x, unsigned nb, unsigned steps, long long* request_id);
 /* Requests completed (or failed) since the previous call, up to max. */

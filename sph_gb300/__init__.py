@@ -36,6 +36,7 @@ FIELDS = {
 }
 
 STATUS_OUT_OF_GRID, STATUS_NONFINITE, STATUS_ITER_CAP, STATUS_ITER_CAP_V, STATUS_DIVERGED = 1, 2, 4, 8, 16
+ERR_CAPACITY = -4   # SPH_ERR_CAPACITY
 
 
 def _phases(fn, handle, check, what):
@@ -138,7 +139,8 @@ class PoolTuning(ctypes.Structure):
 
 
 class ServerDesc(ctypes.Structure):
-    _fields_ = [("epoch_steps", ctypes.c_uint), ("lookahead", ctypes.c_uint), ("keep_results", ctypes.c_int)]
+    _fields_ = [("epoch_steps", ctypes.c_uint), ("lookahead", ctypes.c_uint), ("keep_results", ctypes.c_int),
+                ("max_queued_bytes", ctypes.c_ulonglong)]
 
 
 class RequestInfo(ctypes.Structure):
@@ -168,6 +170,8 @@ class ServerStats(ctypes.Structure):
         ("p50_latency_s", ctypes.c_double),
         ("p99_latency_s", ctypes.c_double),
         ("mean_latency_s", ctypes.c_double),
+        ("rejected", ctypes.c_ulonglong),
+        ("queued_bytes", ctypes.c_ulonglong),
     ]
 
 
@@ -887,11 +891,12 @@ class Server:
     admits queued scenes as capacity frees up and retires completed ones.
     While it exists, nothing else steps the pool."""
 
-    def __init__(self, pool, epoch_steps=10, lookahead=8, keep_results=False):
+    def __init__(self, pool, epoch_steps=10, lookahead=8, keep_results=False, max_queued_bytes=0):
         L = lib()
         d = ServerDesc()
         L.sph_server_desc_init(ctypes.byref(d))
         d.epoch_steps, d.lookahead, d.keep_results = int(epoch_steps), int(lookahead), int(bool(keep_results))
+        d.max_queued_bytes = int(max_queued_bytes)
         self.pool = pool
         self._h = ctypes.c_void_p()
         rc = L.sph_server_create(pool._h, ctypes.byref(d), ctypes.byref(self._h))
@@ -916,14 +921,19 @@ class Server:
             raise SPHError(f"{what} failed ({rc}): {msg.decode() if msg else ''}")
 
     def submit(self, x, v=None, boundary_points=None, steps=1, **params):
+        """Queue a scene; returns its request id, or None when the queue
+        already holds max_queued_bytes (the request is not queued)."""
         x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, 3)
         vv = None if v is None else np.ascontiguousarray(v, dtype=np.float64).reshape(-1, 3)
         b = None if boundary_points is None else np.ascontiguousarray(boundary_points, dtype=np.float64).reshape(-1, 3)
         d = make_desc(**params)
         rid = ctypes.c_longlong()
-        self._check(lib().sph_server_submit(self._h, ctypes.byref(d), _d(x), None if vv is None else _d(vv), x.shape[0],
-                                            None if b is None else _d(b), 0 if b is None else b.shape[0], int(steps),
-                                            ctypes.byref(rid)), "sph_server_submit")
+        rc = lib().sph_server_submit(self._h, ctypes.byref(d), _d(x), None if vv is None else _d(vv), x.shape[0],
+                                     None if b is None else _d(b), 0 if b is None else b.shape[0], int(steps),
+                                     ctypes.byref(rid))
+        if rc == ERR_CAPACITY:
+            return None
+        self._check(rc, "sph_server_submit")
         self._n[rid.value] = x.shape[0]
         return rid.value
 

@@ -44,6 +44,7 @@ struct Request {
     std::vector<double> x, v, b;
     unsigned n = 0, nb = 0, steps = 0;
     Clock::time_point t_submit;
+    size_t bytes() const { return (x.size() + v.size() + b.size()) * sizeof(double); }
 };
 
 struct Record {
@@ -67,7 +68,8 @@ struct sph_server {
     std::vector<long long> completed_unread;
     std::vector<double> latencies;
     long long next_id = 1;
-    unsigned long long submitted = 0, admitted = 0, completed = 0, failed = 0, epochs = 0;
+    unsigned long long submitted = 0, admitted = 0, completed = 0, failed = 0, epochs = 0, rejected = 0;
+    unsigned long long queued_bytes = 0;   // host bytes of the queued requests
     double particle_steps_done = 0.0;
     bool stop = false;
     bool driver_failed = false;
@@ -115,6 +117,7 @@ bool sph_server::admit_locked()
             ++admitted;
             any = true;
         }
+        queued_bytes -= r.bytes();
         it = queue.erase(it);
     }
     return any;
@@ -274,6 +277,12 @@ int sph_server_submit(sph_server* s, const sph_scene_desc* d, const double* x, c
             set_err(s, "the server has stopped");
             return SPH_ERR_INVALID;
         }
+        if (s->desc.max_queued_bytes && s->queued_bytes + r.bytes() > s->desc.max_queued_bytes) {
+            ++s->rejected;
+            set_err(s, "request queue full (max_queued_bytes)");
+            return SPH_ERR_CAPACITY;
+        }
+        s->queued_bytes += r.bytes();
         r.id = s->next_id++;
         Record& rec = s->records[r.id];
         rec.info.id = r.id;
@@ -366,6 +375,8 @@ int sph_server_get_stats(sph_server* s, sph_server_stats* out)
         out->completed = s->completed;
         out->failed = s->failed;
         out->queued = s->queue.size();
+        out->rejected = s->rejected;
+        out->queued_bytes = s->queued_bytes;
         out->resident = s->resident.size();
         out->epochs = s->epochs;
         out->particle_steps = s->particle_steps_done;

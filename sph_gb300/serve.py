@@ -18,12 +18,15 @@ import time
 from . import Server
 
 
-def serve(pool, requests, duration, epoch_steps=10, lookahead=8, keep_results=False):
+def serve(pool, requests, duration, epoch_steps=10, lookahead=8, keep_results=False, max_queued_bytes=0):
     """Submit the stream [(arrival_s, builder)] (builder() -> (x, boundary
     points, params, steps)) at its arrival times for `duration` seconds of
-    wall time, then stop the server.  Returns a summary dict (with the
-    server when keep_results is set, so completed results can be fetched)."""
-    srv = Server(pool, epoch_steps=epoch_steps, lookahead=lookahead, keep_results=keep_results)
+    wall time, then stop the server.  Requests refused because the queue
+    holds max_queued_bytes (0: no bound) are counted as rejected.  Returns a
+    summary dict (with the server when keep_results is set, so completed
+    results can be fetched)."""
+    srv = Server(pool, epoch_steps=epoch_steps, lookahead=lookahead, keep_results=keep_results,
+                 max_queued_bytes=max_queued_bytes)
     t0 = time.perf_counter()
     arrived = 0
     late = 0.0
@@ -37,7 +40,9 @@ def serve(pool, requests, duration, epoch_steps=10, lookahead=8, keep_results=Fa
         else:
             late = max(late, now - arrival)
         x, b, params, steps = builder()
-        ids.append(srv.submit(x, boundary_points=b, steps=steps, **params))
+        rid = srv.submit(x, boundary_points=b, steps=steps, **params)
+        if rid is not None:
+            ids.append(rid)
         arrived += 1
     rest = duration - (time.perf_counter() - t0)
     if rest > 0:
@@ -46,6 +51,7 @@ def serve(pool, requests, duration, epoch_steps=10, lookahead=8, keep_results=Fa
     out = dict(
         wall_s=st["wall_s"], arrived=arrived, admitted=st["admitted"], completed=st["completed"],
         waiting=st["queued"], resident=st["resident"], failed=st["failed"], epochs=st["epochs"],
+        rejected=st["rejected"], queued_bytes=st["queued_bytes"],
         particle_steps=st["particle_steps"], particle_steps_per_s=st["particle_steps_per_s"],
         p50_latency_s=st["p50_latency_s"] if st["completed"] else None,
         p99_latency_s=st["p99_latency_s"] if st["completed"] else None,

@@ -10,6 +10,9 @@
 //   capacity   10 such scenes with capacity 350 (three fit at once), and six
 //              scenes with 10..60 steps: residency over time, joins mid-run
 //   lookahead  small (100 steps), big, small with capacity 920: admission order
+//   backpressure  ten scenes against a queue bound of three while nothing can
+//              be admitted (capacity 0), then capacity for all of them
+#include <atomic>
 #include <chrono>
 #include <cstdio>
 #include <cstring>
@@ -26,7 +29,7 @@ struct FakeScene {
 };
 
 struct sph_pool {
-    unsigned long long capacity = 0;
+    std::atomic<unsigned long long> capacity{0};
     std::map<int, FakeScene> scenes;
     int next = 1;
     std::string err;
@@ -143,10 +146,11 @@ static void report(const char* name, sph_server* s, sph_pool* p)
     sph_server_get_stats(s, &st);
     std::printf("{\"scenario\": \"%s\", \"submitted\": %llu, \"admitted\": %llu, \"completed\": %llu, \"queued\": %llu, "
                 "\"resident\": %llu, \"particle_steps\": %.1f, \"p50\": %.6f, \"p99\": %.6f, \"max_resident\": %u, "
-                "\"max_used\": %llu, \"capacity\": %llu, \"joined_mid_run\": %d, \"order\": [",
+                "\"max_used\": %llu, \"capacity\": %llu, \"joined_mid_run\": %d, \"rejected\": %llu, "
+                "\"queued_bytes\": %llu, \"order\": [",
                 name, st.submitted, st.admitted, st.completed, st.queued, st.resident, st.particle_steps,
-                st.p50_latency_s, st.p99_latency_s, p->max_resident, p->max_used, p->capacity,
-                p->joined_mid_run ? 1 : 0);
+                st.p50_latency_s, st.p99_latency_s, p->max_resident, p->max_used, p->capacity.load(),
+                p->joined_mid_run ? 1 : 0, st.rejected, st.queued_bytes);
     for (size_t k = 0; k < p->admitted_sizes.size(); ++k)
         std::printf("%s%u", k ? ", " : "", p->admitted_sizes[k]);
     std::printf("]}\n");
@@ -177,6 +181,13 @@ int main(int argc, char** argv)
         submit(s, 50, 100, &ids);
         submit(s, 900, 10, &ids);
         submit(s, 50, 10, &ids);
+    } else if (sc == "backpressure") {
+        pool.capacity = 0;
+        sd.max_queued_bytes = 3ull * 100 * 3 * sizeof(double);
+        sph_server_create(&pool, &sd, &s);
+        for (int k = 0; k < 10; ++k) submit(s, 100, 30, &ids);
+        report("backpressure_full", s, &pool);
+        pool.capacity = 1000;
     } else {
         std::fprintf(stderr, "unknown scenario\n");
         return 2;

@@ -8,7 +8,9 @@ counts, taking a fixed wall time as a GPU epoch would.
   the work is counted exactly (particles x steps);
 * admission respects capacity, scenes join while others are mid-run
   (continuous batching);
-* the look-ahead admits a later small scene past one that does not fit.
+* the look-ahead admits a later small scene past one that does not fit;
+* a bound on queued request bytes refuses submissions beyond it (counted as
+  rejected) and the queued ones still complete.
 
 The GPU test (test_server.py) runs the same loop on the real pool."""
 import json
@@ -55,3 +57,10 @@ def test_lookahead_admits_a_later_scene_past_one_that_does_not_fit(exe):
     (out,) = run(exe, "lookahead")
     assert out["completed"] == 3
     assert out["order"] == [50, 50, 900]
+
+
+def test_queue_bound_rejects_submissions_beyond_it(exe):
+    full, out = run(exe, "backpressure")
+    assert full["submitted"] == 3 and full["rejected"] == 7 and full["queued"] == 3
+    assert full["queued_bytes"] == 3 * 100 * 3 * 8
+    assert out["completed"] == 3 and out["queued"] == 0 and out["queued_bytes"] == 0
