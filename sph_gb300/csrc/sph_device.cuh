@@ -121,6 +121,7 @@ struct DevScalars {
     unsigned grid_epoch;           // grid builds so far (cell lifetimes, PCISPH boundary model)
     unsigned n_active;             // active fluid particles (grows when emitters emit)
     unsigned escaped;              // a particle was kept in a border cell since the last grid growth
+    unsigned disp_bits;            // PCISPH: largest predicted displacement of the loop so far (float bits)
 };
 
 enum StatusBits : unsigned {

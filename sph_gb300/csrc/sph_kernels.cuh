@@ -480,6 +480,134 @@ __global__ void k_boundary_psi(Boundary<R> b, GridView g, const uint32_t* __rest
     b.pos[i].w = c.density0 * psi;
 }
 
+// ---------------------------------------------------------------------------
+// PCISPH candidate lists (one lane per particle).  The reference's PCISPH
+// sums run over the particles of the 27 cells found at the start of the step
+// (HashTable::neighborhoodSearch, HashTable.h:136-170), at the current
+// positions (densities, normals, non-pressure forces, pressure
+// accelerations) or the predicted ones (predicted densities).  The density
+// pass records, once per step, every fluid candidate of the 27 cells whose
+// current distance is within REACH = h + margin, in the walk's order, with
+// its cell offset; the later passes visit the list instead of the cells.
+// A candidate left out lies beyond h at the current positions, and beyond h
+// at the predicted ones while every predicted displacement stays below
+// margin / 2 (checked per loop iteration; otherwise the predicted-density
+// pass walks the cells): its terms are the ones the walks skip, so the sums
+// are the same, bit for bit.  A particle with more than kmax candidates
+// walks the cells.
+constexpr uint32_t kCandIdxBits = 27;
+constexpr uint32_t kCandIdxMask = (1u << kCandIdxBits) - 1u;
+
+struct CandLists {
+    const uint32_t* idx;   // kmax * n, slot-major: j | (cell offset code << 27); nullptr: no lists
+    const uint32_t* cnt;   // candidates per particle (may exceed kmax)
+    uint32_t kmax;
+    __device__ __forceinline__ bool has(uint32_t i) const { return idx && cnt[i] <= kmax; }
+};
+
+// walk<R, 1> (rolled out, cells within reach2 of the particle), passing each
+// candidate's cell offset code (dx + 1) * 9 + (dy + 1) * 3 + (dz + 1).
+template <typename R, typename F>
+__device__ __forceinline__ void walk_reach(const GridView& g, const uint32_t* __restrict__ starts, uint32_t pc, V3<R> xi,
+                                           R h, R reach2, F&& f)
+{
+    constexpr bool REL = sizeof(R) == 4;
+    const int cx = cell_x(pc), cy = cell_y(pc), cz = cell_z(pc);
+    const int z0 = cz > 0 ? cz - 1 : 0;
+    const int z1 = cz + 1 < g.nz ? cz + 1 : g.nz - 1;
+    const R ofx = REL ? xi.x : xi.x - (R)(cx + g.ox) * h;
+    const R ofy = REL ? xi.y : xi.y - (R)(cy + g.oy) * h;
+    const R ofz = REL ? xi.z : xi.z - (R)(cz + g.oz) * h;
+    const R gxm = ofx > (R)0 ? ofx * ofx : (R)0, gxp = h - ofx > (R)0 ? (h - ofx) * (h - ofx) : (R)0;
+    const R gym = ofy > (R)0 ? ofy * ofy : (R)0, gyp = h - ofy > (R)0 ? (h - ofy) * (h - ofy) : (R)0;
+    const R gzm = ofz > (R)0 ? ofz * ofz : (R)0, gzp = h - ofz > (R)0 ? (h - ofz) * (h - ofz) : (R)0;
+    const R lim = reach2 * (R)(1.0 + 1e-5);
+    const R szm = xi.z + h, sz0 = xi.z, szp = xi.z - h;
+#pragma unroll 1
+    for (int c = 0; c < 9; ++c) {
+        const int dx = c / 3 - 1, dy = c % 3 - 1;
+        const int x = cx + dx, y = cy + dy;
+        const R gxy = (dx < 0 ? gxm : (dx > 0 ? gxp : (R)0)) + (dy < 0 ? gym : (dy > 0 ? gyp : (R)0));
+        if (x < 0 || x >= g.nx || y < 0 || y >= g.ny || !(gxy <= lim)) continue;
+        const uint32_t base = (__ldg(g.mortx + x) | __ldg(g.morty + y)) * (uint32_t)g.nz;
+        const uint32_t s0 = __ldg(starts + base + z0), sm = __ldg(starts + base + cz);
+        const uint32_t sp = __ldg(starts + base + cz + 1), s1 = __ldg(starts + base + z1 + 1);
+        const uint32_t bb = gxy + gzm <= lim ? s0 : sm, ee = gxy + gzp <= lim ? s1 : sp;
+        V3<R> s = REL ? V3<R>{xi.x - (R)dx * h, xi.y - (R)dy * h, xi.z} : xi;
+#pragma unroll 1
+        for (uint32_t j = bb; j < ee; ++j) {
+            const int dz = j < sm ? -1 : (j < sp ? 0 : 1);
+            if (REL) s.z = dz < 0 ? szm : (dz == 0 ? sz0 : szp);
+            f(j, s, (uint32_t)(c * 3 + dz + 1));
+        }
+    }
+}
+
+// The listed candidates of particle i, with the same shifted position s as
+// the cell walk passes for them.
+template <typename R, typename F>
+__device__ __forceinline__ void list_visit(const CandLists& L, uint32_t n, uint32_t i, V3<R> xi, R h, F&& f)
+{
+    constexpr bool REL = sizeof(R) == 4;
+    const uint32_t cnt = L.cnt[i];
+    const R szm = xi.z + h, sz0 = xi.z, szp = xi.z - h;
+#pragma unroll 1
+    for (uint32_t k = 0; k < cnt; ++k) {
+        const uint32_t e = __ldg(L.idx + (size_t)k * n + i);
+        const uint32_t code = e >> kCandIdxBits;
+        const int dx = (int)(code / 9) - 1, dy = (int)((code / 3) % 3) - 1, dz = (int)(code % 3) - 1;
+        const V3<R> s = REL ? V3<R>{xi.x - (R)dx * h, xi.y - (R)dy * h, dz < 0 ? szm : (dz == 0 ? sz0 : szp)} : xi;
+        f(e & kCandIdxMask, s);
+    }
+}
+
+// Fluid candidates of particle i at lane LANE of G: the list (G = 1 and a
+// stored list) or the cell walk.
+template <typename R, int G, bool TRIM = true, typename F>
+__device__ __forceinline__ void fluid_visit(const CandLists& L, uint32_t n, uint32_t i, const GridView& g,
+                                            const uint32_t* __restrict__ cs, uint32_t pc, V3<R> xi, R h, int lane, F&& f)
+{
+    if (G == 1 && L.has(i)) list_visit<R>(L, n, i, xi, h, f);
+    else walk<R, G, TRIM>(g, cs, pc, xi, h, lane, f);
+}
+
+// PCISPH densities (SPHSolver::computeFluidDensities SPHSolver.cpp:44-91, as
+// k_density<R, 1, false, false>) fused with the candidate lists' build.
+template <typename R>
+__global__ void __launch_bounds__(kBlock) k_pcisph_density_lists(Fluid<R> f, const P4<R>* __restrict__ bpos, GridView g,
+                                                                 const uint32_t* __restrict__ cs,
+                                                                 const uint32_t* __restrict__ bs, Consts<R> c, int akinci,
+                                                                 R reach2, uint32_t* __restrict__ idx,
+                                                                 uint32_t* __restrict__ cnt, uint32_t kmax)
+{
+    const uint32_t i = gtid();
+    if (i >= f.count()) return;
+    const uint32_t n = f.n;
+    const V3<R> xi = xyz(f.pos[i]);
+    const uint32_t pc = f.cell[i];
+    R density = 0;
+    uint32_t m = 0;
+    walk_reach<R>(g, cs, pc, xi, c.h, reach2, [&](uint32_t j, V3<R> s, uint32_t code) {
+        const V3<R> r = s - xyz(ldg4(f.pos + j));
+        const R r2 = dot3(r, r);
+        if (r2 <= reach2) {
+            if (m < kmax) idx[(size_t)m * n + i] = j | (code << kCandIdxBits);
+            ++m;
+        }
+        if (r2 <= c.cull2) density += c.mass * cubic_W(c, sqrt(r2));
+    });
+    if (akinci)
+        walk<R, 1>(g, bs, pc, xi, c.h, 0, [&](uint32_t j, V3<R> s) {
+            const P4<R> pb = ldg4(bpos + j);
+            const V3<R> r = s - xyz(pb);
+            const R r2 = dot3(r, r);
+            if (r2 <= c.cull2) density += pb.w * cubic_W(c, sqrt(r2));
+        });
+    f.rho[i] = density;
+    f.vel[i].w = density;
+    cnt[i] = m;
+}
+
 // SPHSolver::computeFluidDensities SPHSolver.cpp:44-91, fused with
 // DFSPHSolver::computeAlpha DFSPHSolver.cpp:114-189 (ALPHA) or the Tait
 // equation of state WCSPHSolver::computeFluidPressures WCSPHSolver.cpp:80-95
@@ -596,11 +724,12 @@ __global__ void __launch_bounds__(kBlock) k_wcsph_pressure_force(Fluid<R> f, con
 // lane's part of particle i's sum (the caller adds the lanes and scales by h).
 template <typename R, int G>
 __device__ __forceinline__ V3<R> st_normal_sum(uint32_t i, int lane, const Fluid<R>& f, const GridView& g,
-                                               const uint32_t* __restrict__ cs, const Consts<R>& c)
+                                               const uint32_t* __restrict__ cs, const Consts<R>& c,
+                                               const CandLists& L = CandLists{nullptr, nullptr, 0u})
 {
     V3<R> ni = {0, 0, 0};
     const V3<R> xi = xyz(f.pos[i]);
-    walk<R, G>(g, cs, f.cell[i], xi, c.h, lane, [&](uint32_t j, V3<R> s) {
+    fluid_visit<R, G>(L, f.n, i, g, cs, f.cell[i], xi, c.h, lane, [&](uint32_t j, V3<R> s) {
         const V3<R> r = s - xyz(ldg4(f.pos + j));
         const R r2 = dot3(r, r);
         if (r2 <= c.cull2) {
@@ -612,14 +741,15 @@ __device__ __forceinline__ V3<R> st_normal_sum(uint32_t i, int lane, const Fluid
 }
 
 template <typename R, int G>
-__global__ void __launch_bounds__(kBlock) k_st_normals(Fluid<R> f, GridView g, const uint32_t* __restrict__ cs, Consts<R> c)
+__global__ void __launch_bounds__(kBlock) k_st_normals(Fluid<R> f, GridView g, const uint32_t* __restrict__ cs, Consts<R> c,
+                                                       CandLists L = CandLists{nullptr, nullptr, 0u})
 {
     const uint32_t t = gtid();
     const uint32_t i = t / G;
     const int lane = (int)(t % G);
     const bool valid = i < f.count();
     V3<R> ni = {0, 0, 0};
-    if (valid) ni = st_normal_sum<R, G>(i, lane, f, g, cs, c);
+    if (valid) ni = st_normal_sum<R, G>(i, lane, f, g, cs, c, L);
     if (G > 1) ni = group_sum3<G>(ni);
     if (!valid || lane != 0) return;
     ni = ni * ((R)1 * c.h);
@@ -642,7 +772,8 @@ template <typename R, int G>
 __device__ __forceinline__ NPForces<R> npforce_sums(uint32_t i, int lane, const Fluid<R>& f,
                                                     const P4<R>* __restrict__ bpos, const GridView& g,
                                                     const uint32_t* __restrict__ cs, const uint32_t* __restrict__ bs,
-                                                    const Consts<R>& c, int akinci, R dt)
+                                                    const Consts<R>& c, int akinci, R dt,
+                                                    const CandLists& L = CandLists{nullptr, nullptr, 0u})
 {
     const int fl = c.force_flags;
     V3<R> av = {0, 0, 0}, avb = {0, 0, 0}, ast = {0, 0, 0}, aad = {0, 0, 0};
@@ -655,7 +786,7 @@ __device__ __forceinline__ NPForces<R> npforce_sums(uint32_t i, int lane, const 
     const uint32_t pc = f.cell[i];
     const R h2 = c.h * c.h;
     if (fl & (F_XSPH | F_STD_VISC | F_ART_VISC | F_SURFACE_TENSION))
-        walk<R, G>(g, cs, pc, xi, c.h, lane, [&](uint32_t j, V3<R> s) {
+        fluid_visit<R, G>(L, f.n, i, g, cs, pc, xi, c.h, lane, [&](uint32_t j, V3<R> s) {
             const V3<R> r = s - xyz(ldg4(f.pos + j));
             const R r2 = dot3(r, r);
             if (!(r2 <= c.cull2)) return;
@@ -734,14 +865,15 @@ __device__ __forceinline__ void npforce_apply(uint32_t i, const Fluid<R>& f, con
 template <typename R, int G>
 __global__ void __launch_bounds__(kBlock) k_npforce(Fluid<R> f, const P4<R>* __restrict__ bpos, GridView g,
                                                     const uint32_t* __restrict__ cs, const uint32_t* __restrict__ bs,
-                                                    Consts<R> c, int akinci, const DevScalars* __restrict__ scr)
+                                                    Consts<R> c, int akinci, const DevScalars* __restrict__ scr,
+                                                    CandLists L = CandLists{nullptr, nullptr, 0u})
 {
     const uint32_t t = gtid();
     const uint32_t i = t / G;
     const int lane = (int)(t % G);
     const bool valid = i < f.count();
     NPForces<R> s = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-    if (valid) s = npforce_sums<R, G>(i, lane, f, bpos, g, cs, bs, c, akinci, (R)scr->dt);
+    if (valid) s = npforce_sums<R, G>(i, lane, f, bpos, g, cs, bs, c, akinci, (R)scr->dt, L);
     if (G > 1) {
         s.av = group_sum3<G>(s.av); s.avb = group_sum3<G>(s.avb); s.ast = group_sum3<G>(s.ast); s.aad = group_sum3<G>(s.aad);
     }
@@ -1096,23 +1228,47 @@ __global__ void k_pcisph_init(Fluid<R> f)
 static __global__ void k_pcisph_loop_begin(DevScalars* sc, LoopLimits lim, cudaGraphConditionalHandle cond)
 {
     sc->iterations = 0;
+    sc->disp_bits = 0u;
     sc->active = ((sc->maxDensityError > lim.maxError) || (0u < lim.minIt)) && (0u < lim.maxIt);
     if (cond) cudaGraphSetConditional(cond, sc->active);
 }
 
 // PCISPHSolver::predictVelocityAndPosition PCISPHSolver.cpp:122-149
-template <typename R>
-__global__ void k_pcisph_predict(Fluid<R> f, Consts<R> c, const DevScalars* __restrict__ sc)
+// With TRACK, also the largest |predicted - current position| of the loop
+// so far into sc->disp_bits (the candidate lists' validity).
+template <typename R, bool TRACK = false>
+__global__ void k_pcisph_predict(Fluid<R> f, Consts<R> c, DevScalars* __restrict__ sc)
 {
     if (!sc->active) return;
     const uint32_t i = gtid();
-    if (i >= f.count()) return;
-    const R dt = (R)sc->dt;
-    const P4<R> a = f.acc[i], pa = f.pacc[i], v = f.vel[i], x = f.pos[i];
-    const V3<R> acc = {(a.x + pa.x) + c.gx, (a.y + pa.y) + c.gy, (a.z + pa.z) + c.gz};
-    const P4<R> pv = {v.x + acc.x * dt, v.y + acc.y * dt, v.z + acc.z * dt, 0};
-    f.predV[i] = pv;
-    f.predR[i] = P4<R>{x.x + pv.x * dt, x.y + pv.y * dt, x.z + pv.z * dt, 0};
+    float d = 0.f;
+    if (i < f.count()) {
+        const R dt = (R)sc->dt;
+        const P4<R> a = f.acc[i], pa = f.pacc[i], v = f.vel[i], x = f.pos[i];
+        const V3<R> acc = {(a.x + pa.x) + c.gx, (a.y + pa.y) + c.gy, (a.z + pa.z) + c.gz};
+        const P4<R> pv = {v.x + acc.x * dt, v.y + acc.y * dt, v.z + acc.z * dt, 0};
+        f.predV[i] = pv;
+        const P4<R> pr = {x.x + pv.x * dt, x.y + pv.y * dt, x.z + pv.z * dt, 0};
+        f.predR[i] = pr;
+        if (TRACK) {
+            const V3<R> dd = {pr.x - x.x, pr.y - x.y, pr.z - x.z};
+            d = (float)sqrt(dot3(dd, dd));
+            if (!(d >= 0.f)) d = INFINITY;   // NaN: no list
+        }
+    }
+    if (TRACK) {
+        // block maximum, then one atomic per block (blockDim.x <= 1024)
+        __shared__ float wmax[32];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) d = fmaxf(d, __shfl_down_sync(0xffffffffu, d, o));
+        if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = d;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            float m = 0.f;
+            for (unsigned w = 0; w < (blockDim.x + 31) / 32; ++w) m = fmaxf(m, wmax[w]);
+            if (m > 0.f) atomicMax(&sc->disp_bits, __float_as_uint(m));
+        }
+    }
 }
 
 // PCISPHSolver::predictFluidDensities PCISPHSolver.cpp:164-212 (predicted
@@ -1123,7 +1279,9 @@ template <typename R, int G>
 __global__ void __launch_bounds__(kBlock) k_pcisph_density_pressure(Fluid<R> f, const P4<R>* __restrict__ bpos, GridView g,
                                                                     const uint32_t* __restrict__ cs, const uint32_t* __restrict__ bs,
                                                                     Consts<R> c, int akinci, DevScalars* sc, LoopLimits lim,
-                                                                    double* partials)
+                                                                    double* partials,
+                                                                    CandLists L = CandLists{nullptr, nullptr, 0u},
+                                                                    float margin = 0.f)
 {
     __shared__ double sh[33];
     if (!sc->active) return;
@@ -1131,11 +1289,14 @@ __global__ void __launch_bounds__(kBlock) k_pcisph_density_pressure(Fluid<R> f, 
     const uint32_t i = t / G;
     const int lane = (int)(t % G);
     const bool valid = i < f.count();
+    // the lists hold every candidate that can come within h while each
+    // predicted displacement stays below margin / 2 (10 % slack for rounding)
+    if (L.idx && !(2.f * __uint_as_float(sc->disp_bits) <= 0.9f * margin)) L.idx = nullptr;
     R density = 0;
     if (valid) {
         const V3<R> xi = xyz(f.predR[i]);
         const uint32_t pc = f.cell[i];
-        walk<R, G, false>(g, cs, pc, xi, c.h, lane, [&](uint32_t j, V3<R> s) {
+        fluid_visit<R, G, false>(L, f.n, i, g, cs, pc, xi, c.h, lane, [&](uint32_t j, V3<R> s) {
             const V3<R> r = s - xyz(ldg4(f.predR + j));
             const R r2 = dot3(r, r);
             if (r2 <= c.cull2) density += c.mass * cubic_W(c, sqrt(r2));
@@ -1176,7 +1337,8 @@ template <typename R, int G>
 __global__ void __launch_bounds__(kBlock) k_pcisph_pressure_acc(Fluid<R> f, const P4<R>* __restrict__ bpos, GridView g,
                                                                 const uint32_t* __restrict__ cs, const uint32_t* __restrict__ bs,
                                                                 Consts<R> c, int akinci, const DevScalars* __restrict__ sc,
-                                                                const R* __restrict__ bdp)
+                                                                const R* __restrict__ bdp,
+                                                                CandLists L = CandLists{nullptr, nullptr, 0u})
 {
     if (!sc->active) return;
     const uint32_t t = gtid();
@@ -1189,7 +1351,7 @@ __global__ void __launch_bounds__(kBlock) k_pcisph_pressure_acc(Fluid<R> f, cons
         const V3<R> xi = xyz(pi);
         const R dpi = pi.w;
         const uint32_t pc = f.cell[i];
-        walk<R, G>(g, cs, pc, xi, c.h, lane, [&](uint32_t j, V3<R> s) {
+        fluid_visit<R, G>(L, f.n, i, g, cs, pc, xi, c.h, lane, [&](uint32_t j, V3<R> s) {
             const P4<R> pj = ldg4(f.xk + j);
             const V3<R> r = s - xyz(pj);
             const R r2 = dot3(r, r);
