@@ -76,6 +76,9 @@ extern "C" {
 #define SPH_STATUS_DIVERGED 16u     /* pool: a particle's relative solver error exceeded 6e10 / n (n the
                                        scene's particles; 15,000 at 4M): the scene has blown up, its average
                                        error reads +Inf and its loop runs to the cap */
+#define SPH_STATUS_BOUNDS 32u       /* bounds-checked build only (libsph_gb300_checked.so, -DSPH_BOUNDS_CHECK):
+                                       a neighbour index read from a pair record or candidate list was out
+                                       of range and skipped (a pool reports it with every scene) */
 
 typedef struct sph_ctx sph_ctx;
 

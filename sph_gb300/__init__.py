@@ -36,6 +36,7 @@ FIELDS = {
 }
 
 STATUS_OUT_OF_GRID, STATUS_NONFINITE, STATUS_ITER_CAP, STATUS_ITER_CAP_V, STATUS_DIVERGED = 1, 2, 4, 8, 16
+STATUS_BOUNDS = 32  # bounds-checked build only
 ERR_CAPACITY = -4   # SPH_ERR_CAPACITY
 
 
@@ -289,12 +290,14 @@ def build(verbose: bool = False, force: bool = False) -> str:
 
 
 def lib():
-    """Load the CUDA library (raises if it is missing: no fallback)."""
+    """Load the CUDA library (raises if it is missing: no fallback).
+    SPH_GB300_LIBRARY names another build of it (the bounds-checked one)."""
     global _lib
     if _lib is None:
-        if not os.path.exists(LIB_PATH):
-            raise SPHError(f"{LIB_PATH} is missing; build it with sph_gb300.build()")
-        L = ctypes.CDLL(LIB_PATH)
+        path = os.environ.get("SPH_GB300_LIBRARY") or LIB_PATH
+        if not os.path.exists(path):
+            raise SPHError(f"{path} is missing; build it with sph_gb300.build()")
+        L = ctypes.CDLL(path)
         for name, res, args in ABI:
             fn = getattr(L, name)
             fn.restype = res

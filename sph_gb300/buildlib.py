@@ -5,6 +5,11 @@ The translation units compile in parallel and link into
 caller load.  The FP64 parity form is compiled without FMA contraction so its
 sums round as the reference's own (non-fast-math) build does; host code is
 compiled without contraction on every architecture for the same reason.
+
+``build(variant="checked")`` makes ``libsph_gb300_checked.so`` from the same
+sources with ``-DSPH_BOUNDS_CHECK``: neighbour indices read from device data
+are checked and an out-of-range one sets SPH_STATUS_BOUNDS instead of being
+read (a test build; the arithmetic is the same).
 """
 from __future__ import annotations
 
@@ -33,7 +38,10 @@ UNITS = {
     "sph_mesh.cpp": [],
     "sph_serve.cpp": [],
 }
-HEADERS = ["sph_device.cuh", "sph_kernels.cuh", "sph_lists.cuh", "sph_scene.cuh", "sph_scene_base.h", "sph_ctx.h"]
+HEADERS = ["sph_device.cuh", "sph_kernels.cuh", "sph_lists.cuh", "sph_scene.cuh", "sph_scene_base.h", "sph_ctx.h",
+           "sph_phase.cuh"]
+VARIANTS = {"": ([], OBJDIR, LIB),
+            "checked": (["-DSPH_BOUNDS_CHECK"], OBJDIR + "_checked", os.path.join(LIBDIR, "libsph_gb300_checked.so"))}
 
 
 def nvcc() -> str:
@@ -51,16 +59,17 @@ def _stale(obj: str, src: str) -> bool:
     return any(os.path.getmtime(p) > t for p in deps if os.path.exists(p))
 
 
-def build(verbose: bool = False, force: bool = False, extra: list[str] | None = None) -> str:
+def build(verbose: bool = False, force: bool = False, extra: list[str] | None = None, variant: str = "") -> str:
+    vflags, objdir, lib = VARIANTS[variant]
     os.makedirs(LIBDIR, exist_ok=True)
-    os.makedirs(OBJDIR, exist_ok=True)
+    os.makedirs(objdir, exist_ok=True)
     cc = nvcc()
     jobs = []
     for unit, flags in UNITS.items():
         src = os.path.join(CSRC, unit)
-        obj = os.path.join(OBJDIR, os.path.splitext(unit)[0] + ".o")
+        obj = os.path.join(objdir, os.path.splitext(unit)[0] + ".o")
         if force or _stale(obj, src):
-            jobs.append([cc, *COMMON, *flags, *(extra or []), "-c", src, "-o", obj])
+            jobs.append([cc, *COMMON, *flags, *vflags, *(extra or []), "-c", src, "-o", obj])
 
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -72,10 +81,10 @@ def build(verbose: bool = False, force: bool = False, extra: list[str] | None = 
 
     with cf.ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
         list(ex.map(run, jobs))
-    objs = [os.path.join(OBJDIR, os.path.splitext(u)[0] + ".o") for u in UNITS]
-    if jobs or not os.path.exists(LIB):
-        run([cc, ARCH, "-shared", "-o", LIB, *objs, "-lcudart"])
-    return LIB
+    objs = [os.path.join(objdir, os.path.splitext(u)[0] + ".o") for u in UNITS]
+    if jobs or not os.path.exists(lib):
+        run([cc, ARCH, "-shared", "-o", lib, *objs, "-lcudart"])
+    return lib
 
 
 if __name__ == "__main__":

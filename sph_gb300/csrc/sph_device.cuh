@@ -126,7 +126,19 @@ struct DevScalars {
 
 enum StatusBits : unsigned {
     ST_OUT_OF_GRID = 1u, ST_NONFINITE = 2u, ST_ITER_CAP = 4u, ST_ITER_CAP_V = 8u, ST_DIVERGED = 16u,
+    ST_BOUNDS = 32u,
 };
+
+// Index checks of the bounds-checked build (compiled with -DSPH_BOUNDS_CHECK,
+// libsph_gb300_checked.so): a neighbour index read from device data (a pair
+// record, a candidate list entry) that is not below its array's length sets
+// ST_BOUNDS in *FAULT and the access is skipped.  In the ordinary build the
+// check is the constant true and compiles away.
+#ifdef SPH_BOUNDS_CHECK
+#define SPH_INDEX_OK(j, n, fault) ((j) < (n) ? true : ((fault) ? (atomicOr((fault), ST_BOUNDS), false) : false))
+#else
+#define SPH_INDEX_OK(j, n, fault) true
+#endif
 
 // Solver limits used by the device-side loop controls.
 struct LoopLimits {

@@ -502,6 +502,7 @@ struct CandLists {
     const uint32_t* idx;   // kmax * n, slot-major: j | (cell offset code << 27); nullptr: no lists
     const uint32_t* cnt;   // candidates per particle (may exceed kmax)
     uint32_t kmax;
+    unsigned* fault;       // status word of the bounds-checked build (SPH_INDEX_OK)
     __device__ __forceinline__ bool has(uint32_t i) const { return idx && cnt[i] <= kmax; }
 };
 
@@ -557,7 +558,9 @@ __device__ __forceinline__ void list_visit(const CandLists& L, uint32_t n, uint3
         const uint32_t code = e >> kCandIdxBits;
         const int dx = (int)(code / 9) - 1, dy = (int)((code / 3) % 3) - 1, dz = (int)(code % 3) - 1;
         const V3<R> s = REL ? V3<R>{xi.x - (R)dx * h, xi.y - (R)dy * h, dz < 0 ? szm : (dz == 0 ? sz0 : szp)} : xi;
-        f(e & kCandIdxMask, s);
+        const uint32_t j = e & kCandIdxMask;
+        if (!SPH_INDEX_OK(j, n, L.fault)) continue;
+        f(j, s);
     }
 }
 

@@ -40,6 +40,7 @@ template <typename R> struct Lists {
     // the build's cull, two particles per 16-byte word ({x, y, z, unused}
     // half2 pairs, z in the cell's modulo-3 frame), or nullptr
     const uint4* posh;
+    unsigned* fault;    // status word of the bounds-checked build (SPH_INDEX_OK)
 };
 
 // Phase 1 of the FP32 list build from the half-precision positions: the
@@ -224,7 +225,9 @@ __device__ __noinline__ R reread_div(const Fluid<R>& f, const Lists<R>& L, uint3
     R dv = 0;
     for (uint32_t k = 0; k < cnt; ++k) {
         const P4<R> pr = L.pairs[(size_t)k * n + i];
-        dv += dot3(vi - xyz(f.vel[as_idx(pr.w)]), xyz(pr));
+        const uint32_t j = as_idx(pr.w);
+        if (!SPH_INDEX_OK(j, n, L.fault)) continue;
+        dv += dot3(vi - xyz(f.vel[j]), xyz(pr));
     }
     return dv;
 }
@@ -442,7 +445,9 @@ __device__ __forceinline__ V3<R> correct_sum_one(uint32_t i, const Fluid<R>& f, 
 #pragma unroll 8
         for (uint32_t k = 0; k < cnt; ++k) {
             const P4<R> q = ldcs4(p + (size_t)k * n);
-            const R kSum = ki + __ldg(kb_ + as_idx(q.w));
+            const uint32_t j = as_idx(q.w);
+            if (!SPH_INDEX_OK(j, n, L.fault)) continue;
+            const R kSum = ki + __ldg(kb_ + j);
             if (fabs(kSum) > c.eps) sum = sum + kSum * xyz(q);
         }
         const R kb = MODE == 0 ? c.bwarm * ki : ki;
@@ -491,7 +496,9 @@ __device__ __forceinline__ R velocity_div_list(const Fluid<R>& f, const Lists<R>
 #pragma unroll 8
     for (uint32_t k = 0; k < cnt; ++k) {
         const P4<R> q = ldcs4(p + (size_t)k * n);
-        d += dot3(vi - xyz(ldg4(f.vel + as_idx(q.w))), xyz(q));
+        const uint32_t j = as_idx(q.w);
+        if (!SPH_INDEX_OK(j, n, L.fault)) continue;
+        d += dot3(vi - xyz(ldg4(f.vel + j)), xyz(q));
     }
     if (akinci) d += dot3(vi, xyz(L.bgrad[i]));
     return d;

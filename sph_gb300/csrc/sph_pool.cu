@@ -68,7 +68,7 @@ struct PoolScene {
 
 struct PoolCounters {
     unsigned any;                       // some scene's loop is active
-    unsigned pad;
+    unsigned faults;                    // ST_BOUNDS of the bounds-checked build (any scene)
     unsigned long long body_d, body_v;  // loop bodies executed (density / divergence)
 };
 
@@ -1263,6 +1263,12 @@ public:
         out->time = s.time; out->dt = s.dt; out->avg_density_error = s.avgDensError;
         out->avg_divergence_error = s.avgDivError; out->max_velocity = s.maxVel; out->iterations = s.iterations;
         out->iterations_v = s.iterationsV; out->steps = s.steps; out->status = s.status;
+#ifdef SPH_BOUNDS_CHECK
+        // a bad index in any scene's list is reported with every scene
+        unsigned faults = 0u;
+        SPH_CUDA(cudaMemcpy(&faults, &pc_.p->faults, sizeof faults, cudaMemcpyDeviceToHost));
+        out->status |= faults;
+#endif
         out->sum_iterations = s.sumIterations; out->sum_iterations_v = s.sumIterationsV;
         out->num_fluid = t.n; out->num_boundary = t.nb;
         if (done) *done = t.running ? 0 : 1;
@@ -1404,7 +1410,7 @@ private:
     Boundary<float> B(int k) const { return Boundary<float>{bpos_[k].p, bpsi_.p, bcell_[k].p, bid_[k].p, NB_}; }
     Lists<float> LS() const
     {
-        return Lists<float>{pairs_.p, lcount_.p, bgrad_.p, kbuf_.p, kmax_, posh_.p};
+        return Lists<float>{pairs_.p, lcount_.p, bgrad_.p, kbuf_.p, kmax_, posh_.p, &pc_.p->faults};
     }
 
     int scan(uint32_t* out)

@@ -850,7 +850,7 @@ private:
     Fluid<R> F() const { return fl_[cur_]; }
     Lists<R> LS() const
     {
-        return Lists<R>{pairs_.p, lcount_.p, bgrad_.p, kbuf_.p, kmax_, posh_.p};
+        return Lists<R>{pairs_.p, lcount_.p, bgrad_.p, kbuf_.p, kmax_, posh_.p, &sc_.p->status};
     }
     Boundary<R> B(int k) const { return bd_[k]; }
 
@@ -1668,7 +1668,10 @@ private:
     bool cands_ = false;            // PCISPH candidate lists (CandLists)
     uint32_t ckmax_ = 0;
     DevBuf<uint32_t> cand_, candn_;
-    CandLists CL() const { return cands_ ? CandLists{cand_.p, candn_.p, ckmax_} : CandLists{nullptr, nullptr, 0u}; }
+    CandLists CL() const
+    {
+        return cands_ ? CandLists{cand_.p, candn_.p, ckmax_, &sc_.p->status} : CandLists{nullptr, nullptr, 0u, nullptr};
+    }
     // the lists' reach beyond h: predicted displacements up to half of it keep them exact
     R cand_margin() const { return (R)0.1 * c_.h; }
     DevBuf<DevScalars> sc_;
