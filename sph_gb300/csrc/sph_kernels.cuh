@@ -481,14 +481,15 @@ __global__ void k_boundary_psi(Boundary<R> b, GridView g, const uint32_t* __rest
 }
 
 // ---------------------------------------------------------------------------
-// PCISPH candidate lists (one lane per particle).  The reference's PCISPH
-// sums run over the particles of the 27 cells found at the start of the step
-// (HashTable::neighborhoodSearch, HashTable.h:136-170), at the current
-// positions (densities, normals, non-pressure forces, pressure
-// accelerations) or the predicted ones (predicted densities).  The density
-// pass records, once per step, every fluid candidate of the 27 cells whose
-// current distance is within REACH = h + margin, in the walk's order, with
-// its cell offset; the later passes visit the list instead of the cells.
+// PCISPH / WCSPH candidate lists (one lane per particle).  The reference's
+// PCISPH and WCSPH sums run over the particles of the 27 cells found at the
+// start of the step (HashTable::neighborhoodSearch, HashTable.h:136-170), at
+// the current positions (densities, normals, non-pressure forces, pressure
+// accelerations, WCSPH's pressure force) or the predicted ones (PCISPH's
+// predicted densities).  The density pass records, once per step, every
+// fluid candidate of the 27 cells whose current distance is within
+// REACH = h + margin, in the walk's order, with its cell offset; the later
+// passes visit the list instead of the cells.
 // A candidate left out lies beyond h at the current positions, and beyond h
 // at the predicted ones while every predicted displacement stays below
 // margin / 2 (checked per loop iteration; otherwise the predicted-density
@@ -574,14 +575,14 @@ __device__ __forceinline__ void fluid_visit(const CandLists& L, uint32_t n, uint
     else walk<R, G, TRIM>(g, cs, pc, xi, h, lane, f);
 }
 
-// PCISPH densities (SPHSolver::computeFluidDensities SPHSolver.cpp:44-91, as
-// k_density<R, 1, false, false>) fused with the candidate lists' build.
-template <typename R>
-__global__ void __launch_bounds__(kBlock) k_pcisph_density_lists(Fluid<R> f, const P4<R>* __restrict__ bpos, GridView g,
-                                                                 const uint32_t* __restrict__ cs,
-                                                                 const uint32_t* __restrict__ bs, Consts<R> c, int akinci,
-                                                                 R reach2, uint32_t* __restrict__ idx,
-                                                                 uint32_t* __restrict__ cnt, uint32_t kmax)
+// Densities (SPHSolver::computeFluidDensities SPHSolver.cpp:44-91, as
+// k_density<R, 1, false, EOS>, EOS: with WCSPH's equation of state) fused
+// with the candidate lists' build.
+template <typename R, bool EOS = false>
+__global__ void __launch_bounds__(kBlock) k_density_cand(Fluid<R> f, const P4<R>* __restrict__ bpos, GridView g,
+                                                         const uint32_t* __restrict__ cs, const uint32_t* __restrict__ bs,
+                                                         Consts<R> c, int akinci, R reach2, uint32_t* __restrict__ idx,
+                                                         uint32_t* __restrict__ cnt, uint32_t kmax)
 {
     const uint32_t i = gtid();
     if (i >= f.count()) return;
@@ -609,6 +610,11 @@ __global__ void __launch_bounds__(kBlock) k_pcisph_density_lists(Fluid<R> f, con
     f.rho[i] = density;
     f.vel[i].w = density;
     cnt[i] = m;
+    if (EOS) {  // as k_density<R, G, false, true>
+        const R p = fmax((R)0, c.k_eos * (pow(density / c.density0, c.gamma) - (R)1));
+        f.press[i] = p;
+        f.xk[i] = P4<R>{xi.x, xi.y, xi.z, p / (density * density)};
+    }
 }
 
 // SPHSolver::computeFluidDensities SPHSolver.cpp:44-91, fused with
@@ -687,7 +693,8 @@ __global__ void __launch_bounds__(kBlock) k_density(Fluid<R> f, const P4<R>* __r
 template <typename R, int G>
 __global__ void __launch_bounds__(kBlock) k_wcsph_pressure_force(Fluid<R> f, const P4<R>* __restrict__ bpos, GridView g,
                                                                  const uint32_t* __restrict__ cs, const uint32_t* __restrict__ bs,
-                                                                 Consts<R> c, int akinci, const R* __restrict__ bdp)
+                                                                 Consts<R> c, int akinci, const R* __restrict__ bdp,
+                                                                 CandLists L = CandLists{nullptr, nullptr, 0u})
 {
     const uint32_t t = gtid();
     const uint32_t i = t / G;
@@ -699,7 +706,7 @@ __global__ void __launch_bounds__(kBlock) k_wcsph_pressure_force(Fluid<R> f, con
         const V3<R> xi = xyz(pi);
         const R dpi = pi.w;
         const uint32_t pc = f.cell[i];
-        walk<R, G>(g, cs, pc, xi, c.h, lane, [&](uint32_t j, V3<R> s) {
+        fluid_visit<R, G>(L, f.n, i, g, cs, pc, xi, c.h, lane, [&](uint32_t j, V3<R> s) {
             const P4<R> pj = ldg4(f.xk + j);
             const V3<R> r = s - xyz(pj);
             const R r2 = dot3(r, r);

@@ -265,9 +265,10 @@ public:
             const unsigned long long n = std::max<unsigned long long>(hx.size() / 3, 1ull);
             const unsigned long long want = (160000ull + n - 1) / n;
             G = want >= 8 ? 8 : want >= 4 ? 4 : want >= 2 ? 2 : 1;
-            // PCISPH from 40k particles: one lane over candidate lists beats
-            // lanes splitting the cell walks (81k drop: 0.45 vs 0.64 ms/step)
-            if (d.simulation_method == SPH_PCISPH && d.neighbor_list_max > 0 &&
+            // PCISPH / WCSPH from 40k particles: one lane over candidate lists
+            // beats lanes splitting the cell walks (81k PCISPH drop: 0.45 vs
+            // 0.64 ms/step)
+            if ((d.simulation_method == SPH_PCISPH || d.simulation_method == SPH_WCSPH) && d.neighbor_list_max > 0 &&
                 d.boundary_method != SPH_BOUNDARY_PCISPH && n >= 40000ull)
                 G = 1;
         }
@@ -963,11 +964,11 @@ private:
         }
         lists_ = d.simulation_method == SPH_DFSPH && d.neighbor_list_max > 0;
         kmax_ = lists_ ? (uint32_t)d.neighbor_list_max : 0u;
-        // PCISPH candidate lists: one lane per particle, Akinci or no
+        // PCISPH / WCSPH candidate lists: one lane per particle, Akinci or no
         // boundary (the PCISPH boundary model moves predicted positions after
         // the prediction), indices below 2^27
-        cands_ = d.simulation_method == SPH_PCISPH && d.neighbor_list_max > 0 && G_ == 1 && !bh_ &&
-                 n < (size_t)kCandIdxMask;
+        cands_ = (d.simulation_method == SPH_PCISPH || d.simulation_method == SPH_WCSPH) && d.neighbor_list_max > 0 &&
+                 G_ == 1 && !bh_ && n < (size_t)kCandIdxMask;
         if (cands_) {
             ckmax_ = (uint32_t)d.neighbor_list_max;
             SPH_CUDA(cand_.alloc((size_t)ckmax_ * n));
@@ -1081,6 +1082,17 @@ private:
             else
                 run("k_density", [&] { k_density<R, G, false, false><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, hasb_); });
         });
+        SPH_CUDA(cudaGetLastError());
+        return SPH_OK;
+    }
+
+    // Densities (EOS: and WCSPH pressures) with the step's candidate lists.
+    template <bool EOS> int launch_density_cand()
+    {
+        Fluid<R> f = F();
+        const R reach = c_.h + cand_margin();
+        run("k_density_cand", [&] { k_density_cand<R, EOS><<<blocks(n_, kBlock), kBlock, 0, ls_>>>(
+            f, bd_[1].pos, gv_, starts_.p, bstarts_.p, c_, akinci_, reach * reach, cand_.p, candn_.p, ckmax_); });
         SPH_CUDA(cudaGetLastError());
         return SPH_OK;
     }
@@ -1465,7 +1477,7 @@ private:
         if (rc) return rc;
         {
             auto ph = phase("Densities+Pressures");  // the equation of state is fused into the density pass
-            rc = launch_density(false, true);
+            rc = cands_ ? launch_density_cand<true>() : launch_density(false, true);
             if (rc) return rc;
             launch_bh_boundary(1);
         }
@@ -1476,7 +1488,7 @@ private:
             auto ph = phase("Pressure force");
             withG([&](auto gt) {
                 constexpr int G = decltype(gt)::value;
-                run("k_wcsph_pressure_force", [&] { k_wcsph_pressure_force<R, G><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, hasb_, dp); });
+                run("k_wcsph_pressure_force", [&] { k_wcsph_pressure_force<R, G><<<wblocks(), kBlock, 0, ls_>>>(f, bp, gv_, starts_.p, bstarts_.p, c_, hasb_, dp, CL()); });
             });
             SPH_CUDA(cudaGetLastError());
         }
@@ -1511,12 +1523,8 @@ private:
         {
             auto ph = phase("Densities");
             if (cands_) {
-                // densities and the step's candidate lists
-                Fluid<R> f = F();
-                const R reach = c_.h + cand_margin();
-                run("k_pcisph_density_lists", [&] { k_pcisph_density_lists<R><<<blocks(n_, kBlock), kBlock, 0, ls_>>>(
-                    f, bd_[1].pos, gv_, starts_.p, bstarts_.p, c_, akinci_, reach * reach, cand_.p, candn_.p, ckmax_); });
-                SPH_CUDA(cudaGetLastError());
+                rc = launch_density_cand<false>();   // densities and the step's candidate lists
+                if (rc) return rc;
             } else {
                 rc = launch_density(false, false);
                 if (rc) return rc;

@@ -1,16 +1,18 @@
-"""PCISPH candidate lists against the cell walks they replace.
+"""PCISPH / WCSPH candidate lists against the cell walks they replace.
 
 With one lane per particle the PCISPH step records, in its density pass, the
 fluid candidates of the 27 cells within h + 0.1 h at the current positions
 (walk order, with each candidate's cell offset), and the normals, non-pressure
 force, predicted-density and pressure-acceleration passes visit that list
-instead of the cells (CandLists, sph_kernels.cuh).  The terms a list leaves
+instead of the cells (CandLists, sph_kernels.cuh); WCSPH's pressure-force
+and non-pressure-force passes likewise.  The terms a list leaves
 out are exactly the ones the walks skip, so a scene run with lists must equal
 the same scene run with walks (neighbor_list_max = 0) bit for bit: here the
 PCISPH drop (viscosity, surface tension, adhesion, Akinci walls) through its
 impact, in FP32 and FP64; a fast scene whose predicted displacements exceed
 the lists' margin (the predicted-density pass then walks the cells); and
-lists too short for most particles (those walk)."""
+lists too short for most particles (those walk); and the same drop as a
+WCSPH scene (stiffness 1000, gamma 7, with the same forces)."""
 import numpy as np
 import pytest
 
@@ -35,6 +37,11 @@ def drop(case):
     if case == "fast":
         v[:, 1] = -3.0
         p = dict(p, dt=1e-3)
+    if case == "wcsph":
+        top = x[:, 1] > 0.07
+        x[top, 1] -= 0.38
+        v[top, 1] = -3.4
+        p = dict(p, method=0, stiffness=1000.0, gamma=7.0, dt=5e-5)
     return x, v, b, p
 
 
@@ -51,7 +58,7 @@ def run(x, v, b, p, precision, lists, steps, graph):
 
 
 @pytest.mark.parametrize("case,precision,lists", [("impact", "f32", 64), ("impact", "f64", 64), ("fast", "f32", 64),
-                                                  ("impact", "f32", 16)])
+                                                  ("impact", "f32", 16), ("wcsph", "f32", 64), ("wcsph", "f64", 64)])
 @pytest.mark.parametrize("graph", [False, True], ids=["host", "graph"])
 def test_candidate_lists_equal_cell_walks(gpu_lib, case, precision, lists, graph):
     x, v, b, p = drop(case)
@@ -59,11 +66,12 @@ def test_candidate_lists_equal_cell_walks(gpu_lib, case, precision, lists, graph
     a = run(x, v, b, p, precision, lists, steps, graph)
     w = run(x, v, b, p, precision, 0, steps, graph)
     if not graph:
-        assert "k_pcisph_density_lists" in a.profile()
+        assert "k_density_cand" in a.profile()
     for f in ("x", "v", "rho"):
         assert np.array_equal(a.get(f), w.get(f)), f
     sa, sw = a.stats(), w.stats()
     assert sa["sum_iterations"] == sw["sum_iterations"] and sa["status"] == sw["status"]
     if case != "fast":
         assert sa["status"] == 0
+    assert np.isfinite(a.get("x")).all()
     print(case, precision, lists, "graph" if graph else "host", "iterations", sa["sum_iterations"])
