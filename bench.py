@@ -17,6 +17,11 @@ Workloads (seeded, synthetic; sph_gb300/workloads.py):
                    1.5 x 0.8 x 0.8 m Akinci box (60,802 boundary points).
                    (At r = 0.01 m the 50^3 block is 1 m tall and does not
                    fit the 0.8 m box; r = 0.005 m keeps count and box.)
+  pcisph_drop_490k the PCISPH drop impact at r = 2.75 mm: a 9-layer pool and a
+                   0.2 m-radius sphere 0.6 m above it in a 1 m Akinci box
+                   (489,771 fluid, 198,746 boundary particles), standard
+                   viscosity, Akinci surface tension and adhesion, dt 1e-4 s,
+                   one scene in graph mode (candidate lists), 1,000 steps.
 
 One "step" of the headline is one step of every scene of the mix: the pool
 advances all resident scenes with one CUDA graph launch per step (segmented
@@ -31,6 +36,7 @@ K timed steps.  Beside it, on the same mix and the same steps:
              dam break every 10 s: aggregate particle-steps/s, p50/p99 scene
              latency;
   dam_break_125k  the plain solver on the single large scene;
+  pcisph_drop_490k  the PCISPH solver on the full-size drop;
   e2e        the mix through the pool's C ABI with host buffers: scenes
              uploaded from pinned host memory, per-step status read back,
              final positions and velocities downloaded, all timed;
