@@ -41,6 +41,10 @@ template <typename R> struct Lists {
     // half2 pairs, z in the cell's modulo-3 frame), or nullptr
     const uint4* posh;
     unsigned* fault;    // status word of the bounds-checked build (SPH_INDEX_OK)
+    // Akinci boundary points in the same half-precision form (static between
+    // re-layouts) and their cells, for the boundary cull; or nullptr
+    const uint4* bposh;
+    const uint32_t* bcell;
 };
 
 // Phase 1 of the FP32 list build from the half-precision positions: the
@@ -314,10 +318,8 @@ __device__ __forceinline__ void build_lists_one(uint32_t i, const Fluid<R>& f, c
         cnt = b.cnt;
     }
     V3<R> bg = {0, 0, 0};
-    if (akinci)
-        walk<R, 1>(g, bs, pc, xi, c.h, 0, [&](uint32_t j, V3<R> s) {
-            const P4<R> pb = ldg4(bpos + j);
-            const V3<R> r = s - xyz(pb);
+    if (akinci) {
+        auto bterm = [&](const P4<R>& pb, V3<R> r) {
             const R r2 = dot3(r, r);
             if (!(r2 <= c.cull2)) return;
             R w;
@@ -325,7 +327,29 @@ __device__ __forceinline__ void build_lists_one(uint32_t i, const Fluid<R>& f, c
             cubic_W_gradW<FAST>(c, r, r2, &w, &gw);
             density += pb.w * w;
             bg = bg + pb.w * gw;
-        });
+        };
+        // The boundary candidates as the fluid ones: culled from the static
+        // half-precision copy into the (now free) queue, then evaluated in
+        // the walk's order (the same cells, trimmed alike: the same terms in
+        // the same order as the walk, the gradient sum compiled apart from
+        // the walk's, so its last bit may differ); or the walk itself.
+        uint32_t nb = qcap + 1u;
+        if constexpr (FAST && sizeof(R) == 4) {
+            if (half_cull && L.bposh) nb = cull_half(g, bs, pc, xi, c.h, c.cull2, L.bposh, q, qstride, qcap);
+        }
+        if (nb <= qcap) {
+            for (uint32_t k = 0; k < nb; ++k) {
+                const uint32_t j = q[k * qstride + threadIdx.x];
+                const P4<R> pb = ldg4(bpos + j);
+                bterm(pb, pair_vec(xi, pc, pb, __ldg(L.bcell + j), c.h));
+            }
+        } else {
+            walk<R, 1>(g, bs, pc, xi, c.h, 0, [&](uint32_t j, V3<R> s) {
+                const P4<R> pb = ldg4(bpos + j);
+                bterm(pb, s - xyz(pb));
+            });
+        }
+    }
     sumGrad = sumGrad + bg;
     f.rho[i] = density;
     f.vel[i].w = density;

@@ -238,6 +238,23 @@ __global__ void k_pool_bcount(uint32_t N, Boundary<float> b, const uint32_t* __r
     slot[i] = atomicAdd(count + k, 1u);
 }
 
+// The boundary points' half-precision copy for the list build's boundary
+// cull (two points per 16-byte word, {x, y, z in the cell's modulo-3 frame},
+// as the fluid's copy): boundary points do not move, so it is written once
+// per re-layout.
+__global__ void k_pool_boundary_half(uint32_t N, Boundary<float> b, const uint32_t* __restrict__ bsid, const PoolScene* T,
+                                     uint4* __restrict__ posh)
+{
+    const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= N) return;
+    const float h = T[bsid[d]].c.h;
+    const P4<float> x = b.pos[d];
+    __half* ph = reinterpret_cast<__half*>(posh) + (size_t)(d >> 1) * 8 + (d & 1);
+    ph[0] = __float2half_rn(x.x);
+    ph[2] = __float2half_rn(x.y);
+    ph[4] = __float2half_rn(zframe3(x.z, cell_z(b.cell[d]), h));
+}
+
 // AkinciBoundaryModel::computeVolume (AkinciBoundayModel.cpp:11-40) per scene.
 __global__ void k_pool_psi(uint32_t N, Boundary<float> b, const uint32_t* __restrict__ bsid, const PoolScene* T,
                            const uint32_t* __restrict__ bstarts)
@@ -679,6 +696,8 @@ public:
         SPH_CUDA(pairs_.alloc(P * kmax_)); SPH_CUDA(lcount_.alloc(P)); SPH_CUDA(bgrad_.alloc(P));
         SPH_CUDA(posh_.alloc(P / 2 + 2));  // particle pairs, the last one whole, and a spare word for the cull
         SPH_CUDA(cudaMemsetAsync(posh_.p, 0, (P / 2 + 2) * sizeof(uint4), st_));
+        SPH_CUDA(bposh_.alloc(B / 2 + 2));
+        SPH_CUDA(cudaMemsetAsync(bposh_.p, 0, (B / 2 + 2) * sizeof(uint4), st_));
         const size_t M = std::max(P, B);
         SPH_CUDA(key_.alloc(M)); SPH_CUDA(slot_.alloc(M)); SPH_CUDA(tmp_.alloc(M));
         SPH_CUDA(count_.alloc(K)); SPH_CUDA(starts_.alloc(K + 1)); SPH_CUDA(bstarts_.alloc(K + 1));
@@ -1410,7 +1429,8 @@ private:
     Boundary<float> B(int k) const { return Boundary<float>{bpos_[k].p, bpsi_.p, bcell_[k].p, bid_[k].p, NB_}; }
     Lists<float> LS() const
     {
-        return Lists<float>{pairs_.p, lcount_.p, bgrad_.p, kbuf_.p, kmax_, posh_.p, &pc_.p->faults};
+        return Lists<float>{pairs_.p, lcount_.p, bgrad_.p, kbuf_.p, kmax_, posh_.p, &pc_.p->faults,
+                            NB_ ? bposh_.p : nullptr, B(bcur_).cell};
     }
 
     int scan(uint32_t* out)
@@ -1676,6 +1696,8 @@ private:
             bcur_ = 1 - bcur_;
             k_pool_psi<<<blocks(NB_, 128), 128, 0, st_>>>(NB_, B(bcur_), bsid_.p, table_.p, bstarts_.p);
             SPH_CUDA(cudaGetLastError());
+            k_pool_boundary_half<<<blocks(NB_, 256), 256, 0, st_>>>(NB_, B(bcur_), bsid_.p, table_.p, bposh_.p);
+            SPH_CUDA(cudaGetLastError());
         } else {
             SPH_CUDA(cudaMemsetAsync(bstarts_.p, 0, (K_ + 1) * sizeof(uint32_t), st_));
         }
@@ -1919,6 +1941,7 @@ private:
     DevBuf<uint32_t> cell_[2], id_[2], bcell_[2], bid_[2];
     DevBuf<P4<float>> acc_, dummy4_, pairs_, bgrad_, normal_;
     DevBuf<uint4> posh_;  // half-precision positions for the build's cull (particle pairs)
+    DevBuf<uint4> bposh_; // the boundary points' half-precision copy (boundary cull)
     DevBuf<uint8_t> run_;   // per scene: running (poll)
     uint8_t* h_run_ = nullptr;
     DevBuf<float> rho_, alpha_, div_, press_, kbuf_, bpsi_;

@@ -851,7 +851,7 @@ private:
     Fluid<R> F() const { return fl_[cur_]; }
     Lists<R> LS() const
     {
-        return Lists<R>{pairs_.p, lcount_.p, bgrad_.p, kbuf_.p, kmax_, posh_.p, &sc_.p->status};
+        return Lists<R>{pairs_.p, lcount_.p, bgrad_.p, kbuf_.p, kmax_, posh_.p, &sc_.p->status, nullptr, nullptr};
     }
     Boundary<R> B(int k) const { return bd_[k]; }
 
