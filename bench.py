@@ -689,6 +689,7 @@ def main():
     ap.add_argument("--epoch-steps", type=int, default=10)
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--no-sub-saturation", action="store_true", help="served: only the 200 scenes/s stream")
+    ap.add_argument("--serve-rate", type=float, default=200.0, help="arrival rate of the first served stream (scenes/s)")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-dam", action="store_true")
@@ -736,7 +737,7 @@ def main():
     if not args.no_served and world == 1:
         big_load = 4_000_000 * 200 / 10.0
         sub_rate = max(0.5, (0.5 * value - big_load) / stream_mean_work())
-        served = {"saturated": run_served(args, 200.0, args.serve_seconds, 10.0)}
+        served = {"saturated": run_served(args, args.serve_rate, args.serve_seconds, 10.0)}
         if not args.no_sub_saturation:
             served["sub_saturation"] = run_served(args, round(sub_rate, 2), args.serve_seconds, 10.0)
             served["sub_saturation_rate_rule"] = "offered load = half the batched value, 4M dam break included"
